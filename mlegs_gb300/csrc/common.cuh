@@ -1,0 +1,138 @@
+// common.cuh — shared state, error handling and small device helpers of the GB300 library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "../../include/mlegs_gb300.h"
+
+namespace mlg {
+
+typedef double2 cd;   // complex128 as stored in a field (re, im)
+
+// ---------------------------------------------------------------------------------------------
+// errors: every C-ABI call returns a status; the message is kept for mlg_last_error()
+int set_error(int code, const std::string& msg);
+#define MLG_TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
+#define MLG_CUDA(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) \
+    return ::mlg::set_error(MLG_ECUDA, std::string(#x) + ": " + cudaGetErrorString(_e)); } while (0)
+#define MLG_LAUNCH() do { cudaError_t _e = cudaGetLastError(); if (_e != cudaSuccess) \
+    return ::mlg::set_error(MLG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(_e)); } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// a field ("scalar"): device complex128 array (nrdim, npdim, nzdim), Fortran order
+struct Scalar {
+  cd* e = nullptr;        // device data
+  double* ln = nullptr;   // device slot holding the log-term coefficient (ln of type(scalar))
+  char space[4] = {'P', 'P', 'P', 0};
+  int off[3] = {0, 0, 0};
+  int slot = -1;          // index of the ln slot
+  bool is(const char* s) const { return std::strncmp(space, s, 3) == 0; }
+  void set_space(const char* s) { std::memcpy(space, s, 3); space[3] = 0; }
+};
+
+// chop_index (mlegs_scalar_ops.f90:2012-2063) on one process
+struct ChopIdx { int nrc, npc, nzc, nzcu; };
+
+// kernel-time accounting per kernel class (mlg_kernel_timing)
+struct KTimer {
+  bool on = false;
+  double ms[3] = {0, 0, 0};
+  long long n[3] = {0, 0, 0};
+  double work[3] = {0, 0, 0};
+};
+
+struct Ctx {
+  bool kit_set = false;
+  mlg_params P{};
+  int nr = 0, np = 0, nz = 0, nrchop = 0, npchop = 0, nzchop = 0;
+  int nrdim = 0, npdim = 0, nzdim = 0, nrh = 0, ne = 0, chopzl = 0, chopzu = 0, nph = 0;
+  size_t fsize = 0;       // complex entries per field
+  double ell = 0;
+  int precision = MLG_PLAIN_FP64;
+  cudaStream_t stream = 0;
+
+  // kit arrays on the device
+  double *x = nullptr, *w = nullptr, *r = nullptr, *lnx = nullptr, *ak = nullptr;
+  double *lognorm = nullptr;   // (ne, npchop)
+  double *pf = nullptr;        // (nrh, ne, npchop): P_L^m(x_i) normalised, reference layout
+  float *pf32 = nullptr;       // FP32 copy of pf for the mixed form
+  double *at0 = nullptr, *at1 = nullptr;   // (nrchop)
+  double *bd2 = nullptr;       // del2 bands without the -k^2 term: (5, ne, npchop)
+  double *bxx = nullptr;       // xxdx bands: (3, ne+1, npchop)
+  double *tV = nullptr, *tD = nullptr, *tT = nullptr;   // vec2tp matrices (nrh, ne, npchop)
+  float *tV32 = nullptr, *tD32 = nullptr, *tT32 = nullptr;
+  double2 *tw_p = nullptr, *tw_z = nullptr;  // FFT twiddles exp(-2 pi i k/L): L = np/2 (phi), nz (z)
+  double2 *tw_pr = nullptr;    // real-FFT post-processing twiddles exp(-2 pi i k/np), k < np/2+1
+
+  // ln slots of all scalars (device), and per-step scalars (svv gains, flags, scratch reductions)
+  double* ln_slots = nullptr;  int n_slots = 0;  std::vector<int> free_slots;
+  double* dscal = nullptr;     // misc device scalars (see DS_* below)
+
+  // banded-solve scratch: LU work band (7 or more rows) per (m, k) system
+  double* band_ws = nullptr;   size_t band_ws_bytes = 0;
+
+  // pool of field-sized device buffers for out-of-place steps and temporaries
+  std::vector<cd*> pool;
+  std::vector<cd*> all_bufs;
+
+  long long mem_bytes = 0, mem_high = 0;
+  KTimer kt;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+extern Ctx G;
+
+// indices into G.dscal
+enum { DS_SUM0 = 0, DS_SUM1 = 1, DS_GAIN0 = 4, DS_GAIN1 = 5, DS_FLAG = 8, DS_CALC = 16, DS_COUNT = 16 + 2 * 4096 };
+
+// device memory accounting
+int dmalloc(void** p, size_t bytes);
+void dfree(void* p, size_t bytes);
+cd* get_buf();
+void put_buf(cd* b);
+int pool_reserve(int n);
+
+// kernel timing helpers
+void kt_begin(int kind);
+void kt_end(int kind, double work);
+
+// host-side chop_index
+int chop_index(const Scalar& s, ChopIdx& c);
+
+// kernels (host launchers), defined in the .cu files
+int kit_build(const mlg_params* p);
+int kit_free();
+int launch_hfft(Scalar& s, int dir);             // dir -1 forward (1/np), +1 backward
+int launch_vfft(Scalar& s, int dir);             // dir -1 forward (1/nz), +1 backward
+int launch_vfft_buf(cd* e, int dir);
+int launch_rtrans_fwd(Scalar& s);
+int launch_rtrans_bwd(Scalar& s, bool add_ln);
+int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
+int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
+
+// pointwise
+int launch_zero(cd* e);
+int launch_copy(cd* dst, const cd* src);
+int launch_copy_ln(double* dst, const double* src);
+int launch_set_ln(double* dst, double v);
+
+}  // namespace mlg
+
+// ---------------------------------------------------------------------------------------------
+// device helpers
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ float2 caddf(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csubf(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+static inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }

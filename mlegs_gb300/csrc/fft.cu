@@ -1,0 +1,268 @@
+// fft.cu — φ and z FFTs of a field (horizontal_fft_forward/backward, mlegs_scalar_ops.f90:1567-1717;
+// vertical_fft_forward/backward, :1721-1848) in FFTE's conventions:
+//   forward  X_k = sum_j x_j exp(-2 pi i jk/N), then scaled 1/N (the reference divides after FFTE);
+//   backward unnormalised sum with exp(+2 pi i jk/N) (FFTE's 1/N undone by the reference's *N).
+// The φ transform is real: PPP stores two real samples per complex slot, z_j = f(2j) + i f(2j+1),
+// which is exactly the input of a half-length complex FFT; the usual split step turns its result
+// into X_0..X_{N/2}.  Backward, the last complex slot keeps N times its input (FFTE's zdfft2d never
+// writes A(NX/2+1), zdfft2d.f:119-128, and the reference then multiplies by N, :1705).
+//
+// Layout: a field is (nrdim, npdim, nzdim) with r fastest.  Both transforms run along a strided
+// dimension; a CTA takes TR consecutive r (the contiguous batch, so every global access is a run of
+// TR*16 bytes) and TT threads per transform, keeps the TR transforms in shared memory as
+// [point][TR] and runs a Stockham autosort FFT (radix 4, 2, 3, 5) between two shared buffers.
+#include "common.cuh"
+
+namespace mlg {
+
+template <typename T> struct CT;
+template <> struct CT<double> { typedef double2 t; };
+template <> struct CT<float> { typedef float2 t; };
+
+template <typename T> __device__ __forceinline__ typename CT<T>::t mk(T a, T b);
+template <> __device__ __forceinline__ double2 mk<double>(double a, double b) { return make_double2(a, b); }
+template <> __device__ __forceinline__ float2 mk<float>(float a, float b) { return make_float2(a, b); }
+
+template <typename C> __device__ __forceinline__ C c_add(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C c_sub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C c_mul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C> __device__ __forceinline__ C c_muli(C a, int sgn) {  // a * (sgn * i)
+  C r; r.x = -sgn * a.y; r.y = sgn * a.x; return r;
+}
+template <typename C, typename T> __device__ __forceinline__ C c_scale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+
+template <typename T>
+__device__ __forceinline__ typename CT<T>::t load_tw(const double2* tw, int idx, int sgn) {
+  double2 w = tw[idx];
+  return mk<T>((T)w.x, (T)(sgn < 0 ? w.y : -w.y));   // table holds exp(-2 pi i k/L); sgn>0 conjugates
+}
+
+// small DFTs, sign sgn = -1 forward, +1 backward
+template <typename T>
+__device__ __forceinline__ void dft_small(typename CT<T>::t* a, int p, int sgn) {
+  typedef typename CT<T>::t C;
+  if (p == 2) {
+    C t = a[0]; a[0] = c_add(t, a[1]); a[1] = c_sub(t, a[1]);
+  } else if (p == 4) {
+    C t0 = c_add(a[0], a[2]), t1 = c_sub(a[0], a[2]), t2 = c_add(a[1], a[3]), t3 = c_muli(c_sub(a[1], a[3]), sgn);
+    a[0] = c_add(t0, t2); a[2] = c_sub(t0, t2); a[1] = c_add(t1, t3); a[3] = c_sub(t1, t3);
+  } else if (p == 3) {
+    const T c1 = (T)-0.5, s1 = (T)0.86602540378443864676372317075294;  // cos(2pi/3), sin(2pi/3)
+    C t1 = c_add(a[1], a[2]), t2 = c_sub(a[1], a[2]);
+    C m1 = c_add(a[0], c_scale(t1, c1));
+    C m2 = c_muli(c_scale(t2, s1), sgn);
+    a[0] = c_add(a[0], t1); a[1] = c_add(m1, m2); a[2] = c_sub(m1, m2);
+  } else if (p == 5) {
+    const T c1 = (T)0.30901699437494742410229341718282, c2 = (T)-0.80901699437494742410229341718282;
+    const T s1 = (T)0.95105651629515357211643933337938, s2 = (T)0.58778525229247312916870595463907;
+    C t1 = c_add(a[1], a[4]), t2 = c_add(a[2], a[3]), t3 = c_sub(a[1], a[4]), t4 = c_sub(a[2], a[3]);
+    C m1 = c_add(a[0], c_add(c_scale(t1, c1), c_scale(t2, c2)));
+    C m2 = c_add(a[0], c_add(c_scale(t1, c2), c_scale(t2, c1)));
+    C n1 = c_muli(c_add(c_scale(t3, s1), c_scale(t4, s2)), sgn);
+    C n2 = c_muli(c_sub(c_scale(t3, s2), c_scale(t4, s1)), sgn);
+    a[0] = c_add(a[0], c_add(t1, t2));
+    a[1] = c_add(m1, n1); a[4] = c_sub(m1, n1);
+    a[2] = c_add(m2, n2); a[3] = c_sub(m2, n2);
+  }
+}
+
+// Stockham FFT over the TR transforms held in s0 ([L][TR]); result left in *res.
+template <typename T>
+__device__ void stockham(typename CT<T>::t* s0, typename CT<T>::t* s1, typename CT<T>::t** res, int L, int TR,
+                         int tr, int tt, int TT, const double2* tw, int sgn) {
+  typedef typename CT<T>::t C;
+  C* src = s0;
+  C* dst = s1;
+  int rem = L;
+  for (int ns = 1; ns < L;) {
+    int p = (rem % 4 == 0) ? 4 : (rem % 2 == 0) ? 2 : (rem % 3 == 0) ? 3 : 5;
+    int m = L / p;
+    int span = ns * p, twstep = L / span;
+    for (int j = tt; j < m; j += TT) {
+      int k = j % ns;
+      C a[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+        if (r < p) a[r] = src[(j + r * m) * TR + tr];
+      if (k) {
+#pragma unroll
+        for (int r = 1; r < 5; ++r)
+          if (r < p) a[r] = c_mul(a[r], load_tw<T>(tw, (k * r * twstep) % L, sgn));
+      }
+      dft_small<T>(a, p, sgn);
+      int base = (j / ns) * span + k;
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+        if (r < p) dst[(base + r * ns) * TR + tr] = a[r];
+    }
+    __syncthreads();
+    C* t = src; src = dst; dst = t;
+    ns = span;
+    rem /= p;
+  }
+  *res = src;
+}
+
+template <typename T> __device__ __forceinline__ typename CT<T>::t ld(const double2* p) {
+  double2 v = *p; return mk<T>((T)v.x, (T)v.y);
+}
+template <typename T> __device__ __forceinline__ void st(double2* p, typename CT<T>::t v) {
+  *p = make_double2((double)v.x, (double)v.y);
+}
+
+// z FFT of columns (r, m): points at stride nrdim*npdim
+template <typename T>
+__global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
+                       int sgn, double scale) {
+  typedef typename CT<T>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = (C*)smem_raw;
+  C* s1 = s0 + (size_t)L * TR;
+  int tr = threadIdx.x, tt = threadIdx.y, TT = blockDim.y;
+  int r = blockIdx.x * TR + tr;
+  int m = blockIdx.y;
+  bool ok = r < nrdim;
+  size_t pstride = (size_t)nrdim * npdim;
+  double2* base = e + r + (size_t)nrdim * m;
+  for (int pt = tt; pt < L; pt += TT) s0[pt * TR + tr] = ok ? ld<T>(base + pt * pstride) : mk<T>(0, 0);
+  __syncthreads();
+  C* res;
+  stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, sgn);
+  if (ok)
+    for (int pt = tt; pt < L; pt += TT) st<T>(base + pt * pstride, c_scale(res[pt * TR + tr], (T)scale));
+}
+
+// φ forward: packed reals -> X_0..X_{L} (L = np/2) scaled 1/np, in place
+template <typename T>
+__global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
+                           const double2* __restrict__ twr, double scale) {
+  typedef typename CT<T>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = (C*)smem_raw;
+  C* s1 = s0 + (size_t)L * TR;
+  int tr = threadIdx.x, tt = threadIdx.y, TT = blockDim.y;
+  int r = blockIdx.x * TR + tr;
+  int z = blockIdx.y;
+  bool ok = r < nrdim;
+  double2* base = e + r + (size_t)nrdim * npdim * z;
+  for (int pt = tt; pt < L; pt += TT) s0[pt * TR + tr] = ok ? ld<T>(base + (size_t)pt * nrdim) : mk<T>(0, 0);
+  __syncthreads();
+  C* res;
+  stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, -1);
+  if (!ok) return;
+  for (int k = tt; k <= L; k += TT) {
+    C zk = res[(k % L) * TR + tr];
+    C zc = res[((L - k) % L) * TR + tr];
+    zc.y = -zc.y;
+    C fe = c_scale(c_add(zk, zc), (T)0.5);
+    C fo = c_muli(c_scale(c_sub(zk, zc), (T)0.5), -1);   // (zk - zc)/(2i)
+    double2 wd = twr[k];
+    C w = mk<T>((T)wd.x, (T)wd.y);
+    C x = c_add(fe, c_mul(w, fo));
+    st<T>(base + (size_t)k * nrdim, c_scale(x, (T)scale));
+  }
+}
+
+// φ backward: X_0..X_L -> packed reals (unnormalised); slot L <- np * X_L (input), in place
+template <typename T>
+__global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
+                           const double2* __restrict__ twr, double np_d) {
+  typedef typename CT<T>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = (C*)smem_raw;
+  C* s1 = s0 + (size_t)L * TR;
+  int tr = threadIdx.x, tt = threadIdx.y, TT = blockDim.y;
+  int r = blockIdx.x * TR + tr;
+  int z = blockIdx.y;
+  bool ok = r < nrdim;
+  double2* base = e + r + (size_t)nrdim * npdim * z;
+  double2 nyq = make_double2(0, 0);
+  if (ok && tt == 0) nyq = base[(size_t)L * nrdim];
+  for (int k = tt; k < L; k += TT) {
+    C v = mk<T>(0, 0);
+    if (ok) {
+      C xk = ld<T>(base + (size_t)k * nrdim);
+      C xc = ld<T>(base + (size_t)(L - k) * nrdim);
+      if (k == 0) { xk.y = 0; xc.y = 0; }
+      xc.y = -xc.y;
+      C g = c_add(xk, xc);
+      double2 wd = twr[k];
+      C w = mk<T>((T)wd.x, (T)-wd.y);   // exp(+2 pi i k / np)
+      C h = c_mul(c_sub(xk, xc), w);
+      v = c_add(g, c_muli(h, 1));
+    }
+    s0[k * TR + tr] = v;
+  }
+  __syncthreads();
+  C* res;
+  stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, +1);
+  if (!ok) return;
+  for (int pt = tt; pt < L; pt += TT) st<T>(base + (size_t)pt * nrdim, res[pt * TR + tr]);
+  if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
+}
+
+static int pick_tr(int L, size_t elem) {
+  // two shared buffers of L*TR complex values, at most 96 KB
+  int tr = 32;
+  while (tr > 1 && 2ull * L * tr * elem > 96 * 1024) tr /= 2;
+  return tr;
+}
+
+template <typename T>
+static int set_smem(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return 0;
+}
+
+template <typename T>
+static int vfft_t(cd* e, int dir) {
+  int L = G.nz;
+  if (L <= 1) return 0;
+  int TR = pick_tr(L, sizeof(typename CT<T>::t));
+  int TT = std::max(1, std::min(256 / TR, L / 2));
+  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
+  MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
+  dim3 grid(cdiv(G.nrdim, TR), G.npdim), blk(TR, TT);
+  kt_begin(1);
+  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_z, dir, dir < 0 ? 1.0 / L : 1.0);
+  MLG_LAUNCH();
+  kt_end(1, 2.0 * G.fsize * 16);
+  return 0;
+}
+
+int launch_vfft_buf(cd* e, int dir) {
+  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir) : vfft_t<double>(e, dir);
+}
+int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
+
+template <typename T>
+static int hfft_t(cd* e, int dir) {
+  int L = G.nph;
+  if (G.np <= 1) return 0;
+  int TR = pick_tr(L, sizeof(typename CT<T>::t));
+  int TT = std::max(1, std::min(256 / TR, std::max(L / 2, 1)));
+  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
+  dim3 grid(cdiv(G.nrdim, TR), G.nzdim), blk(TR, TT);
+  kt_begin(1);
+  if (dir < 0) {
+    MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
+    k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_p, G.tw_pr, 1.0 / G.np);
+  } else {
+    MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
+    k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_p, G.tw_pr, (double)G.np);
+  }
+  MLG_LAUNCH();
+  kt_end(1, 2.0 * G.fsize * 16);
+  return 0;
+}
+
+int launch_hfft(Scalar& s, int dir) {
+  if (G.npchop + s.off[1] > G.npdim)
+    return set_error(MLG_ECHOP, dir < 0 ? "horizontal_fft_forward: chopping in p too large"
+                                        : "horizontal_fft_fbackard: chopping in p too large");
+  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir) : hfft_t<double>(s.e, dir);
+}
+
+}  // namespace mlg

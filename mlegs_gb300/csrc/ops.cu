@@ -1,0 +1,1125 @@
+// ops.cu — the scalar operator API of the reference (module mlegs_scalar, mlegs_scalar_ops.f90) on
+// device-resident fields, and the 3-D vortex step of src/apps/vortical_flow_3d.f90.  Host code keeps
+// the reference's control flow (space state machine, chop offsets, per-routine order of work); all
+// field arithmetic runs in the kernels of this file, fft.cu, radial.cu and banded.cu.  The log-term
+// coefficient ln of every field lives in device memory, so no step needs a host round trip.
+#include "common.cuh"
+#include <cmath>
+#include <mutex>
+#include <algorithm>
+
+namespace mlg {
+
+Ctx G;
+static std::string g_err;
+
+int set_error(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int dmalloc(void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(MLG_EALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  G.mem_bytes += (long long)bytes;
+  G.mem_high = std::max(G.mem_high, G.mem_bytes);
+  return 0;
+}
+void dfree(void* p, size_t bytes) {
+  if (p) cudaFree(p);
+  G.mem_bytes -= (long long)bytes;
+}
+
+cd* get_buf() {
+  if (!G.pool.empty()) {
+    cd* b = G.pool.back();
+    G.pool.pop_back();
+    return b;
+  }
+  cd* b = nullptr;
+  if (dmalloc((void**)&b, G.fsize * sizeof(cd))) return nullptr;
+  G.all_bufs.push_back(b);
+  return b;
+}
+void put_buf(cd* b) {
+  if (b) G.pool.push_back(b);
+}
+int pool_reserve(int n) {
+  std::vector<cd*> t;
+  for (int i = 0; i < n; ++i) {
+    cd* b = get_buf();
+    if (!b) return MLG_EALLOC;
+    t.push_back(b);
+  }
+  for (cd* b : t) put_buf(b);
+  return 0;
+}
+
+void kt_begin(int kind) {
+  if (!G.kt.on) return;
+  (void)kind;
+  cudaEventRecord(G.ev0, G.stream);
+}
+void kt_end(int kind, double work) {
+  if (!G.kt.on) return;
+  cudaEventRecord(G.ev1, G.stream);
+  cudaEventSynchronize(G.ev1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, G.ev0, G.ev1);
+  G.kt.ms[kind] += ms;
+  G.kt.n[kind] += 1;
+  G.kt.work[kind] += work;
+}
+
+int chop_index(const Scalar& s, ChopIdx& c) {
+  c.nrc = G.nrchop + s.off[0];
+  c.npc = G.npchop + s.off[1];
+  c.nzc = G.chopzl + s.off[2];
+  c.nzcu = G.chopzu - s.off[2];
+  if (c.nrc > G.nrdim) return set_error(MLG_ECHOP, "chop_index: chopping in r too large");
+  if (c.npc > G.npdim) return set_error(MLG_ECHOP, "chop_index: chopping in p too large");
+  if (2 * s.off[2] > c.nzcu - c.nzc) return set_error(MLG_ECHOP, "chop_index: chopping in z too large");
+  if (c.nrc > G.ne) return set_error(MLG_ECHOP, "chop_index: chopping in r beyond the Legendre table");
+  return 0;
+}
+
+int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
+int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
+int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, double beta);
+
+// ------------------------------------------------------------------------------------------------
+// pointwise kernels
+#define GRID_STRIDE(i, n) for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (n); i += (size_t)gridDim.x * blockDim.x)
+static inline int nblk(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+// chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
+__global__ void k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int mode, int f0, int f1, int f2,
+                       int nrc, int npc, int nzc, int nzcu, int pcut, int zcut, int zupper, int np_gt1, int nz_gt1) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    int k = (int)(idx / ((size_t)nrdim * npdim));
+    bool z = false;
+    if (mode == 0) {
+      int nrcs = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
+      if (f0 && i >= nrcs) z = true;
+      if (f1 && m >= npc) z = true;
+      if (f2 && nzc < nzcu && (k + 1) >= nzc + 1 && (k + 1) <= nzcu - 1) z = true;
+    } else {
+      if (np_gt1 && f1 && (m + 1) > pcut) z = true;
+      if (nz_gt1 && f2 && (k + 1) > zcut && (k + 1) < zupper) z = true;
+    }
+    if (z) e[idx] = make_double2(0.0, 0.0);
+  }
+}
+
+// e(:nr, 1, :) += sgn * ln * lnx (trans :193-195, :219-221)
+__global__ void k_ln_adjust(double2* __restrict__ e, const double* __restrict__ lnp, const double* __restrict__ lnx,
+                            int nr, int nrdim, int npdim, int nzdim, double sgn) {
+  double l = *lnp;
+  if (l == 0.0) return;
+  size_t n = (size_t)nr * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nr);
+    int k = (int)(idx / nr);
+    e[i + (size_t)nrdim * npdim * k].x += sgn * l * lnx[i];
+  }
+}
+
+// out = c0*a + c1*b + c2*c + c3*d (null inputs skipped); ln likewise with separate coefficients
+struct LinArgs {
+  double2* out;
+  const double2* in[4];
+  double c[4];
+  double* lnout;
+  const double* lnin[4];
+  double lc[4];
+  double post;     // overall multiplier applied after the sum (e and ln)
+  size_t n;
+};
+__global__ void k_lincomb(LinArgs a) {
+  GRID_STRIDE(idx, a.n) {
+    double2 acc = make_double2(0, 0);
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (a.in[t]) { double2 v = a.in[t][idx]; acc.x += a.c[t] * v.x; acc.y += a.c[t] * v.y; }
+    a.out[idx] = make_double2(a.post * acc.x, a.post * acc.y);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.lnout) {
+    double l = 0.0;
+    for (int t = 0; t < 4; ++t)
+      if (a.lnin[t]) l += a.lc[t] * *a.lnin[t];
+    *a.lnout = a.post * l;
+  }
+}
+
+// calcat (mlegs_scalar_ops.f90:237-309): calc(k) = sum_n e(n, 1, k) * at(n); zeroat1 (:311-325)
+// additionally subtracts calc(k)/at1(1) from e(1, 1, k).  One warp per k.
+__global__ void k_calcat(double2* __restrict__ e, const double* __restrict__ at, int nmax, int nrdim, int npdim,
+                         int nzdim, double2* __restrict__ out, int zero_mode) {
+  int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int lane = threadIdx.x & 31;
+  if (k >= nzdim) return;
+  double2* col = e + (size_t)nrdim * npdim * k;
+  double sx = 0, sy = 0;
+  for (int n = lane; n < nmax; n += 32) { double2 v = col[n]; sx += v.x * at[n]; sy += v.y * at[n]; }
+  for (int o = 16; o; o >>= 1) { sx += __shfl_xor_sync(0xffffffffu, sx, o); sy += __shfl_xor_sync(0xffffffffu, sy, o); }
+  if (lane == 0) {
+    if (out) out[k] = make_double2(sx, sy);
+    if (zero_mode) { col[0].x -= sx / at[0]; col[0].y -= sy / at[0]; }
+  }
+}
+
+// vec2tp: psi%ln = -0.5 * Re(calcat1(up)(1)) (:1366-1367), from the calcat output of k = 1
+__global__ void k_set_ln_from_calc(double* __restrict__ lnp, const double2* __restrict__ calc, double f) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *lnp = f * calc[0].x;
+}
+// up(:nr,1,1) += psi%ln * (1 + x) (:1371-1373)
+__global__ void k_add_ln_x(double2* __restrict__ e, const double* __restrict__ lnp, const double* __restrict__ x, int nr) {
+  double l = *lnp;
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) e[i].x += l * (1.0 + x[i]);
+}
+
+// e(:nr, :, :) *= r  (mode 0) or /= r (mode 1)
+__global__ void k_scale_r(double2* __restrict__ e, const double* __restrict__ r, int nr, int nrdim, size_t ncol, int mode) {
+  size_t n = (size_t)nr * ncol;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nr);
+    size_t c = idx / nr;
+    double2* p = e + i + (size_t)nrdim * c;
+    double v = r[i];
+    if (mode == 0) { p->x *= v; p->y *= v; } else { p->x /= v; p->y /= v; }
+  }
+}
+
+// vecprod (mlegs_scalar_ops.f90:1264-1306) on the packed reals; everything else zero
+__global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, double2* __restrict__ vz,
+                          const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
+                          int nr, int nph, int nrdim, int npdim, int nzdim) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    double2 o1 = make_double2(0, 0), o2 = o1, o3 = o1;
+    if (i < nr && m < nph) {
+      double2 A1 = vr[idx], A2 = vp[idx], A3 = vz[idx], B1 = ur[idx], B2 = up[idx], B3 = uz[idx];
+      o1 = make_double2(A2.x * B3.x - A3.x * B2.x, A2.y * B3.y - A3.y * B2.y);
+      o2 = make_double2(A3.x * B1.x - A1.x * B3.x, A3.y * B1.y - A1.y * B3.y);
+      o3 = make_double2(A1.x * B2.x - A2.x * B1.x, A1.y * B2.y - A2.y * B1.y);
+    }
+    vr[idx] = o1; vp[idx] = o2; vz[idx] = o3;
+  }
+}
+
+// svv_filter (mlegs_scalar_ops.f90:72-155): block partial sums of |e|^2 and of the tail energy
+__device__ __forceinline__ double svv_q(int i, int m, int k, int nrchop, int np, double kmax, const double* ak, int nak) {
+  double q_r = fmin(1.0, (double)max(i, 0) / fmax((double)(nrchop - 1), 1.0));
+  double q_p = fmin(1.0, (double)abs(m) / fmax((double)(np / 2), 1.0));
+  int gk = k + 1;
+  double kv = (gk >= 1 && gk <= nak) ? fabs(ak[k]) : 0.0;
+  double q_z = fmin(1.0, kv / kmax);
+  return fmin(1.0, fmax(q_r, fmax(q_p, q_z)));
+}
+__global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
+                           const double* __restrict__ ak, double cutoff, double* __restrict__ partial) {
+  __shared__ double s0[256], s1[256];
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  double tot = 0, tail = 0;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    int k = (int)(idx / ((size_t)nrdim * npdim));
+    double2 v = e[idx];
+    double a = hypot(v.x, v.y);
+    double a2 = a * a;
+    tot += a2;
+    if (svv_q(i, m, k, nrchop, np, kmax, ak, nzdim) >= cutoff) tail += a2;
+  }
+  s0[threadIdx.x] = tot; s1[threadIdx.x] = tail;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if (threadIdx.x < o) { s0[threadIdx.x] += s0[threadIdx.x + o]; s1[threadIdx.x] += s1[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { partial[2 * blockIdx.x] = s0[0]; partial[2 * blockIdx.x + 1] = s1[0]; }
+}
+// gain relaxation and strength (:119-126); st[0] = strength (0: nothing to do)
+__global__ void k_svv_gain(const double* __restrict__ partial, int nb, double* __restrict__ gain, double* __restrict__ st,
+                           double target, double relax, double strength_max) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double tot = 0, tail = 0;
+  for (int b = 0; b < nb; ++b) { tot += partial[2 * b]; tail += partial[2 * b + 1]; }
+  st[0] = 0.0;
+  if (tot <= 2.2250738585072014e-308) return;
+  double ratio = tail / tot;
+  double fb = fmin(fmax(ratio / target - 1.0, 0.0), 1.0);
+  double rl = fmin(fmax(relax, 0.0), 1.0);
+  double g = (1.0 - rl) * (*gain) + rl * fb;
+  *gain = g;
+  st[0] = fmin(fmax(strength_max, 0.0) * g, 1.0);
+}
+__global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
+                            const double* __restrict__ ak, double cutoff, const double* __restrict__ st) {
+  double strength = st[0];
+  if (strength <= 0.0) return;
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    int k = (int)(idx / ((size_t)nrdim * npdim));
+    double q = svv_q(i, m, k, nrchop, np, kmax, ak, nzdim);
+    if (q > cutoff) {
+      double shape = (q - cutoff) / (1.0 - cutoff);
+      double s2 = shape * shape, s4 = s2 * s2;
+      double f = exp(-strength * (s4 * s4));
+      double2 v = e[idx];
+      e[idx] = make_double2(f * v.x, f * v.y);
+    }
+  }
+}
+
+// delsqp (:327-366) / idelsqp (:368-416), elementwise in place on the active rows of every k;
+// the ln-dependent entry (1,1,1) and the (1,1,:) reset are applied by the same thread.
+__global__ void k_delsqp(double2* __restrict__ e, const double* __restrict__ lnp, const double* __restrict__ lognorm,
+                         int inverse, int nrdim, int npdim, int nzdim, int nrc, int npc, double ell) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  double e2 = pow(ell, 2.0);
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    int nrcs = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
+    double2 v = e[idx];
+    if (i < nrcs) {
+      int in_ = m + i;
+      double dn = (double)in_;
+      if (!inverse) {
+        v.x = -v.x * dn * (dn + 1.0) / e2;
+        v.y = -v.y * dn * (dn + 1.0) / e2;
+      } else if (in_ == 0) {
+        v = make_double2(0, 0);
+      } else {
+        v.x = -v.x / (double)in_ / (in_ + 1.0) * e2;
+        v.y = -v.y / (double)in_ / (in_ + 1.0) * e2;
+      }
+    }
+    if (!inverse && idx == 0) v = make_double2(*lnp / e2 / exp(lognorm[0]), 0.0);
+    if (inverse && i == 0 && m == 0) v = make_double2(0, 0);
+    e[idx] = v;
+  }
+}
+__global__ void k_idelsqp_ln(const double2* __restrict__ e, double* __restrict__ lnp, const double* __restrict__ lognorm,
+                             double ell) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *lnp = e[0].x * pow(ell, 2.0) * exp(lognorm[0]);
+}
+__global__ void k_ln_zero(double* __restrict__ lnp) { if (threadIdx.x == 0) *lnp = 0.0; }
+__global__ void k_ln_set(double* __restrict__ lnp, double v) { if (threadIdx.x == 0) *lnp = v; }
+__global__ void k_ln_copy(double* __restrict__ d, const double* __restrict__ s) { if (threadIdx.x == 0) *d = *s; }
+
+__global__ void k_finite(const double2* __restrict__ a, const double2* __restrict__ b, size_t n, int* __restrict__ flag) {
+  GRID_STRIDE(idx, n) {
+    double2 u = a[idx], v = b[idx];
+    if (!isfinite(u.x) || !isfinite(u.y) || !isfinite(v.x) || !isfinite(v.y)) { atomicExch(flag, 1); }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// launch helpers
+int launch_zero(cd* e) { MLG_CUDA(cudaMemsetAsync(e, 0, G.fsize * sizeof(cd), G.stream)); return 0; }
+int launch_copy(cd* d, const cd* s) {
+  if (d != s) MLG_CUDA(cudaMemcpyAsync(d, s, G.fsize * sizeof(cd), cudaMemcpyDeviceToDevice, G.stream));
+  return 0;
+}
+int launch_copy_ln(double* d, const double* s) {
+  if (d != s) { k_ln_copy<<<1, 32, 0, G.stream>>>(d, s); MLG_LAUNCH(); }
+  return 0;
+}
+int launch_set_ln(double* d, double v) { k_ln_set<<<1, 32, 0, G.stream>>>(d, v); MLG_LAUNCH(); return 0; }
+
+int launch_ln_adjust(Scalar& s, double sign) {
+  size_t n = (size_t)G.nr * G.nzdim;
+  k_ln_adjust<<<nblk(n), 256, 0, G.stream>>>(s.e, s.ln, G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, sign);
+  MLG_LAUNCH();
+  return 0;
+}
+
+static int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+                   std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post = 1.0, bool do_ln = true) {
+  LinArgs a{};
+  a.out = out.e;
+  a.n = G.fsize;
+  a.post = post;
+  int t = 0;
+  for (auto& p : terms) { a.in[t] = p.first ? p.first->e : nullptr; a.c[t] = p.second; ++t; }
+  for (; t < 4; ++t) { a.in[t] = nullptr; a.c[t] = 0; }
+  t = 0;
+  a.lnout = do_ln ? out.ln : nullptr;
+  for (auto& p : lnterms) { a.lnin[t] = p.first ? p.first->ln : nullptr; a.lc[t] = p.second; ++t; }
+  for (; t < 4; ++t) { a.lnin[t] = nullptr; a.lc[t] = 0; }
+  k_lincomb<<<nblk(G.fsize), 256, 0, G.stream>>>(a);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// scalar bookkeeping
+static int alloc_slot() {
+  if (G.free_slots.empty()) return -1;
+  int s = G.free_slots.back();
+  G.free_slots.pop_back();
+  return s;
+}
+static void free_slot(int s) { if (s >= 0) G.free_slots.push_back(s); }
+
+static int scalar_init(Scalar& s) {   // scalar_init (mlegs_scalar_init.f90:6-67): space PPP
+  s.e = get_buf();
+  if (!s.e) return set_error(MLG_EALLOC, "scalar_init: out of device memory");
+  s.slot = alloc_slot();
+  if (s.slot < 0) { put_buf(s.e); s.e = nullptr; return set_error(MLG_ESIZE, "scalar_init: too many scalars"); }
+  s.ln = G.ln_slots + s.slot;
+  s.set_space("PPP");
+  s.off[0] = s.off[1] = s.off[2] = 0;
+  MLG_TRY(launch_set_ln(s.ln, 0.0));
+  return 0;
+}
+static void scalar_release(Scalar& s) {
+  put_buf(s.e);
+  s.e = nullptr;
+  free_slot(s.slot);
+  s.slot = -1;
+  s.ln = nullptr;
+}
+// scalar_copy (mlegs_scalar_init.f90:106-140)
+static int assign(Scalar& d, const Scalar& s) {
+  MLG_TRY(launch_copy(d.e, s.e));
+  MLG_TRY(launch_copy_ln(d.ln, s.ln));
+  std::memcpy(d.space, s.space, 4);
+  for (int i = 0; i < 3; ++i) d.off[i] = s.off[i];
+  return 0;
+}
+
+struct Tmp {
+  Scalar s;
+  int rc = 0;
+  Tmp() { rc = scalar_init(s); }
+  ~Tmp() { if (s.e) scalar_release(s); }
+};
+#define TMP(name) Tmp name##_t; if (name##_t.rc) return name##_t.rc; Scalar& name = name##_t.s
+
+// ------------------------------------------------------------------------------------------------
+// operators (mlegs_scalar_ops.f90)
+static int space_code(const char* sp) {
+  if (!std::strncmp(sp, "PPP", 3)) return 0;
+  if (!std::strncmp(sp, "PFP", 3)) return 1;
+  if (!std::strncmp(sp, "FFP", 3)) return 2;
+  if (!std::strncmp(sp, "FFF", 3)) return 3;
+  return -1;
+}
+
+static int vfft_checked(Scalar& s, int dir) {
+  int nzc = G.chopzl + s.off[2], nzcu = G.chopzu - s.off[2];
+  if (2 * s.off[2] > nzcu - nzc)
+    return set_error(MLG_ECHOP, dir < 0 ? "vertical_fft_forward: chopping in z too large" : "vertical_fft_backward: chopping in z too large");
+  return launch_vfft(s, dir);
+}
+
+// trans (:157-235)
+int op_trans(Scalar& s, const char* space) {
+  int cur = space_code(s.space);
+  if (cur < 0) return set_error(MLG_ESPACE, "trans: scalar space info corrupted (only accepting PPP, PFP, FFP and FFF)");
+  int nw = space_code(space);
+  if (nw < 0) return set_error(MLG_ESPACE, "trans: only taking PPP, PFP, FFP and FFF for spectral transformation");
+  if (cur < nw) {
+    while (true) {
+      if (cur == 0) { if (G.np > 1) MLG_TRY(launch_hfft(s, -1)); s.set_space("PFP"); }
+      if (cur == 1) { MLG_TRY(launch_ln_adjust(s, -1.0)); MLG_TRY(launch_rtrans_fwd(s)); s.set_space("FFP"); }
+      if (cur == 2) { if (G.nz > 1) MLG_TRY(vfft_checked(s, -1)); s.set_space("FFF"); }
+      if (cur == 3) break;
+      cur++;
+      if (cur == nw) break;
+    }
+  }
+  if (cur > nw) {
+    while (true) {
+      if (cur == 3) { if (G.nz > 1) MLG_TRY(vfft_checked(s, +1)); s.set_space("FFP"); }
+      if (cur == 2) { MLG_TRY(launch_rtrans_bwd(s, true)); s.set_space("PFP"); }
+      if (cur == 1) { if (G.np > 1) MLG_TRY(launch_hfft(s, +1)); s.set_space("PPP"); }
+      if (cur == 0) break;
+      cur--;
+      if (cur == nw) break;
+    }
+  }
+  return 0;
+}
+
+int op_chop(Scalar& s) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  k_mask<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F',
+                                              s.space[2] == 'F', c.nrc, c.npc, c.nzc, c.nzcu, 0, 0, 0, 0, 0);
+  MLG_LAUNCH();
+  return 0;
+}
+
+int op_dealias(Scalar& s) {
+  int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
+  k_mask<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F',
+                                              0, 0, 0, 0, pcut, zcut, zupper, G.np > 1, G.nz > 1);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// svv_filter with the gain kept in device memory (gain_dev)
+int op_svv_filter_dev(Scalar& s, double* gain_dev) {
+  if (!G.P.is_svv) return 0;
+  if (!s.is("FFF")) return set_error(MLG_ESPACE, "svv_filter: scalar must be in FFF space");
+  double cutoff = std::min(std::max(G.P.svv_cutoff, 0.0), 0.99);
+  double target = std::max(G.P.svv_target, 1.0e-12);
+  // kmax = max(maxval(abs(ak)), 1) over the kit's ak (mlegs_spectfm_init.f90:132-134)
+  double kmax = 0.0;
+  {
+    std::vector<double> ak(G.nz);
+    for (int i = -G.nz; i <= -1; ++i) ak[i + G.nz] = 2.0 * 3.14159265358979323846 / G.P.zlen * i;
+    for (int i = 0; i <= G.nz / 2; ++i) ak[i] = 2.0 * 3.14159265358979323846 / G.P.zlen * i;
+    for (double a : ak) kmax = std::max(kmax, std::fabs(a));
+    kmax = std::max(kmax, 1.0);
+  }
+  const int NB = 304;
+  double* partial = G.dscal + DS_CALC + 2 * 2048;
+  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff, partial);
+  MLG_LAUNCH();
+  k_svv_gain<<<1, 32, 0, G.stream>>>(partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength);
+  MLG_LAUNCH();
+  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff,
+                                                    G.dscal + DS_SUM0);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// calcat0/1 into dscal[DS_CALC..] (device), optionally zeroat1
+static int calcat_dev(Scalar& s, const double* at, bool zero_mode) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
+  k_calcat<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, at, nmax, G.nrdim, G.npdim, G.nzdim,
+                                                    (double2*)(G.dscal + DS_CALC), zero_mode ? 1 : 0);
+  MLG_LAUNCH();
+  return 0;
+}
+
+int op_calcat(Scalar& s, int which, double* host_out) {
+  if (!s.is("FFF")) {
+    TMP(st);
+    MLG_TRY(assign(st, s));
+    MLG_TRY(op_trans(st, "FFF"));
+    MLG_TRY(calcat_dev(st, which ? G.at1 : G.at0, false));
+  } else {
+    MLG_TRY(calcat_dev(s, which ? G.at1 : G.at0, false));
+  }
+  if (host_out) {
+    MLG_CUDA(cudaMemcpyAsync(host_out, G.dscal + DS_CALC, 2 * G.nz * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+    MLG_CUDA(cudaStreamSynchronize(G.stream));
+  }
+  return 0;
+}
+
+int op_zeroat1(Scalar& s) {
+  if (!s.is("FFF")) MLG_TRY(op_trans(s, "FFF"));
+  return calcat_dev(s, G.at1, true);
+}
+
+static int require_fff(Scalar& s) {
+  if (!s.is("FFF")) MLG_TRY(op_trans(s, "FFF"));
+  return 0;
+}
+
+int op_delsqp(Scalar& s, bool inverse) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  if (inverse) { k_idelsqp_ln<<<1, 32, 0, G.stream>>>(s.e, s.ln, G.lognorm, G.ell); MLG_LAUNCH(); }
+  k_delsqp<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, s.ln, G.lognorm, inverse ? 1 : 0, G.nrdim, G.npdim, G.nzdim, c.nrc,
+                                                c.npc, G.ell);
+  MLG_LAUNCH();
+  if (!inverse) { k_ln_zero<<<1, 32, 0, G.stream>>>(s.ln); MLG_LAUNCH(); }
+  return 0;
+}
+
+int op_band(Scalar& s, int op) {   // xxdx (op 0), del2h (1), del2 (2)
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  return launch_band_apply(s, op, c);
+}
+
+int op_idel2(Scalar& s, bool pre, double preln) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  return launch_band_solve(s, pre ? 2 : 1, c, 0.0, 0.0, preln, 0);
+}
+
+int op_ihelm(Scalar& s, double alpha) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  if (std::fabs(alpha) < 5.0e-14)
+    return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
+  return launch_band_solve(s, 0, c, alpha, 0.0, 0.0, 0);
+}
+
+// helm (:762-789): the reference forms del2(s)+alpha*s in a temporary and never assigns it back,
+// so the call leaves s unchanged (it only moves s to FFF first).
+int op_helm(Scalar& s, double alpha) {
+  (void)alpha;
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  return require_fff(s);
+}
+
+int op_helmp(Scalar& s, int power, double alpha, double beta) {
+  if (!(power % 2 == 0 && power >= 4)) return set_error(MLG_EPOWER, "helmp: even power greater than or equal to 4");
+  if (power > 8) return set_error(MLG_EPOWER, "helmp: power must be less than or equal to 8 (supported power = 4, 6 or 8)");
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  TMP(s2);
+  MLG_TRY(assign(s2, s));
+  MLG_TRY(op_band(s2, 2));
+  TMP(sp);
+  MLG_TRY(assign(sp, s2));
+  for (int n = 1; n <= power / 2 - 1; ++n) MLG_TRY(op_band(sp, 2));
+  // so%e = sp%e + beta*s2%e + alpha*s%e; so%ln = alpha*s%ln
+  MLG_TRY(lincomb(s, {{&sp, 1.0}, {&s2, beta}, {&s, alpha}}, {{&s, alpha}}));
+  return 0;
+}
+
+int op_ihelmp(Scalar& s, int power, double alpha, double beta) {
+  if (!(power % 2 == 0 && power >= 4)) return set_error(MLG_EPOWER, "ihelmp: even power greater than or equal to 4");
+  if (power > 8) return set_error(MLG_EPOWER, "ihelmp: power must be less than or equal to 8 (supported power = 4, 6 or 8)");
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(require_fff(s));
+  if (std::fabs(alpha) < 5.0e-14)
+    return set_error(MLG_EALPHA, "ihelmp: alpha equals to zero. Inversion of 0*identity is impossible");
+  MLG_TRY(launch_ihelmp_pre(s, c, power, alpha, beta));
+  return launch_band_solve(s, 3, c, alpha, beta, 0.0, power);
+}
+
+// ------------------------------------------------------------------------------------------------
+// time steppers (:1065-1262)
+static double hsign() { return (((G.P.hyperpow / 2 + 1) % 2) == 0) ? 1.0 : -1.0; }
+
+static int lterm(Scalar& svis) {   // svis <- visc*del2(svis) / hyperviscous operator; ln as the reference
+  if (G.P.hyperpow == 0) {
+    if (G.P.visc < 5.0e-14) { MLG_TRY(launch_zero(svis.e)); }
+    else {
+      MLG_TRY(op_band(svis, 2));
+      MLG_TRY(lincomb(svis, {{&svis, G.P.visc}}, {}, 1.0, false));
+    }
+  } else {
+    double hv = G.P.hypervisc * hsign();
+    MLG_TRY(op_helmp(svis, G.P.hyperpow, 0.0, G.P.visc / hv));
+    MLG_TRY(lincomb(svis, {{&svis, hv}}, {}, 1.0, false));
+  }
+  return 0;
+}
+
+static bool fff4(const Scalar& a, const Scalar& b) { return a.is("FFF") && b.is("FFF"); }
+
+int op_fefe(Scalar& s, const Scalar& nl, double dt) {
+  if (!fff4(s, nl)) return set_error(MLG_ESPACE, "fefe: all input scalars must be in FFF for time stepping");
+  TMP(svis);
+  MLG_TRY(assign(svis, s));
+  MLG_TRY(lterm(svis));
+  MLG_TRY(lincomb(s, {{&s, 1.0}, {&nl, dt}, {&svis, dt}}, {{&s, 1.0}, {&nl, dt}, {&svis, dt}}));
+  return 0;
+}
+
+int op_abab(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, double dt, bool is2nd) {
+  if (!fff4(s, nl) || !fff4(s_p, nl_p)) return set_error(MLG_ESPACE, "fefe: all input scalars must be in FFF for time stepping");
+  TMP(svis);
+  MLG_TRY(assign(svis, s));
+  MLG_TRY(lterm(svis));
+  TMP(svis_p);
+  MLG_TRY(assign(svis_p, s_p));
+  if (!is2nd) {
+    if (G.P.hyperpow == 0) {
+      if (G.P.visc < 5.0e-14) { MLG_TRY(launch_zero(svis.e)); }   // (:1135) zeroes svis, not svis_p
+      else { MLG_TRY(op_band(svis_p, 2)); MLG_TRY(lincomb(svis_p, {{&svis_p, G.P.visc}}, {}, 1.0, false)); }
+    } else {
+      double hv = G.P.hypervisc * hsign();
+      MLG_TRY(op_helmp(svis_p, G.P.hyperpow, 0.0, G.P.visc / hv));
+      MLG_TRY(lincomb(svis_p, {{&svis_p, hv}}, {}, 1.0, false));
+    }
+  }
+  // s = s + dt*(1.5*(nl + svis) - .5*(nl_p + svis_p)), in two passes (four-input combination)
+  TMP(acc);
+  MLG_TRY(lincomb(acc, {{&nl, 1.5 * dt}, {&svis, 1.5 * dt}, {&nl_p, -.5 * dt}, {&svis_p, -.5 * dt}},
+                  {{&nl, 1.5 * dt}, {&svis, 1.5 * dt}, {&nl_p, -.5 * dt}, {&svis_p, -.5 * dt}}));
+  MLG_TRY(lincomb(s, {{&s, 1.0}, {&acc, 1.0}}, {{&s, 1.0}, {&acc, 1.0}}));
+  MLG_TRY(assign(s_p, s));
+  MLG_TRY(assign(nl_p, nl));
+  return 0;
+}
+
+int op_febe(Scalar& s, const Scalar& nl, double dt) {
+  if (!fff4(s, nl)) return set_error(MLG_ESPACE, "fefe: all input scalars must be in FFF for time stepping");
+  if (G.P.hyperpow == 0) {
+    if (G.P.visc < 5.0e-14) return set_error(MLG_EINVISCID, "febe: inviscid case and no linear term in rhs. semi-implicit time adv is impossible");
+    double a = -1.0 / (dt * G.P.visc);
+    // sh = a*(s + dt*nl) (both e and ln), then ihelm(sh, a); s = sh
+    MLG_TRY(lincomb(s, {{&s, 1.0}, {&nl, dt}}, {{&s, 1.0}, {&nl, dt}}, a));
+    MLG_TRY(op_ihelm(s, a));
+  } else {
+    double hv = G.P.hypervisc * hsign();
+    double a = -1.0 / (dt * hv), b = G.P.visc / hv;
+    MLG_TRY(lincomb(s, {{&s, 1.0}, {&nl, dt}}, {{&s, 1.0}, {&nl, dt}}, a));
+    MLG_TRY(op_ihelmp(s, G.P.hyperpow, a, b));
+  }
+  return 0;
+}
+
+int op_abcn(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, double dt) {
+  if (!fff4(s, nl) || !fff4(s_p, nl_p)) return set_error(MLG_ESPACE, "fefe: all input scalars must be in FFF for time stepping");
+  if (G.P.hyperpow == 0 && G.P.visc < 5.0e-14)
+    return set_error(MLG_EINVISCID, "abcn: inviscid case and no linear term in rhs. semi-implicit time adv is impossible");
+  TMP(svis);
+  MLG_TRY(assign(svis, s));
+  MLG_TRY(lterm(svis));
+  double a;
+  if (G.P.hyperpow == 0) a = -2.0 / (dt * G.P.visc);
+  else a = -2.0 / (dt * (G.P.hypervisc * hsign()));
+  // sh = s + dt*(1.5 nl - .5 nl_p); sh = a*(sh + dt/2*svis)
+  MLG_TRY(lincomb(s, {{&s, 1.0}, {&nl, 1.5 * dt}, {&nl_p, -.5 * dt}, {&svis, dt / 2.0}},
+                  {{&s, 1.0}, {&nl, 1.5 * dt}, {&nl_p, -.5 * dt}, {&svis, dt / 2.0}}, a));
+  if (G.P.hyperpow == 0) MLG_TRY(op_ihelm(s, a));
+  else MLG_TRY(op_ihelmp(s, G.P.hyperpow, a, G.P.visc / (G.P.hypervisc * hsign())));
+  MLG_TRY(assign(s_p, s));
+  MLG_TRY(assign(nl_p, nl));
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// vector fields (:1264-1560)
+int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
+  for (const Scalar* q : {(const Scalar*)&vr, (const Scalar*)&vp, (const Scalar*)&vz, &ur, &up, &uz})
+    if (!q->is("PPP")) return set_error(MLG_ESPACE, "vector_product: to compute v x u, all inputs must be in PPP");
+  k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
+  MLG_LAUNCH();
+  for (Scalar* q : {&vr, &vp, &vz}) { MLG_TRY(launch_set_ln(q->ln, 0.0)); q->off[0] = q->off[1] = q->off[2] = 0; }
+  return 0;
+}
+
+static int scale_r(Scalar& s, int mode) {
+  size_t ncol = (size_t)G.npdim * G.nzdim;
+  k_scale_r<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, G.r, G.nr, G.nrdim, ncol, mode);
+  MLG_LAUNCH();
+  return 0;
+}
+
+int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi) {
+  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
+  if (!psi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
+  if (!chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: chi must be in FFF");
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(assign(ur, vr)); MLG_TRY(assign(up, vp)); MLG_TRY(assign(uz, vz));
+  MLG_TRY(scale_r(ur, 0)); MLG_TRY(scale_r(up, 0));
+  MLG_TRY(op_trans(ur, "PFP"));
+  if (G.nz > 1) MLG_TRY(vfft_checked(ur, -1));
+  ur.set_space("PFF");
+  MLG_TRY(op_trans(up, "FFF"));
+  MLG_TRY(calcat_dev(up, G.at1, false));
+  k_set_ln_from_calc<<<1, 32, 0, G.stream>>>(psi.ln, (const double2*)(G.dscal + DS_CALC), -1.0 / 2.0);
+  MLG_LAUNCH();
+  MLG_TRY(launch_rtrans_bwd(up, false));
+  up.set_space("PFF");
+  k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
+  MLG_LAUNCH();
+  MLG_TRY(op_trans(uz, "PFP"));
+  if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
+  uz.set_space("PFF");
+  // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331); psi%ln was set above from calcat1
+  MLG_TRY(launch_zero(psi.e));
+  MLG_TRY(launch_zero(chi.e));
+  MLG_TRY(launch_set_ln(chi.ln, 0.0));
+  MLG_TRY(launch_vec2tp_contract(ur.e, up.e, uz.e, psi.e, chi.e, 3));
+  MLG_TRY(op_idel2(chi, false, 0.0));
+  psi.off[0] = psi.off[1] = psi.off[2] = 0;
+  chi.off[0] = chi.off[1] = chi.off[2] = 0;
+  MLG_TRY(op_chop(psi)); MLG_TRY(op_chop(chi));
+  MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
+  return 0;
+}
+
+// combination step of vector_reconstruction (:1488-1502)
+__global__ void k_tp2vec_mix(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
+                             const double2* __restrict__ uz, const double* __restrict__ ak, int nrdim, int npdim, int nzdim,
+                             int nrc, int npc, int nzc, int nzcu) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % nrdim);
+    int m = (int)((idx / nrdim) % npdim);
+    int k = (int)(idx / ((size_t)nrdim * npdim));
+    if (m >= npc) continue;
+    int nn = max(min(nrc, nrc - m), 0);
+    int kk = k + 1;
+    if (i >= nn || !(kk <= nzc || kk >= nzcu)) continue;
+    double kv = ak[k], mv = (double)m;
+    double2 p = psi[idx], a = ur[idx], b = up[idx], c = uz[idx];
+    // ur = i*mv*psi + i*kv*ur; up = -up - mv*kv*uz
+    ur[idx] = make_double2(-mv * p.y - kv * a.y, mv * p.x + kv * a.x);
+    up[idx] = make_double2(-b.x - mv * kv * c.x, -b.y - mv * kv * c.y);
+  }
+}
+
+int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scalar& vz) {
+  if (!psi.is("FFF") || !chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
+  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(assign(ur, chi)); ur.off[0] = 3; ur.off[1] = ur.off[2] = 0;
+  MLG_TRY(assign(up, psi)); up.off[0] = 3; up.off[1] = up.off[2] = 0;
+  MLG_TRY(assign(uz, chi)); uz.off[0] = 3; uz.off[1] = uz.off[2] = 0;
+  ChopIdx c;
+  MLG_TRY(chop_index(ur, c));
+  MLG_TRY(op_band(ur, 0));
+  MLG_TRY(op_band(up, 0));
+  k_tp2vec_mix<<<nblk(G.fsize), 256, 0, G.stream>>>(ur.e, up.e, psi.e, uz.e, G.ak, G.nrdim, G.npdim, G.nzdim, c.nrc, c.npc,
+                                                     c.nzc, c.nzcu);
+  MLG_LAUNCH();
+  ur.off[0] = 0; up.off[0] = 0;
+  MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
+  MLG_TRY(op_trans(ur, "PPP")); MLG_TRY(op_trans(up, "PPP"));
+  MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
+  MLG_TRY(op_band(uz, 1));
+  MLG_TRY(lincomb(uz, {{&uz, -1.0}}, {}, 1.0, false));
+  uz.off[0] = 0;
+  MLG_TRY(op_chop(uz));
+  MLG_TRY(op_trans(uz, "PPP"));
+  MLG_TRY(assign(vr, ur)); MLG_TRY(assign(vp, up)); MLG_TRY(assign(vz, uz));
+  return 0;
+}
+
+int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, Scalar& wz) {
+  TMP(md);
+  MLG_TRY(assign(md, chi));
+  md.set_space("FFF");
+  MLG_TRY(op_band(md, 2));
+  MLG_TRY(lincomb(md, {{&md, -1.0}}, {}, 1.0, false));
+  return op_tp2vec(md, psi, wr, wp, wz);
+}
+
+// advection_rhs (vortical_flow_3d.f90:353-395)
+int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz) {
+  if (!psi.is("FFF") || !chi.is("FFF") || !nlpsi.is("FFF") || !nlchi.is("FFF") || !uz.is("PPP"))
+    return set_error(MLG_ESPACE, "advection_rhs: psi, chi, nlpsi, nlchi must be in FFF and uz in PPP");
+  MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
+  TMP(vr); TMP(vp); TMP(vz); TMP(wr); TMP(wp); TMP(wz);
+  MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
+  MLG_TRY(lincomb(vz, {{&vz, 1.0}, {&uz, 1.0}}, {}, 1.0, false));
+  MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
+  MLG_TRY(op_vecprod(vr, vp, vz, wr, wp, wz));
+  MLG_TRY(op_vec2tp(vr, vp, vz, nlpsi, nlchi));
+  MLG_TRY(launch_set_ln(nlpsi.ln, 0.0)); MLG_TRY(launch_set_ln(nlchi.ln, 0.0));
+  MLG_TRY(op_dealias(nlpsi)); MLG_TRY(op_dealias(nlchi));
+  return 0;
+}
+
+// main-loop step (vortical_flow_3d.f90:168-180) with the gains in device memory
+int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev) {
+  for (Scalar* q : {&psi, &chi, &nlpsi, &nlchi, &psip, &chip, &nlpsip, &nlchip}) MLG_TRY(op_trans(*q, "FFF"));
+  MLG_TRY(op_abcn(psi, psip, nlpsi, nlpsip, dt));
+  MLG_TRY(op_abcn(chi, chip, nlchi, nlchip, dt));
+  MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
+  MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
+  MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
+  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz));
+  k_finite<<<nblk(G.fsize), 256, 0, G.stream>>>(psi.e, chi.e, G.fsize, (int*)(G.dscal + DS_FLAG));
+  MLG_LAUNCH();
+  return 0;
+}
+
+}  // namespace mlg
+
+// =================================================================================================
+// C ABI
+using namespace mlg;
+
+static int need_kit() { return G.kit_set ? 0 : set_error(MLG_ENOKIT, "transformation kit is not initialized"); }
+#define NEED_KIT() MLG_TRY(need_kit())
+#define SC(p) if (!(p) || !(p)->e) return set_error(MLG_EHANDLE, "invalid scalar handle")
+static Scalar* S(mlg_scalar h) { return reinterpret_cast<Scalar*>(h); }
+
+extern "C" {
+
+void mlg_params_default(mlg_params* p) {
+  p->nr = 256; p->np = 128; p->nz = 128; p->nrchop = 256; p->npchop = 65; p->nzchop = 65;
+  p->ell = 4.0; p->zlen = 2.0 * 3.14159265358979323846; p->visc = 1.0e-3; p->hyperpow = 0; p->hypervisc = 0.0;
+  p->is_svv = 1; p->svv_cutoff = 0.75; p->svv_target = 2.0e-2; p->svv_strength = 0.12; p->svv_relax = 0.25;
+}
+
+const char* mlg_last_error(void) { return g_err.c_str(); }
+
+int mlg_init(const mlg_params* p) {
+  if (!p) return set_error(MLG_EHANDLE, "mlg_init: null parameters");
+  if (!G.ev0) { cudaEventCreate(&G.ev0); cudaEventCreate(&G.ev1); }
+  int rc = kit_build(p);
+  if (rc) return rc;
+  G.n_slots = 4096;
+  MLG_TRY(dmalloc((void**)&G.ln_slots, G.n_slots * sizeof(double)));
+  MLG_CUDA(cudaMemset(G.ln_slots, 0, G.n_slots * sizeof(double)));
+  G.free_slots.clear();
+  for (int i = G.n_slots - 1; i >= 0; --i) G.free_slots.push_back(i);
+  return 0;
+}
+
+int mlg_finalize(void) {
+  if (!G.kit_set) return 0;
+  cudaStreamSynchronize(G.stream);
+  for (cd* b : G.all_bufs) cudaFree(b);
+  void* arrs[] = {G.x, G.w, G.r, G.lnx, G.ak, G.lognorm, G.pf, G.pf32, G.at0, G.at1, G.bd2, G.bxx, G.tV, G.tD, G.tT,
+                  G.tV32, G.tD32, G.tT32, G.tw_p, G.tw_z, G.tw_pr, G.ln_slots, G.dscal, G.band_ws};
+  for (void* a : arrs) if (a) cudaFree(a);
+  cudaStream_t st = G.stream;
+  cudaEvent_t e0 = G.ev0, e1 = G.ev1;
+  G = Ctx();
+  G.stream = st;
+  G.ev0 = e0; G.ev1 = e1;
+  return 0;
+}
+
+int mlg_kit_dims(int* d) {
+  NEED_KIT();
+  d[0] = G.nrdim; d[1] = G.npdim; d[2] = G.nzdim; d[3] = G.chopzl; d[4] = G.chopzu; d[5] = G.nrh; d[6] = G.ne;
+  d[7] = G.npchop; d[8] = G.nr;
+  return 0;
+}
+
+int mlg_kit_get(const char* name, double* out, long long count) {
+  NEED_KIT();
+  std::string n(name ? name : "");
+  const double* src = nullptr;
+  long long cnt = 0;
+  if (n == "x") { src = G.x; cnt = G.nr; } else if (n == "w") { src = G.w; cnt = G.nr; }
+  else if (n == "r") { src = G.r; cnt = G.nr; } else if (n == "ln") { src = G.lnx; cnt = G.nr; }
+  else if (n == "ak") { src = G.ak; cnt = G.nz; }
+  else if (n == "lognorm") { src = G.lognorm; cnt = (long long)G.ne * G.npchop; }
+  else if (n == "pf") { src = G.pf; cnt = (long long)G.nrh * G.ne * G.npchop; }
+  else if (n == "at0") { src = G.at0; cnt = G.nrchop; } else if (n == "at1") { src = G.at1; cnt = G.nrchop; }
+  if (!src) return set_error(MLG_EHANDLE, "mlg_kit_get: unknown array name");
+  if (count < cnt) return set_error(MLG_ESIZE, "mlg_kit_get: output buffer too small");
+  MLG_CUDA(cudaMemcpyAsync(out, src, cnt * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  return 0;
+}
+
+int mlg_set_precision(int mode) {
+  if (mode != MLG_PLAIN_FP64 && mode != MLG_MIXED) return set_error(MLG_EPARAM, "mlg_set_precision: unknown mode");
+  G.precision = mode;
+  return 0;
+}
+int mlg_get_precision(int* mode) { *mode = G.precision; return 0; }
+int mlg_set_stream(void* stream) { G.stream = (cudaStream_t)stream; return 0; }
+int mlg_sync(void) {
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  if (G.kit_set) {
+    int flags[2] = {0, 0};
+    MLG_CUDA(cudaMemcpy(flags, G.dscal + DS_FLAG, sizeof(double), cudaMemcpyDeviceToHost));
+    int sing = 0;
+    MLG_CUDA(cudaMemcpy(&sing, (int*)(G.dscal + DS_FLAG + 1), sizeof(int), cudaMemcpyDeviceToHost));
+    if (sing) {
+      cudaMemset(G.dscal + DS_FLAG + 1, 0, sizeof(double));
+      return set_error(MLG_ESINGULAR, "lurc: lu factorization resulted in failure");
+    }
+  }
+  return 0;
+}
+long long mlg_mem_bytes(void) { return G.mem_bytes; }
+long long mlg_mem_high_water(void) { return G.mem_high; }
+
+int mlg_scalar_alloc(mlg_scalar* out) {
+  NEED_KIT();
+  Scalar* s = new Scalar;
+  int rc = scalar_init(*s);
+  if (rc) { delete s; return rc; }
+  MLG_CUDA(cudaMemsetAsync(s->e, 0, G.fsize * sizeof(cd), G.stream));
+  *out = reinterpret_cast<mlg_scalar>(s);
+  return 0;
+}
+int mlg_scalar_free(mlg_scalar h) {
+  Scalar* s = S(h);
+  if (!s) return 0;
+  if (G.kit_set && s->e) scalar_release(*s);
+  delete s;
+  return 0;
+}
+static int set_space_checked(Scalar& s, const char* sp) {
+  if (!sp || space_code(sp) < 0) return set_error(MLG_ESPACE, "space must be PPP, PFP, FFP or FFF");
+  s.set_space(sp);
+  return 0;
+}
+int mlg_scalar_upload(mlg_scalar h, const double* e, double ln, const char* space) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  MLG_TRY(set_space_checked(*s, space));
+  MLG_CUDA(cudaMemcpyAsync(s->e, e, G.fsize * sizeof(cd), cudaMemcpyHostToDevice, G.stream));
+  MLG_TRY(launch_set_ln(s->ln, ln));
+  return 0;
+}
+int mlg_scalar_upload_device(mlg_scalar h, const void* e, double ln, const char* space) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  MLG_TRY(set_space_checked(*s, space));
+  MLG_CUDA(cudaMemcpyAsync(s->e, e, G.fsize * sizeof(cd), cudaMemcpyDeviceToDevice, G.stream));
+  MLG_TRY(launch_set_ln(s->ln, ln));
+  return 0;
+}
+int mlg_scalar_download(mlg_scalar h, double* e, double* ln, char* space4) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  if (e) MLG_CUDA(cudaMemcpyAsync(e, s->e, G.fsize * sizeof(cd), cudaMemcpyDeviceToHost, G.stream));
+  if (ln) MLG_CUDA(cudaMemcpyAsync(ln, s->ln, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  if (space4) { std::memcpy(space4, s->space, 4); }
+  return 0;
+}
+int mlg_scalar_download_device(mlg_scalar h, void* e, double* ln, char* space4) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  if (e) MLG_CUDA(cudaMemcpyAsync(e, s->e, G.fsize * sizeof(cd), cudaMemcpyDeviceToDevice, G.stream));
+  if (ln) {
+    MLG_CUDA(cudaMemcpyAsync(ln, s->ln, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+    MLG_CUDA(cudaStreamSynchronize(G.stream));
+  }
+  if (space4) { std::memcpy(space4, s->space, 4); }
+  return 0;
+}
+int mlg_scalar_copy(mlg_scalar d, mlg_scalar s) {
+  NEED_KIT(); SC(S(d)); SC(S(s));
+  return assign(*S(d), *S(s));
+}
+int mlg_scalar_chop_offset(mlg_scalar h, int a, int b, int c) {
+  Scalar* s = S(h); SC(s);
+  s->off[0] = a; s->off[1] = b; s->off[2] = c;
+  return 0;
+}
+int mlg_scalar_get_meta(mlg_scalar h, double* ln, char* space4, int* offs) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  if (ln) {
+    MLG_CUDA(cudaMemcpyAsync(ln, s->ln, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+    MLG_CUDA(cudaStreamSynchronize(G.stream));
+  }
+  if (space4) std::memcpy(space4, s->space, 4);
+  if (offs) for (int i = 0; i < 3; ++i) offs[i] = s->off[i];
+  return 0;
+}
+int mlg_scalar_set_ln(mlg_scalar h, double ln) { NEED_KIT(); Scalar* s = S(h); SC(s); return launch_set_ln(s->ln, ln); }
+int mlg_scalar_set_space(mlg_scalar h, const char* sp) { Scalar* s = S(h); SC(s); return set_space_checked(*s, sp); }
+int mlg_scalar_axpby(mlg_scalar d, double a, mlg_scalar x, double b, mlg_scalar y) {
+  NEED_KIT(); SC(S(d)); SC(S(x));
+  if (y) { SC(S(y)); return lincomb(*S(d), {{S(x), a}, {S(y), b}}, {}, 1.0, false); }
+  return lincomb(*S(d), {{S(x), a}}, {}, 1.0, false);
+}
+void* mlg_scalar_device_ptr(mlg_scalar h) { Scalar* s = S(h); return s ? (void*)s->e : nullptr; }
+
+#define OP1(name, call) int name(mlg_scalar h) { NEED_KIT(); Scalar* s = S(h); SC(s); return call; }
+OP1(mlg_chop, op_chop(*s))
+OP1(mlg_dealias, op_dealias(*s))
+OP1(mlg_zeroat1, op_zeroat1(*s))
+OP1(mlg_delsqp, op_delsqp(*s, false))
+OP1(mlg_idelsqp, op_delsqp(*s, true))
+OP1(mlg_xxdx, op_band(*s, 0))
+OP1(mlg_del2h, op_band(*s, 1))
+OP1(mlg_del2, op_band(*s, 2))
+OP1(mlg_idel2_proln, op_idel2(*s, false, 0.0))
+
+int mlg_trans(mlg_scalar h, const char* space) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_trans(*s, space ? space : ""); }
+int mlg_svv_filter(mlg_scalar h, double* gain) {
+  NEED_KIT(); Scalar* s = S(h); SC(s);
+  if (!gain) return set_error(MLG_EHANDLE, "svv_filter: null gain");
+  double* gd = G.dscal + DS_GAIN0 + 2;
+  MLG_CUDA(cudaMemcpyAsync(gd, gain, sizeof(double), cudaMemcpyHostToDevice, G.stream));
+  MLG_TRY(op_svv_filter_dev(*s, gd));
+  MLG_CUDA(cudaMemcpyAsync(gain, gd, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  return 0;
+}
+int mlg_calcat0(mlg_scalar h, double* out) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_calcat(*s, 0, out); }
+int mlg_calcat1(mlg_scalar h, double* out) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_calcat(*s, 1, out); }
+int mlg_idel2_preln(mlg_scalar h, double preln) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_idel2(*s, true, preln); }
+int mlg_helm(mlg_scalar h, double a) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_helm(*s, a); }
+int mlg_ihelm(mlg_scalar h, double a) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_ihelm(*s, a); }
+int mlg_helmp(mlg_scalar h, int p, double a, double b) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_helmp(*s, p, a, b); }
+int mlg_ihelmp(mlg_scalar h, int p, double a, double b) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_ihelmp(*s, p, a, b); }
+
+int mlg_fefe(mlg_scalar h, mlg_scalar nl, double dt) { NEED_KIT(); SC(S(h)); SC(S(nl)); return op_fefe(*S(h), *S(nl), dt); }
+int mlg_febe(mlg_scalar h, mlg_scalar nl, double dt) { NEED_KIT(); SC(S(h)); SC(S(nl)); return op_febe(*S(h), *S(nl), dt); }
+int mlg_abab(mlg_scalar h, mlg_scalar hp, mlg_scalar nl, mlg_scalar nlp, double dt, int is2nd) {
+  NEED_KIT(); SC(S(h)); SC(S(hp)); SC(S(nl)); SC(S(nlp));
+  return op_abab(*S(h), *S(hp), *S(nl), *S(nlp), dt, is2nd != 0);
+}
+int mlg_abcn(mlg_scalar h, mlg_scalar hp, mlg_scalar nl, mlg_scalar nlp, double dt) {
+  NEED_KIT(); SC(S(h)); SC(S(hp)); SC(S(nl)); SC(S(nlp));
+  return op_abcn(*S(h), *S(hp), *S(nl), *S(nlp), dt);
+}
+int mlg_vecprod(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f) {
+  NEED_KIT(); SC(S(a)); SC(S(b)); SC(S(c)); SC(S(d)); SC(S(e)); SC(S(f));
+  return op_vecprod(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f));
+}
+int mlg_vec2tp(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e) {
+  NEED_KIT(); SC(S(a)); SC(S(b)); SC(S(c)); SC(S(d)); SC(S(e));
+  return op_vec2tp(*S(a), *S(b), *S(c), *S(d), *S(e));
+}
+int mlg_tp2vec(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e) {
+  NEED_KIT(); SC(S(a)); SC(S(b)); SC(S(c)); SC(S(d)); SC(S(e));
+  return op_tp2vec(*S(a), *S(b), *S(c), *S(d), *S(e));
+}
+int mlg_tp2curlvec(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e) {
+  NEED_KIT(); SC(S(a)); SC(S(b)); SC(S(c)); SC(S(d)); SC(S(e));
+  return op_tp2curlvec(*S(a), *S(b), *S(c), *S(d), *S(e));
+}
+int mlg_advection_rhs(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e) {
+  NEED_KIT(); SC(S(a)); SC(S(b)); SC(S(c)); SC(S(d)); SC(S(e));
+  return op_advection_rhs(*S(a), *S(b), *S(c), *S(d), *S(e));
+}
+
+static int vortex_loop(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f, mlg_scalar g,
+                       mlg_scalar h, mlg_scalar u, double dt, int nsteps, double* gains) {
+  NEED_KIT();
+  for (mlg_scalar q : {a, b, c, d, e, f, g, h, u}) SC(S(q));
+  if (!gains) return set_error(MLG_EHANDLE, "vortex step: null gains");
+  double* gd = G.dscal + DS_GAIN0;
+  MLG_CUDA(cudaMemcpyAsync(gd, gains, 2 * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+  MLG_CUDA(cudaMemsetAsync(G.dscal + DS_FLAG, 0, sizeof(double), G.stream));
+  for (int t = 0; t < nsteps; ++t)
+    MLG_TRY(op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd));
+  MLG_CUDA(cudaMemcpyAsync(gains, gd, 2 * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  int flag = 0;
+  MLG_CUDA(cudaMemcpyAsync(&flag, G.dscal + DS_FLAG, sizeof(int), cudaMemcpyDeviceToHost, G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  if (flag) return set_error(MLG_ENONFINITE, "ERROR: non-finite vortex state");
+  return 0;
+}
+int mlg_vortex_step(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f, mlg_scalar g,
+                    mlg_scalar h, mlg_scalar u, double dt, double* gains) {
+  return vortex_loop(a, b, c, d, e, f, g, h, u, dt, 1, gains);
+}
+int mlg_vortex_run(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f, mlg_scalar g,
+                   mlg_scalar h, mlg_scalar u, double dt, int nsteps, double* gains) {
+  return vortex_loop(a, b, c, d, e, f, g, h, u, dt, nsteps, gains);
+}
+
+int mlg_kernel_timing(int enable) {
+  G.kt.on = enable != 0;
+  for (int i = 0; i < 3; ++i) { G.kt.ms[i] = 0; G.kt.n[i] = 0; G.kt.work[i] = 0; }
+  return 0;
+}
+int mlg_kernel_timing_read(int kind, double* ms, long long* n, double* work) {
+  if (kind < 0 || kind > 2) return set_error(MLG_EPARAM, "mlg_kernel_timing_read: kind 0..2");
+  if (ms) *ms = G.kt.ms[kind];
+  if (n) *n = G.kt.n[kind];
+  if (work) *work = G.kt.work[kind];
+  return 0;
+}
+
+}  // extern "C"

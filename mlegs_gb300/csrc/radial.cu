@@ -1,0 +1,370 @@
+// radial.cu — the mapped-Legendre radial transforms as ragged batches of dense contractions, one
+// group per azimuthal mode m:
+//   forward  (rtrans_forward, mlegs_scalar_ops.f90:1852-1927)
+//     c(j, m, z) = sum_{i<nr/2} pf(i, j, m) * (f(i) +- f(nr-1-i)) * w(i),  j < nn(m) = nrc - m,
+//     '+' for even j (0-based), '-' for odd j;
+//   backward (rtrans_backward, :1931-2008)
+//     be(i) = sum_{j even} pf(i, j, m) c(j),  bo(i) = sum_{j odd} pf(i, j, m) c(j),
+//     f(i) = be + bo,  f(nr-1-i) = be - bo;
+//   vec2tp projection (:1402-1438), five contractions against the V, D, T matrices with the
+//     eomul / oemul parity folds (:2067-2145), combined into psi and chi.
+// Each CTA owns one m, one parity of rows and one tile of z columns; the folded input (f(i) +- f(nr-1-i))
+// is formed while staging the K-chunk in shared memory.  The plain form accumulates in FP64 (DFMA),
+// the mixed form in FP32.
+#include "common.cuh"
+
+namespace mlg {
+
+template <typename T> struct V2;
+template <> struct V2<double> { typedef double2 t; };
+template <> struct V2<float> { typedef float2 t; };
+
+template <typename T> __device__ __forceinline__ typename V2<T>::t ldc(const double2* p) {
+  double2 v = *p; typename V2<T>::t r; r.x = (T)v.x; r.y = (T)v.y; return r;
+}
+
+// forward: grid (ztiles, 2*ttiles, npc); block (ZT/ZPT, MT/MPT)
+template <typename T, int MT, int ZT, int KC, int MPT, int ZPT>
+__global__ void __launch_bounds__((MT / MPT) * (ZT / ZPT))
+k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T* __restrict__ pf,
+             const double* __restrict__ w, int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc) {
+  typedef typename V2<T>::t C;
+  __shared__ T As[KC][MT + 1];
+  __shared__ C Bs[KC][ZT];
+  int m = blockIdx.z;
+  int par = blockIdx.y & 1;
+  int t0 = (blockIdx.y >> 1) * MT;
+  int nn = max(min(nrc, nrc - m), 0);
+  if (2 * t0 + par >= nn) return;
+  int z0 = blockIdx.x * ZT;
+  int tx = threadIdx.x, ty = threadIdx.y;
+  int nthr = blockDim.x * blockDim.y, tid = ty * blockDim.x + tx;
+  T acc_r[MPT][ZPT], acc_i[MPT][ZPT];
+#pragma unroll
+  for (int a = 0; a < MPT; ++a)
+#pragma unroll
+    for (int b = 0; b < ZPT; ++b) { acc_r[a][b] = 0; acc_i[a][b] = 0; }
+  const T sgn = par ? (T)-1 : (T)1;
+  for (int i0 = 0; i0 < nrh; i0 += KC) {
+    // A chunk: rows j = 2(t0+tt)+par, columns i0..i0+KC
+    for (int idx = tid; idx < KC * MT; idx += nthr) {
+      int ii = idx % KC, tt = idx / KC;
+      int j = 2 * (t0 + tt) + par, i = i0 + ii;
+      T v = 0;
+      if (j < nn && i < nrh) v = pf[i + (size_t)nrh * (j + (size_t)ne * m)];
+      As[ii][tt] = v;
+    }
+    // B chunk: folded columns (f(i) +- f(nr-1-i)) * w(i)
+    for (int idx = tid; idx < KC * ZT; idx += nthr) {
+      int ii = idx % KC, zz = idx / KC;
+      int i = i0 + ii, z = z0 + zz;
+      C v; v.x = 0; v.y = 0;
+      if (i < nrh && z < nzdim) {
+        const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * z);
+        double2 a = col[i], b = col[nr - 1 - i];
+        double wi = w[i];
+        v.x = (T)((a.x + (double)sgn * b.x) * wi);
+        v.y = (T)((a.y + (double)sgn * b.y) * wi);
+      }
+      Bs[ii][zz] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < KC; ++ii) {
+      T av[MPT];
+      C bv[ZPT];
+#pragma unroll
+      for (int a = 0; a < MPT; ++a) av[a] = As[ii][ty * MPT + a];
+#pragma unroll
+      for (int b = 0; b < ZPT; ++b) bv[b] = Bs[ii][tx + b * (ZT / ZPT)];
+#pragma unroll
+      for (int a = 0; a < MPT; ++a)
+#pragma unroll
+        for (int b = 0; b < ZPT; ++b) {
+          acc_r[a][b] = fma(av[a], bv[b].x, acc_r[a][b]);
+          acc_i[a][b] = fma(av[a], bv[b].y, acc_i[a][b]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < MPT; ++a) {
+    int j = 2 * (t0 + ty * MPT + a) + par;
+    if (j >= nn) continue;
+#pragma unroll
+    for (int b = 0; b < ZPT; ++b) {
+      int z = z0 + tx + b * (ZT / ZPT);
+      if (z < nzdim) out[j + (size_t)nrdim * (m + (size_t)npdim * z)] = make_double2((double)acc_r[a][b], (double)acc_i[a][b]);
+    }
+  }
+}
+
+// backward: grid (ztiles, itiles, npc); each thread owns IPT rows i and ZPT columns and both parities
+template <typename T, int IT, int ZT, int KC, int IPT, int ZPT>
+__global__ void __launch_bounds__((IT / IPT) * (ZT / ZPT))
+k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T* __restrict__ pf,
+             const double* __restrict__ lnx, const double* __restrict__ lnp, int add_ln, int nr, int nrh, int ne,
+             int nrdim, int npdim, int nzdim, int nrc) {
+  typedef typename V2<T>::t C;
+  __shared__ T Ae[KC][IT + 1], Ao[KC][IT + 1];
+  __shared__ C Be[KC][ZT], Bo[KC][ZT];
+  int m = blockIdx.z;
+  int i0 = blockIdx.y * IT;
+  int z0 = blockIdx.x * ZT;
+  int nn = max(min(nrc, nrc - m), 0);
+  int tx = threadIdx.x, ty = threadIdx.y;
+  int nthr = blockDim.x * blockDim.y, tid = ty * blockDim.x + tx;
+  T er[IPT][ZPT], ei[IPT][ZPT], orr[IPT][ZPT], oi[IPT][ZPT];
+#pragma unroll
+  for (int a = 0; a < IPT; ++a)
+#pragma unroll
+    for (int b = 0; b < ZPT; ++b) { er[a][b] = 0; ei[a][b] = 0; orr[a][b] = 0; oi[a][b] = 0; }
+  int nt = (nn + 1) / 2;
+  for (int t0 = 0; t0 < nt; t0 += KC) {
+    for (int idx = tid; idx < KC * IT; idx += nthr) {
+      int ii = idx % IT, tt = idx / IT;
+      int i = i0 + ii, je = 2 * (t0 + tt), jo = je + 1;
+      T ve = 0, vo = 0;
+      if (i < nrh) {
+        if (je < nn) ve = pf[i + (size_t)nrh * (je + (size_t)ne * m)];
+        if (jo < nn) vo = pf[i + (size_t)nrh * (jo + (size_t)ne * m)];
+      }
+      Ae[tt][ii] = ve; Ao[tt][ii] = vo;
+    }
+    for (int idx = tid; idx < KC * ZT * 2; idx += nthr) {
+      int jj = idx % (2 * KC), zz = idx / (2 * KC);
+      int j = 2 * t0 + jj, z = z0 + zz;
+      C v; v.x = 0; v.y = 0;
+      if (j < nn && z < nzdim) v = ldc<T>(in + j + (size_t)nrdim * (m + (size_t)npdim * z));
+      if (jj & 1) Bo[jj >> 1][zz] = v; else Be[jj >> 1][zz] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int tt = 0; tt < KC; ++tt) {
+      T ae[IPT], ao[IPT];
+      C be[ZPT], bo[ZPT];
+#pragma unroll
+      for (int a = 0; a < IPT; ++a) { ae[a] = Ae[tt][ty * IPT + a]; ao[a] = Ao[tt][ty * IPT + a]; }
+#pragma unroll
+      for (int b = 0; b < ZPT; ++b) { be[b] = Be[tt][tx + b * (ZT / ZPT)]; bo[b] = Bo[tt][tx + b * (ZT / ZPT)]; }
+#pragma unroll
+      for (int a = 0; a < IPT; ++a)
+#pragma unroll
+        for (int b = 0; b < ZPT; ++b) {
+          er[a][b] = fma(ae[a], be[b].x, er[a][b]);
+          ei[a][b] = fma(ae[a], be[b].y, ei[a][b]);
+          orr[a][b] = fma(ao[a], bo[b].x, orr[a][b]);
+          oi[a][b] = fma(ao[a], bo[b].y, oi[a][b]);
+        }
+    }
+    __syncthreads();
+  }
+  double lnv = (add_ln && m == 0) ? *lnp : 0.0;
+#pragma unroll
+  for (int a = 0; a < IPT; ++a) {
+    int i = i0 + ty * IPT + a;
+    if (i >= nrh) continue;
+#pragma unroll
+    for (int b = 0; b < ZPT; ++b) {
+      int z = z0 + tx + b * (ZT / ZPT);
+      if (z >= nzdim) continue;
+      size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
+      double2 p = make_double2((double)er[a][b] + (double)orr[a][b], (double)ei[a][b] + (double)oi[a][b]);
+      double2 q = make_double2((double)er[a][b] - (double)orr[a][b], (double)ei[a][b] - (double)oi[a][b]);
+      if (lnv != 0.0) { p.x += lnv * lnx[i]; q.x += lnv * lnx[nr - 1 - i]; }
+      out[base + i] = p;
+      out[base + nr - 1 - i] = q;
+    }
+  }
+}
+
+// vec2tp: psi(j) = -i m (V.F_s(ur))_j - (D.F_o(up))_j,
+//         chi(j) = i k (D.F_o(ur))_j + m k (V.F_s(up))_j - (T.F_s(uz))_j
+// F_s is the fold of the row's own parity (eomul), F_o the other one (oemul); no weights (they are
+// inside V, D, T).  Only k slots 1..nzc and nzcu..nzdim are produced.
+template <typename T, int MT, int ZT, int KC, int ZPT>
+__global__ void __launch_bounds__(MT * (ZT / ZPT))
+k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
+         double2* __restrict__ psi, double2* __restrict__ chi, const T* __restrict__ tV, const T* __restrict__ tD,
+         const T* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
+         int nzdim, int nrc, int nzc, int nzcu) {
+  typedef typename V2<T>::t C;
+  __shared__ T Av[KC][MT + 1], Ad[KC][MT + 1], At[KC][MT + 1];
+  __shared__ C Brs[KC][ZT], Bro[KC][ZT], Bps[KC][ZT], Bpo[KC][ZT], Bzs[KC][ZT];
+  int m = blockIdx.z;
+  int par = blockIdx.y & 1;
+  int t0 = (blockIdx.y >> 1) * MT;
+  int nn = max(min(nrc, nrc - m), 0);
+  if (2 * t0 + par >= nn) return;
+  int z0 = blockIdx.x * ZT;
+  int tx = threadIdx.x, ty = threadIdx.y;
+  int nthr = blockDim.x * blockDim.y, tid = ty * blockDim.x + tx;
+  C a1[ZPT], a2[ZPT], a3[ZPT], a4[ZPT], a5[ZPT];
+#pragma unroll
+  for (int b = 0; b < ZPT; ++b) {
+    a1[b].x = a1[b].y = 0; a2[b].x = a2[b].y = 0; a3[b].x = a3[b].y = 0; a4[b].x = a4[b].y = 0; a5[b].x = a5[b].y = 0;
+  }
+  const double ss = par ? -1.0 : 1.0;   // own-parity fold sign
+  for (int i0 = 0; i0 < nrh; i0 += KC) {
+    for (int idx = tid; idx < KC * MT; idx += nthr) {
+      int ii = idx % KC, tt = idx / KC;
+      int j = 2 * (t0 + tt) + par, i = i0 + ii;
+      T v = 0, d = 0, t = 0;
+      if (j < nn && i < nrh) {
+        size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
+        v = tV[o]; d = tD[o]; t = tT[o];
+      }
+      Av[ii][tt] = v; Ad[ii][tt] = d; At[ii][tt] = t;
+    }
+    for (int idx = tid; idx < KC * ZT; idx += nthr) {
+      int ii = idx % KC, zz = idx / KC;
+      int i = i0 + ii, z = z0 + zz;
+      C rs, ro, ps, po, zs;
+      rs.x = rs.y = ro.x = ro.y = ps.x = ps.y = po.x = po.y = zs.x = zs.y = 0;
+      if (i < nrh && z < nzdim) {
+        size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
+        double2 a = ur[base + i], b = ur[base + nr - 1 - i];
+        rs.x = (T)(a.x + ss * b.x); rs.y = (T)(a.y + ss * b.y);
+        ro.x = (T)(a.x - ss * b.x); ro.y = (T)(a.y - ss * b.y);
+        a = up[base + i]; b = up[base + nr - 1 - i];
+        ps.x = (T)(a.x + ss * b.x); ps.y = (T)(a.y + ss * b.y);
+        po.x = (T)(a.x - ss * b.x); po.y = (T)(a.y - ss * b.y);
+        a = uz[base + i]; b = uz[base + nr - 1 - i];
+        zs.x = (T)(a.x + ss * b.x); zs.y = (T)(a.y + ss * b.y);
+      }
+      Brs[ii][zz] = rs; Bro[ii][zz] = ro; Bps[ii][zz] = ps; Bpo[ii][zz] = po; Bzs[ii][zz] = zs;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int ii = 0; ii < KC; ++ii) {
+      T v = Av[ii][ty], d = Ad[ii][ty], t = At[ii][ty];
+#pragma unroll
+      for (int b = 0; b < ZPT; ++b) {
+        int zz = tx + b * (ZT / ZPT);
+        C rs = Brs[ii][zz], ro = Bro[ii][zz], ps = Bps[ii][zz], po = Bpo[ii][zz], zs = Bzs[ii][zz];
+        a1[b].x = fma(v, rs.x, a1[b].x); a1[b].y = fma(v, rs.y, a1[b].y);   // V.F_s(ur)
+        a2[b].x = fma(d, po.x, a2[b].x); a2[b].y = fma(d, po.y, a2[b].y);   // D.F_o(up)
+        a3[b].x = fma(d, ro.x, a3[b].x); a3[b].y = fma(d, ro.y, a3[b].y);   // D.F_o(ur)
+        a4[b].x = fma(v, ps.x, a4[b].x); a4[b].y = fma(v, ps.y, a4[b].y);   // V.F_s(up)
+        a5[b].x = fma(t, zs.x, a5[b].x); a5[b].y = fma(t, zs.y, a5[b].y);   // T.F_s(uz)
+      }
+    }
+    __syncthreads();
+  }
+  int j = 2 * (t0 + ty) + par;
+  if (j >= nn) return;
+  double mv = (double)m;
+#pragma unroll
+  for (int b = 0; b < ZPT; ++b) {
+    int z = z0 + tx + b * (ZT / ZPT);
+    if (z >= nzdim) continue;
+    int kk = z + 1;
+    if (!(kk <= nzc || kk >= nzcu)) continue;
+    double kv = ak[z];
+    double w1x = m ? (double)a1[b].x : 0.0, w1y = m ? (double)a1[b].y : 0.0;
+    double w2x = (double)a2[b].x, w2y = (double)a2[b].y;
+    // psi = -i*mv*w1 - w2
+    double2 p = make_double2(mv * w1y - w2x, -mv * w1x - w2y);
+    double v1x = (double)a3[b].x, v1y = (double)a3[b].y;
+    double v2x = m ? (double)a4[b].x : 0.0, v2y = m ? (double)a4[b].y : 0.0;
+    double cx = (double)a5[b].x, cy = (double)a5[b].y;
+    // chi = i*kv*w1' + mv*kv*w2' - c
+    double2 q = make_double2(-kv * v1y + mv * kv * v2x - cx, kv * v1x + mv * kv * v2y - cy);
+    size_t o = j + (size_t)nrdim * (m + (size_t)npdim * z);
+    psi[o] = p;
+    chi[o] = q;
+  }
+}
+
+static int rtrans_check(const Scalar& s, int& nrc, int& npc, const char* who) {
+  nrc = G.nrchop + s.off[0];
+  npc = G.npchop + s.off[1];
+  if (nrc > G.nrdim || nrc > G.ne) return set_error(MLG_ECHOP, std::string(who) + ": chopping in r too large");
+  if (npc > G.npdim) return set_error(MLG_ECHOP, std::string(who) + ": chopping in p too large");
+  if (npc > G.npchop) return set_error(MLG_ECHOP, std::string(who) + ": chopping in p beyond the table");
+  return 0;
+}
+
+static double fwd_flops(int nrc, int npc) {
+  double f = 0;
+  for (int m = 0; m < npc; ++m) f += 4.0 * std::max(std::min(nrc, nrc - m), 0) * G.nrh * G.nzdim;
+  return f;
+}
+
+int launch_rtrans_fwd(Scalar& s) {
+  int nrc, npc;
+  MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_forward"));
+  cd* out = get_buf();
+  if (!out) return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
+  MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  kt_begin(0);
+  if (npc > 0) {
+    if (G.precision == MLG_MIXED) {
+      constexpr int MT = 32, ZT = 64, KC = 32, MPT = 2, ZPT = 4;
+      int tt = cdiv((nrc + 1) / 2, MT);
+      dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT / MPT);
+      k_rtrans_fwd<float, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf32, G.w, G.nr, G.nrh, G.ne,
+                                                                             G.nrdim, G.npdim, G.nzdim, nrc);
+    } else {
+      constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
+      int tt = cdiv((nrc + 1) / 2, MT);
+      dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT / MPT);
+      k_rtrans_fwd<double, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.w, G.nr, G.nrh, G.ne,
+                                                                              G.nrdim, G.npdim, G.nzdim, nrc);
+    }
+    MLG_LAUNCH();
+  }
+  kt_end(0, fwd_flops(nrc, npc));
+  put_buf(s.e);
+  s.e = out;
+  return 0;
+}
+
+int launch_rtrans_bwd(Scalar& s, bool add_ln) {
+  int nrc, npc;
+  MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_backward"));
+  cd* out = get_buf();
+  if (!out) return set_error(MLG_EALLOC, "rtrans_backward: out of device memory");
+  MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  kt_begin(0);
+  if (npc > 0) {
+    if (G.precision == MLG_MIXED) {
+      constexpr int IT = 32, ZT = 64, KC = 16, IPT = 2, ZPT = 4;
+      dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
+      k_rtrans_bwd<float, IT, ZT, KC, IPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf32, G.lnx, s.ln, add_ln ? 1 : 0,
+                                                                            G.nr, G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
+    } else {
+      constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
+      dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
+      k_rtrans_bwd<double, IT, ZT, KC, IPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.lnx, s.ln, add_ln ? 1 : 0,
+                                                                             G.nr, G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
+    }
+    MLG_LAUNCH();
+  }
+  kt_end(0, fwd_flops(nrc, npc));
+  put_buf(s.e);
+  s.e = out;
+  return 0;
+}
+
+// ur, up, uz in (r physical, m, k) space; psi and chi zeroed by the caller
+int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off) {
+  int nrc = G.nrchop + nrc_off, npc = G.npchop;
+  int nzc = G.chopzl, nzcu = G.chopzu;
+  if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
+  kt_begin(0);
+  constexpr int MT = 16, ZT = 32, KC = 16, ZPT = 4;
+  int tt = cdiv((nrc + 1) / 2, MT);
+  dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
+  if (G.precision == MLG_MIXED)
+    k_vec2tp<float, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV32, G.tD32, G.tT32, G.ak, G.nr,
+                                                                  G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+  else
+    k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
+                                                                   G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+  MLG_LAUNCH();
+  kt_end(0, 5.0 * fwd_flops(nrc, npc));
+  return 0;
+}
+
+}  // namespace mlg

@@ -1,0 +1,207 @@
+"""GPU parity: every operator of the C ABI against the CPU oracle on the same seeded inputs.
+
+The plain form (all FP64) must agree with the oracle's FP64 restatement of the reference to the
+spec bar of 1e-12 relative (L2 over the field); the 100-step run compounds rounding over many
+solves and is held to 1e-11.  The mixed form is checked against the same oracle at 1e-5 per operator.
+"""
+import numpy as np
+import pytest
+
+from mlegs_gb300 import fields
+from helpers import CONFIGS, params, compare, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module", params=["c1", "t2d", "odd", "hyp"])
+def pair(request):
+    from mlegs_gb300.kit import Kit
+    from oracle.oracle import Oracle
+    p = params(request.param)
+    o = Oracle(p)
+    k = Kit(p)
+    yield request.param, k, o
+    k.close()
+    o.close()
+
+
+def both(k, o, e, ln=0.0, space="FFF"):
+    return k.scalar(e, ln, space), o.scalar(e, ln, space)
+
+
+def fff_input(p, dims, seed, amp=1.0):
+    return fields.spectral_noise(p, dims, seed, amp=amp, decay=0.05)
+
+
+def test_kit_arrays(pair):
+    name, k, o = pair
+    for a in ["x", "w", "r", "ln", "ak", "lognorm", "at0", "at1"]:
+        g, c = k.kit_get(a), o.kit_get(a)
+        assert np.array_equal(g, c) or rel_l2(g, c) < 1e-15, (a, rel_l2(g, c))
+    g, c = k.kit_get("pf"), o.kit_get("pf")
+    # the table: double-double recurrence on the GPU, binary128 in the oracle, both rounded to FP64
+    big = np.abs(c) > 1e-250
+    rel = np.abs(g[big] - c[big]) / np.abs(c[big])
+    assert rel.max() < 1e-14, rel.max()
+    assert np.all(np.abs(g[~big]) < 1e-240)
+
+
+def test_trans_roundtrip(pair):
+    name, k, o = pair
+    p = k.params
+    e = fields.ppp_random(p, k.dims, seed=11)
+    gs, os_ = both(k, o, e, 0.0, "PPP")
+    for sp in ["PFP", "FFP", "FFF"]:
+        k.trans(gs, sp); o.trans(os_, sp)
+        compare(gs, os_, TOL, what=f"{name} PPP->{sp}")
+    c = fff_input(p, k.dims, 12)
+    gs, os_ = both(k, o, c, 0.3, "FFF")
+    for sp in ["FFP", "PFP", "PPP"]:
+        k.trans(gs, sp); o.trans(os_, sp)
+        compare(gs, os_, TOL, what=f"{name} FFF->{sp}")
+    k.trans(gs, "FFF"); o.trans(os_, "FFF")
+    compare(gs, os_, TOL, what=f"{name} round trip")
+
+
+@pytest.mark.parametrize("op", ["chop", "dealias", "zeroat1", "delsqp", "idelsqp", "xxdx", "del2h", "del2",
+                                "idel2_pro", "idel2_pre", "helm", "ihelm", "svv"])
+def test_single_operator(pair, op):
+    name, k, o = pair
+    p = k.params
+    c = fff_input(p, k.dims, 21)
+    for ln in (0.0, 0.7):
+        gs, os_ = both(k, o, c, ln, "FFF")
+        if op == "idel2_pro":
+            k.idel2(gs); o.idel2(os_)
+        elif op == "idel2_pre":
+            k.idel2(gs, 0.25); o.idel2(os_, 0.25)
+        elif op in ("helm", "ihelm"):
+            getattr(k, op)(gs, -3.5e3); getattr(o, op)(os_, -3.5e3)
+        elif op == "svv":
+            # a field with a heavy tail, so that the filter engages
+            big = fields.spectral_noise(p, k.dims, 22, amp=1.0, decay=0.0)
+            gs.set(big, ln, "FFF"); os_.set(big, ln, "FFF")
+            g1 = k.svv_filter(gs, 0.5)
+            g2 = o.svv_filter(os_, 0.5)
+            assert abs(g1 - g2) <= 1e-14 * max(1.0, abs(g2)), (g1, g2)
+        else:
+            getattr(k, op)(gs); getattr(o, op)(os_)
+        compare(gs, os_, TOL, what=f"{name} {op} ln={ln}")
+
+
+def test_chop_offset_and_partial_space(pair):
+    name, k, o = pair
+    p = k.params
+    c = fff_input(p, k.dims, 31)
+    gs, os_ = both(k, o, c, 0.0, "FFF")
+    gs.chop_offset(3); os_.chop_offset(3)
+    k.xxdx(gs); o.xxdx(os_)
+    compare(gs, os_, TOL, what=f"{name} xxdx offset 3")
+    k.del2h(gs); o.del2h(os_)
+    compare(gs, os_, TOL, what=f"{name} del2h offset 3")
+    gs.chop_offset(0); os_.chop_offset(0)
+    k.chop(gs); o.chop(os_)
+    compare(gs, os_, TOL, what=f"{name} chop")
+
+
+def test_calcat(pair):
+    name, k, o = pair
+    p = k.params
+    c = fff_input(p, k.dims, 41)
+    gs, os_ = both(k, o, c, 0.0, "FFF")
+    for f in ("calcat0", "calcat1"):
+        g, r = getattr(k, f)(gs), getattr(o, f)(os_)
+        assert rel_l2(g, r) < TOL, (f, rel_l2(g, r))
+    # from a physical field (calcat transforms a copy)
+    e = fields.ppp_random(p, k.dims, seed=42)
+    gs, os_ = both(k, o, e, 0.0, "PPP")
+    g, r = k.calcat0(gs), o.calcat0(os_)
+    assert rel_l2(g, r) < TOL
+    compare(gs, os_, 0.0, what="calcat leaves its argument unchanged")
+
+
+@pytest.mark.parametrize("op", ["helmp", "ihelmp"])
+def test_powered_helmholtz(pair, op):
+    name, k, o = pair
+    p = k.params
+    c = fff_input(p, k.dims, 51)
+    for power in (4, 6, 8):
+        gs, os_ = both(k, o, c, 0.2, "FFF")
+        getattr(k, op)(gs, power, -2.0e3, 0.5); getattr(o, op)(os_, power, -2.0e3, 0.5)
+        compare(gs, os_, 1e-11, what=f"{name} {op} p={power}")
+
+
+@pytest.mark.parametrize("op", ["fefe", "abab", "febe", "abcn"])
+def test_steppers(pair, op):
+    name, k, o = pair
+    p = k.params
+    s0, sp0 = fff_input(p, k.dims, 61), fff_input(p, k.dims, 62)
+    n0, np0 = fff_input(p, k.dims, 63, 0.1), fff_input(p, k.dims, 64, 0.1)
+    g = [k.scalar(a, ln, "FFF") for a, ln in ((s0, 0.1), (sp0, 0.2), (n0, 0.05), (np0, 0.0))]
+    r = [o.scalar(a, ln, "FFF") for a, ln in ((s0, 0.1), (sp0, 0.2), (n0, 0.05), (np0, 0.0))]
+    dt = 1e-3
+    for _ in range(3):
+        if op in ("fefe", "febe"):
+            getattr(k, op)(g[0], g[2], dt); getattr(o, op)(r[0], r[2], dt)
+        else:
+            getattr(k, op)(g[0], g[1], g[2], g[3], dt); getattr(o, op)(r[0], r[1], r[2], r[3], dt)
+    for i in range(4):
+        compare(g[i], r[i], 1e-11, what=f"{name} {op} arg{i}")
+
+
+def test_vector_fields(pair):
+    name, k, o = pair
+    p = k.params
+    if p.np < 4:
+        pytest.skip("needs an azimuthal direction")
+    psi, chi = fff_input(p, k.dims, 71), fff_input(p, k.dims, 72)
+    gp, op_ = both(k, o, psi, 0.0, "FFF")
+    gc, oc = both(k, o, chi, 0.0, "FFF")
+    gv = [k.scalar() for _ in range(3)]
+    ov = [o.scalar() for _ in range(3)]
+    k.tp2vec(gp, gc, *gv); o.tp2vec(op_, oc, *ov)
+    for i in range(3):
+        compare(gv[i], ov[i], TOL, what=f"{name} tp2vec {i}")
+    gw = [k.scalar() for _ in range(3)]
+    ow = [o.scalar() for _ in range(3)]
+    k.tp2curlvec(gp, gc, *gw); o.tp2curlvec(op_, oc, *ow)
+    for i in range(3):
+        compare(gw[i], ow[i], TOL, what=f"{name} tp2curlvec {i}")
+    k.vecprod(*gv, *gw); o.vecprod(*ov, *ow)
+    for i in range(3):
+        compare(gv[i], ov[i], TOL, what=f"{name} vecprod {i}")
+    gq = [k.scalar(np.zeros(k.dims, complex, order="F"), 0.0, "FFF") for _ in range(2)]
+    oq = [o.scalar(np.zeros(k.dims, complex, order="F"), 0.0, "FFF") for _ in range(2)]
+    k.vec2tp(*gv, *gq); o.vec2tp(*ov, *oq)
+    for i in range(2):
+        compare(gq[i], oq[i], 1e-11, what=f"{name} vec2tp {i}")
+
+
+def test_vortex_steps(pair):
+    name, k, o = pair
+    p = k.params
+    if p.nz < 4 or p.np < 4:
+        pytest.skip("3-D case only")
+    from mlegs_gb300 import vortex
+    # identical initial state on both sides: the oracle builds it, the GPU receives the same bytes
+    so = vortex.VortexState(o)
+    pert = (fields.spectral_noise(p, o.dims, 81, amp=1e-3, decay=0.3, m_max=4, k_max=8),
+            fields.spectral_noise(p, o.dims, 82, amp=1e-3, decay=0.3, m_max=4, k_max=8))
+    vortex.qvort_init(o, so, q=4.0, uz_b=-0.5, pert=pert)
+    sg = vortex.VortexState(k)
+    for n in vortex.VortexState.names:
+        e, ln, sp, _ = getattr(so, n).get()
+        getattr(sg, n).set(e, ln, sp)
+    dt = 1e-3
+    vortex.bootstrap(k, sg, dt)
+    vortex.bootstrap(o, so, dt)
+    for n in ("psi", "chi", "nlpsi", "nlchi"):
+        compare(getattr(sg, n), getattr(so, n), 1e-11, what=f"{name} bootstrap {n}")
+    for _ in range(5):
+        vortex.step(k, sg, dt)
+        vortex.step(o, so, dt)
+    for n in ("psi", "chi", "nlpsi", "nlchi", "psi_p", "nlpsi_p"):
+        compare(getattr(sg, n), getattr(so, n), 1e-11, what=f"{name} 5 steps {n}")
+    assert abs(sg.gains[0] - so.gains[0]) < 1e-12 and abs(sg.gains[1] - so.gains[1]) < 1e-12
