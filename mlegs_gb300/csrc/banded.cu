@@ -94,6 +94,7 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
 }
 
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   size_t sm = 2ull * G.nrdim * sizeof(double2);
   if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   dim3 grid(G.nzdim, std::max(c.npc, 1));
@@ -311,6 +312,7 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 
 // kind as in SolveArgs; the band scratch grows to fit (kl, ku)
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   int kl = 2, ku = 2;
   if (kind == 2) kl = 3;
   if (kind == 3) { kl = power; ku = power; }
