@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark: 3-D vortex Navier-Stokes steps/s at NR x NP x NZ = 192 x 128 x 128 on one GB300.
+
+Workload (the metric's configuration): Batchelor q-vortex (q = 4) at the origin built by the
+reference's qvort_dist_tp recipe, Re = 1e4 (visc = 1e-4), ELL = 4, full chops (NRCHOP=192,
+NPCHOP=65, NZCHOP=65), dt = 1e-3, SVV filter on with the reference defaults, background u_z = 0,
+plus a seeded perturbation of amplitude 1e-4 on the (psi, chi) coefficients with |m| <= 4, |k| <= 8.
+A step is one main-loop iteration of src/apps/vortical_flow_3d.f90 (abcn x2, dealias, svv_filter,
+zeroat1, advection_rhs, check_stability).  Data: synthetic (seeded); every field is 26 MB and the
+step touches ~20 of them, so the working set exceeds the 129 MB L2 and no flush is needed.
+
+Arms:
+  default          the GPU library (mixed form timed as `value`; the plain FP64 form timed beside it,
+                   with the relative error of mixed against FP64 per field)
+  --impl reference the reference's CPU path for this workload: the oracle port (C++ restatement of
+                   the Fortran, OpenMP over the host cores), since the Fortran reference cannot be
+                   built here (no Fortran compiler / MPI / LAPACK)
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path does not
+shard on one GPU per box: replicas only); value = total steps/s over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(nr=192, np=128, nz=128, nrchop=192, npchop=65, nzchop=65, ell=4.0, visc=1.0e-4)
+DT = 1.0e-3
+Q = 4.0
+PERT = 1.0e-4
+METRIC = "steps/s @192x128x128 (3-D vortex NS step, mixed precision on GPU)"
+
+
+def workload_params():
+    from mlegs_gb300.params import make_params
+    return make_params(**WORKLOAD)
+
+
+def perturbation(p, dims):
+    from mlegs_gb300 import fields
+    return (fields.spectral_noise(p, dims, 1001, amp=PERT, decay=0.3, m_max=4, k_max=8),
+            fields.spectral_noise(p, dims, 1002, amp=PERT, decay=0.3, m_max=4, k_max=8))
+
+
+def config_dict():
+    return {"workload": "vortex3d NR=192 NP=128 NZ=128 ELL=4 NRCHOP=192 NPCHOP=65 NZCHOP=65 q=4 Re=1e4 dt=1e-3 "
+                        "SVV on, perturbation 1e-4 |m|<=4 |k|<=8",
+            "field_MB": 195 * 65 * 128 * 16 / 1e6,
+            "l2_policy": "inputs larger than L2 (working set ~20 fields x 26 MB), no flush"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1].split()[0]))
+                smax.append(float(f[2].split()[0]))
+            except ValueError:
+                continue
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("MLG_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def run_reference(args, rank, world, pg):
+    """The reference arm: the CPU path (oracle port) on this host's cores, rank 0 only."""
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle
+    from mlegs_gb300 import vortex
+    threads = os.cpu_count() or 1
+    p = workload_params()
+    o = Oracle(p, threads=threads)
+    st = vortex.VortexState(o)
+    vortex.qvort_init(o, st, q=Q, uz_b=0.0, pert=perturbation(p, o.dims))
+    # untimed start-up: one advection_rhs and the history copies (the cost of a step does not depend
+    # on whether the Richardson start-up ran)
+    o.advection_rhs(st.psi, st.chi, st.nlpsi, st.nlchi, st.uz)
+    for a, b in (("psi_p", "psi"), ("chi_p", "chi"), ("nlpsi_p", "nlpsi"), ("nlchi_p", "nlchi")):
+        getattr(st, a).copy_from(getattr(st, b))
+    t0 = time.perf_counter()
+    for _ in range(max(args.warmup, 1) if args.warmup else 1):
+        vortex.step(o, st, DT)
+        if time.perf_counter() - t0 > 60:
+            break
+    per = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # a bounded sample: at most ~90 s of CPU work, at least one step
+    k = max(1, min(args.steps, int(90.0 / max(per, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        vortex.step(o, st, DT)
+    dt_s = time.perf_counter() - t0
+    value = k / dt_s
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config_dict(),
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} timed steps (of {args.steps} requested) after {args.warmup} warm-up, "
+                                       "oracle C++ restatement with OpenMP"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def snapshot(st):
+    return {n: getattr(st, n).get() for n in st.names}
+
+
+def restore(st, snap):
+    for n, (e, ln, sp, _) in snap.items():
+        getattr(st, n).set(e, ln, sp)
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb else float(np.linalg.norm(a))
+
+
+def run_ours(args, rank, world, local, pg):
+    import torch
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    from mlegs_gb300 import vortex
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    p = workload_params()
+    with torch.cuda.stream(stream):
+        t_init0 = time.perf_counter()
+        kit = Kit(p, stream=stream.cuda_stream)
+        kit.sync()
+        t_init = time.perf_counter() - t_init0
+        st = vortex.VortexState(kit)
+        vortex.qvort_init(kit, st, q=Q, uz_b=0.0, pert=perturbation(p, kit.dims))
+        vortex.bootstrap(kit, st, DT)
+        kit.sync()
+        snap0 = snapshot(st)
+
+        def timed(mode, steps, warmup, clocks=None):
+            kit.set_precision(mode)
+            restore(st, snap0)
+            st.gains = [0.0, 0.0]
+            if warmup:
+                kit.vortex_run(*st.args(), DT, warmup, st.gains)
+            kit.sync()
+            if pg:
+                pg.barrier()
+            torch.cuda.synchronize()
+            if clocks:
+                clocks.start()
+            l0 = kit.launch_count()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            kit.vortex_run(*st.args(), DT, steps, st.gains)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            if pg:
+                pg.barrier()
+            ck = clocks.stop() if clocks else None
+            ms = ev0.elapsed_time(ev1)
+            return ms, kit.launch_count() - l0, ck
+
+        clocks = Clocks(local)
+        ms_mixed, launches, ck = timed(MIXED, args.steps, args.warmup, clocks)
+        if pg:
+            t = torch.tensor([ms_mixed], device="cuda")
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            ms_mixed = float(t.item())
+        value = world * args.steps / (ms_mixed / 1e3)
+
+        # plain FP64 over the same steps, and the error of mixed against it
+        k_cmp = min(args.steps, 20)
+        ms_plain, _, _ = timed(PLAIN_FP64, k_cmp, 2)
+        plain_sps = k_cmp / (ms_plain / 1e3)
+        errs = {}
+        for mode in (PLAIN_FP64, MIXED):
+            kit.set_precision(mode)
+            restore(st, snap0)
+            st.gains = [0.0, 0.0]
+            kit.vortex_run(*st.args(), DT, k_cmp, st.gains)
+            kit.sync()
+            errs[mode] = {n: getattr(st, n).e for n in ("psi", "chi", "nlpsi", "nlchi")}
+        err = {n: rel_l2(errs[MIXED][n], errs[PLAIN_FP64][n]) for n in errs[MIXED]}
+
+        # kernel classes timed launch by launch (CUDA events on the library's stream)
+        kit.set_precision(MIXED)
+        restore(st, snap0)
+        kit.kernel_timing(True)
+        kit.vortex_run(*st.args(), DT, 2, st.gains)
+        kt = {name: kit.kernel_timing_read(i) for i, name in
+              enumerate(["radial_fwd", "fft", "banded", "radial_bwd", "vec2tp"])}
+        kit.kernel_timing(False)
+        kit.sync()
+
+        # end to end through the C ABI with host buffers: every step uploads psi and chi (e and ln)
+        # from pinned host memory, steps, and downloads psi and chi into pinned host memory
+        import ctypes
+        from mlegs_gb300.kit import load
+        L = load()
+        kit.set_precision(MIXED)
+        restore(st, snap0)
+        dims = kit.dims
+        host = [torch.empty(dims[::-1], dtype=torch.complex128, pin_memory=True).numpy().T for _ in range(2)]
+        lns = [ctypes.c_double(0.0), ctypes.c_double(0.0)]
+        sp = ctypes.create_string_buffer(4)
+        for h, n, l in zip(host, ("psi", "chi"), lns):
+            L.mlg_scalar_download(getattr(st, n).h, h.ctypes.data, ctypes.byref(l), sp)
+        k_e2e = min(args.steps, 20)
+        kit.sync()
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            for h, n, l in zip(host, ("psi", "chi"), lns):
+                L.mlg_scalar_upload(getattr(st, n).h, h.ctypes.data, l.value, b"FFF")
+            kit.vortex_step(*st.args(), DT, st.gains)
+            for h, n, l in zip(host, ("psi", "chi"), lns):
+                L.mlg_scalar_download(getattr(st, n).h, h.ctypes.data, ctypes.byref(l), sp)
+        e2e_s = time.perf_counter() - t0
+        fbytes = int(np.prod(dims) * 16)
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # dominant kernel class by time per step
+    dom = max(kt, key=lambda n: kt[n][0])
+    d_ms, d_n, d_work = kt[dom]
+    avg_ms = d_ms / max(d_n, 1)
+    # algorithmic bytes per launch of the radial contractions (mixed form): FP64 field columns in and
+    # out once, FP32 tables once (forward: nr rows x npc columns in, sum nn rows out; backward the
+    # reverse; vec2tp: three fields in, two out, three tables)
+    nrh, nz, fb = 96, 128, 16
+    sum_nn = sum(max(min(192, 192 - m), 0) for m in range(65))
+    sum_nn3 = sum(max(min(195, 195 - m), 0) for m in range(65))
+    alg = {"radial_fwd": 192 * 65 * nz * fb + sum_nn * nz * fb + sum_nn * nrh * 4,
+           "radial_bwd": 192 * 65 * nz * fb + sum_nn * nz * fb + sum_nn * nrh * 4,
+           "vec2tp": 3 * 192 * 65 * nz * fb + 2 * sum_nn3 * nz * fb + 3 * sum_nn3 * nrh * 4,
+           "fft": 2 * 195 * 65 * 128 * fb, "banded": 2 * 195 * 65 * 128 * fb}
+    bytes_launch = alg[dom]
+    achieved_gbs = bytes_launch / (avg_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded)",
+        "config": config_dict(),
+        "fp64_plain": {"value": plain_sps, "unit": "steps/s", "steps": k_cmp,
+                       "mixed_speedup": value / world / plain_sps},
+        "mixed_vs_fp64_rel_l2_after_steps": err,
+        "kit_init_s": t_init,
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": launches / args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm, "traffic": None, "avg_launch_us": 1e3 * avg_ms,
+                     "launches_per_step": d_n / 2, "algorithmic_bytes_per_launch": bytes_launch,
+                     "work_per_launch": d_work / max(d_n, 1), "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "kernel_classes_ms_per_step": {n: v[0] / 2 for n, v in kt.items()},
+        "kernel_classes_launches_per_step": {n: v[1] / 2 for n, v in kt.items()},
+        "clocks": ck,
+        "e2e": {"value": k_e2e / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * fbytes,
+                "d2h_bytes_per_step": 2 * fbytes, "steps": k_e2e},
+        "mem_high_water_MB": kit.mem_high_water() / 1e6,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle.oracle import Oracle
+        from mlegs_gb300 import vortex as vx
+        threads = os.cpu_count() or 1
+        o = Oracle(p, threads=threads)
+        so = vx.VortexState(o)
+        restore(so, snap0)
+        t0 = time.perf_counter()
+        nstep = 0
+        while nstep < 1 or (time.perf_counter() - t0 < 15.0 and nstep < 5):
+            vx.step(o, so, DT)
+            nstep += 1
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nstep / cpu_s, "unit": "steps/s", "cores": threads, "kind": "port",
+                                "sample": f"{nstep} steps of the same workload from the same state"}
+        o.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_profile(args):
+    """--profile-run: only the set-up and W + K steps of the chosen form (for ncu launch lists)."""
+    from mlegs_gb300 import vortex
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    p = workload_params()
+    kit = Kit(p, precision=PLAIN_FP64 if args.precision == "plain" else MIXED)
+    st = vortex.VortexState(kit)
+    vortex.qvort_init(kit, st, q=Q, uz_b=0.0, pert=perturbation(p, kit.dims))
+    kit.advection_rhs(st.psi, st.chi, st.nlpsi, st.nlchi, st.uz)
+    for a, b in (("psi_p", "psi"), ("chi_p", "chi"), ("nlpsi_p", "nlpsi"), ("nlchi_p", "nlchi")):
+        getattr(st, a).copy_from(getattr(st, b))
+    kit.vortex_run(*st.args(), DT, args.warmup, st.gains)
+    l0 = kit.launch_count()
+    t0 = time.perf_counter()
+    kit.vortex_run(*st.args(), DT, args.steps, st.gains)
+    kit.sync()
+    dt_s = time.perf_counter() - t0
+    print(json.dumps({"profile_run": args.precision, "steps": args.steps, "ms_per_step_wall": 1e3 * dt_s / args.steps,
+                      "launches_per_step": (kit.launch_count() - l0) / args.steps}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-run", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
+    args = ap.parse_args()
+    if args.profile_run:
+        run_profile(args)
+        return
+    rank, world, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, pg)
+    else:
+        run_ours(args, rank, world, local, pg)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -84,6 +84,8 @@ const char* mlg_last_error(void);
 /* Bytes of device memory currently held by the library (fields, tables, workspaces). */
 long long mlg_mem_bytes(void);
 long long mlg_mem_high_water(void);
+/* Number of kernels the library has launched since mlg_init. */
+long long mlg_launch_count(void);
 
 /* ---- scalar container: type(scalar) (mlegs_scalar.f90:15-49, mlegs_scalar_init.f90) ------ */
 int mlg_scalar_alloc(mlg_scalar* s);               /* scalar_init: space 'PPP', ln 0, offsets 0 */
@@ -157,7 +159,9 @@ int mlg_vortex_run(mlg_scalar psi, mlg_scalar chi, mlg_scalar nlpsi, mlg_scalar 
                    mlg_scalar uz, double dt, int nsteps, double* gains);
 
 /* ---- kernel timing (CUDA events around each launch of one kernel class) ----------------- */
-/* kind: 0 = radial Legendre contraction (forward, backward and vec2tp), 1 = FFTs, 2 = banded. */
+/* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators and solves,
+ *       3 = backward radial contraction, 4 = vec2tp projection contraction.  work = flops for the
+ *       contractions, bytes moved for the others. */
 int mlg_kernel_timing(int enable);
 int mlg_kernel_timing_read(int kind, double* total_ms, long long* launches, double* flops_or_bytes);
 

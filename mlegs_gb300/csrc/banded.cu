@@ -12,6 +12,10 @@
 // Every per-(m,k) loop of the reference visits k = 1..nzc and then k = nzcu..nzdim; when nzc == nzcu
 // (nzchop = nz/2+1) the shared slot is processed twice, and so it is here.
 #include "common.cuh"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
 
 namespace mlg {
 
@@ -40,6 +44,7 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
     for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = g[i];
     __syncthreads();
     double akv = ak[k];
+    double akv2 = akv * akv;   // akval**2 (mlegs_spectfm_diff.f90:144)
     for (int rep = 0; rep < cnt; ++rep) {
       for (int i = threadIdx.x; i < nn; i += blockDim.x) {
         double2 acc = make_double2(0, 0);
@@ -54,7 +59,7 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
             int j = i - 2 + c;
             if (j < 0 || j >= nn) continue;
             double v = b[c];
-            if (c == 2 && op == 2) v = v - pow(akv, 2.0);
+            if (c == 2 && op == 2) v = v - akv2;
             acc.x += v * c0[j].x;
             acc.y += v * c0[j].y;
           }
@@ -126,6 +131,7 @@ struct SolveArgs {
   double alpha, beta, ell, preln;
   int kind;             // 0 ihelm, 1 idel2_proln, 2 idel2_preln, 3 ihelmp
   int power;
+  int skip_root;        // substitution: leave the (0,0) column to the bordered solve
 };
 
 // entry (i, j) (0-based) of D(m,k) = D0(m) - ak^2 I for an n x n truncation
@@ -134,7 +140,7 @@ __device__ __forceinline__ double dmat(const SolveArgs& a, int m, double akv, in
   int c = j - i + 2;
   if (c < 0 || c > 4) return 0.0;
   double v = a.bd2[c + 5 * ((size_t)i + (size_t)a.ne * m)];
-  if (c == 2) v = v - pow(akv, 2.0);
+  if (c == 2) v = v - akv * akv;
   return v;
 }
 
@@ -268,6 +274,350 @@ __global__ void k_band_solve(SolveArgs a) {
   if (special) *a.lnp = x[0].x * exp(a.lognorm[0]);
 }
 
+// Entry (i, j) of the system matrix of (m, k) for kinds 0..2 (0-based, n x n truncation).
+__device__ __forceinline__ double sys_entry(const SolveArgs& a, int kind, bool special, int m, double akv, int nn,
+                                            double alpha, double e2, int i, int j) {
+  if (i < 0 || j < 0 || i >= nn || j >= nn) return 0.0;
+  if (special && kind == 1) {
+    double v = dmat(a, 0, akv, nn, i, j);
+    if (j == 0) {
+      if (i == 0) v += 4.0 / 3.0 / e2;
+      if (i == 1) v -= 2.0 / 1.0 / e2 * exp(a.lognorm[0] - a.lognorm[1]);
+      if (i == 2) v += 2.0 / 3.0 / e2 * exp(a.lognorm[0] - a.lognorm[2]);
+    }
+    return v;
+  }
+  if (special && kind == 2) {   // shifted rows, bordered by the ln unknown (:609-617)
+    if (i == 0) return (j == 0) ? 1.0 : 0.0;
+    double v = dmat(a, 0, akv, nn, i - 1, j);
+    if (j == 0) {
+      if (i == 1) v += 4.0 / 3.0 / e2;
+      if (i == 2) v -= 2.0 / 1.0 / e2 * exp(a.lognorm[0] - a.lognorm[1]);
+      if (i == 3) v += 2.0 / 3.0 / e2 * exp(a.lognorm[0] - a.lognorm[2]);
+    }
+    return v;
+  }
+  double v = dmat(a, m, akv, nn, i, j);
+  if (i == j) v += alpha;
+  return v;
+}
+
+// Banded LU with partial pivoting (gbtrf semantics) on a sliding window held in registers: at
+// column j only rows j..j+KL and columns j..j+KL+KU are live.  The finished U row (KL+KU+1 values)
+// and its transformed right-hand side are streamed to the scratch band ([row][slot][system], so a
+// warp writes consecutive addresses) and read back in reverse for the back substitution.
+template <int KL, int KU>
+__device__ void window_solve(const SolveArgs& a, int sys, int kind, bool special, int m, double akv, int nn,
+                             double alpha, double e2, double2* __restrict__ x) {
+  constexpr int WC = KL + KU + 1;     // window columns
+  constexpr int SL = WC + 2;          // scratch slots per row: U row + complex rhs
+  const size_t ns = a.nsys;
+  double W[KL + 1][WC];
+  double2 r[KL + 1];
+#pragma unroll
+  for (int t = 0; t <= KL; ++t) {
+#pragma unroll
+    for (int c = 0; c < WC; ++c) W[t][c] = sys_entry(a, kind, special, m, akv, nn, alpha, e2, t, c);
+    r[t] = (t < nn) ? x[t] : make_double2(0.0, 0.0);
+  }
+  for (int j = 0; j < nn; ++j) {
+    int km = min(KL, nn - 1 - j);
+    // pivot: first row of maximal |a| among window rows 0..km
+    int p = 0;
+    double best = fabs(W[0][0]);
+#pragma unroll
+    for (int t = 1; t <= KL; ++t)
+      if (t <= km && fabs(W[t][0]) > best) { best = fabs(W[t][0]); p = t; }
+    if (best == 0.0) { atomicExch(a.status, 1); return; }
+#pragma unroll
+    for (int t = 1; t <= KL; ++t)
+      if (t == p) {
+#pragma unroll
+        for (int c = 0; c < WC; ++c) { double q = W[0][c]; W[0][c] = W[t][c]; W[t][c] = q; }
+        double2 q = r[0]; r[0] = r[t]; r[t] = q;
+      }
+    double rp = 1.0 / W[0][0];
+#pragma unroll
+    for (int t = 1; t <= KL; ++t)
+      if (t <= km) {
+        double l = W[t][0] * rp;
+#pragma unroll
+        for (int c = 1; c < WC; ++c) W[t][c] -= l * W[0][c];
+        r[t].x -= l * r[0].x;
+        r[t].y -= l * r[0].y;
+      }
+    // stream out U row j (its diagonal as the reciprocal) and its right-hand side
+    a.ws[((size_t)j * SL) * ns + sys] = rp;
+#pragma unroll
+    for (int c = 1; c < WC; ++c) a.ws[((size_t)j * SL + c) * ns + sys] = W[0][c];
+    a.ws[((size_t)j * SL + WC) * ns + sys] = r[0].x;
+    a.ws[((size_t)j * SL + WC + 1) * ns + sys] = r[0].y;
+    // slide the window by one row and one column; the new last row enters unreduced
+#pragma unroll
+    for (int t = 0; t < KL; ++t) {
+#pragma unroll
+      for (int c = 0; c < WC - 1; ++c) W[t][c] = W[t + 1][c + 1];
+      W[t][WC - 1] = 0.0;
+      r[t] = r[t + 1];
+    }
+    int nr_ = j + 1 + KL;
+#pragma unroll
+    for (int c = 0; c < WC; ++c) W[KL][c] = sys_entry(a, kind, special, m, akv, nn, alpha, e2, nr_, j + 1 + c);
+    r[KL] = (nr_ < nn) ? x[nr_] : make_double2(0.0, 0.0);
+  }
+  // back substitution with U (bandwidth KL+KU), x(j+1..j+KL+KU) kept in registers
+  double2 xs[WC - 1];
+#pragma unroll
+  for (int c = 0; c < WC - 1; ++c) xs[c] = make_double2(0.0, 0.0);
+  for (int j = nn - 1; j >= 0; --j) {
+    double2 acc;
+    acc.x = a.ws[((size_t)j * SL + WC) * ns + sys];
+    acc.y = a.ws[((size_t)j * SL + WC + 1) * ns + sys];
+#pragma unroll
+    for (int c = 1; c < WC; ++c) {
+      double u = a.ws[((size_t)j * SL + c) * ns + sys];
+      acc.x -= u * xs[c - 1].x;
+      acc.y -= u * xs[c - 1].y;
+    }
+    double rd = a.ws[((size_t)j * SL) * ns + sys];
+    double2 xj = make_double2(acc.x * rd, acc.y * rd);
+    x[j] = xj;
+#pragma unroll
+    for (int c = WC - 2; c >= 1; --c) xs[c] = xs[c - 1];
+    xs[0] = xj;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Factor cache.  The matrix of system (m, k) depends only on (kind, alpha, m, k), and the steppers
+// call ihelm with the same alpha every step (and vec2tp calls idel2), so the LU factors are computed
+// once per key and every later call is a forward and a back substitution.  Per row j the cache
+// holds, [row][slot][system] so that a warp reads consecutive addresses:
+//   slot 0..KL-1     multipliers l(j+1..j+KL) (0 beyond the matrix)
+//   slot KL          pivot row offset p in 0..KL (gbtrf's ipiv(j) - j)
+//   slot KL+1        1 / U(j, j)
+//   slot KL+2 ..     U(j, j+1 .. j+KL+KU)
+constexpr int FKL = 2, FKU = 2, FSL = 2 * FKL + FKU + 2;
+
+__global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restrict__ fac) {
+  int sys = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sys >= a.nsys) return;
+  int m = sys / a.nzdim, k = sys % a.nzdim;
+  int nn = max(min(a.nrc, a.nrc - m), 0);
+  if (m >= a.npc || nn < 1 || k_count(k, a.nzc, a.nzcu, a.nzdim) == 0) return;
+  bool special = (m == 0 && k == 0) && a.kind == 1;
+  double akv = a.ak[k];
+  double alpha = (a.kind == 0) ? a.alpha : 0.0;
+  double e2 = a.ell * a.ell;
+  constexpr int WC = FKL + FKU + 1;
+  const size_t ns = a.nsys;
+  double W[FKL + 1][WC];
+#pragma unroll
+  for (int t = 0; t <= FKL; ++t)
+#pragma unroll
+    for (int c = 0; c < WC; ++c) W[t][c] = sys_entry(a, a.kind, special, m, akv, nn, alpha, e2, t, c);
+  for (int j = 0; j < nn; ++j) {
+    int km = min(FKL, nn - 1 - j);
+    int p = 0;
+    double best = fabs(W[0][0]);
+#pragma unroll
+    for (int t = 1; t <= FKL; ++t)
+      if (t <= km && fabs(W[t][0]) > best) { best = fabs(W[t][0]); p = t; }
+    if (best == 0.0) { atomicExch(a.status, 1); return; }
+#pragma unroll
+    for (int t = 1; t <= FKL; ++t)
+      if (t == p) {
+#pragma unroll
+        for (int c = 0; c < WC; ++c) { double q = W[0][c]; W[0][c] = W[t][c]; W[t][c] = q; }
+      }
+    double rp = 1.0 / W[0][0];
+    double* f = fac + (size_t)j * FSL * ns + sys;
+#pragma unroll
+    for (int t = 1; t <= FKL; ++t) {
+      double l = 0.0;
+      if (t <= km) {
+        l = W[t][0] * rp;
+#pragma unroll
+        for (int c = 1; c < WC; ++c) W[t][c] -= l * W[0][c];
+      }
+      f[(t - 1) * ns] = l;
+    }
+    f[FKL * ns] = (double)p;
+    f[(FKL + 1) * ns] = rp;
+#pragma unroll
+    for (int c = 1; c < WC; ++c) f[(FKL + 1 + c) * ns] = W[0][c];
+#pragma unroll
+    for (int t = 0; t < FKL; ++t) {
+#pragma unroll
+      for (int c = 0; c < WC - 1; ++c) W[t][c] = W[t + 1][c + 1];
+      W[t][WC - 1] = 0.0;
+    }
+    int nr_ = j + 1 + FKL;
+#pragma unroll
+    for (int c = 0; c < WC; ++c) W[FKL][c] = sys_entry(a, a.kind, special, m, akv, nn, alpha, e2, nr_, j + 1 + c);
+  }
+}
+
+// cp.async helpers (each thread copies only the words it later reads itself, so a wait_group on
+// the thread is enough and no block barrier is needed)
+__device__ __forceinline__ void cpa8(void* sdst, const void* gsrc, bool pred) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
+  int sz = pred ? 8 : 0;   // src-size 0 fills the destination with zeros
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
+}
+__device__ __forceinline__ void cpa16(void* sdst, const void* gsrc, bool pred) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
+  int sz = pred ? 16 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// forward and back substitution with the cached factors (gbtrs 'N', NRHS = 1), in place on the
+// column.  One warp = 32 systems; factor rows and right-hand-side values are staged into shared
+// memory SST groups ahead of use by cp.async, so DRAM latency overlaps the recurrences.
+constexpr int SGR = 8, SST = 3, SNU = FKL + FKU;
+struct SubstSmem {
+  double f[SST][SGR][SNU + 1][64];   // fwd: l1, l2, pivot; bwd: 1/U(j,j), U(j,j+1..j+4)
+  double v[SST][SGR][64];            // fwd: entering right-hand side; bwd: y(j)
+};
+
+// The matrices are real, so the real and imaginary parts of a right-hand side are two independent
+// real systems with the same factors: block = 64 threads, threads 0-31 take the real parts of 32
+// consecutive systems and threads 32-63 the imaginary parts (twice the warps in flight for the
+// serial recurrences).  Only the real-part thread of system (0,0) touches ln and the log terms,
+// which all act on real parts.
+__global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __restrict__ fac) {
+  extern __shared__ __align__(16) unsigned char subst_smem[];
+  SubstSmem& sm = *reinterpret_cast<SubstSmem*>(subst_smem);
+  int th = threadIdx.x;
+  int comp = th >> 5;
+  int sys = blockIdx.x * 32 + (th & 31);
+  bool valid = sys < a.nsys;
+  int m = valid ? sys / a.nzdim : 0, k = valid ? sys % a.nzdim : 0;
+  int cnt = valid ? k_count(k, a.nzc, a.nzcu, a.nzdim) : 0;
+  int nn = max(min(a.nrc, a.nrc - m), 0);
+  bool root = valid && (m == 0 && k == 0);
+  if (root && a.skip_root) cnt = 0;
+  if (root && comp == 0 && a.kind == 0 && !a.skip_root) {   // ihelm: so%ln = s%ln/alpha, log terms (:818-824)
+    double e2 = a.ell * a.ell;
+    double lno = *a.lnp / a.alpha;
+    *a.lnp = lno;
+    double2* g = a.e;
+    g[0].x -= 4.0 / 3.0 / e2 / exp(a.lognorm[0]) * lno;
+    g[1].x += 2.0 / 1.0 / e2 / exp(a.lognorm[1]) * lno;
+    g[2].x -= 2.0 / 3.0 / e2 / exp(a.lognorm[2]) * lno;
+  }
+  if (!valid || m >= a.npc || nn < 1) cnt = 0;
+  double* x = reinterpret_cast<double*>(a.e + (size_t)a.nrdim * (m + (size_t)a.npdim * k)) + comp;  // stride 2
+  const size_t ns = a.nsys;
+  int nnw = (cnt > 0) ? nn : 0;
+  for (int o = 16; o; o >>= 1) nnw = max(nnw, __shfl_xor_sync(0xffffffffu, nnw, o));
+  int cntw = cnt;
+  for (int o = 16; o; o >>= 1) cntw = max(cntw, __shfl_xor_sync(0xffffffffu, cntw, o));
+  int ng = (nnw + SGR - 1) / SGR;
+  const double* dummy = fac;
+  for (int rep = 0; rep < cntw; ++rep) {
+    bool act = rep < cnt;
+    auto issue_f = [&](int g) {
+      int st = g % SST;
+#pragma unroll
+      for (int u = 0; u < SGR; ++u) {
+        int jr = g * SGR + u;
+        bool ok = act && jr < nn;
+        const double* f = fac + (size_t)jr * FSL * ns + sys;
+#pragma unroll
+        for (int t = 0; t <= FKL; ++t) cpa8(&sm.f[st][u][t][th], ok ? f + t * ns : dummy, ok);
+        int jn = jr + 1 + FKL;
+        bool okx = act && jn < nn;
+        cpa8(&sm.v[st][u][th], okx ? (const void*)(x + 2 * jn) : (const void*)dummy, okx);
+      }
+    };
+    double r[FKL + 1];
+#pragma unroll
+    for (int t = 0; t <= FKL; ++t) r[t] = (act && t < nn) ? x[2 * t] : 0.0;
+    for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_f(g); cpa_commit(); }
+    for (int g = 0; g < ng; ++g) {
+      if (g + SST - 1 < ng) issue_f(g + SST - 1);
+      cpa_commit();
+      cpa_wait<SST - 1>();
+      int st = g % SST;
+#pragma unroll
+      for (int u = 0; u < SGR; ++u) {
+        int jr = g * SGR + u;
+        if (!act || jr >= nn) break;
+        double pv = sm.f[st][u][FKL][th];
+#pragma unroll
+        for (int t = 1; t <= FKL; ++t)
+          if (pv == (double)t) { double q = r[0]; r[0] = r[t]; r[t] = q; }
+#pragma unroll
+        for (int t = 1; t <= FKL; ++t) r[t] -= sm.f[st][u][t - 1][th] * r[0];
+        x[2 * jr] = r[0];
+#pragma unroll
+        for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
+        r[FKL] = sm.v[st][u][th];
+      }
+    }
+    cpa_wait<0>();
+    __threadfence_block();   // the y(j) just stored are read back below by this thread's cp.async
+    auto issue_b = [&](int g) {
+      int st = g % SST;
+#pragma unroll
+      for (int u = 0; u < SGR; ++u) {
+        int jr = nn - 1 - (g * SGR + u);
+        bool ok = act && jr >= 0;
+        const double* f = fac + (size_t)max(jr, 0) * FSL * ns + sys;
+#pragma unroll
+        for (int c = 0; c <= SNU; ++c) cpa8(&sm.f[st][u][c][th], ok ? f + (FKL + 1 + c) * ns : dummy, ok);
+        cpa8(&sm.v[st][u][th], ok ? (const void*)(x + 2 * jr) : (const void*)dummy, ok);
+      }
+    };
+    double xs[SNU];
+#pragma unroll
+    for (int c = 0; c < SNU; ++c) xs[c] = 0.0;
+    for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_b(g); cpa_commit(); }
+    for (int g = 0; g < ng; ++g) {
+      if (g + SST - 1 < ng) issue_b(g + SST - 1);
+      cpa_commit();
+      cpa_wait<SST - 1>();
+      int st = g % SST;
+#pragma unroll
+      for (int u = 0; u < SGR; ++u) {
+        int jr = nn - 1 - (g * SGR + u);
+        if (!act || jr < 0) break;
+        // y - U(j,j+1..j+4) . x(j+1..j+4), summed as a tree to shorten the dependency chain
+        double p1 = sm.f[st][u][1][th] * xs[0] + sm.f[st][u][2][th] * xs[1];
+        double p2 = sm.f[st][u][3][th] * xs[2] + sm.f[st][u][4][th] * xs[3];
+        double xj = (sm.v[st][u][th] - (p1 + p2)) * sm.f[st][u][0][th];
+        x[2 * jr] = xj;
+#pragma unroll
+        for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
+        xs[0] = xj;
+      }
+    }
+    cpa_wait<0>();
+    __threadfence_block();
+  }
+  if (root && comp == 0 && a.kind == 1 && !a.skip_root && cnt > 0) *a.lnp = x[0] * exp(a.lognorm[0]);
+}
+
+// the bordered (0,0) system of idel2_preln (KL = 3), single thread, after the batch
+__global__ void k_band_solve_special(SolveArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int nn = max(a.nrc, 0);
+  if (a.npc < 1 || nn < 1) return;
+  int cnt = k_count(0, a.nzc, a.nzcu, a.nzdim);
+  if (cnt == 0) return;
+  double e2 = pow(a.ell, 2.0);
+  double2* x = a.e;
+  for (int i = nn - 1; i >= 1; --i) x[i] = x[i - 1];
+  x[0] = make_double2(a.preln / exp(a.lognorm[0]), 0.0);
+  SolveArgs b = a;
+  b.nsys = 1;   // scratch rows of this single system are contiguous
+  for (int rep = 0; rep < cnt; ++rep) window_solve<3, 2>(b, 0, 2, true, 0, a.ak[0], nn, 0.0, e2, x);
+  *a.lnp = x[0].x * exp(a.lognorm[0]);
+}
+
 // ihelmp's log-term pre-step (mlegs_scalar_ops.f90:937-951): ln <- ln/alpha, then
 // e(:nrc,1,1) -= D(0,0)^(q-1) bl2 + beta bl2 with bl2 = (4/3, -2, 2/3)/ell^2/exp(lognorm) * ln.
 __global__ void k_ihelmp_pre(double2* __restrict__ e, double* __restrict__ lnp, const double* __restrict__ bd2,
@@ -310,13 +660,49 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
   return 0;
 }
 
+// LRU cache of factor sets, keyed by (kind, alpha, chop window)
+struct LUEntry {
+  int kind; double alpha; int nrc, npc, nzc, nzcu; double* buf; size_t bytes; unsigned long long used;
+};
+static std::vector<LUEntry> g_lu;
+static unsigned long long g_lu_clock = 0;
+static const size_t LU_MAX_ENTRIES = 4;
+
+void lu_cache_clear() {
+  for (auto& e : g_lu) dfree(e.buf, e.bytes);
+  g_lu.clear();
+}
+
+template <class F>
+static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsys, double** out, F factor) {
+  for (auto& e : g_lu)
+    if (e.kind == kind && e.alpha == alpha && e.nrc == c.nrc && e.npc == c.npc && e.nzc == c.nzc && e.nzcu == c.nzcu) {
+      e.used = ++g_lu_clock;
+      *out = e.buf;
+      return 0;
+    }
+  int nnmax = std::max(std::min(c.nrc, G.nrdim), 1);
+  size_t bytes = (size_t)nnmax * FSL * nsys * sizeof(double);
+  if (g_lu.size() >= LU_MAX_ENTRIES) {
+    auto it = std::min_element(g_lu.begin(), g_lu.end(), [](const LUEntry& x, const LUEntry& y) { return x.used < y.used; });
+    dfree(it->buf, it->bytes);
+    g_lu.erase(it);
+  }
+  LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock};
+  MLG_TRY(dmalloc((void**)&e.buf, bytes));
+  MLG_TRY(factor(e.buf));
+  g_lu.push_back(e);
+  *out = e.buf;
+  return 0;
+}
+
 // kind as in SolveArgs; the band scratch grows to fit (kl, ku)
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   int kl = 2, ku = 2;
   if (kind == 2) kl = 3;
   if (kind == 3) { kl = power; ku = power; }
-  int W = 2 * kl + ku + 1;
+  int W = std::max(2 * kl + ku + 1, kl + ku + 3);
   int npc = std::max(c.npc, 1);
   size_t nsys = (size_t)npc * G.nzdim;
   int nnmax = std::max(std::min(c.nrc, G.nrdim), 1);
@@ -333,10 +719,33 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
   a.status = (int*)(G.dscal + DS_FLAG + 1);
   a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
   a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = beta; a.ell = G.ell; a.preln = preln;
-  a.kind = kind; a.power = power;
+  a.kind = kind; a.power = power; a.skip_root = 0;
   kt_begin(2);
-  k_band_solve<<<cdiv(nsys, 64), 64, 0, G.stream>>>(a);
-  MLG_LAUNCH();
+  if (kind == 3) {
+    k_band_solve<<<cdiv(nsys, 64), 64, 0, G.stream>>>(a);
+    MLG_LAUNCH();
+  } else {
+    // kinds 0 and 1 (and the batch of kind 2): cached factors, substitution only; the bordered
+    // (0,0) system of kind 2 is skipped by the batch and solved on its own afterwards
+    int fkind = (kind == 2) ? 1 : kind;
+    double* fac = nullptr;
+    SolveArgs b = a;
+    b.kind = fkind;
+    b.skip_root = (kind == 2) ? 1 : 0;
+    MLG_TRY(lu_cache_get(fkind, alpha, c, nsys, &fac, [&](double* buf) -> int {
+      k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(b, buf);
+      MLG_LAUNCH();
+      return 0;
+    }));
+    size_t smb = sizeof(SubstSmem);
+    MLG_CUDA(cudaFuncSetAttribute(k_band_subst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    k_band_subst<<<cdiv(nsys, 32), 64, smb, G.stream>>>(b, fac);
+    MLG_LAUNCH();
+    if (kind == 2) {
+      k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
+      MLG_LAUNCH();
+    }
+  }
   kt_end(2, 2.0 * G.fsize * 16);
   return 0;
 }

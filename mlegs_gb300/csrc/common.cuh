@@ -18,7 +18,7 @@ int set_error(int code, const std::string& msg);
 #define MLG_TRY(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 #define MLG_CUDA(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) \
     return ::mlg::set_error(MLG_ECUDA, std::string(#x) + ": " + cudaGetErrorString(_e)); } while (0)
-#define MLG_LAUNCH() do { cudaError_t _e = cudaGetLastError(); if (_e != cudaSuccess) \
+#define MLG_LAUNCH() do { ++::mlg::G.launches; cudaError_t _e = cudaGetLastError(); if (_e != cudaSuccess) \
     return ::mlg::set_error(MLG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(_e)); } while (0)
 
 // ---------------------------------------------------------------------------------------------
@@ -37,11 +37,12 @@ struct Scalar {
 struct ChopIdx { int nrc, npc, nzc, nzcu; };
 
 // kernel-time accounting per kernel class (mlg_kernel_timing)
+enum { KT_RFWD = 0, KT_FFT = 1, KT_BAND = 2, KT_RBWD = 3, KT_V2TP = 4, KT_N = 5 };
 struct KTimer {
   bool on = false;
-  double ms[3] = {0, 0, 0};
-  long long n[3] = {0, 0, 0};
-  double work[3] = {0, 0, 0};
+  double ms[KT_N] = {0, 0, 0, 0, 0};
+  long long n[KT_N] = {0, 0, 0, 0, 0};
+  double work[KT_N] = {0, 0, 0, 0, 0};
 };
 
 struct Ctx {
@@ -55,7 +56,8 @@ struct Ctx {
   cudaStream_t stream = 0;
 
   // kit arrays on the device
-  double *x = nullptr, *w = nullptr, *r = nullptr, *lnx = nullptr, *ak = nullptr;
+  double *x = nullptr, *w = nullptr, *r = nullptr, *rinv = nullptr, *lnx = nullptr, *ak = nullptr;
+  bool svv_q_ready = false;
   double *lognorm = nullptr;   // (ne, npchop)
   double *pf = nullptr;        // (nrh, ne, npchop): P_L^m(x_i) normalised, reference layout
   float *pf32 = nullptr;       // FP32 copy of pf for the mixed form
@@ -79,6 +81,7 @@ struct Ctx {
   std::vector<cd*> all_bufs;
 
   long long mem_bytes = 0, mem_high = 0;
+  long long launches = 0;     // kernels launched by the library since mlg_init
   KTimer kt;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -110,6 +113,7 @@ int launch_vfft_buf(cd* e, int dir);
 int launch_rtrans_fwd(Scalar& s);
 int launch_rtrans_bwd(Scalar& s, bool add_ln);
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
+void lu_cache_clear();
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
 
 // pointwise

@@ -74,8 +74,9 @@ __device__ dd dd_exp2k(dd a, int* kout) {
   dd r = dd_sub(a, dd_mul_d(LN2, kd));
   r = dd_ldexp(r, -10);
   dd s = {1.0, 0.0};
-  for (int n = 12; n >= 1; --n) s = dd_add({1.0, 0.0}, dd_mul(dd_div_d(r, (double)n), s));
-  s = dd_mul(r, s);  // e^r - 1
+  // e^r - 1 = r (1 + r/2 (1 + r/3 (1 + ... (1 + r/13))))
+  for (int n = 13; n >= 2; --n) s = dd_add({1.0, 0.0}, dd_mul(dd_div_d(r, (double)n), s));
+  s = dd_mul(r, s);
   for (int i = 0; i < 10; ++i) s = dd_add(dd_mul_d(s, 2.0), dd_mul(s, s));
   *kout = (int)kd;
   return dd_add({1.0, 0.0}, s);
@@ -312,7 +313,9 @@ int kit_build(const mlg_params* P) {
   std::vector<double> logfact(nlf);
   for (int m = 0; m < nlf; ++m) logfact[m] = std::lgamma(2 * m + 1.0) - m * std::log(2.0) - std::lgamma(m + 1.0);
 
-  MLG_TRY(upload(&G.x, x)); MLG_TRY(upload(&G.w, w)); MLG_TRY(upload(&G.r, r));
+  std::vector<double> rinv(nr);
+  for (int i = 0; i < nr; ++i) rinv[i] = 1.0 / r[i];
+  MLG_TRY(upload(&G.x, x)); MLG_TRY(upload(&G.w, w)); MLG_TRY(upload(&G.r, r)); MLG_TRY(upload(&G.rinv, rinv));
   MLG_TRY(upload(&G.lnx, lnx)); MLG_TRY(upload(&G.ak, ak)); MLG_TRY(upload(&G.lognorm, lognorm));
   double* d_logfact = nullptr;
   MLG_TRY(upload(&d_logfact, logfact));

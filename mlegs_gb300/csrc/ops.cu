@@ -92,7 +92,7 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 
 // ------------------------------------------------------------------------------------------------
 // pointwise kernels
-#define GRID_STRIDE(i, n) for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (n); i += (size_t)gridDim.x * blockDim.x)
+#define GRID_STRIDE(i, n) for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < (unsigned)(n); i += gridDim.x * blockDim.x)
 static inline int nblk(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 // chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
@@ -100,9 +100,9 @@ __global__ void k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim,
                        int nrc, int npc, int nzc, int nzcu, int pcut, int zcut, int zupper, int np_gt1, int nz_gt1) {
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
-    int k = (int)(idx / ((size_t)nrdim * npdim));
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    int k = (int)(idx / (unsigned)(nrdim * npdim));
     bool z = false;
     if (mode == 0) {
       int nrcs = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
@@ -124,8 +124,8 @@ __global__ void k_ln_adjust(double2* __restrict__ e, const double* __restrict__ 
   if (l == 0.0) return;
   size_t n = (size_t)nr * nzdim;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nr);
-    int k = (int)(idx / nr);
+    int i = (int)(idx % (unsigned)nr);
+    int k = (int)(idx / (unsigned)nr);
     e[i + (size_t)nrdim * npdim * k].x += sgn * l * lnx[i];
   }
 }
@@ -184,15 +184,15 @@ __global__ void k_add_ln_x(double2* __restrict__ e, const double* __restrict__ l
   for (int i = threadIdx.x; i < nr; i += blockDim.x) e[i].x += l * (1.0 + x[i]);
 }
 
-// e(:nr, :, :) *= r  (mode 0) or /= r (mode 1)
-__global__ void k_scale_r(double2* __restrict__ e, const double* __restrict__ r, int nr, int nrdim, size_t ncol, int mode) {
+// e(:nr, :, :) *= r (rows scaled by the table passed: r, or 1/r for the division of tp2vec)
+__global__ void k_scale_r(double2* __restrict__ e, const double* __restrict__ r, int nr, int nrdim, size_t ncol) {
   size_t n = (size_t)nr * ncol;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nr);
-    size_t c = idx / nr;
+    int i = (int)(idx % (unsigned)nr);
+    unsigned c = idx / (unsigned)nr;
     double2* p = e + i + (size_t)nrdim * c;
     double v = r[i];
-    if (mode == 0) { p->x *= v; p->y *= v; } else { p->x /= v; p->y /= v; }
+    p->x *= v; p->y *= v;
   }
 }
 
@@ -202,8 +202,8 @@ __global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, do
                           int nr, int nph, int nrdim, int npdim, int nzdim) {
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
     double2 o1 = make_double2(0, 0), o2 = o1, o3 = o1;
     if (i < nr && m < nph) {
       double2 A1 = vr[idx], A2 = vp[idx], A3 = vz[idx], B1 = ur[idx], B2 = up[idx], B3 = uz[idx];
@@ -215,29 +215,33 @@ __global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, do
   }
 }
 
-// svv_filter (mlegs_scalar_ops.f90:72-155): block partial sums of |e|^2 and of the tail energy
-__device__ __forceinline__ double svv_q(int i, int m, int k, int nrchop, int np, double kmax, const double* ak, int nak) {
-  double q_r = fmin(1.0, (double)max(i, 0) / fmax((double)(nrchop - 1), 1.0));
-  double q_p = fmin(1.0, (double)abs(m) / fmax((double)(np / 2), 1.0));
+// svv_filter (mlegs_scalar_ops.f90:72-155).  q = min(1, max(q_r(n), q_p(m), q_z(k))) with cutoff < 1,
+// so "q >= cutoff" is "any of the three >= cutoff", and since the filter exp(-s*shape(q)^8) decreases
+// in q, its value at the maximum is the minimum of its values at q_r, q_p, q_z: the per-element work
+// reduces to 1-D tables (filled once per call) and a min.
+__device__ __forceinline__ double svv_qr(int i, int nrchop) {
+  return fmin(1.0, (double)max(i, 0) / fmax((double)(nrchop - 1), 1.0));
+}
+__device__ __forceinline__ double svv_qp(int m, int np) { return fmin(1.0, (double)abs(m) / fmax((double)(np / 2), 1.0)); }
+__device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, double kmax) {
   int gk = k + 1;
   double kv = (gk >= 1 && gk <= nak) ? fabs(ak[k]) : 0.0;
-  double q_z = fmin(1.0, kv / kmax);
-  return fmin(1.0, fmax(q_r, fmax(q_p, q_z)));
+  return fmin(1.0, kv / kmax);
 }
-__global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
-                           const double* __restrict__ ak, double cutoff, double* __restrict__ partial) {
+__global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ qt,
+                           double cutoff, double* __restrict__ partial) {
   __shared__ double s0[256], s1[256];
   size_t n = (size_t)nrdim * npdim * nzdim;
   double tot = 0, tail = 0;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
-    int k = (int)(idx / ((size_t)nrdim * npdim));
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    int k = (int)(idx / (unsigned)(nrdim * npdim));
     double2 v = e[idx];
-    double a = hypot(v.x, v.y);
-    double a2 = a * a;
+    double a2 = v.x * v.x + v.y * v.y;
     tot += a2;
-    if (svv_q(i, m, k, nrchop, np, kmax, ak, nzdim) >= cutoff) tail += a2;
+    double q = fmin(1.0, fmax(qt[i], fmax(qt[nrdim + m], qt[nrdim + npdim + k])));
+    if (q >= cutoff) tail += a2;
   }
   s0[threadIdx.x] = tot; s1[threadIdx.x] = tail;
   __syncthreads();
@@ -247,35 +251,61 @@ __global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, 
   }
   if (threadIdx.x == 0) { partial[2 * blockIdx.x] = s0[0]; partial[2 * blockIdx.x + 1] = s1[0]; }
 }
-// gain relaxation and strength (:119-126); st[0] = strength (0: nothing to do)
+// gain relaxation and strength (:119-126); st[0] = strength (0: nothing to do); then the 1-D factor
+// tables ft[0..nrdim) (n), ft[nrdim..+npdim) (m), ft[..+nzdim) (k): exp(-s*shape^8) where q > cutoff, 1 elsewhere
 __global__ void k_svv_gain(const double* __restrict__ partial, int nb, double* __restrict__ gain, double* __restrict__ st,
-                           double target, double relax, double strength_max) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double tot = 0, tail = 0;
-  for (int b = 0; b < nb; ++b) { tot += partial[2 * b]; tail += partial[2 * b + 1]; }
-  st[0] = 0.0;
-  if (tot <= 2.2250738585072014e-308) return;
-  double ratio = tail / tot;
-  double fb = fmin(fmax(ratio / target - 1.0, 0.0), 1.0);
-  double rl = fmin(fmax(relax, 0.0), 1.0);
-  double g = (1.0 - rl) * (*gain) + rl * fb;
-  *gain = g;
-  st[0] = fmin(fmax(strength_max, 0.0) * g, 1.0);
-}
-__global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
-                            const double* __restrict__ ak, double cutoff, const double* __restrict__ st) {
-  double strength = st[0];
-  if (strength <= 0.0) return;
-  size_t n = (size_t)nrdim * npdim * nzdim;
-  GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
-    int k = (int)(idx / ((size_t)nrdim * npdim));
-    double q = svv_q(i, m, k, nrchop, np, kmax, ak, nzdim);
-    if (q > cutoff) {
+                           double target, double relax, double strength_max, double* __restrict__ ft, int nrdim, int npdim,
+                           int nzdim, int nrchop, int np, double kmax, const double* __restrict__ ak, double cutoff) {
+  __shared__ double str;
+  if (threadIdx.x == 0) {
+    double tot = 0, tail = 0;
+    for (int b = 0; b < nb; ++b) { tot += partial[2 * b]; tail += partial[2 * b + 1]; }
+    double sv = 0.0;
+    if (tot > 2.2250738585072014e-308) {
+      double ratio = tail / tot;
+      double fb = fmin(fmax(ratio / target - 1.0, 0.0), 1.0);
+      double rl = fmin(fmax(relax, 0.0), 1.0);
+      double g = (1.0 - rl) * (*gain) + rl * fb;
+      *gain = g;
+      sv = fmin(fmax(strength_max, 0.0) * g, 1.0);
+    }
+    st[0] = sv;
+    str = sv;
+  }
+  __syncthreads();
+  double sv = str;
+  int ntot = nrdim + npdim + nzdim;
+  for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+    double q = (t < nrdim) ? svv_qr(t, nrchop) : (t < nrdim + npdim) ? svv_qp(t - nrdim, np)
+                                                                       : svv_qz(t - nrdim - npdim, ak, nzdim, kmax);
+    q = fmin(1.0, q);
+    double f = 1.0;
+    if (sv > 0.0 && q > cutoff) {
       double shape = (q - cutoff) / (1.0 - cutoff);
       double s2 = shape * shape, s4 = s2 * s2;
-      double f = exp(-strength * (s4 * s4));
+      f = exp(-sv * (s4 * s4));
+    }
+    ft[t] = f;
+  }
+}
+// q_r, q_p, q_z of every row, azimuthal slot and axial slot (:96-110), filled once
+__global__ void k_svv_qtab(double* __restrict__ qt, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
+                           const double* __restrict__ ak) {
+  int ntot = nrdim + npdim + nzdim;
+  for (int t = threadIdx.x; t < ntot; t += blockDim.x)
+    qt[t] = (t < nrdim) ? svv_qr(t, nrchop) : (t < nrdim + npdim) ? svv_qp(t - nrdim, np)
+                                                                 : svv_qz(t - nrdim - npdim, ak, nzdim, kmax);
+}
+__global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ st,
+                            const double* __restrict__ ft) {
+  if (st[0] <= 0.0) return;
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    int k = (int)(idx / (unsigned)(nrdim * npdim));
+    double f = fmin(ft[i], fmin(ft[nrdim + m], ft[nrdim + npdim + k]));
+    if (f != 1.0) {
       double2 v = e[idx];
       e[idx] = make_double2(f * v.x, f * v.y);
     }
@@ -287,10 +317,10 @@ __global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int n
 __global__ void k_delsqp(double2* __restrict__ e, const double* __restrict__ lnp, const double* __restrict__ lognorm,
                          int inverse, int nrdim, int npdim, int nzdim, int nrc, int npc, double ell) {
   size_t n = (size_t)nrdim * npdim * nzdim;
-  double e2 = pow(ell, 2.0);
+  double e2 = ell * ell;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
     int nrcs = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
     double2 v = e[idx];
     if (i < nrcs) {
@@ -318,6 +348,13 @@ __global__ void k_idelsqp_ln(const double2* __restrict__ e, double* __restrict__
 __global__ void k_ln_zero(double* __restrict__ lnp) { if (threadIdx.x == 0) *lnp = 0.0; }
 __global__ void k_ln_set(double* __restrict__ lnp, double v) { if (threadIdx.x == 0) *lnp = v; }
 __global__ void k_ln_copy(double* __restrict__ d, const double* __restrict__ s) { if (threadIdx.x == 0) *d = *s; }
+
+// field copy that also carries the ln slot (assignment(=), mlegs_scalar_init.f90:106-140)
+__global__ void k_copy_scalar(double2* __restrict__ d, const double2* __restrict__ s, size_t n, double* __restrict__ dln,
+                              const double* __restrict__ sln) {
+  GRID_STRIDE(idx, n) d[idx] = s[idx];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *dln = *sln;
+}
 
 __global__ void k_finite(const double2* __restrict__ a, const double2* __restrict__ b, size_t n, int* __restrict__ flag) {
   GRID_STRIDE(idx, n) {
@@ -374,7 +411,7 @@ static int alloc_slot() {
 }
 static void free_slot(int s) { if (s >= 0) G.free_slots.push_back(s); }
 
-static int scalar_init(Scalar& s) {   // scalar_init (mlegs_scalar_init.f90:6-67): space PPP
+static int scalar_init(Scalar& s, bool zero_ln = true) {   // scalar_init (mlegs_scalar_init.f90:6-67): space PPP
   s.e = get_buf();
   if (!s.e) return set_error(MLG_EALLOC, "scalar_init: out of device memory");
   s.slot = alloc_slot();
@@ -382,7 +419,7 @@ static int scalar_init(Scalar& s) {   // scalar_init (mlegs_scalar_init.f90:6-67
   s.ln = G.ln_slots + s.slot;
   s.set_space("PPP");
   s.off[0] = s.off[1] = s.off[2] = 0;
-  MLG_TRY(launch_set_ln(s.ln, 0.0));
+  if (zero_ln) MLG_TRY(launch_set_ln(s.ln, 0.0));
   return 0;
 }
 static void scalar_release(Scalar& s) {
@@ -394,8 +431,12 @@ static void scalar_release(Scalar& s) {
 }
 // scalar_copy (mlegs_scalar_init.f90:106-140)
 static int assign(Scalar& d, const Scalar& s) {
-  MLG_TRY(launch_copy(d.e, s.e));
-  MLG_TRY(launch_copy_ln(d.ln, s.ln));
+  if (d.e != s.e) {
+    k_copy_scalar<<<nblk(G.fsize), 256, 0, G.stream>>>(d.e, s.e, G.fsize, d.ln, s.ln);
+    MLG_LAUNCH();
+  } else {
+    MLG_TRY(launch_copy_ln(d.ln, s.ln));
+  }
   std::memcpy(d.space, s.space, 4);
   for (int i = 0; i < 3; ++i) d.off[i] = s.off[i];
   return 0;
@@ -404,7 +445,7 @@ static int assign(Scalar& d, const Scalar& s) {
 struct Tmp {
   Scalar s;
   int rc = 0;
-  Tmp() { rc = scalar_init(s); }
+  Tmp() { rc = scalar_init(s, false); }   // every temporary is assigned (e and ln) before it is read
   ~Tmp() { if (s.e) scalar_release(s); }
 };
 #define TMP(name) Tmp name##_t; if (name##_t.rc) return name##_t.rc; Scalar& name = name##_t.s
@@ -489,12 +530,21 @@ int op_svv_filter_dev(Scalar& s, double* gain_dev) {
   }
   const int NB = 304;
   double* partial = G.dscal + DS_CALC + 2 * 2048;
-  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff, partial);
+  double* ft = G.dscal + DS_CALC + 2 * 2048 + 2 * NB;
+  if (2 * (G.nrdim + G.npdim + G.nzdim) > DS_COUNT - (DS_CALC + 2 * 2048 + 2 * NB))
+    return set_error(MLG_ESIZE, "svv_filter: grid too large for the filter tables");
+  double* qt = ft + (G.nrdim + G.npdim + G.nzdim);
+  if (!G.svv_q_ready) {
+    k_svv_qtab<<<1, 256, 0, G.stream>>>(qt, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak);
+    MLG_LAUNCH();
+    G.svv_q_ready = true;
+  }
+  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, qt, cutoff, partial);
   MLG_LAUNCH();
-  k_svv_gain<<<1, 32, 0, G.stream>>>(partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength);
+  k_svv_gain<<<1, 256, 0, G.stream>>>(partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength,
+                                      ft, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff);
   MLG_LAUNCH();
-  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff,
-                                                    G.dscal + DS_SUM0);
+  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.dscal + DS_SUM0, ft);
   MLG_LAUNCH();
   return 0;
 }
@@ -716,7 +766,7 @@ int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scala
 
 static int scale_r(Scalar& s, int mode) {
   size_t ncol = (size_t)G.npdim * G.nzdim;
-  k_scale_r<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, G.r, G.nr, G.nrdim, ncol, mode);
+  k_scale_r<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, mode == 0 ? G.r : G.rinv, G.nr, G.nrdim, ncol);
   MLG_LAUNCH();
   return 0;
 }
@@ -761,9 +811,9 @@ __global__ void k_tp2vec_mix(double2* __restrict__ ur, double2* __restrict__ up,
                              int nrc, int npc, int nzc, int nzcu) {
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
-    int i = (int)(idx % nrdim);
-    int m = (int)((idx / nrdim) % npdim);
-    int k = (int)(idx / ((size_t)nrdim * npdim));
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    int k = (int)(idx / (unsigned)(nrdim * npdim));
     if (m >= npc) continue;
     int nn = max(min(nrc, nrc - m), 0);
     int kk = k + 1;
@@ -880,8 +930,9 @@ int mlg_init(const mlg_params* p) {
 int mlg_finalize(void) {
   if (!G.kit_set) return 0;
   cudaStreamSynchronize(G.stream);
+  lu_cache_clear();
   for (cd* b : G.all_bufs) cudaFree(b);
-  void* arrs[] = {G.x, G.w, G.r, G.lnx, G.ak, G.lognorm, G.pf, G.pf32, G.at0, G.at1, G.bd2, G.bxx, G.tV, G.tD, G.tT,
+  void* arrs[] = {G.x, G.w, G.r, G.rinv, G.lnx, G.ak, G.lognorm, G.pf, G.pf32, G.at0, G.at1, G.bd2, G.bxx, G.tV, G.tD, G.tT,
                   G.tV32, G.tD32, G.tT32, G.tw_p, G.tw_z, G.tw_pr, G.ln_slots, G.dscal, G.band_ws};
   for (void* a : arrs) if (a) cudaFree(a);
   cudaStream_t st = G.stream;
@@ -940,6 +991,7 @@ int mlg_sync(void) {
 }
 long long mlg_mem_bytes(void) { return G.mem_bytes; }
 long long mlg_mem_high_water(void) { return G.mem_high; }
+long long mlg_launch_count(void) { return G.launches; }
 
 int mlg_scalar_alloc(mlg_scalar* out) {
   NEED_KIT();
@@ -1111,11 +1163,11 @@ int mlg_vortex_run(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_s
 
 int mlg_kernel_timing(int enable) {
   G.kt.on = enable != 0;
-  for (int i = 0; i < 3; ++i) { G.kt.ms[i] = 0; G.kt.n[i] = 0; G.kt.work[i] = 0; }
+  for (int i = 0; i < KT_N; ++i) { G.kt.ms[i] = 0; G.kt.n[i] = 0; G.kt.work[i] = 0; }
   return 0;
 }
 int mlg_kernel_timing_read(int kind, double* ms, long long* n, double* work) {
-  if (kind < 0 || kind > 2) return set_error(MLG_EPARAM, "mlg_kernel_timing_read: kind 0..2");
+  if (kind < 0 || kind >= KT_N) return set_error(MLG_EPARAM, "mlg_kernel_timing_read: kind 0..4");
   if (ms) *ms = G.kt.ms[kind];
   if (n) *n = G.kt.n[kind];
   if (work) *work = G.kt.work[kind];

@@ -297,7 +297,7 @@ int launch_rtrans_fwd(Scalar& s) {
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
   MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
-  kt_begin(0);
+  kt_begin(KT_RFWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
       constexpr int MT = 32, ZT = 64, KC = 32, MPT = 2, ZPT = 4;
@@ -314,7 +314,7 @@ int launch_rtrans_fwd(Scalar& s) {
     }
     MLG_LAUNCH();
   }
-  kt_end(0, fwd_flops(nrc, npc));
+  kt_end(KT_RFWD, fwd_flops(nrc, npc));
   put_buf(s.e);
   s.e = out;
   return 0;
@@ -326,7 +326,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_backward: out of device memory");
   MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
-  kt_begin(0);
+  kt_begin(KT_RBWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
       constexpr int IT = 32, ZT = 64, KC = 16, IPT = 2, ZPT = 4;
@@ -341,7 +341,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
     }
     MLG_LAUNCH();
   }
-  kt_end(0, fwd_flops(nrc, npc));
+  kt_end(KT_RBWD, fwd_flops(nrc, npc));
   put_buf(s.e);
   s.e = out;
   return 0;
@@ -352,7 +352,7 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int nrc = G.nrchop + nrc_off, npc = G.npchop;
   int nzc = G.chopzl, nzcu = G.chopzu;
   if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
-  kt_begin(0);
+  kt_begin(KT_V2TP);
   constexpr int MT = 16, ZT = 32, KC = 16, ZPT = 4;
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
@@ -363,7 +363,7 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
     k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
                                                                    G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
   MLG_LAUNCH();
-  kt_end(0, 5.0 * fwd_flops(nrc, npc));
+  kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
   return 0;
 }
 

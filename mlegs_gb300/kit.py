@@ -36,6 +36,7 @@ def load(path=None):
     L.mlg_last_error.restype = ctypes.c_char_p
     L.mlg_mem_bytes.restype = ctypes.c_longlong
     L.mlg_mem_high_water.restype = ctypes.c_longlong
+    L.mlg_launch_count.restype = ctypes.c_longlong
     L.mlg_scalar_device_ptr.restype = _P
     L.mlg_scalar_device_ptr.argtypes = [_P]
     sig = {
@@ -169,6 +170,9 @@ class Kit:
 
     def mem_high_water(self):
         return load().mlg_mem_high_water()
+
+    def launch_count(self):
+        return load().mlg_launch_count()
 
     def kit_get(self, name):
         sizes = {"x": self.nr, "w": self.nr, "r": self.nr, "ln": self.nr, "ak": self.dims[2],

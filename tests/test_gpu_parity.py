@@ -13,6 +13,9 @@ from helpers import CONFIGS, params, compare, rel_l2
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+# Poisson solves (idel2) are not diagonally dominant: their condition number (~1e4 at these sizes)
+# multiplies the rounding difference between two correct FP64 evaluations.
+TOL_POISSON = 1e-11
 
 
 @pytest.fixture(scope="module", params=["c1", "t2d", "odd", "hyp"])
@@ -88,7 +91,7 @@ def test_single_operator(pair, op):
             assert abs(g1 - g2) <= 1e-14 * max(1.0, abs(g2)), (g1, g2)
         else:
             getattr(k, op)(gs); getattr(o, op)(os_)
-        compare(gs, os_, TOL, what=f"{name} {op} ln={ln}")
+        compare(gs, os_, TOL_POISSON if op.startswith("idel2") else TOL, what=f"{name} {op} ln={ln}")
 
 
 def test_chop_offset_and_partial_space(pair):
@@ -127,9 +130,11 @@ def test_powered_helmholtz(pair, op):
     name, k, o = pair
     p = k.params
     c = fff_input(p, k.dims, 51)
+    # alpha = -2/(dt*hypervisc) as the steppers use it (dt = 1e-3, hypervisc = 1e-6): the identity
+    # term dominates, as in every hyperviscous step of the reference
     for power in (4, 6, 8):
         gs, os_ = both(k, o, c, 0.2, "FFF")
-        getattr(k, op)(gs, power, -2.0e3, 0.5); getattr(o, op)(os_, power, -2.0e3, 0.5)
+        getattr(k, op)(gs, power, -2.0e9, 0.5); getattr(o, op)(os_, power, -2.0e9, 0.5)
         compare(gs, os_, 1e-11, what=f"{name} {op} p={power}")
 
 
