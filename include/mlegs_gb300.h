@@ -5,7 +5,7 @@
  * (module mlegs_scalar, src/modules/mlegs_scalar.f90:95-450, and the kit initialiser
  * tfm_kit_init, src/submodules/mlegs_spectfm_init.f90:6-154).  The Fortran side binds these
  * through ISO_C_BINDING (interface module include/mlegs_gb300_iface.f90); Python binds them
- * through ctypes (mlegs_gb300/_lib.py).
+ * through ctypes (mlegs_gb300/kit.py).
  *
  * Conventions
  *  - A field ("scalar") is an opaque handle owning a device-resident complex128 array of
