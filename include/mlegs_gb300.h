@@ -126,6 +126,16 @@ int mlg_idel2_preln(mlg_scalar s, double preln);            /* :575-669  */
 int mlg_idel2_proln(mlg_scalar s);                          /* :671-760  */
 int mlg_helm(mlg_scalar s, double alpha);                   /* :762-789  */
 int mlg_ihelm(mlg_scalar s, double alpha);                  /* :791-854  */
+/* ihelm without any device allocation; no counterpart in the reference.  For callers whose host
+ * owns all device memory (a fixed arena or its own allocator) or that forbid allocation inside
+ * their step loop.  e_dev: caller-owned device field (nrdim, npdim, nzdim) complex128 in FFF space
+ * with zero chop offsets, solved in place; *ln: the field's ln on input, ln/alpha on output.  The
+ * only workspace is a fixed 16 MiB device array inside the library (held by every GPU that loads
+ * it); radial systems are processed in batches that fit it, and a single system that does not fit
+ * is rejected with MLG_ESIZE.  The first call with a given device current looks up that array's
+ * device address; make that call before any stream capture.  Calls that overlap on the GPU share
+ * the array and race. */
+int mlg_ihelm_noalloc(void* e_dev, double* ln, double alpha);
 int mlg_helmp(mlg_scalar s, int power, double alpha, double beta);   /* :856-903  */
 int mlg_ihelmp(mlg_scalar s, int power, double alpha, double beta);  /* :905-1000 */
 

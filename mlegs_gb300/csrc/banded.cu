@@ -660,6 +660,83 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
   return 0;
 }
 
+// ------------------------------------------------------------------------------------------------
+// Helmholtz solve that allocates nothing (mlg_ihelm_noalloc).
+//
+// Some callers cannot let a library call cudaMalloc: Fortran or C hosts whose own device allocator
+// or fixed arena owns all GPU memory (an extra cudaMalloc would fail or fragment it), and codes that
+// forbid device allocation inside their time-stepping loop.  For them this variant of the ihelm
+// solve keeps its only workspace (the U rows of the on-the-fly band LU) in the fixed-size device
+// array below, present on every GPU that loads the library until the process exits.  Systems are
+// processed in batches that fit it, so any grid size works; a single system larger than the array
+// is rejected.  All calls share the array: calls that overlap on the GPU (other streams, other host
+// threads) race on it.  Every word a launch reads was written earlier by the same launch, so nothing
+// needs clearing between calls.
+constexpr size_t NOALLOC_DOUBLES = 2u << 20;   // 16 MiB
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
+
+__global__ void __launch_bounds__(32) k_ihelm_noalloc(SolveArgs a, int s0, int batch, double lno) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = s0 + b;
+  if (b >= batch || sys >= a.nsys) return;
+  int m = sys / a.nzdim, k = sys % a.nzdim;
+  int cnt = k_count(k, a.nzc, a.nzcu, a.nzdim);
+  int nn = max(min(a.nrc, a.nrc - m), 0);
+  double e2 = a.ell * a.ell;
+  if (sys == 0) {   // so%ln = s%ln/alpha is lno; its log terms on e(1..3,1,1) (:818-824)
+    double2* g = a.e;
+    g[0].x -= 4.0 / 3.0 / e2 / exp(a.lognorm[0]) * lno;
+    g[1].x += 2.0 / 1.0 / e2 / exp(a.lognorm[1]) * lno;
+    g[2].x -= 2.0 / 3.0 / e2 / exp(a.lognorm[2]) * lno;
+  }
+  if (m >= a.npc || nn < 1 || cnt == 0) return;
+  double2* x = a.e + (size_t)a.nrdim * (m + (size_t)a.npdim * k);
+  SolveArgs w = a;
+  w.nsys = batch;   // scratch rows are laid out [row][slot][batch]
+  for (int rep = 0; rep < cnt; ++rep) window_solve<2, 2>(w, b, 0, false, m, a.ak[k], nn, a.alpha, e2, x);
+}
+
+// per-device address of g_noalloc_scratch, looked up on the first call made with that device current
+static double* g_noalloc_ptr[64] = {nullptr};
+
+int ihelm_noalloc(void* e_dev, double* ln, double alpha) {
+  int dev = 0;
+  MLG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(MLG_ESIZE, "ihelm_noalloc: device index beyond 63");
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return set_error(MLG_ECUDA, std::string("ihelm_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = (double*)ptr;
+  }
+  if (std::fabs(alpha) < 5.0e-14)
+    return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
+  int nrc = G.nrchop, npc = G.npchop;
+  int nnmax = std::max(std::min(nrc, G.nrdim), 1);
+  constexpr int SL = 2 + 2 + 1 + 2;   // U row (5) + complex right-hand side (2), as in window_solve<2,2>
+  size_t per_sys = (size_t)nnmax * SL;
+  size_t batch = NOALLOC_DOUBLES / per_sys;
+  if (batch < 1)
+    return set_error(MLG_ESIZE, "ihelm_noalloc: one radial system (" + std::to_string(nnmax) +
+                                    " rows) exceeds the fixed 16 MiB workspace");
+  size_t nsys = (size_t)npc * G.nzdim;
+  double lno = *ln / alpha;
+  SolveArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.e = (double2*)e_dev; a.ws = g_noalloc_ptr[dev]; a.lnp = nullptr; a.bd2 = G.bd2; a.ak = G.ak; a.lognorm = G.lognorm;
+  a.status = (int*)(G.dscal + DS_FLAG + 1);
+  a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = nrc; a.npc = npc; a.nzc = G.chopzl; a.nzcu = G.chopzu;
+  a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.ell = G.ell; a.kind = 0;
+  for (size_t s0 = 0; s0 < nsys; s0 += batch) {
+    int nb = (int)std::min(batch, nsys - s0);
+    k_ihelm_noalloc<<<cdiv(nb, 32), 32, 0, G.stream>>>(a, (int)s0, nb, lno);
+    MLG_LAUNCH();
+  }
+  *ln = lno;
+  return 0;
+}
+
 // LRU cache of factor sets, keyed by (kind, alpha, chop window)
 struct LUEntry {
   int kind; double alpha; int nrc, npc, nzc, nzcu; double* buf; size_t bytes; unsigned long long used;

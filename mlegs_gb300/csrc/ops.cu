@@ -468,6 +468,8 @@ static int vfft_checked(Scalar& s, int dir) {
 }
 
 // trans (:157-235)
+int ihelm_noalloc(void* e_dev, double* ln, double alpha);
+
 int op_trans(Scalar& s, const char* space) {
   int cur = space_code(s.space);
   if (cur < 0) return set_error(MLG_ESPACE, "trans: scalar space info corrupted (only accepting PPP, PFP, FFP and FFF)");
@@ -1101,6 +1103,11 @@ int mlg_calcat1(mlg_scalar h, double* out) { NEED_KIT(); Scalar* s = S(h); SC(s)
 int mlg_idel2_preln(mlg_scalar h, double preln) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_idel2(*s, true, preln); }
 int mlg_helm(mlg_scalar h, double a) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_helm(*s, a); }
 int mlg_ihelm(mlg_scalar h, double a) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_ihelm(*s, a); }
+int mlg_ihelm_noalloc(void* e_dev, double* ln, double alpha) {
+  NEED_KIT();
+  if (!e_dev || !ln) return set_error(MLG_EHANDLE, "ihelm_noalloc: null field or ln");
+  return ihelm_noalloc(e_dev, ln, alpha);
+}
 int mlg_helmp(mlg_scalar h, int p, double a, double b) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_helmp(*s, p, a, b); }
 int mlg_ihelmp(mlg_scalar h, int p, double a, double b) { NEED_KIT(); Scalar* s = S(h); SC(s); return op_ihelmp(*s, p, a, b); }
 
