@@ -26,13 +26,31 @@ __device__ __forceinline__ int k_count(int k0, int nzc, int nzcu, int nzdim) {  
 
 // op: 0 = xxdx, 1 = del2h, 2 = del2
 // ln handling (column (m=0,k=0) only): the ln terms added after the band product, and ln <- 0.
+// T = double: the plain form; T = float: the mixed form (stencil in FP32, conversions on the integer
+// pipe, the ln terms still in FP64).
+template <typename T> struct BC;
+template <> struct BC<double> {
+  typedef double2 C;
+  static __device__ __forceinline__ C ld(const double2* p) { return *p; }
+  static __device__ __forceinline__ void st(double2* p, C v) { *p = v; }
+  static __device__ __forceinline__ double cv(double v) { return v; }
+};
+template <> struct BC<float> {
+  typedef float2 C;
+  static __device__ __forceinline__ C ld(const double2* p) { return ld_c32(p); }
+  static __device__ __forceinline__ void st(double2* p, C v) { st_c32(p, v); }
+  static __device__ __forceinline__ float cv(double v) { return d2f_fast(v); }
+};
+
+template <typename T>
 __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__ bd2, const double* __restrict__ bxx,
                              const double* __restrict__ ak, double* __restrict__ lnp, const double* __restrict__ lognorm,
                              int op, int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim,
                              double ell) {
-  extern __shared__ double2 col[];
-  double2* c0 = col;
-  double2* c1 = col + nrdim;
+  typedef typename BC<T>::C C;
+  extern __shared__ __align__(16) unsigned char band_smem[];
+  C* c0 = (C*)band_smem;
+  C* c1 = c0 + nrdim;
   int m = blockIdx.y, k = blockIdx.x;
   int nn = max(min(nrc, nrc - m), 0);
   int cnt = k_count(k, nzc, nzcu, nzdim);
@@ -41,24 +59,24 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
   double lnin = 0.0;
   if (lnblk) lnin = *lnp;
   if (m < npc && nn > 0 && cnt > 0) {
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = g[i];
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(g + i);
     __syncthreads();
-    double akv = ak[k];
-    double akv2 = akv * akv;   // akval**2 (mlegs_spectfm_diff.f90:144)
+    double akd = ak[k];
+    T akv2 = BC<T>::cv(akd * akd);   // akval**2 (mlegs_spectfm_diff.f90:144)
     for (int rep = 0; rep < cnt; ++rep) {
       for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-        double2 acc = make_double2(0, 0);
+        C acc; acc.x = 0; acc.y = 0;
         if (op == 0) {
           const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
-          if (i - 1 >= 0) { acc.x += b[0] * c0[i - 1].x; acc.y += b[0] * c0[i - 1].y; }
-          if (i + 1 < nn) { acc.x += b[2] * c0[i + 1].x; acc.y += b[2] * c0[i + 1].y; }
+          if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+          if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
         } else {
           const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
 #pragma unroll
           for (int c = 0; c < 5; ++c) {
             int j = i - 2 + c;
             if (j < 0 || j >= nn) continue;
-            double v = b[c];
+            T v = BC<T>::cv(b[c]);
             if (c == 2 && op == 2) v = v - akv2;
             acc.x += v * c0[j].x;
             acc.y += v * c0[j].y;
@@ -70,42 +88,39 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
       for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
       __syncthreads();
     }
-    if (lnblk && threadIdx.x == 0) {
-      if (op == 0) {   // r d/dr of the log term (:452-456)
-        c0[0].x += 1.0 / exp(lognorm[0]) * lnin;
-        if (nn > 1) c0[1].x += 1.0 / exp(lognorm[1]) * lnin;
-      } else {         // (:506-511, :561-566)
-        double e2 = pow(ell, 2.0);
-        c0[0].x += 4.0 / 3.0 / e2 / exp(lognorm[0]) * lnin;
-        if (nn > 1) c0[1].x -= 2.0 / 1.0 / e2 / exp(lognorm[1]) * lnin;
-        if (nn > 2) c0[2].x += 2.0 / 3.0 / e2 / exp(lognorm[2]) * lnin;
-      }
-    }
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(g + i, c0[i]);
     __syncthreads();
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) g[i] = c0[i];
-  } else if (lnblk && threadIdx.x == 0) {
-    // the (1,1,1) column is not active: the ln terms still land on it
-    double e2 = pow(ell, 2.0);
-    if (op == 0) {
+  }
+  if (lnblk && threadIdx.x == 0) {
+    // the log-term contributions land on e(1..3,1,1) whether or not the column was active
+    double e2 = ell * ell;
+    if (op == 0) {   // r d/dr of the log term (:452-456)
       g[0].x += 1.0 / exp(lognorm[0]) * lnin;
       g[1].x += 1.0 / exp(lognorm[1]) * lnin;
-    } else {
+    } else {         // (:506-511, :561-566)
       g[0].x += 4.0 / 3.0 / e2 / exp(lognorm[0]) * lnin;
       g[1].x -= 2.0 / 1.0 / e2 / exp(lognorm[1]) * lnin;
       g[2].x += 2.0 / 3.0 / e2 / exp(lognorm[2]) * lnin;
     }
+    *lnp = 0.0;
   }
-  if (lnblk && threadIdx.x == 0) *lnp = 0.0;
 }
 
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
-  size_t sm = 2ull * G.nrdim * sizeof(double2);
-  if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   dim3 grid(G.nzdim, std::max(c.npc, 1));
   kt_begin(2);
-  k_band_apply<<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne, c.nrc,
-                                            c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  if (G.precision == MLG_MIXED) {
+    size_t sm = 2ull * G.nrdim * sizeof(float2);
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply<float><<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+                                                     c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  } else {
+    size_t sm = 2ull * G.nrdim * sizeof(double2);
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply<double><<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+                                                      c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  }
   MLG_LAUNCH();
   kt_end(2, 2.0 * G.fsize * 16);
   return 0;

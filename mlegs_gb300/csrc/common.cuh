@@ -57,6 +57,7 @@ struct Ctx {
 
   // kit arrays on the device
   double *x = nullptr, *w = nullptr, *r = nullptr, *rinv = nullptr, *lnx = nullptr, *ak = nullptr;
+  float* w32 = nullptr;        // FP32 quadrature weights (mixed form)
   bool svv_q_ready = false;
   double *lognorm = nullptr;   // (ne, npchop)
   double *pf = nullptr;        // (nrh, ne, npchop): P_L^m(x_i) normalised, reference layout
@@ -68,6 +69,7 @@ struct Ctx {
   float *tV32 = nullptr, *tD32 = nullptr, *tT32 = nullptr;
   double2 *tw_p = nullptr, *tw_z = nullptr;  // FFT twiddles exp(-2 pi i k/L): L = np/2 (phi), nz (z)
   double2 *tw_pr = nullptr;    // real-FFT post-processing twiddles exp(-2 pi i k/np), k < np/2+1
+  float2 *tw_p32 = nullptr, *tw_z32 = nullptr, *tw_pr32 = nullptr;   // FP32 copies for the mixed form
 
   // ln slots of all scalars (device), and per-step scalars (svv gains, flags, scratch reductions)
   double* ln_slots = nullptr;  int n_slots = 0;  std::vector<int> free_slots;
@@ -138,5 +140,36 @@ __device__ __forceinline__ float2 csubf(float2 a, float2 b) { return make_float2
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+
+// FP64 <-> FP32 conversions on the integer pipe.  On GB300 the FP64 pipe runs ~1.3 ops per clock
+// per SM, and cvt.f32.f64 / cvt.f64.f32 execute there; the mixed form converts every field element
+// it touches, so doing it with integer ops keeps those kernels off the FP64 pipe.
+// Round to nearest even; magnitudes below 2^-126 become signed zero; inf and NaN are kept.
+__device__ __forceinline__ float d2f_fast(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  unsigned sign = hi & 0x80000000u;
+  int e = (int)((hi >> 20) & 0x7FFu);
+  unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  unsigned rest = lo & 0x1FFFFFFFu;
+  int e32 = e - 1023 + 127;
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u));
+  if (e32 <= 0) return __uint_as_float(sign);
+  if (e32 >= 255) return __uint_as_float(sign | 0x7F800000u);
+  unsigned r = sign | ((unsigned)e32 << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;   // carries into the exponent
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ double f2d_fast(float y) {   // exact (FP32 subnormals become zero)
+  unsigned f = __float_as_uint(y);
+  unsigned sign = f & 0x80000000u;
+  unsigned e = (f >> 23) & 0xFFu;
+  unsigned m = f & 0x7FFFFFu;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  unsigned hi = (e == 255u) ? (sign | 0x7FF00000u | (m >> 3)) : (sign | ((e + 896u) << 20) | (m >> 3));
+  return __hiloint2double((int)hi, (int)(m << 29));
+}
+__device__ __forceinline__ float2 ld_c32(const double2* p) { double2 v = *p; return make_float2(d2f_fast(v.x), d2f_fast(v.y)); }
+__device__ __forceinline__ void st_c32(double2* p, float2 v) { *p = make_double2(f2d_fast(v.x), f2d_fast(v.y)); }
 
 static inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }

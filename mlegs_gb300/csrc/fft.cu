@@ -33,10 +33,15 @@ template <typename C> __device__ __forceinline__ C c_muli(C a, int sgn) {  // a 
 }
 template <typename C, typename T> __device__ __forceinline__ C c_scale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
 
+// twiddle tables hold exp(-2 pi i k/L) (FP64 for the plain form, FP32 for the mixed form); sgn > 0
+// conjugates
+template <typename T> struct TW;
+template <> struct TW<double> { typedef double2 t; };
+template <> struct TW<float> { typedef float2 t; };
 template <typename T>
-__device__ __forceinline__ typename CT<T>::t load_tw(const double2* tw, int idx, int sgn) {
-  double2 w = tw[idx];
-  return mk<T>((T)w.x, (T)(sgn < 0 ? w.y : -w.y));   // table holds exp(-2 pi i k/L); sgn>0 conjugates
+__device__ __forceinline__ typename CT<T>::t load_tw(const typename TW<T>::t* tw, int idx, int sgn) {
+  typename TW<T>::t w = tw[idx];
+  return mk<T>(w.x, sgn < 0 ? w.y : -w.y);
 }
 
 // small DFTs, sign sgn = -1 forward, +1 backward
@@ -71,7 +76,7 @@ __device__ __forceinline__ void dft_small(typename CT<T>::t* a, int p, int sgn) 
 // Stockham FFT over the TR transforms held in s0 ([L][TR]); result left in *res.
 template <typename T>
 __device__ void stockham(typename CT<T>::t* s0, typename CT<T>::t* s1, typename CT<T>::t** res, int L, int TR,
-                         int tr, int tt, int TT, const double2* tw, int sgn) {
+                         int tr, int tt, int TT, const typename TW<T>::t* tw, int sgn) {
   typedef typename CT<T>::t C;
   C* src = s0;
   C* dst = s1;
@@ -105,17 +110,17 @@ __device__ void stockham(typename CT<T>::t* s0, typename CT<T>::t* s1, typename 
   *res = src;
 }
 
-template <typename T> __device__ __forceinline__ typename CT<T>::t ld(const double2* p) {
-  double2 v = *p; return mk<T>((T)v.x, (T)v.y);
-}
-template <typename T> __device__ __forceinline__ void st(double2* p, typename CT<T>::t v) {
-  *p = make_double2((double)v.x, (double)v.y);
-}
+template <typename T> __device__ __forceinline__ typename CT<T>::t ld(const double2* p);
+template <> __device__ __forceinline__ double2 ld<double>(const double2* p) { return *p; }
+template <> __device__ __forceinline__ float2 ld<float>(const double2* p) { return ld_c32(p); }
+template <typename T> __device__ __forceinline__ void st(double2* p, typename CT<T>::t v);
+template <> __device__ __forceinline__ void st<double>(double2* p, double2 v) { *p = v; }
+template <> __device__ __forceinline__ void st<float>(double2* p, float2 v) { st_c32(p, v); }
 
 // z FFT of columns (r, m): points at stride nrdim*npdim
 template <typename T>
-__global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
-                       int sgn, double scale) {
+__global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
+                       const typename TW<T>::t* __restrict__ tw, int sgn, T scale) {
   typedef typename CT<T>::t C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
@@ -136,8 +141,8 @@ __global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int
 
 // φ forward: packed reals -> X_0..X_{L} (L = np/2) scaled 1/np, in place
 template <typename T>
-__global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
-                           const double2* __restrict__ twr, double scale) {
+__global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
+                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, T scale) {
   typedef typename CT<T>::t C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
@@ -158,8 +163,8 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
     zc.y = -zc.y;
     C fe = c_scale(c_add(zk, zc), (T)0.5);
     C fo = c_muli(c_scale(c_sub(zk, zc), (T)0.5), -1);   // (zk - zc)/(2i)
-    double2 wd = twr[k];
-    C w = mk<T>((T)wd.x, (T)wd.y);
+    typename TW<T>::t wd = twr[k];
+    C w = mk<T>(wd.x, wd.y);
     C x = c_add(fe, c_mul(w, fo));
     st<T>(base + (size_t)k * nrdim, c_scale(x, (T)scale));
   }
@@ -167,8 +172,8 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
 
 // φ backward: X_0..X_L -> packed reals (unnormalised); slot L <- np * X_L (input), in place
 template <typename T>
-__global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR, const double2* __restrict__ tw,
-                           const double2* __restrict__ twr, double np_d) {
+__global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
+                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, double np_d) {
   typedef typename CT<T>::t C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
@@ -188,8 +193,8 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
       if (k == 0) { xk.y = 0; xc.y = 0; }
       xc.y = -xc.y;
       C g = c_add(xk, xc);
-      double2 wd = twr[k];
-      C w = mk<T>((T)wd.x, (T)-wd.y);   // exp(+2 pi i k / np)
+      typename TW<T>::t wd = twr[k];
+      C w = mk<T>(wd.x, -wd.y);   // exp(+2 pi i k / np)
       C h = c_mul(c_sub(xk, xc), w);
       v = c_add(g, c_muli(h, 1));
     }
@@ -202,6 +207,10 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   for (int pt = tt; pt < L; pt += TT) st<T>(base + (size_t)pt * nrdim, res[pt * TR + tr]);
   if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
 }
+
+template <typename T> const typename TW<T>::t* tw_of(const double2* d, const float2* f);
+template <> const double2* tw_of<double>(const double2* d, const float2* f) { (void)f; return d; }
+template <> const float2* tw_of<float>(const double2* d, const float2* f) { (void)d; return f; }
 
 static int pick_tr(int L, size_t elem) {
   // two shared buffers of L*TR complex values, at most 96 KB
@@ -226,7 +235,8 @@ static int vfft_t(cd* e, int dir) {
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), G.npdim), blk(TR, TT);
   kt_begin(1);
-  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_z, dir, dir < 0 ? 1.0 / L : 1.0);
+  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir,
+                                         (T)(dir < 0 ? 1.0 / L : 1.0));
   MLG_LAUNCH();
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;
@@ -248,10 +258,12 @@ static int hfft_t(cd* e, int dir) {
   kt_begin(1);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
-    k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_p, G.tw_pr, 1.0 / G.np);
+    k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
+                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)(1.0 / G.np));
   } else {
     MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
-    k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, G.tw_p, G.tw_pr, (double)G.np);
+    k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
+                                                tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np);
   }
   MLG_LAUNCH();
   kt_end(1, 2.0 * G.fsize * 16);

@@ -315,6 +315,9 @@ int kit_build(const mlg_params* P) {
 
   std::vector<double> rinv(nr);
   for (int i = 0; i < nr; ++i) rinv[i] = 1.0 / r[i];
+  std::vector<float> w32(nr);
+  for (int i = 0; i < nr; ++i) w32[i] = (float)w[i];
+  MLG_TRY(upload(&G.w32, w32));
   MLG_TRY(upload(&G.x, x)); MLG_TRY(upload(&G.w, w)); MLG_TRY(upload(&G.r, r)); MLG_TRY(upload(&G.rinv, rinv));
   MLG_TRY(upload(&G.lnx, lnx)); MLG_TRY(upload(&G.ak, ak)); MLG_TRY(upload(&G.lognorm, lognorm));
   double* d_logfact = nullptr;
@@ -371,9 +374,19 @@ int kit_build(const mlg_params* P) {
     }
     return t;
   };
-  MLG_TRY(upload(&G.tw_p, twid(std::max(G.nph, 1), std::max(G.nph, 1))));
-  MLG_TRY(upload(&G.tw_pr, twid(std::max(np, 1), G.nph + 1)));
-  MLG_TRY(upload(&G.tw_z, twid(nz, nz)));
+  auto to32 = [](const std::vector<double2>& t) {
+    std::vector<float2> f(t.size());
+    for (size_t i = 0; i < t.size(); ++i) f[i] = make_float2((float)t[i].x, (float)t[i].y);
+    return f;
+  };
+  std::vector<double2> tp = twid(std::max(G.nph, 1), std::max(G.nph, 1)), tpr = twid(std::max(np, 1), G.nph + 1),
+                       tz = twid(nz, nz);
+  MLG_TRY(upload(&G.tw_p, tp));
+  MLG_TRY(upload(&G.tw_pr, tpr));
+  MLG_TRY(upload(&G.tw_z, tz));
+  MLG_TRY(upload(&G.tw_p32, to32(tp)));
+  MLG_TRY(upload(&G.tw_pr32, to32(tpr)));
+  MLG_TRY(upload(&G.tw_z32, to32(tz)));
 
   MLG_CUDA(cudaStreamSynchronize(G.stream));
   dfree(d_logfact, logfact.size() * sizeof(double));

@@ -19,15 +19,26 @@ template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 t; };
 template <> struct V2<float> { typedef float2 t; };
 
-template <typename T> __device__ __forceinline__ typename V2<T>::t ldc(const double2* p) {
-  double2 v = *p; typename V2<T>::t r; r.x = (T)v.x; r.y = (T)v.y; return r;
+// field loads / stores: FP64 as is for the plain form; for the mixed form the conversions run on
+// the integer pipe (d2f_fast / f2d_fast), keeping these kernels off GB300's narrow FP64 pipe
+template <typename T> __device__ __forceinline__ typename V2<T>::t ldc(const double2* p);
+template <> __device__ __forceinline__ double2 ldc<double>(const double2* p) { return *p; }
+template <> __device__ __forceinline__ float2 ldc<float>(const double2* p) { return ld_c32(p); }
+template <typename T> __device__ __forceinline__ double2 to_d2(T re, T im);
+template <> __device__ __forceinline__ double2 to_d2<double>(double re, double im) { return make_double2(re, im); }
+template <> __device__ __forceinline__ double2 to_d2<float>(float re, float im) {
+  return make_double2(f2d_fast(re), f2d_fast(im));
 }
+template <typename T> __device__ __forceinline__ T wsel(const double* w, const float* w32, int i);
+template <> __device__ __forceinline__ double wsel<double>(const double* w, const float* w32, int i) { (void)w32; return w[i]; }
+template <> __device__ __forceinline__ float wsel<float>(const double* w, const float* w32, int i) { (void)w; return w32[i]; }
 
 // forward: grid (ztiles, 2*ttiles, npc); block (ZT/ZPT, MT/MPT)
 template <typename T, int MT, int ZT, int KC, int MPT, int ZPT>
 __global__ void __launch_bounds__((MT / MPT) * (ZT / ZPT))
 k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T* __restrict__ pf,
-             const double* __restrict__ w, int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc) {
+             const double* __restrict__ w, const float* __restrict__ w32, int nr, int nrh, int ne, int nrdim, int npdim,
+             int nzdim, int nrc) {
   typedef typename V2<T>::t C;
   __shared__ T As[KC][MT + 1];
   __shared__ C Bs[KC][ZT];
@@ -61,10 +72,10 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       C v; v.x = 0; v.y = 0;
       if (i < nrh && z < nzdim) {
         const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * z);
-        double2 a = col[i], b = col[nr - 1 - i];
-        double wi = w[i];
-        v.x = (T)((a.x + (double)sgn * b.x) * wi);
-        v.y = (T)((a.y + (double)sgn * b.y) * wi);
+        C a = ldc<T>(col + i), b = ldc<T>(col + nr - 1 - i);
+        T wi = wsel<T>(w, w32, i);
+        v.x = (a.x + sgn * b.x) * wi;
+        v.y = (a.y + sgn * b.y) * wi;
       }
       Bs[ii][zz] = v;
     }
@@ -94,7 +105,7 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
 #pragma unroll
     for (int b = 0; b < ZPT; ++b) {
       int z = z0 + tx + b * (ZT / ZPT);
-      if (z < nzdim) out[j + (size_t)nrdim * (m + (size_t)npdim * z)] = make_double2((double)acc_r[a][b], (double)acc_i[a][b]);
+      if (z < nzdim) out[j + (size_t)nrdim * (m + (size_t)npdim * z)] = to_d2<T>(acc_r[a][b], acc_i[a][b]);
     }
   }
 }
@@ -169,8 +180,8 @@ k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       int z = z0 + tx + b * (ZT / ZPT);
       if (z >= nzdim) continue;
       size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
-      double2 p = make_double2((double)er[a][b] + (double)orr[a][b], (double)ei[a][b] + (double)oi[a][b]);
-      double2 q = make_double2((double)er[a][b] - (double)orr[a][b], (double)ei[a][b] - (double)oi[a][b]);
+      double2 p = to_d2<T>(er[a][b] + orr[a][b], ei[a][b] + oi[a][b]);
+      double2 q = to_d2<T>(er[a][b] - orr[a][b], ei[a][b] - oi[a][b]);
       if (lnv != 0.0) { p.x += lnv * lnx[i]; q.x += lnv * lnx[nr - 1 - i]; }
       out[base + i] = p;
       out[base + nr - 1 - i] = q;
@@ -204,7 +215,7 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
   for (int b = 0; b < ZPT; ++b) {
     a1[b].x = a1[b].y = 0; a2[b].x = a2[b].y = 0; a3[b].x = a3[b].y = 0; a4[b].x = a4[b].y = 0; a5[b].x = a5[b].y = 0;
   }
-  const double ss = par ? -1.0 : 1.0;   // own-parity fold sign
+  const T ss = par ? (T)-1 : (T)1;   // own-parity fold sign
   for (int i0 = 0; i0 < nrh; i0 += KC) {
     for (int idx = tid; idx < KC * MT; idx += nthr) {
       int ii = idx % KC, tt = idx / KC;
@@ -223,14 +234,14 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
       rs.x = rs.y = ro.x = ro.y = ps.x = ps.y = po.x = po.y = zs.x = zs.y = 0;
       if (i < nrh && z < nzdim) {
         size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
-        double2 a = ur[base + i], b = ur[base + nr - 1 - i];
-        rs.x = (T)(a.x + ss * b.x); rs.y = (T)(a.y + ss * b.y);
-        ro.x = (T)(a.x - ss * b.x); ro.y = (T)(a.y - ss * b.y);
-        a = up[base + i]; b = up[base + nr - 1 - i];
-        ps.x = (T)(a.x + ss * b.x); ps.y = (T)(a.y + ss * b.y);
-        po.x = (T)(a.x - ss * b.x); po.y = (T)(a.y - ss * b.y);
-        a = uz[base + i]; b = uz[base + nr - 1 - i];
-        zs.x = (T)(a.x + ss * b.x); zs.y = (T)(a.y + ss * b.y);
+        C a = ldc<T>(ur + base + i), b = ldc<T>(ur + base + nr - 1 - i);
+        rs.x = a.x + ss * b.x; rs.y = a.y + ss * b.y;
+        ro.x = a.x - ss * b.x; ro.y = a.y - ss * b.y;
+        a = ldc<T>(up + base + i); b = ldc<T>(up + base + nr - 1 - i);
+        ps.x = a.x + ss * b.x; ps.y = a.y + ss * b.y;
+        po.x = a.x - ss * b.x; po.y = a.y - ss * b.y;
+        a = ldc<T>(uz + base + i); b = ldc<T>(uz + base + nr - 1 - i);
+        zs.x = a.x + ss * b.x; zs.y = a.y + ss * b.y;
       }
       Brs[ii][zz] = rs; Bro[ii][zz] = ro; Bps[ii][zz] = ps; Bpo[ii][zz] = po; Bzs[ii][zz] = zs;
     }
@@ -253,23 +264,23 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
   }
   int j = 2 * (t0 + ty) + par;
   if (j >= nn) return;
-  double mv = (double)m;
+  T mv = (T)m;
 #pragma unroll
   for (int b = 0; b < ZPT; ++b) {
     int z = z0 + tx + b * (ZT / ZPT);
     if (z >= nzdim) continue;
     int kk = z + 1;
     if (!(kk <= nzc || kk >= nzcu)) continue;
-    double kv = ak[z];
-    double w1x = m ? (double)a1[b].x : 0.0, w1y = m ? (double)a1[b].y : 0.0;
-    double w2x = (double)a2[b].x, w2y = (double)a2[b].y;
+    T kv = (T)ak[z];
+    T w1x = m ? a1[b].x : (T)0, w1y = m ? a1[b].y : (T)0;
+    T w2x = a2[b].x, w2y = a2[b].y;
     // psi = -i*mv*w1 - w2
-    double2 p = make_double2(mv * w1y - w2x, -mv * w1x - w2y);
-    double v1x = (double)a3[b].x, v1y = (double)a3[b].y;
-    double v2x = m ? (double)a4[b].x : 0.0, v2y = m ? (double)a4[b].y : 0.0;
-    double cx = (double)a5[b].x, cy = (double)a5[b].y;
+    double2 p = to_d2<T>(mv * w1y - w2x, -mv * w1x - w2y);
+    T v1x = a3[b].x, v1y = a3[b].y;
+    T v2x = m ? a4[b].x : (T)0, v2y = m ? a4[b].y : (T)0;
+    T cx = a5[b].x, cy = a5[b].y;
     // chi = i*kv*w1' + mv*kv*w2' - c
-    double2 q = make_double2(-kv * v1y + mv * kv * v2x - cx, kv * v1x + mv * kv * v2y - cy);
+    double2 q = to_d2<T>(-kv * v1y + mv * kv * v2x - cx, kv * v1x + mv * kv * v2y - cy);
     size_t o = j + (size_t)nrdim * (m + (size_t)npdim * z);
     psi[o] = p;
     chi[o] = q;
@@ -303,13 +314,13 @@ int launch_rtrans_fwd(Scalar& s) {
       constexpr int MT = 32, ZT = 64, KC = 32, MPT = 2, ZPT = 4;
       int tt = cdiv((nrc + 1) / 2, MT);
       dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT / MPT);
-      k_rtrans_fwd<float, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf32, G.w, G.nr, G.nrh, G.ne,
+      k_rtrans_fwd<float, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf32, G.w, G.w32, G.nr, G.nrh, G.ne,
                                                                              G.nrdim, G.npdim, G.nzdim, nrc);
     } else {
       constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
       int tt = cdiv((nrc + 1) / 2, MT);
       dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT / MPT);
-      k_rtrans_fwd<double, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.w, G.nr, G.nrh, G.ne,
+      k_rtrans_fwd<double, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne,
                                                                               G.nrdim, G.npdim, G.nzdim, nrc);
     }
     MLG_LAUNCH();

@@ -210,3 +210,55 @@ def test_vortex_steps(pair):
     for n in ("psi", "chi", "nlpsi", "nlchi", "psi_p", "nlpsi_p"):
         compare(getattr(sg, n), getattr(so, n), 1e-11, what=f"{name} 5 steps {n}")
     assert abs(sg.gains[0] - so.gains[0]) < 1e-12 and abs(sg.gains[1] - so.gains[1]) < 1e-12
+
+
+# ---- the mixed form (FP32 contractions and FFTs; FP64 state, solves and reductions) ----
+MIXED_TOL = 2e-6
+
+
+@pytest.fixture(scope="module", params=["c1", "odd", "big"])
+def mixed_pair(request):
+    from mlegs_gb300.kit import Kit, MIXED
+    from oracle.oracle import Oracle
+    from mlegs_gb300.params import make_params
+    if request.param == "big":
+        # the benchmark grid: radial contractions of the full size
+        p = make_params(nr=192, np=128, nz=128, nrchop=192, npchop=65, nzchop=65, ell=4.0, visc=1.0e-4)
+    else:
+        p = params(request.param)
+    o = Oracle(p)
+    k = Kit(p, precision=MIXED)
+    yield request.param, k, o
+    k.close()
+    o.close()
+
+
+def test_mixed_transforms(mixed_pair):
+    name, k, o = mixed_pair
+    p = k.params
+    e = fields.ppp_random(p, k.dims, seed=91)
+    gs, os_ = both(k, o, e, 0.0, "PPP")
+    k.trans(gs, "FFF"); o.trans(os_, "FFF")
+    compare(gs, os_, MIXED_TOL, ln_tol=1.0, what=f"{name} mixed forward")
+    c = fff_input(p, k.dims, 92)
+    gs, os_ = both(k, o, c, 0.0, "FFF")
+    k.trans(gs, "PPP"); o.trans(os_, "PPP")
+    compare(gs, os_, MIXED_TOL, ln_tol=1.0, what=f"{name} mixed backward")
+
+
+def test_mixed_vector_fields(mixed_pair):
+    name, k, o = mixed_pair
+    p = k.params
+    psi, chi = fff_input(p, k.dims, 93), fff_input(p, k.dims, 94)
+    gp, op_ = both(k, o, psi, 0.0, "FFF")
+    gc, oc = both(k, o, chi, 0.0, "FFF")
+    gv = [k.scalar() for _ in range(3)]
+    ov = [o.scalar() for _ in range(3)]
+    k.tp2vec(gp, gc, *gv); o.tp2vec(op_, oc, *ov)
+    for i in range(3):
+        compare(gv[i], ov[i], MIXED_TOL, ln_tol=1.0, what=f"{name} mixed tp2vec {i}")
+    gq = [k.scalar(np.zeros(k.dims, complex, order="F"), 0.0, "FFF") for _ in range(2)]
+    oq = [o.scalar(np.zeros(k.dims, complex, order="F"), 0.0, "FFF") for _ in range(2)]
+    k.vec2tp(*gv, *gq); o.vec2tp(*ov, *oq)
+    for i in range(2):
+        compare(gq[i], oq[i], 1e-5, ln_tol=1.0, what=f"{name} mixed vec2tp {i}")
