@@ -773,6 +773,13 @@ static int scale_r(Scalar& s, int mode) {
   return 0;
 }
 
+// restores the precision form on scope exit
+struct PrecisionScope {
+  int saved;
+  explicit PrecisionScope(int mode) : saved(G.precision) { G.precision = mode; }
+  ~PrecisionScope() { G.precision = saved; }
+};
+
 int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi) {
   if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
   if (!psi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
@@ -791,8 +798,13 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
   up.set_space("PFF");
   k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
   MLG_LAUNCH();
-  MLG_TRY(op_trans(uz, "PFP"));
-  if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
+  {
+    // u_z enters chi through an inverse horizontal Laplacian, which lifts rounding of the strong
+    // high-wavenumber part of u_z into the weak low modes; its two FFTs stay FP64 in every form
+    PrecisionScope fp64(MLG_PLAIN_FP64);
+    MLG_TRY(op_trans(uz, "PFP"));
+    if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
+  }
   uz.set_space("PFF");
   // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331); psi%ln was set above from calcat1
   MLG_TRY(launch_zero(psi.e));
@@ -933,9 +945,10 @@ int mlg_finalize(void) {
   if (!G.kit_set) return 0;
   cudaStreamSynchronize(G.stream);
   lu_cache_clear();
+  tc_free();
   for (cd* b : G.all_bufs) cudaFree(b);
   void* arrs[] = {G.x, G.w, G.w32, G.r, G.rinv, G.lnx, G.ak, G.lognorm, G.pf, G.pf32, G.at0, G.at1, G.bd2, G.bxx, G.tV, G.tD, G.tT,
-                  G.tV32, G.tD32, G.tT32, G.tw_p, G.tw_z, G.tw_pr, G.tw_p32, G.tw_z32, G.tw_pr32, G.ln_slots, G.dscal, G.band_ws};
+                  G.tV32, G.tD32, G.tT32, G.tT32lo, G.tw_p, G.tw_z, G.tw_pr, G.tw_p32, G.tw_z32, G.tw_pr32, G.ln_slots, G.dscal, G.band_ws};
   for (void* a : arrs) if (a) cudaFree(a);
   cudaStream_t st = G.stream;
   cudaEvent_t e0 = G.ev0, e1 = G.ev1;

@@ -1,0 +1,418 @@
+// tc_radial.cu — the mixed form's radial Legendre contractions on the 5th-generation tensor cores.
+//
+// Forward (rtrans_forward, mlegs_scalar_ops.f90:1852-1927): for every azimuthal mode m and both
+// row parities, C_par(t, n) = sum_i A_par(t, i) B_par(i, n) with A_par(t, i) = pf(i, 2t+par, m) and
+// B_par(i, n) = (f(i) +- f(nr-1-i)) w(i) (n runs over re/im of the z columns).
+//
+// Precision: split BF16.  Each FP32 operand x is written as x0 + x1 + x2 with x0 = bf16(x),
+// x1 = bf16(x - x0), x2 = bf16(x - x0 - x1) (each residual is exact in FP32), and the product keeps
+// the six terms with i + j <= 2; every BF16 x BF16 product is exact in the FP32 accumulator, so the
+// result carries ~2^-24 relative error like an FP32 contraction (the omitted terms are below 2^-24).
+//
+// Backward (rtrans_backward, :1931-2008): D_par(i, n) = sum_t A_par(i, t) B_par(t, n) with
+// A_par(i, t) = pf(i, 2t+par, m) and B_par(t, n) = c(2t+par, m, z); the epilogue forms
+// f(i) = D_0 + D_1 and f(nr-1-i) = D_0 - D_1 (and adds the log term at m = 0).
+//
+// Engine: one CTA per (m, 128-row tile, 32 complex z columns), 128 threads, 72 KiB of shared memory
+// (three CTAs per SM).
+//  * The table operand is split and laid out at kit init in the UMMA canonical no-swizzle K-major
+//    layout (8x8 BF16 core matrices, 16-byte rows) per (m, row tile, K chunk): one K chunk of both
+//    parities and all three splits (48 KiB) arrives by one cp.async.bulk on the TMA engine,
+//    completing on an mbarrier.
+//  * The field operand is folded (FP32, conversions on the integer pipe), split and stored by the
+//    threads into the same layout, then made visible to the tensor core (fence.proxy.async).
+//  * One elected thread issues tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM, one
+//    accumulator per parity; M=128, N=64, K=16 per instruction) and commits to an mbarrier; while the
+//    tensor core runs, the threads already load the next K chunk of the field into registers.
+//  * Epilogue: tcgen05.ld of each warp's 32 TMEM lanes, FP32 -> FP64 on the integer pipe.
+// Every wait is bounded (about a second of clock); a timeout sets the library's status flag, and the
+// CTA still releases its TMEM.
+#include "common.cuh"
+#include <cstdint>
+
+namespace mlg {
+
+// ------------------------------------------------------------------------------------------------
+// PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait (~1 s of SM clock); false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+  long long t0 = clock64();
+  while (!mbar_try_wait(bar, phase))
+    if (clock64() - t0 > 2000000000LL) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// 32 TMEM lanes x 16 consecutive 32-bit columns into each thread (lane = thread of the warp)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major; LBO = byte distance between the two core
+// matrices adjacent in K, SBO = byte distance between core matrices adjacent in M/N
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+// instruction descriptor: kind::f16 with BF16 A and B, FP32 D, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// BF16 split of an FP32 value (round to nearest even on the integer pipe)
+__device__ __forceinline__ uint16_t bf16_rn(float x) {
+  uint32_t u = __float_as_uint(x);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+__device__ __forceinline__ float bf16_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+__device__ __forceinline__ void split3(float x, uint16_t& s0, uint16_t& s1, uint16_t& s2) {
+  s0 = bf16_rn(x);
+  float r = x - bf16_f(s0);
+  s1 = bf16_rn(r);
+  r = r - bf16_f(s1);
+  s2 = bf16_rn(r);
+}
+
+// canonical layout of one operand tile of R rows x KC columns (BF16): byte offset of (row, k)
+constexpr int TC_KC = 32;                       // K chunk
+constexpr int TC_SBO = TC_KC * 16;              // 8 rows x KC cols: (KC/8) core matrices of 128 B
+constexpr int TC_LBO = 128;
+__host__ __device__ constexpr int tc_off(int row, int k) {
+  return (row >> 3) * TC_SBO + (k >> 3) * TC_LBO + (row & 7) * 16 + (k & 7) * 2;
+}
+constexpr int TC_TILE_BYTES = 128 * TC_KC * 2;  // 8 KiB: 128 rows x 32 BF16 (table tiles, M = 128)
+constexpr int TC_NZ = 32;                       // complex z columns per CTA (N = 64)
+constexpr int TC_BTILE_BYTES = 2 * TC_NZ * TC_KC * 2;   // 4 KiB: 64 rows x 32 BF16 (field tiles)
+constexpr int TC_THREADS = 128;
+
+// ------------------------------------------------------------------------------------------------
+// table images, split and laid out once per kit: for (m, row tile, K chunk): [par 2][split 3][tile]
+//  fwd: rows t (A(t, i) = pf(i, 2t+par, m)), K = i
+//  bwd: rows i (A(i, t) = pf(i, 2t+par, m)), K = t
+__global__ void k_tc_table(const double* __restrict__ pf, uint16_t* __restrict__ img, int nrh, int ne, int nmt,
+                           int nkc, int nrc, int bwd) {
+  size_t blk = blockIdx.x;   // (m, mt, kc)
+  int kc = blk % nkc;
+  int mt = (blk / nkc) % nmt;
+  int m = blk / ((size_t)nkc * nmt);
+  int nn = max(min(nrc, nrc - m), 0);
+  uint8_t* base = (uint8_t*)img + blk * (size_t)(6 * TC_TILE_BYTES);
+  for (int idx = threadIdx.x; idx < 2 * 128 * TC_KC; idx += blockDim.x) {
+    int k = idx % TC_KC, r = (idx / TC_KC) % 128, par = idx / (TC_KC * 128);
+    int row = mt * 128 + r, kk = kc * TC_KC + k;
+    int i = bwd ? row : kk, t = bwd ? kk : row;
+    int j = 2 * t + par;
+    double a = 0.0;
+    if (j < nn && i < nrh) a = pf[i + (size_t)nrh * (j + (size_t)ne * m)];
+    uint16_t s0 = bf16_rn((float)a);
+    double r1 = a - (double)bf16_f(s0);
+    uint16_t s1 = bf16_rn((float)r1);
+    double r2 = r1 - (double)bf16_f(s1);
+    uint16_t s2 = bf16_rn((float)r2);
+    int off = tc_off(r, k);
+    *(uint16_t*)(base + (par * 3 + 0) * TC_TILE_BYTES + off) = s0;
+    *(uint16_t*)(base + (par * 3 + 1) * TC_TILE_BYTES + off) = s1;
+    *(uint16_t*)(base + (par * 3 + 2) * TC_TILE_BYTES + off) = s2;
+  }
+}
+
+struct TcSmem {
+  uint8_t a[6 * TC_TILE_BYTES];    // [par][split] table tiles (bulk-copied), 48 KiB
+  uint8_t b[6 * TC_BTILE_BYTES];   // [par][split] field tiles (written by the threads), 24 KiB
+  uint64_t bar_a, bar_mma;
+  uint32_t tmem;
+};
+
+// store the 8 values of one K group of one field row (n) as the three BF16 splits
+__device__ __forceinline__ void store_split8(uint8_t* b, int par, int n, int kg, const float* v) {
+  uint16_t h[3][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) split3(v[q], h[0][q], h[1][q], h[2][q]);
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    uint4 u;
+    u.x = (uint32_t)h[s][0] | ((uint32_t)h[s][1] << 16);
+    u.y = (uint32_t)h[s][2] | ((uint32_t)h[s][3] << 16);
+    u.z = (uint32_t)h[s][4] | ((uint32_t)h[s][5] << 16);
+    u.w = (uint32_t)h[s][6] | ((uint32_t)h[s][7] << 16);
+    *(uint4*)(b + (par * 3 + s) * TC_BTILE_BYTES + tc_off(n, kg * 8)) = u;
+  }
+}
+
+// the two-parity bf16x3 MMA group of one K chunk: D_par += A_par * B_par, six split products
+__device__ __forceinline__ void tc_issue_chunk(TcSmem& sm, uint32_t tmem, bool first) {
+  const uint32_t idesc = idesc_bf16(128, 2 * TC_NZ);
+  const int SA[6] = {0, 0, 1, 0, 1, 2}, SB[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+  for (int par = 0; par < 2; ++par)
+#pragma unroll
+    for (int ks = 0; ks < TC_KC / 16; ++ks)
+#pragma unroll
+      for (int p = 0; p < 6; ++p) {
+        uint32_t aaddr = smem_u32(sm.a + (par * 3 + SA[p]) * TC_TILE_BYTES) + ks * 2 * TC_LBO;
+        uint32_t baddr = smem_u32(sm.b + (par * 3 + SB[p]) * TC_BTILE_BYTES) + ks * 2 * TC_LBO;
+        uint32_t acc = (!first || ks > 0 || p > 0) ? 1u : 0u;
+        umma_bf16(tmem + par * (2 * TC_NZ), sdesc(aaddr, TC_LBO, TC_SBO), sdesc(baddr, TC_LBO, TC_SBO), idesc, acc);
+      }
+}
+
+// mode 0 = forward (rtrans_forward), mode 1 = backward (rtrans_backward, + ln term at m = 0)
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restrict__ in, double2* __restrict__ out,
+                                                          const uint16_t* __restrict__ img, const float* __restrict__ w32,
+                                                          const double* __restrict__ lnx, const double* __restrict__ lnp,
+                                                          int add_ln, int nr, int nrh, int nrdim, int npdim, int nzdim,
+                                                          int nrc, int nmt, int nkc, int* __restrict__ status) {
+  extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(tc_smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int z0 = blockIdx.x * TC_NZ, mt = blockIdx.y, m = blockIdx.z;
+  const int nn = max(min(nrc, nrc - m), 0);
+  if (MODE == 0 && 2 * (mt * 128) >= nn) return;   // no rows of either parity in this tile
+  if (MODE == 1 && (nn == 0 || mt * 128 >= nrh)) return;
+  const int nkc_m = (MODE == 0) ? nkc : min(nkc, (((nn + 1) / 2) + TC_KC - 1) / TC_KC);   // bwd: K = rows t
+  if (tid == 0) {
+    mbar_init(&sm.bar_a, 1);
+    mbar_init(&sm.bar_mma, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&sm.tmem, 128);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem;
+  bool ok = true;
+  const uint8_t* img_m = (const uint8_t*)img + ((size_t)m * nmt + mt) * nkc * (size_t)(6 * TC_TILE_BYTES);
+  // staging item of this thread: z column zz and K group kg (8 consecutive K indices)
+  const int zz = tid % TC_NZ, kg = tid / TC_NZ;
+  const int z = z0 + zz;
+  const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * min(z, nzdim - 1));
+  float2 ra[8], rb[8];
+  float wv[8];
+  auto fetch = [&](int kc) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      int k = kc * TC_KC + kg * 8 + q;
+      ra[q] = make_float2(0.f, 0.f); rb[q] = make_float2(0.f, 0.f); wv[q] = 0.f;
+      if (MODE == 0) {
+        if (k < nrh && z < nzdim) { ra[q] = ld_c32(col + k); rb[q] = ld_c32(col + nr - 1 - k); wv[q] = w32[k]; }
+      } else {
+        int je = 2 * k, jo = 2 * k + 1;
+        if (z < nzdim) {
+          if (je < nn) ra[q] = ld_c32(col + je);
+          if (jo < nn) rb[q] = ld_c32(col + jo);
+        }
+      }
+    }
+  };
+  fetch(0);
+  for (int kc = 0; kc < nkc_m; ++kc) {
+    if (tid == 0) {
+      mbar_expect_tx(&sm.bar_a, 6 * TC_TILE_BYTES);
+      bulk_g2s(sm.a, img_m + (size_t)kc * (6 * TC_TILE_BYTES), 6 * TC_TILE_BYTES, &sm.bar_a);
+    }
+    {
+      float v[8];
+      if (MODE == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x + rb[q].x) * wv[q];
+        store_split8(sm.b, 0, 2 * zz, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y + rb[q].y) * wv[q];
+        store_split8(sm.b, 0, 2 * zz + 1, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x - rb[q].x) * wv[q];
+        store_split8(sm.b, 1, 2 * zz, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y - rb[q].y) * wv[q];
+        store_split8(sm.b, 1, 2 * zz + 1, kg, v);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = ra[q].x;
+        store_split8(sm.b, 0, 2 * zz, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = ra[q].y;
+        store_split8(sm.b, 0, 2 * zz + 1, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = rb[q].x;
+        store_split8(sm.b, 1, 2 * zz, kg, v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = rb[q].y;
+        store_split8(sm.b, 1, 2 * zz + 1, kg, v);
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      ok = ok && mbar_wait(&sm.bar_a, kc & 1);
+      tc_fence_after();
+      if (ok) tc_issue_chunk(sm, tmem, kc == 0);
+      umma_commit(&sm.bar_mma);
+    }
+    if (kc + 1 < nkc_m) fetch(kc + 1);   // the next chunk's loads overlap the MMAs
+    bool done = mbar_wait(&sm.bar_mma, kc & 1);
+    if (!done || (tid == 0 && !ok)) atomicExch(status, 2);
+    __syncthreads();
+  }
+  tc_fence_after();
+  if (MODE == 0) {
+    // warp w holds rows t = mt*128 + 32w + lane of both parities
+    const int t = mt * 128 + warp * 32 + lane;
+#pragma unroll
+    for (int par = 0; par < 2; ++par) {
+      int j = 2 * t + par;
+#pragma unroll
+      for (int cb = 0; cb < (2 * TC_NZ) / 16; ++cb) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + par * (2 * TC_NZ) + cb * 16, v);
+        if (j < nn) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            int zo = z0 + cb * 8 + q;
+            if (zo < nzdim)
+              out[j + (size_t)nrdim * (m + (size_t)npdim * zo)] = make_double2(f2d_fast(v[2 * q]), f2d_fast(v[2 * q + 1]));
+          }
+        }
+      }
+    }
+  } else {
+    // warp w holds radial points i = mt*128 + 32w + lane: f(i) = be + bo, f(nr-1-i) = be - bo
+    const int i = mt * 128 + warp * 32 + lane;
+    double lnv = (add_ln && m == 0) ? *lnp : 0.0;
+#pragma unroll
+    for (int cb = 0; cb < (2 * TC_NZ) / 16; ++cb) {
+      float ve[16], vo[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 0 * (2 * TC_NZ) + cb * 16, ve);
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 1 * (2 * TC_NZ) + cb * 16, vo);
+      if (i < nrh) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          int zo = z0 + cb * 8 + q;
+          if (zo >= nzdim) continue;
+          size_t b0 = (size_t)nrdim * (m + (size_t)npdim * zo);
+          double2 p = make_double2(f2d_fast(ve[2 * q] + vo[2 * q]), f2d_fast(ve[2 * q + 1] + vo[2 * q + 1]));
+          double2 qq = make_double2(f2d_fast(ve[2 * q] - vo[2 * q]), f2d_fast(ve[2 * q + 1] - vo[2 * q + 1]));
+          if (lnv != 0.0) { p.x += lnv * lnx[i]; qq.x += lnv * lnx[nr - 1 - i]; }
+          out[b0 + i] = p;
+          out[b0 + nr - 1 - i] = qq;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ------------------------------------------------------------------------------------------------
+struct TcImg {
+  uint16_t* p = nullptr;
+  size_t bytes = 0;
+  int nrc = -1, npc = -1;
+};
+static TcImg g_img[2];
+
+void tc_free() {
+  for (auto& t : g_img) {
+    if (t.p) dfree(t.p, t.bytes);
+    t = TcImg();
+  }
+}
+
+// forward (mode 0) / backward (mode 1) contraction on the tensor cores; out zeroed by the caller
+static int tc_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln) {
+  int nrows = (mode == 0) ? (nrc + 1) / 2 : G.nrh;           // M: rows of a parity (fwd) / radial points (bwd)
+  int nk = (mode == 0) ? G.nrh : (nrc + 1) / 2;              // K: radial points (fwd) / rows of a parity (bwd)
+  int nmt = cdiv(nrows, 128), nkc = cdiv(nk, TC_KC);
+  TcImg& im = g_img[mode];
+  if (im.nrc != nrc || im.npc != npc || !im.p) {
+    if (im.p) dfree(im.p, im.bytes);
+    im = TcImg();
+    im.bytes = (size_t)npc * nmt * nkc * 6 * TC_TILE_BYTES;
+    MLG_TRY(dmalloc((void**)&im.p, im.bytes));
+    k_tc_table<<<npc * nmt * nkc, 256, 0, G.stream>>>(G.pf, im.p, G.nrh, G.ne, nmt, nkc, nrc, mode);
+    MLG_LAUNCH();
+    im.nrc = nrc;
+    im.npc = npc;
+  }
+  size_t sm = sizeof(TcSmem) + 1024;
+  dim3 grid(cdiv(G.nzdim, TC_NZ), nmt, npc);
+  int* st = (int*)(G.dscal + DS_FLAG + 1) + 1;
+  if (mode == 0) {
+    MLG_CUDA(cudaFuncSetAttribute(k_tc_rtrans<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_tc_rtrans<0><<<grid, TC_THREADS, sm, G.stream>>>(in, out, im.p, G.w32, G.lnx, lnp, 0, G.nr, G.nrh, G.nrdim, G.npdim,
+                                                       G.nzdim, nrc, nmt, nkc, st);
+  } else {
+    MLG_CUDA(cudaFuncSetAttribute(k_tc_rtrans<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_tc_rtrans<1><<<grid, TC_THREADS, sm, G.stream>>>(in, out, im.p, G.w32, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
+                                                       G.nrdim, G.npdim, G.nzdim, nrc, nmt, nkc, st);
+  }
+  MLG_LAUNCH();
+  return 0;
+}
+
+int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc) { return tc_rtrans(0, in, out, nrc, npc, nullptr, false); }
+int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln) {
+  return tc_rtrans(1, in, out, nrc, npc, lnp, add_ln);
+}
+
+}  // namespace mlg
