@@ -116,6 +116,22 @@ def dist_setup(n_gpus):
     return rank, world, local, pg
 
 
+def max_over_ranks(pg, ms):
+    """The slowest rank's time: replicas run concurrently, the job ends with the last one."""
+    if pg is None:
+        return ms
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_steps_per_s(world, steps, ms):
+    """Whole-job throughput: every rank advanced its own replica by `steps` in `ms` (max over ranks)."""
+    return world * steps / (ms / 1e3)
+
+
 def run_reference(args, rank, world, pg):
     """The reference arm: the CPU path (oracle port) on this host's cores, rank 0 only."""
     if rank != 0:
@@ -215,11 +231,8 @@ def run_ours(args, rank, world, local, pg):
 
         clocks = Clocks(local)
         ms_mixed, launches, ck = timed(MIXED, args.steps, args.warmup, clocks)
-        if pg:
-            t = torch.tensor([ms_mixed], device="cuda")
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            ms_mixed = float(t.item())
-        value = world * args.steps / (ms_mixed / 1e3)
+        ms_mixed = max_over_ranks(pg, ms_mixed)
+        value = job_steps_per_s(world, args.steps, ms_mixed)
 
         # plain FP64 over the same steps, and the error of mixed against it
         k_cmp = min(args.steps, 20)
