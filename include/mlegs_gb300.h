@@ -168,6 +168,33 @@ int mlg_vortex_run(mlg_scalar psi, mlg_scalar chi, mlg_scalar nlpsi, mlg_scalar 
                    mlg_scalar psi_p, mlg_scalar chi_p, mlg_scalar nlpsi_p, mlg_scalar nlchi_p,
                    mlg_scalar uz, double dt, int nsteps, double* gains);
 
+/* ---- adjoint (no counterpart in the reference) ------------------------------------------- */
+/* Inner product for every adjoint below: <a, b> = sum over the whole stored array of
+ * Re(conj(a.e) b.e) + a.ln * b.ln.  Each mlg_adj_* applies the exact transpose of the named forward
+ * entry point (as implemented here) in place on an adjoint variable.  Requires is_svv = 0 and
+ * hyperpow = 0 (MLG_EPARAM otherwise). */
+/* The gradient of J = 1/2 sum W |u'|^2 at step nsteps of the vortex step sequence started from
+ * (psi0, chi0) [psi <- psi0, nl <- advection_rhs, nl_p <- nl, then mlg_vortex_step nsteps times],
+ * u' the velocity without the (m = 0, k = 0) column and ln, W the volume quadrature weights
+ * w_i r_i^2/(1-x_i^2) (2 pi/np)(zlen/nz).  The forward state is kept every k_ckpt steps and each
+ * segment recomputed on the way back.  grad_psi/grad_chi NULL: J only.  psi0, chi0 unchanged. */
+int mlg_adjoint_run(mlg_scalar psi0, mlg_scalar chi0, mlg_scalar uz, double dt, int nsteps, int k_ckpt,
+                    mlg_scalar grad_psi, mlg_scalar grad_chi, double* J);
+/* One step: state = (psi, chi, nlpsi, nlchi, nlpsi_p, nlchi_p) at the step's start (unchanged);
+ * adj = the adjoint of the state at its end, replaced by the adjoint at its start. */
+int mlg_adj_vortex_step(const mlg_scalar* state, mlg_scalar uz, double dt, const mlg_scalar* adj);
+int mlg_adj_trans(mlg_scalar s, const char* forward_from_space);  /* s.space: the forward's target */
+int mlg_adj_band(mlg_scalar s, int op);          /* op 0 xxdx, 1 del2h, 2 del2 */
+int mlg_adj_ihelm(mlg_scalar s, double alpha);
+int mlg_adj_idel2_proln(mlg_scalar s);
+int mlg_adj_zeroat1(mlg_scalar s);
+int mlg_adj_tp2vec(mlg_scalar vr_bar, mlg_scalar vp_bar, mlg_scalar vz_bar, mlg_scalar psi_bar, mlg_scalar chi_bar);
+int mlg_adj_tp2curlvec(mlg_scalar wr_bar, mlg_scalar wp_bar, mlg_scalar wz_bar, mlg_scalar psi_bar, mlg_scalar chi_bar);
+int mlg_adj_vec2tp(mlg_scalar psi_bar, mlg_scalar chi_bar, mlg_scalar vr_bar, mlg_scalar vp_bar, mlg_scalar vz_bar);
+/* advection_rhs linearised at (psi, chi) (not modified): (nlpsi_bar, nlchi_bar) -> (psi_bar, chi_bar) */
+int mlg_adj_advection(mlg_scalar psi, mlg_scalar chi, mlg_scalar uz, mlg_scalar nlpsi_bar, mlg_scalar nlchi_bar,
+                      mlg_scalar psi_bar, mlg_scalar chi_bar);
+
 /* ---- kernel timing (CUDA events around each launch of one kernel class) ----------------- */
 /* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators and solves,
  *       3 = backward radial contraction, 4 = vec2tp projection contraction.  work = flops for the

@@ -1,0 +1,904 @@
+// adjoint.cu — the discrete adjoint of the 3-D vortex step and of the operators it is built from.
+// The reference has no adjoint; this is new functionality behind the same scalar API.
+//
+// Inner product.  <a, b> = sum over every stored entry of Re(conj(a.e) b.e) + a.ln * b.ln: the
+// Euclidean product of the real and imaginary parts of the whole (nrdim, npdim, nzdim) array plus
+// the log-term coefficient.  Every *_T routine applies the exact transpose, under this product, of
+// the forward routine it is named after, as that routine is implemented in this library (padding
+// rows, chopped slots, the shared Nyquist slot and the log-term bookkeeping included), so
+// <F x, y> = <x, F^T y> holds to rounding for each of them.  An adjoint variable is stored in a
+// Scalar and labelled with the space of the forward quantity it is the adjoint of.
+//
+// The step.  With SVV off and hyperpow = 0 the vortex step is a polynomial map of its state
+// (psi, chi, nl_psi, nl_chi, nl_psi_prev, nl_chi_prev): linear operators around one bilinear
+// product u x omega.  Its transpose needs the state at the end of the step (the point the next
+// nonlinear term is evaluated at); the driver keeps the full state every K steps and recomputes
+// each K-step segment forward before sweeping it backward.
+//
+// Objective.  J = 1/2 sum_{i < nr, phi, z} W_i |u'|^2 with u' the velocity of (psi, chi) without
+// their axisymmetric, z-independent column (m = 0, k = 0, all n, and ln), and
+// W_i = w_i r_i^2 / (1 - x_i^2) * (2 pi / np) * (zlen / nz) the quadrature of the volume integral
+// r dr dphi dz over the mapped Gauss-Legendre points (dr/dx = r / (1 - x^2)).
+#include "common.cuh"
+#include <cmath>
+#include <vector>
+
+namespace mlg {
+
+int vfft_checked_T(Scalar& s, int dir);
+
+// ------------------------------------------------------------------------------------------------
+// kernels
+
+// hfft forward^T, before the half-complex-to-real sum: slot 0 and slot L scaled 1/np, the interior
+// 1/(2 np) (the forward's X_k for 0 < k < L stands for two conjugate terms of the real sum)
+__global__ void k_hfftT_pre(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int L, double np) {
+  size_t n = (size_t)nrdim * (L + 1) * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int k = (int)((idx / (unsigned)nrdim) % (unsigned)(L + 1));
+    int z = (int)(idx / (unsigned)(nrdim * (L + 1)));
+    double f = (k == 0 || k == L) ? 1.0 / np : 0.5 / np;
+    double2* p = e + i + (size_t)nrdim * (k + (size_t)npdim * z);
+    p->x *= f; p->y *= f;
+  }
+}
+
+// slot L of every (r, z) row: saved to buf (save = 1) or zeroed (save = 0)
+__global__ void k_slotL(double2* __restrict__ e, double2* __restrict__ buf, int nrdim, int npdim, int nzdim, int L, int save) {
+  size_t n = (size_t)nrdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int z = (int)(idx / (unsigned)nrdim);
+    double2* p = e + i + (size_t)nrdim * (L + (size_t)npdim * z);
+    if (save) buf[idx] = *p;
+    else *p = make_double2(0.0, 0.0);
+  }
+}
+
+// hfft backward^T, after the unnormalised real-to-half-complex sum X_k = sum_j f_j e^{-2 pi i jk/np}:
+// interior doubled; slot L also takes np times the saved adjoint of the forward's slot-L copy
+__global__ void k_hfftT_post(double2* __restrict__ e, const double2* __restrict__ buf, int nrdim, int npdim, int nzdim,
+                             int L, double np) {
+  size_t n = (size_t)nrdim * (L + 1) * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int k = (int)((idx / (unsigned)nrdim) % (unsigned)(L + 1));
+    int z = (int)(idx / (unsigned)(nrdim * (L + 1)));
+    double2* p = e + i + (size_t)nrdim * (k + (size_t)npdim * z);
+    if (k > 0 && k < L) { p->x *= 2.0; p->y *= 2.0; }
+    if (k == L) { double2 b = buf[i + (size_t)nrdim * z]; p->x += np * b.x; p->y += np * b.y; }
+  }
+}
+
+// rows i < nr of every column scaled by tab[i] (inv = 0) or divided by it (inv = 1)
+__global__ void k_scale_tab(double2* __restrict__ e, const double* __restrict__ tab, int nr, int nrdim, size_t ncol, int inv) {
+  size_t n = (size_t)nr * ncol;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nr);
+    unsigned c = idx / (unsigned)nr;
+    double2* p = e + i + (size_t)nrdim * c;
+    double v = inv ? 1.0 / tab[i] : tab[i];
+    p->x *= v; p->y *= v;
+  }
+}
+
+// *lnp += sgn * sum_{i < nr, z} lnx_i Re e(i, 0, z): the adjoint of e(:nr, 1, :) += ln * lnx
+__global__ void k_ln_dot(const double2* __restrict__ e, const double* __restrict__ lnx, int nr, int nrdim, int npdim,
+                         int nzdim, double* __restrict__ lnp, double sgn) {
+  __shared__ double red[256];
+  double s = 0.0;
+  size_t n = (size_t)nr * nzdim;
+  for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    int i = (int)(idx % (unsigned)nr);
+    int z = (int)(idx / (unsigned)nr);
+    s += lnx[i] * e[i + (size_t)nrdim * npdim * z].x;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *lnp += sgn * red[0];
+}
+
+// zeroat1^T: the forward sets e(0,0,k) <- e(0,0,k) - sum_{n<nmax} at_n e(n,0,k) / at_0, so
+// e_bar(n,0,k) -= at_n / at_0 * e_bar(0,0,k) for n < nmax (which leaves e_bar(0,0,k) = 0); warp per k
+__global__ void k_zeroat1_T(double2* __restrict__ e, const double* __restrict__ at, int nmax, int nrdim, int npdim, int nzdim) {
+  int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int lane = threadIdx.x & 31;
+  if (k >= nzdim) return;
+  double2* col = e + (size_t)nrdim * npdim * k;
+  double bx = 0.0, by = 0.0;
+  if (lane == 0) { bx = col[0].x; by = col[0].y; }
+  bx = __shfl_sync(0xffffffffu, bx, 0);
+  by = __shfl_sync(0xffffffffu, by, 0);
+  double a0 = at[0];
+  for (int n = lane; n < nmax; n += 32) {
+    double f = at[n] / a0;
+    col[n].x -= f * bx;
+    col[n].y -= f * by;
+  }
+}
+
+// ihelm^T log term, after the transposed solve: the forward took lno = ln / alpha and
+// e(n,0,0).x -= cf_n lno with cf = (4/3, -2, 2/3) / (ell^2 exp(lognorm_n))
+__global__ void k_ihelm_T_ln(const double2* __restrict__ e, double* __restrict__ lnp, const double* __restrict__ lognorm,
+                             double ell, double alpha) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double e2 = ell * ell;
+  double lno = *lnp - (4.0 / 3.0 / e2 / exp(lognorm[0]) * e[0].x - 2.0 / 1.0 / e2 / exp(lognorm[1]) * e[1].x +
+                       2.0 / 3.0 / e2 / exp(lognorm[2]) * e[2].x);
+  *lnp = lno / alpha;
+}
+
+// idel2_proln^T log term, before the transposed solve: the forward set ln = Re x(0,0,0) exp(lognorm_0)
+// and ignored the incoming ln
+__global__ void k_idel2_T_ln(double2* __restrict__ e, double* __restrict__ lnp, const double* __restrict__ lognorm) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  e[0].x += *lnp * exp(lognorm[0]);
+  *lnp = 0.0;
+}
+
+// calcat^T of vec2tp: the forward set psi%ln = -1/2 Re sum_{n<nmax} at1_n up(n,0,0)
+__global__ void k_calcat_T(double2* __restrict__ e, const double* __restrict__ at, int nmax, const double* __restrict__ lnbar,
+                           double f) {
+  double l = *lnbar;
+  for (int n = threadIdx.x; n < nmax; n += blockDim.x) e[n].x += f * at[n] * l;
+}
+
+// *lnp += sum_{i < nr} (1 + x_i) Re e(i, 0, 0): the adjoint of k_add_ln_x
+__global__ void k_add_ln_x_T(const double2* __restrict__ e, const double* __restrict__ x, int nr, double* __restrict__ lnp) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) s += (1.0 + x[i]) * e[i].x;
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *lnp += red[0];
+}
+
+// k_tp2vec_mix^T.  Forward on the active entries: ur <- i m psi + i k ur, up <- -up - m k uz;
+// transposed (conjugate coefficients): psi_bar += -i m ur_bar, uz_bar += -m k up_bar,
+// ur_bar <- -i k ur_bar, up_bar <- -up_bar; the other entries pass through unchanged.
+__global__ void k_tp2vec_mix_T(double2* __restrict__ ur, double2* __restrict__ up, double2* __restrict__ psi,
+                               double2* __restrict__ uz, const double* __restrict__ ak, int nrdim, int npdim, int nzdim,
+                               int nrc, int npc, int nzc, int nzcu) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    int k = (int)(idx / (unsigned)(nrdim * npdim));
+    if (m >= npc) continue;
+    int nn = max(min(nrc, nrc - m), 0);
+    int kk = k + 1;
+    if (i >= nn || !(kk <= nzc || kk >= nzcu)) continue;
+    double kv = ak[k], mv = (double)m;
+    double2 a = ur[idx], b = up[idx];
+    psi[idx].x += mv * a.y;  psi[idx].y -= mv * a.x;   // -i m a
+    uz[idx].x -= mv * kv * b.x;  uz[idx].y -= mv * kv * b.y;
+    ur[idx] = make_double2(kv * a.y, -kv * a.x);        // -i k a
+    up[idx] = make_double2(-b.x, -b.y);
+  }
+}
+
+// vecprod^T around (v, w): the forward o = v x w on each packed real (i < nr, slots < np/2; zero
+// elsewhere); <o_bar, dv x w + v x dw> gives v_bar = w x o_bar, w_bar = o_bar x v
+__global__ void k_vecprod_T(double2* __restrict__ vbr, double2* __restrict__ vbp, double2* __restrict__ vbz,
+                            double2* __restrict__ wbr, double2* __restrict__ wbp, double2* __restrict__ wbz,
+                            const double2* __restrict__ vr, const double2* __restrict__ vp, const double2* __restrict__ vz,
+                            const double2* __restrict__ wr, const double2* __restrict__ wp, const double2* __restrict__ wz,
+                            const double2* __restrict__ obr, const double2* __restrict__ obp, const double2* __restrict__ obz,
+                            int nr, int nph, int nrdim, int npdim, int nzdim) {
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    double2 a1 = make_double2(0, 0), a2 = a1, a3 = a1, b1 = a1, b2 = a1, b3 = a1;
+    if (i < nr && m < nph) {
+      double2 V1 = vr[idx], V2 = vp[idx], V3 = vz[idx], W1 = wr[idx], W2 = wp[idx], W3 = wz[idx];
+      double2 O1 = obr[idx], O2 = obp[idx], O3 = obz[idx];
+      // w x o
+      a1 = make_double2(W2.x * O3.x - W3.x * O2.x, W2.y * O3.y - W3.y * O2.y);
+      a2 = make_double2(W3.x * O1.x - W1.x * O3.x, W3.y * O1.y - W1.y * O3.y);
+      a3 = make_double2(W1.x * O2.x - W2.x * O1.x, W1.y * O2.y - W2.y * O1.y);
+      // o x v
+      b1 = make_double2(O2.x * V3.x - O3.x * V2.x, O2.y * V3.y - O3.y * V2.y);
+      b2 = make_double2(O3.x * V1.x - O1.x * V3.x, O3.y * V1.y - O1.y * V3.y);
+      b3 = make_double2(O1.x * V2.x - O2.x * V1.x, O1.y * V2.y - O2.y * V1.y);
+    }
+    vbr[idx] = a1; vbp[idx] = a2; vbz[idx] = a3;
+    wbr[idx] = b1; wbp[idx] = b2; wbz[idx] = b3;
+  }
+}
+
+// The vec2tp contraction transposed.  Forward, row j of parity p (sign s = +1 for even p, -1 odd):
+//   psi_j = -i m (V F_s(ur))_j - (D F_o(up))_j
+//   chi_j = i k (D F_o(ur))_j + m k (V F_s(up))_j - (T F_s(uz))_j
+// with F_s(u)_i = u_i + s u_{nr-1-i}, F_o(u)_i = u_i - s u_{nr-1-i}, i < nr/2.  Transposed, per
+// parity: S1 = V^T psi_bar, S2 = D^T psi_bar, S3 = D^T chi_bar, S4 = V^T chi_bar, S5 = T^T chi_bar
+// (sums over that parity's rows), then F_s_bar(ur) = i m S1, F_o_bar(ur) = -i k S3,
+// F_s_bar(up) = m k S4, F_o_bar(up) = -S2, F_s_bar(uz) = -S5, unfolded as
+// u_bar_i += F_s_bar + F_o_bar, u_bar_{nr-1-i} += s (F_s_bar - F_o_bar).
+// One CTA per (m, z tile, i tile); each thread one (i, z) pair; rows staged in shared memory.
+template <int IT, int ZT, int KC>
+__global__ void __launch_bounds__(IT * ZT / 2)
+k_vec2tp_T(const double2* __restrict__ psib, const double2* __restrict__ chib, double2* __restrict__ urb,
+           double2* __restrict__ upb, double2* __restrict__ uzb, const double* __restrict__ tV, const double* __restrict__ tD,
+           const double* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
+           int nzdim, int nrc, int nzc, int nzcu) {
+  __shared__ double Vs[KC][IT + 1], Ds[KC][IT + 1], Ts[KC][IT + 1];
+  __shared__ double2 Ps[KC][ZT], Cs[KC][ZT];
+  int m = blockIdx.z;
+  int i0 = blockIdx.y * IT, z0 = blockIdx.x * ZT;
+  int nn = max(min(nrc, nrc - m), 0);
+  int tz = threadIdx.x % ZT, ti = threadIdx.x / ZT;   // ZT columns x (IT/2) rows of threads
+  constexpr int NT = IT * ZT / 2;
+  // two i per thread: ti and ti + IT/2
+  double2 S[2][2][5];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) S[a][p][q] = make_double2(0.0, 0.0);
+  int z = z0 + tz;
+  int kk = z + 1;
+  bool zact = z < nzdim && (kk <= nzc || kk >= nzcu);
+  for (int j0 = 0; j0 < nn; j0 += KC) {
+    for (int idx = threadIdx.x; idx < KC * IT; idx += NT) {
+      int jj = idx / IT, ii = idx % IT;
+      int j = j0 + jj, i = i0 + ii;
+      double v = 0.0, d = 0.0, t = 0.0;
+      if (j < nn && i < nrh) {
+        size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
+        v = tV[o]; d = tD[o]; t = tT[o];
+      }
+      Vs[jj][ii] = v; Ds[jj][ii] = d; Ts[jj][ii] = t;
+    }
+    for (int idx = threadIdx.x; idx < KC * ZT; idx += NT) {
+      int jj = idx / ZT, zz = idx % ZT;
+      int j = j0 + jj, zg = z0 + zz;
+      double2 pv = make_double2(0.0, 0.0), cv = pv;
+      if (j < nn && zg < nzdim) {
+        size_t o = j + (size_t)nrdim * (m + (size_t)npdim * zg);
+        pv = psib[o]; cv = chib[o];
+      }
+      Ps[jj][zz] = pv; Cs[jj][zz] = cv;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < KC; ++jj) {
+      int p = (j0 + jj) & 1;
+      double2 pv = Ps[jj][tz], cv = Cs[jj][tz];
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        int ii = ti + a * (IT / 2);
+        double v = Vs[jj][ii], d = Ds[jj][ii], t = Ts[jj][ii];
+        S[a][p][0].x += v * pv.x; S[a][p][0].y += v * pv.y;
+        S[a][p][1].x += d * pv.x; S[a][p][1].y += d * pv.y;
+        S[a][p][2].x += d * cv.x; S[a][p][2].y += d * cv.y;
+        S[a][p][3].x += v * cv.x; S[a][p][3].y += v * cv.y;
+        S[a][p][4].x += t * cv.x; S[a][p][4].y += t * cv.y;
+      }
+    }
+    __syncthreads();
+  }
+  if (!zact) return;
+  double kv = ak[z], mv = (double)m;
+  size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    int i = i0 + ti + a * (IT / 2);
+    if (i >= nrh) continue;
+    double2 r_lo = make_double2(0, 0), r_hi = r_lo, p_lo = r_lo, p_hi = r_lo, z_lo = r_lo, z_hi = r_lo;
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      double s = p ? -1.0 : 1.0;
+      double2 S1 = S[a][p][0], S2 = S[a][p][1], S3 = S[a][p][2], S4 = S[a][p][3], S5 = S[a][p][4];
+      double2 fs_r = make_double2(-mv * S1.y, mv * S1.x);    // i m S1
+      double2 fo_r = make_double2(kv * S3.y, -kv * S3.x);    // -i k S3
+      double2 fs_p = make_double2(mv * kv * S4.x, mv * kv * S4.y);
+      double2 fo_p = make_double2(-S2.x, -S2.y);
+      double2 fs_z = make_double2(-S5.x, -S5.y);
+      r_lo.x += fs_r.x + fo_r.x; r_lo.y += fs_r.y + fo_r.y;
+      r_hi.x += s * (fs_r.x - fo_r.x); r_hi.y += s * (fs_r.y - fo_r.y);
+      p_lo.x += fs_p.x + fo_p.x; p_lo.y += fs_p.y + fo_p.y;
+      p_hi.x += s * (fs_p.x - fo_p.x); p_hi.y += s * (fs_p.y - fo_p.y);
+      z_lo.x += fs_z.x; z_lo.y += fs_z.y;
+      z_hi.x += s * fs_z.x; z_hi.y += s * fs_z.y;
+    }
+    urb[base + i] = r_lo; urb[base + nr - 1 - i] = r_hi;
+    upb[base + i] = p_lo; upb[base + nr - 1 - i] = p_hi;
+    uzb[base + i] = z_lo; uzb[base + nr - 1 - i] = z_hi;
+  }
+}
+
+// J = 1/2 sum W_i |u|^2 over i < nr, slots < np/2 (both packed reals), every z; u_bar = W u
+// (zero elsewhere); one partial sum per block
+__global__ void k_energy(double2* __restrict__ ubr, double2* __restrict__ ubp, double2* __restrict__ ubz,
+                         const double2* __restrict__ vr, const double2* __restrict__ vp, const double2* __restrict__ vz,
+                         const double* __restrict__ wq, int nr, int nph, int nrdim, int npdim, int nzdim,
+                         double* __restrict__ partial) {
+  __shared__ double red[256];
+  double s = 0.0;
+  size_t n = (size_t)nrdim * npdim * nzdim;
+  GRID_STRIDE(idx, n) {
+    int i = (int)(idx % (unsigned)nrdim);
+    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
+    double2 a = vr[idx], b = vp[idx], c = vz[idx];
+    double q = (i < nr && m < nph) ? wq[i] : 0.0;
+    s += 0.5 * q * (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y);
+    if (ubr) {
+      ubr[idx] = make_double2(q * a.x, q * a.y);
+      ubp[idx] = make_double2(q * b.x, q * b.y);
+      ubz[idx] = make_double2(q * c.x, q * c.y);
+    }
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// W_i = w_i r_i^2 / (1 - x_i^2) * dphi * dz
+__global__ void k_energy_weights(double* __restrict__ wq, const double* __restrict__ x, const double* __restrict__ w,
+                                 const double* __restrict__ r, int nr, double dpz) {
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) wq[i] = w[i] * r[i] * r[i] / (1.0 - x[i] * x[i]) * dpz;
+}
+
+// the perturbation: the (m = 0, k = 0) column and ln removed
+__global__ void k_drop_mean(double2* __restrict__ e, double* __restrict__ lnp, int nrdim) {
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) e[i] = make_double2(0.0, 0.0);
+  if (threadIdx.x == 0) *lnp = 0.0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// transposed operators on Scalars (each in place on the adjoint variable s)
+
+static int hfft_fwd_T(Scalar& s) {   // PFP-side adjoint -> PPP-side
+  if (G.np <= 1) return 0;
+  int L = G.np / 2;
+  k_hfftT_pre<<<nblk((size_t)G.nrdim * (L + 1) * G.nzdim), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, L, (double)G.np);
+  MLG_LAUNCH();
+  MLG_TRY(launch_hfft_bwd_buf(s.e));
+  k_slotL<<<nblk((size_t)G.nrdim * G.nzdim), 256, 0, G.stream>>>(s.e, nullptr, G.nrdim, G.npdim, G.nzdim, L, 0);
+  MLG_LAUNCH();
+  return 0;
+}
+
+static int hfft_bwd_T(Scalar& s) {   // PPP-side adjoint -> PFP-side
+  if (G.np <= 1) return 0;
+  int L = G.np / 2;
+  cd* buf = get_buf();
+  if (!buf) return set_error(MLG_EALLOC, "adjoint: out of device memory");
+  k_slotL<<<nblk((size_t)G.nrdim * G.nzdim), 256, 0, G.stream>>>(s.e, (double2*)buf, G.nrdim, G.npdim, G.nzdim, L, 1);
+  MLG_LAUNCH();
+  int rc = launch_hfft_fwd_scaled(s.e, 1.0);
+  if (!rc) {
+    k_hfftT_post<<<nblk((size_t)G.nrdim * (L + 1) * G.nzdim), 256, 0, G.stream>>>(s.e, (const double2*)buf, G.nrdim,
+                                                                                  G.npdim, G.nzdim, L, (double)G.np);
+    ++G.launches;
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) rc = set_error(MLG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+  }
+  put_buf(buf);
+  return rc;
+}
+
+static int scale_tab(Scalar& s, const double* tab, int inv) {
+  size_t ncol = (size_t)G.npdim * G.nzdim;
+  k_scale_tab<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, tab, G.nr, G.nrdim, ncol, inv);
+  MLG_LAUNCH();
+  return 0;
+}
+
+static int ln_dot(Scalar& s, double sgn) {
+  k_ln_dot<<<1, 256, 0, G.stream>>>(s.e, G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, s.ln, sgn);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// the PFP -> FFP step (e(:nr,1,:) -= ln lnx, then rtrans_forward) transposed: FFP-side -> PFP-side.
+// rtrans_forward^T = w * rtrans_backward (the quadrature weights are symmetric about the fold).
+static int rtrans_fwd_T(Scalar& s) {
+  MLG_TRY(launch_rtrans_bwd(s, false));
+  MLG_TRY(scale_tab(s, G.w, 0));
+  return ln_dot(s, -1.0);
+}
+
+// the FFP -> PFP step (rtrans_backward with the log term) transposed: PFP-side -> FFP-side.
+// rtrans_backward^T = rtrans_forward of the input divided by the weights.
+static int rtrans_bwd_T(Scalar& s, bool with_ln) {
+  if (with_ln) MLG_TRY(ln_dot(s, 1.0));
+  MLG_TRY(scale_tab(s, G.w, 1));
+  return launch_rtrans_fwd(s);
+}
+
+int vfft_checked_T(Scalar& s, int dir) {   // transpose of vertical_fft (dir -1 forward, +1 backward)
+  if (G.nz <= 1) return 0;
+  int nzc = G.chopzl + s.off[2], nzcu = G.chopzu - s.off[2];
+  if (2 * s.off[2] > nzcu - nzc) return set_error(MLG_ECHOP, "vertical_fft: chopping in z too large");
+  // forward: (1/nz) sum e^{-}; its transpose (1/nz) sum e^{+}.  backward: sum e^{+}; transpose sum e^{-}
+  return dir < 0 ? launch_vfft_scaled(s.e, +1, 1.0 / G.nz) : launch_vfft_scaled(s.e, -1, 1.0);
+}
+
+static int space_idx(const char* sp) {
+  if (!std::strncmp(sp, "PPP", 3)) return 0;
+  if (!std::strncmp(sp, "PFP", 3)) return 1;
+  if (!std::strncmp(sp, "FFP", 3)) return 2;
+  if (!std::strncmp(sp, "FFF", 3)) return 3;
+  return -1;
+}
+static const char* SPACES[4] = {"PPP", "PFP", "FFP", "FFF"};
+
+// trans^T: s holds the adjoint of trans(x, s.space) applied to an x in fwd_from; afterwards s holds
+// the adjoint w.r.t. x (labelled fwd_from)
+int trans_T(Scalar& s, const char* fwd_from) {
+  int to = space_idx(s.space), from = space_idx(fwd_from);
+  if (to < 0 || from < 0) return set_error(MLG_ESPACE, "trans adjoint: unknown space");
+  if (from < to) {          // forward went up: undo the steps from the top
+    for (int c = to; c > from; --c) {
+      if (c == 3) MLG_TRY(vfft_checked_T(s, -1));
+      if (c == 2) MLG_TRY(rtrans_fwd_T(s));
+      if (c == 1) MLG_TRY(hfft_fwd_T(s));
+      s.set_space(SPACES[c - 1]);
+    }
+  } else if (from > to) {   // forward went down
+    for (int c = to; c < from; ++c) {
+      if (c == 0) MLG_TRY(hfft_bwd_T(s));
+      if (c == 1) MLG_TRY(rtrans_bwd_T(s, true));
+      if (c == 2) MLG_TRY(vfft_checked_T(s, +1));
+      s.set_space(SPACES[c + 1]);
+    }
+  }
+  return 0;
+}
+
+int band_T(Scalar& s, int op) {   // xxdx (0), del2h (1), del2 (2)
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  return launch_band_apply_T(s, op, c);
+}
+
+int ihelm_T(Scalar& s, double alpha) {
+  if (std::fabs(alpha) < 5.0e-14) return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  MLG_TRY(launch_band_solve_T(s, 0, c, alpha));
+  k_ihelm_T_ln<<<1, 32, 0, G.stream>>>(s.e, s.ln, G.lognorm, G.ell, alpha);
+  MLG_LAUNCH();
+  return 0;
+}
+
+int idel2_proln_T(Scalar& s) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  k_idel2_T_ln<<<1, 32, 0, G.stream>>>(s.e, s.ln, G.lognorm);
+  MLG_LAUNCH();
+  return launch_band_solve_T(s, 1, c, 0.0);
+}
+
+int zeroat1_T(Scalar& s) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
+  k_zeroat1_T<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, G.at1, nmax, G.nrdim, G.npdim, G.nzdim);
+  MLG_LAUNCH();
+  return 0;
+}
+
+static int set_fff0(Scalar& s) { s.set_space("FFF"); s.off[0] = s.off[1] = s.off[2] = 0; return 0; }
+
+// op_tp2vec^T: (vr_bar, vp_bar, vz_bar) in PPP -> (psi_bar, chi_bar) in FFF, overwritten
+int tp2vec_T(const Scalar& vrb, const Scalar& vpb, const Scalar& vzb, Scalar& psib, Scalar& chib) {
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(assign(ur, vrb)); MLG_TRY(assign(up, vpb)); MLG_TRY(assign(uz, vzb));
+  for (Scalar* q : {&ur, &up, &uz}) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
+  // u_z branch: del2h (offset 3), negation, chop, trans to PPP
+  MLG_TRY(trans_T(uz, "FFF"));
+  MLG_TRY(op_chop(uz));
+  MLG_TRY(lincomb(uz, {{&uz, -1.0}}, {}, 1.0, false));
+  uz.off[0] = 3;
+  MLG_TRY(band_T(uz, 1));
+  // u_r, u_phi branches: xxdx (offset 3), combination, chop, trans to PPP, division by r
+  MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
+  MLG_TRY(trans_T(ur, "FFF")); MLG_TRY(trans_T(up, "FFF"));
+  MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
+  ur.off[0] = 3; up.off[0] = 3;
+  ChopIdx c;
+  MLG_TRY(chop_index(ur, c));
+  MLG_TRY(launch_zero(psib.e));
+  k_tp2vec_mix_T<<<nblk(G.fsize), 256, 0, G.stream>>>(ur.e, up.e, psib.e, uz.e, G.ak, G.nrdim, G.npdim, G.nzdim, c.nrc,
+                                                       c.npc, c.nzc, c.nzcu);
+  MLG_LAUNCH();
+  MLG_TRY(band_T(ur, 0));
+  MLG_TRY(band_T(up, 0));
+  set_fff0(psib); set_fff0(chib);
+  MLG_TRY(lincomb(chib, {{&ur, 1.0}, {&uz, 1.0}}, {{&ur, 1.0}, {&uz, 1.0}}));
+  MLG_TRY(lincomb(psib, {{&psib, 1.0}, {&up, 1.0}}, {{&up, 1.0}}));
+  return 0;
+}
+
+// op_tp2curlvec^T: tp2vec^T, then the first output through (-del2)^T
+int tp2curlvec_T(const Scalar& wrb, const Scalar& wpb, const Scalar& wzb, Scalar& psib, Scalar& chib) {
+  TMP(md);
+  MLG_TRY(tp2vec_T(wrb, wpb, wzb, md, psib));   // tp2vec(md, psi): md is its first argument
+  MLG_TRY(lincomb(md, {{&md, -1.0}}, {}, 1.0, false));
+  md.off[0] = md.off[1] = md.off[2] = 0;
+  MLG_TRY(band_T(md, 2));
+  MLG_TRY(assign(chib, md));
+  set_fff0(chib);
+  return 0;
+}
+
+// op_vec2tp^T: (psi_bar, chi_bar) in FFF (with ln) -> (vr_bar, vp_bar, vz_bar) in PPP, overwritten
+int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& vpb, Scalar& vzb) {
+  TMP(pb); TMP(cb);
+  MLG_TRY(assign(pb, psib_in)); MLG_TRY(assign(cb, chib_in));
+  set_fff0(pb); set_fff0(cb);
+  MLG_TRY(zeroat1_T(pb)); MLG_TRY(zeroat1_T(cb));
+  MLG_TRY(op_chop(pb)); MLG_TRY(op_chop(cb));
+  MLG_TRY(idel2_proln_T(cb));
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(launch_zero(ur.e)); MLG_TRY(launch_zero(up.e)); MLG_TRY(launch_zero(uz.e));
+  {
+    int nrc = G.nrchop + 3, npc = G.npchop;
+    if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
+    constexpr int IT = 32, ZT = 16, KC = 16;
+    dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc);
+    kt_begin(KT_V2TP);
+    k_vec2tp_T<IT, ZT, KC><<<grid, IT * ZT / 2, 0, G.stream>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV, G.tD, G.tT, G.ak, G.nr,
+                                                               G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, G.chopzl,
+                                                               G.chopzu);
+    MLG_LAUNCH();
+    kt_end(KT_V2TP, 0.0);
+  }
+  for (Scalar* q : {&ur, &up, &uz}) { q->set_space("PFF"); q->off[0] = q->off[1] = q->off[2] = 0; }
+  // psi%ln = -1/2 Re calcat1(up)(k=1), used in up(:nr,1,1) += psi%ln (1 + x) and kept as psi%ln
+  MLG_TRY(launch_copy_ln(up.ln, pb.ln));
+  k_add_ln_x_T<<<1, 256, 0, G.stream>>>(up.e, G.x, G.nr, up.ln);
+  MLG_LAUNCH();
+  MLG_TRY(rtrans_bwd_T(up, false));
+  up.set_space("FFF");
+  {
+    ChopIdx c;
+    MLG_TRY(chop_index(up, c));
+    int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
+    k_calcat_T<<<1, 256, 0, G.stream>>>(up.e, G.at1, nmax, up.ln, -0.5);
+    MLG_LAUNCH();
+  }
+  MLG_TRY(launch_set_ln(up.ln, 0.0));
+  MLG_TRY(trans_T(up, "PPP"));
+  MLG_TRY(scale_r(up, 0));
+  // u_r: hfft + vfft forward of r*vr
+  ur.set_space("FFP");   // the PFF adjoint walks back through the z and phi steps only
+  MLG_TRY(vfft_checked_T(ur, -1));
+  MLG_TRY(hfft_fwd_T(ur));
+  MLG_TRY(launch_set_ln(ur.ln, 0.0));
+  MLG_TRY(scale_r(ur, 0));
+  {
+    PrecisionScope fp64(MLG_PLAIN_FP64);   // the forward's u_z FFTs run in FP64 in every form
+    MLG_TRY(vfft_checked_T(uz, -1));
+    MLG_TRY(hfft_fwd_T(uz));
+  }
+  MLG_TRY(launch_set_ln(uz.ln, 0.0));
+  MLG_TRY(assign(vrb, ur)); MLG_TRY(assign(vpb, up)); MLG_TRY(assign(vzb, uz));
+  for (Scalar* q : {&vrb, &vpb, &vzb}) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
+  return 0;
+}
+
+// the nonlinear term around (psi, chi) (already dealiased, FFF): nl = dealias(vec2tp(v x w)), nl%ln = 0,
+// v = tp2vec(psi, chi) + (0, 0, uz), w = tp2curlvec(psi, chi).  (nlpsi_bar, nlchi_bar) -> (psi_bar, chi_bar)
+int nlcore_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scalar& nlpb, const Scalar& nlcb, Scalar& psib,
+             Scalar& chib) {
+  TMP(np_); TMP(nc_);
+  MLG_TRY(assign(np_, nlpb)); MLG_TRY(assign(nc_, nlcb));
+  set_fff0(np_); set_fff0(nc_);
+  MLG_TRY(op_dealias(np_)); MLG_TRY(op_dealias(nc_));
+  MLG_TRY(launch_set_ln(np_.ln, 0.0)); MLG_TRY(launch_set_ln(nc_.ln, 0.0));
+  TMP(obr); TMP(obp); TMP(obz);
+  MLG_TRY(vec2tp_T(np_, nc_, obr, obp, obz));
+  // the linearisation point: v and w of the forward
+  TMP(vr); TMP(vp); TMP(vz); TMP(wr); TMP(wp); TMP(wz);
+  MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
+  MLG_TRY(lincomb(vz, {{&vz, 1.0}, {&uzb, 1.0}}, {}, 1.0, false));
+  MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
+  TMP(vbr); TMP(vbp); TMP(vbz); TMP(wbr); TMP(wbp); TMP(wbz);
+  k_vecprod_T<<<nblk(G.fsize), 256, 0, G.stream>>>(vbr.e, vbp.e, vbz.e, wbr.e, wbp.e, wbz.e, vr.e, vp.e, vz.e, wr.e, wp.e,
+                                                    wz.e, obr.e, obp.e, obz.e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
+  MLG_LAUNCH();
+  for (Scalar* q : {&vbr, &vbp, &vbz, &wbr, &wbp, &wbz}) {
+    q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0;
+    MLG_TRY(launch_set_ln(q->ln, 0.0));
+  }
+  TMP(pa); TMP(ca);
+  MLG_TRY(tp2vec_T(vbr, vbp, vbz, pa, ca));
+  MLG_TRY(tp2curlvec_T(wbr, wbp, wbz, psib, chib));
+  MLG_TRY(lincomb(psib, {{&psib, 1.0}, {&pa, 1.0}}, {{&psib, 1.0}, {&pa, 1.0}}));
+  MLG_TRY(lincomb(chib, {{&chib, 1.0}, {&ca, 1.0}}, {{&chib, 1.0}, {&ca, 1.0}}));
+  return 0;
+}
+
+// op_advection_rhs^T (its in-place dealias of psi and chi included): (psi, chi) is the point the
+// forward was called at
+int advection_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scalar& nlpb, const Scalar& nlcb, Scalar& psib,
+                Scalar& chib) {
+  TMP(p3); TMP(c3);
+  MLG_TRY(assign(p3, psi)); MLG_TRY(assign(c3, chi));
+  MLG_TRY(op_dealias(p3)); MLG_TRY(op_dealias(c3));
+  MLG_TRY(nlcore_T(p3, c3, uzb, nlpb, nlcb, psib, chib));
+  MLG_TRY(op_dealias(psib)); MLG_TRY(op_dealias(chib));
+  return 0;
+}
+
+// abcn^T (hyperpow = 0): sb holds the adjoint of the new s; on return sb holds the adjoint w.r.t.
+// the old s, and nlb, nlpb have received the adjoints w.r.t. nl and nl_p (added)
+static int abcn_T(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt) {
+  double a = -2.0 / (dt * G.P.visc);
+  MLG_TRY(ihelm_T(sb, a));
+  MLG_TRY(lincomb(nlb, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}));
+  MLG_TRY(lincomb(nlpb, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}));
+  TMP(t);
+  MLG_TRY(assign(t, sb));
+  MLG_TRY(lincomb(t, {{&t, G.P.visc * a * dt / 2.0}}, {}, 1.0, false));
+  MLG_TRY(band_T(t, 2));   // t.e <- del2^T t.e; t.ln <- the log-term adjoint
+  MLG_TRY(lincomb(sb, {{&sb, a}, {&t, 1.0}}, {{&sb, a}, {&t, 1.0}}));
+  return 0;
+}
+
+static int adjoint_supported() {
+  if (G.P.is_svv) return set_error(MLG_EPARAM, "adjoint: SVV must be off (is_svv = 0): the filter's energy gain is not differentiated");
+  if (G.P.hyperpow != 0) return set_error(MLG_EPARAM, "adjoint: hyperviscosity (hyperpow > 0) is not supported");
+  if (G.P.visc < 5.0e-14) return set_error(MLG_EINVISCID, "adjoint: inviscid case has no implicit step");
+  return 0;
+}
+
+// One step backward.  st = (psi, chi, nlpsi, nlchi, nlpsi_p, nlchi_p) at the step's end (the point
+// its nonlinear term was evaluated at); ad = the adjoint of that state, replaced by the adjoint of
+// the state at the step's start.
+static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const ad[6]) {
+  Scalar& pb = *ad[0]; Scalar& cb = *ad[1];
+  Scalar& npb = *ad[2]; Scalar& ncb = *ad[3];
+  Scalar& nppb = *ad[4]; Scalar& ncpb = *ad[5];
+  TMP(xp); TMP(xc);
+  MLG_TRY(nlcore_T(*st[0], *st[1], uzb, npb, ncb, xp, xc));
+  MLG_TRY(lincomb(pb, {{&pb, 1.0}, {&xp, 1.0}}, {{&pb, 1.0}, {&xp, 1.0}}));
+  MLG_TRY(lincomb(cb, {{&cb, 1.0}, {&xc, 1.0}}, {{&cb, 1.0}, {&xc, 1.0}}));
+  for (Scalar* q : {&pb, &cb}) {
+    MLG_TRY(op_dealias(*q));   // advection_rhs's in-place dealias
+    MLG_TRY(zeroat1_T(*q));
+    MLG_TRY(op_dealias(*q));   // the step's dealias
+  }
+  // nl_p(out) = nl(in); the new nl(in) and nl_p(in) adjoints come from abcn^T
+  MLG_TRY(assign(npb, nppb)); MLG_TRY(assign(ncb, ncpb));
+  MLG_TRY(launch_zero(nppb.e)); MLG_TRY(launch_set_ln(nppb.ln, 0.0));
+  MLG_TRY(launch_zero(ncpb.e)); MLG_TRY(launch_set_ln(ncpb.ln, 0.0));
+  MLG_TRY(abcn_T(pb, npb, nppb, dt));
+  MLG_TRY(abcn_T(cb, ncb, ncpb, dt));
+  for (int i = 0; i < 6; ++i) set_fff0(*ad[i]);
+  return 0;
+}
+
+static int forward_step(Scalar* const st[6], const Scalar& uzb, double dt) {
+  TMP(pp); TMP(cp);
+  MLG_TRY(assign(pp, *st[0])); MLG_TRY(assign(cp, *st[1]));
+  return op_vortex_step_dev(*st[0], *st[1], *st[2], *st[3], pp, cp, *st[4], *st[5], uzb, dt, G.dscal + DS_GAIN0);
+}
+
+// startup from (psi0, chi0): psi <- dealias(psi0), nl <- advection_rhs, nl_p <- nl
+static int startup(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, Scalar* const st[6]) {
+  MLG_TRY(assign(*st[0], psi0)); MLG_TRY(assign(*st[1], chi0));
+  for (int i = 2; i < 6; ++i) { MLG_TRY(launch_zero(st[i]->e)); MLG_TRY(launch_set_ln(st[i]->ln, 0.0)); set_fff0(*st[i]); }
+  MLG_TRY(op_advection_rhs(*st[0], *st[1], *st[2], *st[3], uzb));
+  MLG_TRY(assign(*st[4], *st[2])); MLG_TRY(assign(*st[5], *st[3]));
+  return 0;
+}
+
+// J and, if seeds are given, (psi_bar, chi_bar) = dJ/d(psi, chi)
+static int energy(const Scalar& psi, const Scalar& chi, double* J, Scalar* psib, Scalar* chib) {
+  TMP(p); TMP(c);
+  MLG_TRY(assign(p, psi)); MLG_TRY(assign(c, chi));
+  k_drop_mean<<<1, 256, 0, G.stream>>>(p.e, p.ln, G.nrdim); MLG_LAUNCH();
+  k_drop_mean<<<1, 256, 0, G.stream>>>(c.e, c.ln, G.nrdim); MLG_LAUNCH();
+  TMP(vr); TMP(vp); TMP(vz);
+  MLG_TRY(op_tp2vec(p, c, vr, vp, vz));
+  double* wq = G.dscal + DS_CALC + 2 * 2048;                  // nr weights
+  double* partial = wq + G.nrdim;                               // block sums
+  const int NB = 152;
+  if ((size_t)(DS_CALC + 2 * 2048 + G.nrdim + NB) > (size_t)DS_COUNT) return set_error(MLG_ESIZE, "adjoint: grid too large");
+  double dpz = (2.0 * 3.14159265358979323846 / G.np) * (G.P.zlen / G.nz);
+  k_energy_weights<<<1, 256, 0, G.stream>>>(wq, G.x, G.w, G.r, G.nr, dpz); MLG_LAUNCH();
+  TMP(ur); TMP(upp); TMP(uzz);
+  bool seed = psib && chib;
+  k_energy<<<NB, 256, 0, G.stream>>>(seed ? ur.e : nullptr, upp.e, uzz.e, vr.e, vp.e, vz.e, wq, G.nr, G.np / 2, G.nrdim,
+                                     G.npdim, G.nzdim, partial);
+  MLG_LAUNCH();
+  std::vector<double> h(NB);
+  MLG_CUDA(cudaMemcpyAsync(h.data(), partial, NB * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  double s = 0.0;
+  for (double v : h) s += v;
+  *J = s;
+  if (seed) {
+    for (Scalar* q : {&ur, &upp, &uzz}) {
+      q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0;
+      MLG_TRY(launch_set_ln(q->ln, 0.0));
+    }
+    MLG_TRY(tp2vec_T(ur, upp, uzz, *psib, *chib));
+    k_drop_mean<<<1, 256, 0, G.stream>>>(psib->e, psib->ln, G.nrdim); MLG_LAUNCH();
+    k_drop_mean<<<1, 256, 0, G.stream>>>(chib->e, chib->ln, G.nrdim); MLG_LAUNCH();
+  }
+  return 0;
+}
+
+struct State {
+  Tmp t[6];
+  Scalar* p[6];
+  int rc = 0;
+  State() { for (int i = 0; i < 6; ++i) { p[i] = &t[i].s; if (t[i].rc) rc = t[i].rc; } }
+};
+
+static int copy_state(Scalar* const d[6], Scalar* const s[6]) {
+  for (int i = 0; i < 6; ++i) MLG_TRY(assign(*d[i], *s[i]));
+  return 0;
+}
+
+// the gradient of J(T) w.r.t. (psi0, chi0) through nsteps steps, the state kept every k_ckpt steps
+int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, double dt, int nsteps, int k_ckpt, Scalar* gpsi,
+                Scalar* gchi, double* J) {
+  MLG_TRY(adjoint_supported());
+  if (nsteps < 0) return set_error(MLG_EPARAM, "adjoint: nsteps must be >= 0");
+  if (k_ckpt < 1) k_ckpt = 1;
+  if (!psi0.is("FFF") || !chi0.is("FFF") || !uzb.is("PPP"))
+    return set_error(MLG_ESPACE, "adjoint: psi0 and chi0 must be in FFF and uz in PPP");
+  std::vector<State*> ck;
+  int rc = 0;
+  auto cleanup = [&]() { for (State* s : ck) delete s; ck.clear(); };
+  State cur;
+  if (cur.rc) return cur.rc;
+  // forward sweep, keeping the state at steps 0, K, 2K, ...
+  rc = startup(psi0, chi0, uzb, cur.p);
+  for (int s = 0; s < nsteps && !rc; ++s) {
+    if (s % k_ckpt == 0) {
+      State* c = new State();
+      if (c->rc) { rc = c->rc; delete c; break; }
+      ck.push_back(c);
+      rc = copy_state(c->p, cur.p);
+      if (rc) break;
+    }
+    rc = forward_step(cur.p, uzb, dt);
+  }
+  if (rc) { cleanup(); return rc; }
+  if (!gpsi || !gchi) {
+    rc = energy(*cur.p[0], *cur.p[1], J, nullptr, nullptr);
+    cleanup();
+    return rc;
+  }
+  State ad;
+  if (ad.rc) { cleanup(); return ad.rc; }
+  rc = energy(*cur.p[0], *cur.p[1], J, ad.p[0], ad.p[1]);
+  for (int i = 2; i < 6 && !rc; ++i) { rc = launch_zero(ad.p[i]->e); if (!rc) rc = launch_set_ln(ad.p[i]->ln, 0.0); set_fff0(*ad.p[i]); }
+  // backward sweep, segment by segment: recompute the end-of-step states, then step back
+  std::vector<State*> seg;
+  for (int c = (int)ck.size() - 1; c >= 0 && !rc; --c) {
+    int s0 = c * k_ckpt, s1 = std::min(nsteps, s0 + k_ckpt);
+    int len = s1 - s0;
+    while ((int)seg.size() < len) {
+      State* t = new State();
+      if (t->rc) { rc = t->rc; delete t; break; }
+      seg.push_back(t);
+    }
+    if (rc) break;
+    rc = copy_state(cur.p, ck[c]->p);
+    for (int q = 0; q < len && !rc; ++q) {
+      rc = forward_step(cur.p, uzb, dt);
+      if (!rc) rc = copy_state(seg[q]->p, cur.p);
+    }
+    for (int q = len - 1; q >= 0 && !rc; --q) rc = step_T(seg[q]->p, uzb, dt, ad.p);
+  }
+  for (State* t : seg) delete t;
+  if (!rc) {
+    // through the startup: nl(0) = nl_p(0) = advection_rhs(psi0, chi0)
+    TMP(nb); TMP(cb2);
+    rc = lincomb(*ad.p[2], {{ad.p[2], 1.0}, {ad.p[4], 1.0}}, {{ad.p[2], 1.0}, {ad.p[4], 1.0}});
+    if (!rc) rc = lincomb(*ad.p[3], {{ad.p[3], 1.0}, {ad.p[5], 1.0}}, {{ad.p[3], 1.0}, {ad.p[5], 1.0}});
+    if (!rc) rc = advection_T(psi0, chi0, uzb, *ad.p[2], *ad.p[3], nb, cb2);
+    if (!rc) rc = lincomb(*gpsi, {{ad.p[0], 1.0}, {&nb, 1.0}}, {{ad.p[0], 1.0}, {&nb, 1.0}});
+    if (!rc) rc = lincomb(*gchi, {{ad.p[1], 1.0}, {&cb2, 1.0}}, {{ad.p[1], 1.0}, {&cb2, 1.0}});
+    // the startup's psi <- psi0 passes through advection_rhs's in-place dealias
+    if (!rc) rc = op_dealias(*gpsi);
+    if (!rc) rc = op_dealias(*gchi);
+    set_fff0(*gpsi); set_fff0(*gchi);
+  }
+  cleanup();
+  return rc;
+}
+
+int adjoint_step(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const ad[6]) {
+  MLG_TRY(adjoint_supported());
+  State e;
+  if (e.rc) return e.rc;
+  MLG_TRY(copy_state(e.p, st));
+  MLG_TRY(forward_step(e.p, uzb, dt));
+  return step_T(e.p, uzb, dt, ad);
+}
+
+}  // namespace mlg
+
+// =================================================================================================
+// C ABI
+using namespace mlg;
+
+static int adj_need(void* p) {
+  if (!G.kit_set) return set_error(MLG_ENOKIT, "transformation kit is not initialized");
+  if (!p || !reinterpret_cast<Scalar*>(p)->e) return set_error(MLG_EHANDLE, "invalid scalar handle");
+  return adjoint_supported();
+}
+#define ADJ_S(h) MLG_TRY(adj_need(h)); Scalar& h##_ = *reinterpret_cast<Scalar*>(h)
+
+extern "C" {
+
+int mlg_adjoint_run(mlg_scalar psi0, mlg_scalar chi0, mlg_scalar uz, double dt, int nsteps, int k_ckpt,
+                    mlg_scalar grad_psi, mlg_scalar grad_chi, double* J) {
+  ADJ_S(psi0); ADJ_S(chi0); ADJ_S(uz);
+  if (!J) return set_error(MLG_EHANDLE, "adjoint: null J");
+  Scalar* gp = nullptr;
+  Scalar* gc = nullptr;
+  if (grad_psi && grad_chi) {
+    MLG_TRY(adj_need(grad_psi)); MLG_TRY(adj_need(grad_chi));
+    gp = reinterpret_cast<Scalar*>(grad_psi);
+    gc = reinterpret_cast<Scalar*>(grad_chi);
+  }
+  return adjoint_run(psi0_, chi0_, uz_, dt, nsteps, k_ckpt, gp, gc, J);
+}
+
+int mlg_adj_vortex_step(const mlg_scalar* state, mlg_scalar uz, double dt, const mlg_scalar* adj) {
+  ADJ_S(uz);
+  if (!state || !adj) return set_error(MLG_EHANDLE, "invalid scalar handle");
+  Scalar* st[6];
+  Scalar* ad[6];
+  for (int i = 0; i < 6; ++i) {
+    MLG_TRY(adj_need(state[i])); MLG_TRY(adj_need(adj[i]));
+    st[i] = reinterpret_cast<Scalar*>(state[i]);
+    ad[i] = reinterpret_cast<Scalar*>(adj[i]);
+    if (!st[i]->is("FFF") || !ad[i]->is("FFF")) return set_error(MLG_ESPACE, "adjoint: the step state must be in FFF");
+  }
+  return adjoint_step(st, uz_, dt, ad);
+}
+
+int mlg_adj_trans(mlg_scalar s, const char* from) { ADJ_S(s); return trans_T(s_, from); }
+int mlg_adj_band(mlg_scalar s, int op) {
+  ADJ_S(s);
+  if (op < 0 || op > 2) return set_error(MLG_EPARAM, "adjoint: band op is 0, 1 or 2");
+  return band_T(s_, op);
+}
+int mlg_adj_ihelm(mlg_scalar s, double alpha) { ADJ_S(s); return ihelm_T(s_, alpha); }
+int mlg_adj_idel2_proln(mlg_scalar s) { ADJ_S(s); return idel2_proln_T(s_); }
+int mlg_adj_zeroat1(mlg_scalar s) { ADJ_S(s); return zeroat1_T(s_); }
+int mlg_adj_tp2vec(mlg_scalar vr, mlg_scalar vp, mlg_scalar vz, mlg_scalar psi, mlg_scalar chi) {
+  ADJ_S(vr); ADJ_S(vp); ADJ_S(vz); ADJ_S(psi); ADJ_S(chi);
+  return tp2vec_T(vr_, vp_, vz_, psi_, chi_);
+}
+int mlg_adj_tp2curlvec(mlg_scalar wr, mlg_scalar wp, mlg_scalar wz, mlg_scalar psi, mlg_scalar chi) {
+  ADJ_S(wr); ADJ_S(wp); ADJ_S(wz); ADJ_S(psi); ADJ_S(chi);
+  return tp2curlvec_T(wr_, wp_, wz_, psi_, chi_);
+}
+int mlg_adj_vec2tp(mlg_scalar psi, mlg_scalar chi, mlg_scalar vr, mlg_scalar vp, mlg_scalar vz) {
+  ADJ_S(psi); ADJ_S(chi); ADJ_S(vr); ADJ_S(vp); ADJ_S(vz);
+  return vec2tp_T(psi_, chi_, vr_, vp_, vz_);
+}
+int mlg_adj_advection(mlg_scalar psi, mlg_scalar chi, mlg_scalar uz, mlg_scalar nlpsi_bar, mlg_scalar nlchi_bar,
+                      mlg_scalar psi_bar, mlg_scalar chi_bar) {
+  ADJ_S(psi); ADJ_S(chi); ADJ_S(uz); ADJ_S(nlpsi_bar); ADJ_S(nlchi_bar); ADJ_S(psi_bar); ADJ_S(chi_bar);
+  return advection_T(psi_, chi_, uz_, nlpsi_bar_, nlchi_bar_, psi_bar_, chi_bar_);
+}
+
+}  // extern "C"

@@ -147,6 +147,8 @@ struct SolveArgs {
   int kind;             // 0 ihelm, 1 idel2_proln, 2 idel2_preln, 3 ihelmp
   int power;
   int skip_root;        // substitution: leave the (0,0) column to the bordered solve
+  int transpose;        // factor / solve A^T (kinds 0 and 1): the adjoint's systems
+  int no_ln;            // substitution: skip the log-term handling of the (0,0) column
 };
 
 // entry (i, j) (0-based) of D(m,k) = D0(m) - ak^2 I for an n x n truncation
@@ -292,6 +294,7 @@ __global__ void k_band_solve(SolveArgs a) {
 // Entry (i, j) of the system matrix of (m, k) for kinds 0..2 (0-based, n x n truncation).
 __device__ __forceinline__ double sys_entry(const SolveArgs& a, int kind, bool special, int m, double akv, int nn,
                                             double alpha, double e2, int i, int j) {
+  if (a.transpose) { int t = i; i = j; j = t; }
   if (i < 0 || j < 0 || i >= nn || j >= nn) return 0.0;
   if (special && kind == 1) {
     double v = dmat(a, 0, akv, nn, i, j);
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
   int nn = max(min(a.nrc, a.nrc - m), 0);
   bool root = valid && (m == 0 && k == 0);
   if (root && a.skip_root) cnt = 0;
-  if (root && comp == 0 && a.kind == 0 && !a.skip_root) {   // ihelm: so%ln = s%ln/alpha, log terms (:818-824)
+  if (root && comp == 0 && a.kind == 0 && !a.skip_root && !a.no_ln) {   // ihelm: so%ln = s%ln/alpha, log terms (:818-824)
     double e2 = a.ell * a.ell;
     double lno = *a.lnp / a.alpha;
     *a.lnp = lno;
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
     cpa_wait<0>();
     __threadfence_block();
   }
-  if (root && comp == 0 && a.kind == 1 && !a.skip_root && cnt > 0) *a.lnp = x[0] * exp(a.lognorm[0]);
+  if (root && comp == 0 && a.kind == 1 && !a.skip_root && !a.no_ln && cnt > 0) *a.lnp = x[0] * exp(a.lognorm[0]);
 }
 
 // the bordered (0,0) system of idel2_preln (KL = 3), single thread, after the batch
@@ -811,7 +814,7 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
   a.status = (int*)(G.dscal + DS_FLAG + 1);
   a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
   a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = beta; a.ell = G.ell; a.preln = preln;
-  a.kind = kind; a.power = power; a.skip_root = 0;
+  a.kind = kind; a.power = power; a.skip_root = 0; a.transpose = 0; a.no_ln = 0;
   kt_begin(2);
   if (kind == 3) {
     k_band_solve<<<cdiv(nsys, 64), 64, 0, G.stream>>>(a);
@@ -838,6 +841,100 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
       MLG_LAUNCH();
     }
   }
+  kt_end(2, 2.0 * G.fsize * 16);
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// transposes for the adjoint (FP64 in both forms)
+
+// k_band_apply^T: x <- B^T x per active column (cnt times, as the forward), rows >= nn and inactive
+// columns untouched (the forward is the identity there).  The forward adds c_n * ln to Re e(n,0,0)
+// after the product and zeroes ln, so the adjoint of ln is read off the incoming adjoint of e first:
+// ln_bar = sum_n c_n Re(e_bar(n,0,0)); the adjoint of the output ln (a constant zero) is dropped.
+__global__ void k_band_apply_T(double2* __restrict__ e, const double* __restrict__ bd2, const double* __restrict__ bxx,
+                               const double* __restrict__ ak, double* __restrict__ lnp, const double* __restrict__ lognorm,
+                               int op, int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim,
+                               double ell) {
+  extern __shared__ __align__(16) unsigned char bandt_smem[];
+  double2* c0 = (double2*)bandt_smem;
+  double2* c1 = c0 + nrdim;
+  int m = blockIdx.y, k = blockIdx.x;
+  int nn = max(min(nrc, nrc - m), 0);
+  int cnt = k_count(k, nzc, nzcu, nzdim);
+  double2* g = e + (size_t)nrdim * (m + (size_t)npdim * k);
+  if (m == 0 && k == 0 && threadIdx.x == 0) {
+    double e2 = ell * ell;
+    if (op == 0) *lnp = g[0].x / exp(lognorm[0]) + g[1].x / exp(lognorm[1]);
+    else *lnp = 4.0 / 3.0 / e2 / exp(lognorm[0]) * g[0].x - 2.0 / 1.0 / e2 / exp(lognorm[1]) * g[1].x +
+                2.0 / 3.0 / e2 / exp(lognorm[2]) * g[2].x;
+  }
+  __syncthreads();
+  if (m >= npc || nn <= 0 || cnt <= 0) return;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = g[i];
+  __syncthreads();
+  double akd = ak[k], akv2 = akd * akd;
+  for (int rep = 0; rep < cnt; ++rep) {
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      if (op == 0) {
+        if (j + 1 < nn) { double v = bxx[3 * ((size_t)(j + 1) + (size_t)ne * m) + 0]; acc.x += v * c0[j + 1].x; acc.y += v * c0[j + 1].y; }
+        if (j - 1 >= 0) { double v = bxx[3 * ((size_t)(j - 1) + (size_t)ne * m) + 2]; acc.x += v * c0[j - 1].x; acc.y += v * c0[j - 1].y; }
+      } else {
+        for (int i = max(0, j - 2); i <= min(nn - 1, j + 2); ++i) {
+          double v = bd2[(j - i + 2) + 5 * ((size_t)i + (size_t)ne * m)];
+          if (i == j && op == 2) v -= akv2;
+          acc.x += v * c0[i].x;
+          acc.y += v * c0[i].y;
+        }
+      }
+      c1[j] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) g[i] = c0[i];
+}
+
+int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  dim3 grid(G.nzdim, std::max(c.npc, 1));
+  size_t sm = 2ull * G.nrdim * sizeof(double2);
+  if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_T, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  kt_begin(2);
+  k_band_apply_T<<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne, c.nrc,
+                                              c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  MLG_LAUNCH();
+  kt_end(2, 2.0 * G.fsize * 16);
+  return 0;
+}
+
+// A^T x = b for kind 0 (D(m,k) + alpha I) and kind 1 (idel2_proln: the root system with its
+// column-1 log-term entries), all columns, no log-term handling; the factors of A^T are cached
+// beside those of A.
+int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
+  if (kind != 0 && kind != 1) return set_error(MLG_EPARAM, "transposed band solve: kinds 0 and 1 only");
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  int npc = std::max(c.npc, 1);
+  size_t nsys = (size_t)npc * G.nzdim;
+  SolveArgs a;
+  a.e = s.e; a.ws = G.band_ws; a.lnp = s.ln; a.bd2 = G.bd2; a.ak = G.ak; a.lognorm = G.lognorm;
+  a.status = (int*)(G.dscal + DS_FLAG + 1);
+  a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
+  a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = 0.0; a.ell = G.ell; a.preln = 0.0;
+  a.kind = kind; a.power = 0; a.skip_root = 0; a.transpose = 1; a.no_ln = 1;
+  kt_begin(2);
+  double* fac = nullptr;
+  MLG_TRY(lu_cache_get(kind + 8, alpha, c, nsys, &fac, [&](double* buf) -> int {
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    MLG_LAUNCH();
+    return 0;
+  }));
+  size_t smb = sizeof(SubstSmem);
+  MLG_CUDA(cudaFuncSetAttribute(k_band_subst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+  k_band_subst<<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
+  MLG_LAUNCH();
   kt_end(2, 2.0 * G.fsize * 16);
   return 0;
 }

@@ -5,6 +5,9 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <initializer_list>
+#include <utility>
+#include <algorithm>
 #include <vector>
 #include "../../include/mlegs_gb300.h"
 
@@ -112,6 +115,9 @@ int kit_free();
 int launch_hfft(Scalar& s, int dir);             // dir -1 forward (1/np), +1 backward
 int launch_vfft(Scalar& s, int dir);             // dir -1 forward (1/nz), +1 backward
 int launch_vfft_buf(cd* e, int dir);
+int launch_vfft_scaled(cd* e, int dir, double scale);
+int launch_hfft_fwd_scaled(cd* e, double scale);
+int launch_hfft_bwd_buf(cd* e);
 int launch_rtrans_fwd(Scalar& s);
 int launch_rtrans_bwd(Scalar& s, bool add_ln);
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
@@ -126,6 +132,49 @@ int launch_zero(cd* e);
 int launch_copy(cd* dst, const cd* src);
 int launch_copy_ln(double* dst, const double* src);
 int launch_set_ln(double* dst, double v);
+
+// grid-stride loop over n elements (32-bit indices: a field has < 2^32 entries)
+#define GRID_STRIDE(i, n) for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < (unsigned)(n); i += gridDim.x * blockDim.x)
+static inline int nblk(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+// scalar bookkeeping and operators shared by ops.cu and adjoint.cu
+int scalar_init(Scalar& s, bool zero_ln = true);
+void scalar_release(Scalar& s);
+int assign(Scalar& d, const Scalar& s);   // e, ln, space, offsets
+// out = post * sum c_i in_i (e), ln likewise from lnterms unless do_ln is false
+int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+            std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post = 1.0, bool do_ln = true);
+struct Tmp {
+  Scalar s;
+  int rc = 0;
+  Tmp() { rc = scalar_init(s, false); }   // every temporary is assigned (e and ln) before it is read
+  ~Tmp() { if (s.e) scalar_release(s); }
+};
+#define TMP(name) Tmp name##_t; if (name##_t.rc) return name##_t.rc; Scalar& name = name##_t.s
+// restores the precision form on scope exit
+struct PrecisionScope {
+  int saved;
+  explicit PrecisionScope(int mode) : saved(G.precision) { G.precision = mode; }
+  ~PrecisionScope() { G.precision = saved; }
+};
+int calcat_dev(Scalar& s, const double* at, bool zero_mode);
+int scale_r(Scalar& s, int mode);   // rows i < nr times r_i (mode 0) or 1/r_i (mode 1)
+int op_trans(Scalar& s, const char* space);
+int op_chop(Scalar& s);
+int op_dealias(Scalar& s);
+int op_zeroat1(Scalar& s);
+int op_band(Scalar& s, int op);
+int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scalar& vz);
+int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, Scalar& wz);
+int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz);
+int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi);
+int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz);
+int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev);
+int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
+int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);
+int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
+int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha);
 
 }  // namespace mlg
 

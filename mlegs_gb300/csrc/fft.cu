@@ -226,7 +226,7 @@ static int set_smem(const void* fn, size_t bytes) {
 }
 
 template <typename T>
-static int vfft_t(cd* e, int dir) {
+static int vfft_t(cd* e, int dir, double scale) {
   int L = G.nz;
   if (L <= 1) return 0;
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
@@ -235,20 +235,24 @@ static int vfft_t(cd* e, int dir) {
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), G.npdim), blk(TR, TT);
   kt_begin(1);
-  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir,
-                                         (T)(dir < 0 ? 1.0 / L : 1.0));
+  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale);
   MLG_LAUNCH();
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;
 }
 
 int launch_vfft_buf(cd* e, int dir) {
-  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir) : vfft_t<double>(e, dir);
+  double scale = dir < 0 ? 1.0 / G.nz : 1.0;
+  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir, scale) : vfft_t<double>(e, dir, scale);
+}
+// sum_j x_j exp(dir 2 pi i jk/nz) * scale, any direction and scale (the adjoint's FFTs)
+int launch_vfft_scaled(cd* e, int dir, double scale) {
+  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir, scale) : vfft_t<double>(e, dir, scale);
 }
 int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
 
 template <typename T>
-static int hfft_t(cd* e, int dir) {
+static int hfft_t(cd* e, int dir, double scale) {
   int L = G.nph;
   if (G.np <= 1) return 0;
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
@@ -259,7 +263,7 @@ static int hfft_t(cd* e, int dir) {
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
     k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)(1.0 / G.np));
+                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
     k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
@@ -274,7 +278,15 @@ int launch_hfft(Scalar& s, int dir) {
   if (G.npchop + s.off[1] > G.npdim)
     return set_error(MLG_ECHOP, dir < 0 ? "horizontal_fft_forward: chopping in p too large"
                                         : "horizontal_fft_fbackard: chopping in p too large");
-  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir) : hfft_t<double>(s.e, dir);
+  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir, 1.0 / G.np) : hfft_t<double>(s.e, dir, 1.0 / G.np);
+}
+// the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs)
+int launch_hfft_fwd_scaled(cd* e, double scale) {
+  return G.precision == MLG_MIXED ? hfft_t<float>(e, -1, scale) : hfft_t<double>(e, -1, scale);
+}
+// the half-complex-to-real sum (unnormalised, Nyquist slot kept times np), on a raw buffer
+int launch_hfft_bwd_buf(cd* e) {
+  return G.precision == MLG_MIXED ? hfft_t<float>(e, +1, 1.0) : hfft_t<double>(e, +1, 1.0);
 }
 
 }  // namespace mlg

@@ -92,8 +92,6 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 
 // ------------------------------------------------------------------------------------------------
 // pointwise kernels
-#define GRID_STRIDE(i, n) for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < (unsigned)(n); i += gridDim.x * blockDim.x)
-static inline int nblk(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 // chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
 __global__ void k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int mode, int f0, int f1, int f2,
@@ -383,8 +381,8 @@ int launch_ln_adjust(Scalar& s, double sign) {
   return 0;
 }
 
-static int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
-                   std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post = 1.0, bool do_ln = true) {
+int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+            std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post, bool do_ln) {
   LinArgs a{};
   a.out = out.e;
   a.n = G.fsize;
@@ -411,7 +409,7 @@ static int alloc_slot() {
 }
 static void free_slot(int s) { if (s >= 0) G.free_slots.push_back(s); }
 
-static int scalar_init(Scalar& s, bool zero_ln = true) {   // scalar_init (mlegs_scalar_init.f90:6-67): space PPP
+int scalar_init(Scalar& s, bool zero_ln) {   // scalar_init (mlegs_scalar_init.f90:6-67): space PPP
   s.e = get_buf();
   if (!s.e) return set_error(MLG_EALLOC, "scalar_init: out of device memory");
   s.slot = alloc_slot();
@@ -422,7 +420,7 @@ static int scalar_init(Scalar& s, bool zero_ln = true) {   // scalar_init (mlegs
   if (zero_ln) MLG_TRY(launch_set_ln(s.ln, 0.0));
   return 0;
 }
-static void scalar_release(Scalar& s) {
+void scalar_release(Scalar& s) {
   put_buf(s.e);
   s.e = nullptr;
   free_slot(s.slot);
@@ -430,7 +428,7 @@ static void scalar_release(Scalar& s) {
   s.ln = nullptr;
 }
 // scalar_copy (mlegs_scalar_init.f90:106-140)
-static int assign(Scalar& d, const Scalar& s) {
+int assign(Scalar& d, const Scalar& s) {
   if (d.e != s.e) {
     k_copy_scalar<<<nblk(G.fsize), 256, 0, G.stream>>>(d.e, s.e, G.fsize, d.ln, s.ln);
     MLG_LAUNCH();
@@ -442,13 +440,6 @@ static int assign(Scalar& d, const Scalar& s) {
   return 0;
 }
 
-struct Tmp {
-  Scalar s;
-  int rc = 0;
-  Tmp() { rc = scalar_init(s, false); }   // every temporary is assigned (e and ln) before it is read
-  ~Tmp() { if (s.e) scalar_release(s); }
-};
-#define TMP(name) Tmp name##_t; if (name##_t.rc) return name##_t.rc; Scalar& name = name##_t.s
 
 // ------------------------------------------------------------------------------------------------
 // operators (mlegs_scalar_ops.f90)
@@ -552,7 +543,7 @@ int op_svv_filter_dev(Scalar& s, double* gain_dev) {
 }
 
 // calcat0/1 into dscal[DS_CALC..] (device), optionally zeroat1
-static int calcat_dev(Scalar& s, const double* at, bool zero_mode) {
+int calcat_dev(Scalar& s, const double* at, bool zero_mode) {
   ChopIdx c;
   MLG_TRY(chop_index(s, c));
   int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
@@ -766,19 +757,13 @@ int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scala
   return 0;
 }
 
-static int scale_r(Scalar& s, int mode) {
+int scale_r(Scalar& s, int mode) {
   size_t ncol = (size_t)G.npdim * G.nzdim;
   k_scale_r<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, mode == 0 ? G.r : G.rinv, G.nr, G.nrdim, ncol);
   MLG_LAUNCH();
   return 0;
 }
 
-// restores the precision form on scope exit
-struct PrecisionScope {
-  int saved;
-  explicit PrecisionScope(int mode) : saved(G.precision) { G.precision = mode; }
-  ~PrecisionScope() { G.precision = saved; }
-};
 
 int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi) {
   if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");

@@ -60,6 +60,11 @@ def load(path=None):
         "mlg_vortex_step": [_P] * 9 + [_D, _P], "mlg_vortex_run": [_P] * 9 + [_D, _I, _P],
         "mlg_scalar_axpby": [_P, _D, _P, _D, _P],
         "mlg_kernel_timing": [_I], "mlg_kernel_timing_read": [_I, _P, _P, _P],
+        "mlg_adjoint_run": [_P, _P, _P, _D, _I, _I, _P, _P, _P], "mlg_adj_vortex_step": [_P, _P, _D, _P],
+        "mlg_adj_trans": [_P, ctypes.c_char_p], "mlg_adj_band": [_P, _I], "mlg_adj_ihelm": [_P, _D],
+        "mlg_adj_idel2_proln": [_P], "mlg_adj_zeroat1": [_P],
+        "mlg_adj_tp2vec": [_P] * 5, "mlg_adj_tp2curlvec": [_P] * 5, "mlg_adj_vec2tp": [_P] * 5,
+        "mlg_adj_advection": [_P] * 7,
     }
     for name in ["mlg_chop", "mlg_dealias", "mlg_zeroat1", "mlg_delsqp", "mlg_idelsqp", "mlg_xxdx", "mlg_del2h",
                  "mlg_del2", "mlg_idel2_proln"]:
@@ -260,6 +265,32 @@ class Kit:
     def axpby(self, d, a, x, b=0.0, y=None):
         """d%e = a*x%e + b*y%e (the apps' direct array arithmetic on s%e)."""
         _chk(load().mlg_scalar_axpby(d.h, float(a), x.h, float(b), y.h if y is not None else None))
+
+    # ---- adjoint (no counterpart in the reference) ----
+    def adjoint_run(self, psi0, chi0, uz, dt, nsteps, k_ckpt, grad_psi=None, grad_chi=None):
+        """J at step nsteps and, with grad scalars given, dJ/d(psi0, chi0) written into them."""
+        J = ctypes.c_double()
+        _chk(load().mlg_adjoint_run(psi0.h, chi0.h, uz.h, float(dt), int(nsteps), int(k_ckpt),
+                                    grad_psi.h if grad_psi is not None else None,
+                                    grad_chi.h if grad_chi is not None else None, ctypes.byref(J)))
+        return J.value
+
+    def adj_vortex_step(self, state, uz, dt, adj):
+        st = (_P * 6)(*[q.h.value for q in state])
+        ad = (_P * 6)(*[q.h.value for q in adj])
+        _chk(load().mlg_adj_vortex_step(st, uz.h, float(dt), ad))
+
+    def adj_trans(self, s, forward_from): _chk(load().mlg_adj_trans(s.h, forward_from.encode()))
+    def adj_band(self, s, op): _chk(load().mlg_adj_band(s.h, int(op)))
+    def adj_ihelm(self, s, alpha): _chk(load().mlg_adj_ihelm(s.h, float(alpha)))
+    def adj_idel2_proln(self, s): _chk(load().mlg_adj_idel2_proln(s.h))
+    def adj_zeroat1(self, s): _chk(load().mlg_adj_zeroat1(s.h))
+    def adj_tp2vec(self, vr, vp, vz, psi, chi): _chk(load().mlg_adj_tp2vec(vr.h, vp.h, vz.h, psi.h, chi.h))
+    def adj_tp2curlvec(self, wr, wp, wz, psi, chi): _chk(load().mlg_adj_tp2curlvec(wr.h, wp.h, wz.h, psi.h, chi.h))
+    def adj_vec2tp(self, psi, chi, vr, vp, vz): _chk(load().mlg_adj_vec2tp(psi.h, chi.h, vr.h, vp.h, vz.h))
+
+    def adj_advection(self, psi, chi, uz, nlpsi_bar, nlchi_bar, psi_bar, chi_bar):
+        _chk(load().mlg_adj_advection(psi.h, chi.h, uz.h, nlpsi_bar.h, nlchi_bar.h, psi_bar.h, chi_bar.h))
 
     # ---- kernel timing ----
     def kernel_timing(self, enable):
