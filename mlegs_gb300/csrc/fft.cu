@@ -7,11 +7,21 @@
 // into X_0..X_{N/2}.  Backward, the last complex slot keeps N times its input (FFTE's zdfft2d never
 // writes A(NX/2+1), zdfft2d.f:119-128, and the reference then multiplies by N, :1705).
 //
+// Mixed form (T = float): the DC coefficient of a transform line is carried in FP64 and the FP32 FFT
+// runs on the mean-free residual.  Forward, the line's FP64 sum gives the k = 0 output and its mean is
+// subtracted (in FP64) before the samples are rounded to FP32; backward, the k = 0 input is left out of
+// the FP32 transform and added (in FP64) to every output sample.  A vortex field is dominated by its
+// axisymmetric, axially uniform mean flow; without this the FP32 rounding of that mean (relative
+// 2^-24 of an O(1) value) would land on every other wavenumber, where the perturbation lives.  The
+// φ lines all get it (their DC is the m = 0 coefficient); of the z lines only those of the m = 0
+// plane (their DC is the (m = 0, k = 0) coefficient) do.
+//
 // Layout: a field is (nrdim, npdim, nzdim) with r fastest.  Both transforms run along a strided
 // dimension; a CTA takes TR consecutive r (the contiguous batch, so every global access is a run of
 // TR*16 bytes) and TT threads per transform, keeps the TR transforms in shared memory as
 // [point][TR] and runs a Stockham autosort FFT (radix 4, 2, 3, 5) between two shared buffers.
 #include "common.cuh"
+#include <type_traits>
 
 namespace mlg {
 
@@ -117,10 +127,12 @@ template <typename T> __device__ __forceinline__ void st(double2* p, typename CT
 template <> __device__ __forceinline__ void st<double>(double2* p, double2 v) { *p = v; }
 template <> __device__ __forceinline__ void st<float>(double2* p, float2 v) { st_c32(p, v); }
 
-// z FFT of columns (r, m): points at stride nrdim*npdim
+// z FFT of columns (r, m): points at stride nrdim*npdim.  Lines of the first dc_m m-columns carry
+// their DC in FP64 (mixed form only; dc_m = 0 for the plain form).
 template <typename T>
 __global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
-                       const typename TW<T>::t* __restrict__ tw, int sgn, T scale) {
+                       const typename TW<T>::t* __restrict__ tw, int sgn, T scale, double scale_d, double inv_l,
+                       int dc_m) {
   typedef typename CT<T>::t C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
@@ -131,19 +143,62 @@ __global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int
   bool ok = r < nrdim;
   size_t pstride = (size_t)nrdim * npdim;
   double2* base = e + r + (size_t)nrdim * m;
-  for (int pt = tt; pt < L; pt += TT) s0[pt * TR + tr] = ok ? ld<T>(base + pt * pstride) : mk<T>(0, 0);
+  bool dc = m < dc_m;                      // uniform over the CTA
+  double2 dcv = make_double2(0.0, 0.0);    // forward: sum of the line; backward: its k = 0 input
+  double2 mu = make_double2(0.0, 0.0);
+  if (dc) {
+    if (sgn < 0) {
+      double2* red = (double2*)(s1 + (size_t)L * TR);
+      double2 part = make_double2(0.0, 0.0);
+      if (ok)
+        for (int pt = tt; pt < L; pt += TT) { double2 v = base[pt * pstride]; part.x += v.x; part.y += v.y; }
+      red[tt * TR + tr] = part;
+      __syncthreads();
+      for (int q = 0; q < TT; ++q) { dcv.x += red[q * TR + tr].x; dcv.y += red[q * TR + tr].y; }
+      mu = make_double2(dcv.x * inv_l, dcv.y * inv_l);
+    } else if (ok) {
+      dcv = base[0];
+    }
+  }
+  for (int pt = tt; pt < L; pt += TT) {
+    C v = mk<T>(0, 0);
+    if (ok) {
+      if (dc) {
+        double2 d = base[pt * pstride];
+        if (sgn < 0) { d.x -= mu.x; d.y -= mu.y; }
+        else if (pt == 0) d = make_double2(0.0, 0.0);
+        v = mk<T>((T)d2f_fast(d.x), (T)d2f_fast(d.y));
+      } else {
+        v = ld<T>(base + pt * pstride);
+      }
+    }
+    s0[pt * TR + tr] = v;
+  }
   __syncthreads();
   C* res;
   stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, sgn);
-  if (ok)
-    for (int pt = tt; pt < L; pt += TT) st<T>(base + pt * pstride, c_scale(res[pt * TR + tr], (T)scale));
+  if (!ok) return;
+  double2 dcs = make_double2(dcv.x * scale_d, dcv.y * scale_d);
+  for (int pt = tt; pt < L; pt += TT) {
+    C y = c_scale(res[pt * TR + tr], (T)scale);
+    if (dc) {
+      double2 o = make_double2(f2d_fast((float)y.x), f2d_fast((float)y.y));
+      if (sgn > 0 || pt == 0) { o.x += dcs.x; o.y += dcs.y; }
+      base[pt * pstride] = o;
+    } else {
+      st<T>(base + pt * pstride, y);
+    }
+  }
 }
 
-// φ forward: packed reals -> X_0..X_{L} (L = np/2) scaled 1/np, in place
+// φ forward: packed reals -> X_0..X_{L} (L = np/2) scaled 1/np, in place.  Mixed form: X_0 from the
+// FP64 sum of the row, the FP32 FFT on the samples minus their FP64 mean.
 template <typename T>
 __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
-                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, T scale) {
+                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, T scale,
+                           double scale_d, double inv_np) {
   typedef typename CT<T>::t C;
+  constexpr bool DC = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
   C* s1 = s0 + (size_t)L * TR;
@@ -152,7 +207,29 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   int z = blockIdx.y;
   bool ok = r < nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
-  for (int pt = tt; pt < L; pt += TT) s0[pt * TR + tr] = ok ? ld<T>(base + (size_t)pt * nrdim) : mk<T>(0, 0);
+  double sum = 0.0, mu = 0.0;
+  if (DC) {
+    double* red = (double*)(s1 + (size_t)L * TR);
+    double part = 0.0;
+    if (ok)
+      for (int pt = tt; pt < L; pt += TT) { double2 v = base[(size_t)pt * nrdim]; part += v.x + v.y; }
+    red[tt * TR + tr] = part;
+    __syncthreads();
+    for (int q = 0; q < TT; ++q) sum += red[q * TR + tr];
+    mu = sum * inv_np;
+  }
+  for (int pt = tt; pt < L; pt += TT) {
+    C v = mk<T>(0, 0);
+    if (ok) {
+      if (DC) {
+        double2 d = base[(size_t)pt * nrdim];
+        v = mk<T>((T)d2f_fast(d.x - mu), (T)d2f_fast(d.y - mu));
+      } else {
+        v = ld<T>(base + (size_t)pt * nrdim);
+      }
+    }
+    s0[pt * TR + tr] = v;
+  }
   __syncthreads();
   C* res;
   stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, -1);
@@ -165,16 +242,22 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
     C fo = c_muli(c_scale(c_sub(zk, zc), (T)0.5), -1);   // (zk - zc)/(2i)
     typename TW<T>::t wd = twr[k];
     C w = mk<T>(wd.x, wd.y);
-    C x = c_add(fe, c_mul(w, fo));
-    st<T>(base + (size_t)k * nrdim, c_scale(x, (T)scale));
+    C x = c_scale(c_add(fe, c_mul(w, fo)), (T)scale);
+    if (DC && k == 0) {
+      base[0] = make_double2(f2d_fast((float)x.x) + sum * scale_d, f2d_fast((float)x.y));
+    } else {
+      st<T>(base + (size_t)k * nrdim, x);
+    }
   }
 }
 
-// φ backward: X_0..X_L -> packed reals (unnormalised); slot L <- np * X_L (input), in place
+// φ backward: X_0..X_L -> packed reals (unnormalised); slot L <- np * X_L (input), in place.  Mixed
+// form: Re X_0 is left out of the FP32 FFT and added to every sample in FP64.
 template <typename T>
 __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
                            const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, double np_d) {
   typedef typename CT<T>::t C;
+  constexpr bool DC = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
   C* s1 = s0 + (size_t)L * TR;
@@ -184,13 +267,15 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   bool ok = r < nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
   double2 nyq = make_double2(0, 0);
+  double dc = 0.0;
   if (ok && tt == 0) nyq = base[(size_t)L * nrdim];
+  if (DC && ok) dc = base[0].x;
   for (int k = tt; k < L; k += TT) {
     C v = mk<T>(0, 0);
     if (ok) {
       C xk = ld<T>(base + (size_t)k * nrdim);
       C xc = ld<T>(base + (size_t)(L - k) * nrdim);
-      if (k == 0) { xk.y = 0; xc.y = 0; }
+      if (k == 0) { xk.y = 0; xc.y = 0; if (DC) xk.x = 0; }
       xc.y = -xc.y;
       C g = c_add(xk, xc);
       typename TW<T>::t wd = twr[k];
@@ -204,7 +289,14 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   C* res;
   stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, +1);
   if (!ok) return;
-  for (int pt = tt; pt < L; pt += TT) st<T>(base + (size_t)pt * nrdim, res[pt * TR + tr]);
+  for (int pt = tt; pt < L; pt += TT) {
+    if (DC) {
+      C y = res[pt * TR + tr];
+      base[(size_t)pt * nrdim] = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+    } else {
+      st<T>(base + (size_t)pt * nrdim, res[pt * TR + tr]);
+    }
+  }
   if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
 }
 
@@ -231,11 +323,13 @@ static int vfft_t(cd* e, int dir, double scale) {
   if (L <= 1) return 0;
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
   int TT = std::max(1, std::min(256 / TR, L / 2));
-  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
+  constexpr bool DC = std::is_same<T, float>::value;
+  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t) + (DC ? (size_t)TT * TR * sizeof(double2) : 0);
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), G.npdim), blk(TR, TT);
   kt_begin(1);
-  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale);
+  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, scale,
+                                          1.0 / L, DC ? 1 : 0);
   MLG_LAUNCH();
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;
@@ -257,13 +351,15 @@ static int hfft_t(cd* e, int dir, double scale) {
   if (G.np <= 1) return 0;
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
   int TT = std::max(1, std::min(256 / TR, std::max(L / 2, 1)));
-  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
+  constexpr bool DC = std::is_same<T, float>::value;
+  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t) + (DC ? (size_t)TT * TR * sizeof(double) : 0);
   dim3 grid(cdiv(G.nrdim, TR), G.nzdim), blk(TR, TT);
   kt_begin(1);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
     k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale);
+                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale,
+                                                scale, 1.0 / G.np);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
     k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
