@@ -584,11 +584,8 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
   MLG_TRY(hfft_fwd_T(ur));
   MLG_TRY(launch_set_ln(ur.ln, 0.0));
   MLG_TRY(scale_r(ur, 0));
-  {
-    PrecisionScope fp64(MLG_PLAIN_FP64);   // the forward's u_z FFTs run in FP64 in every form
-    MLG_TRY(vfft_checked_T(uz, -1));
-    MLG_TRY(hfft_fwd_T(uz));
-  }
+  MLG_TRY(vfft_checked_T(uz, -1));
+  MLG_TRY(hfft_fwd_T(uz));
   MLG_TRY(launch_set_ln(uz.ln, 0.0));
   MLG_TRY(assign(vrb, ur)); MLG_TRY(assign(vpb, up)); MLG_TRY(assign(vzb, uz));
   for (Scalar* q : {&vrb, &vpb, &vzb}) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }

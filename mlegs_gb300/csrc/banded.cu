@@ -42,15 +42,54 @@ template <> struct BC<float> {
   static __device__ __forceinline__ float cv(double v) { return d2f_fast(v); }
 };
 
+// one (m, k) column of nn rows, applied cnt times in place through shared memory
+template <typename T>
+__device__ __forceinline__ void band_col(double2* __restrict__ g, const double* __restrict__ bd2,
+                                         const double* __restrict__ bxx, double akd, int op, int m, int ne, int nn,
+                                         int cnt, unsigned char* smem, int nrdim) {
+  typedef typename BC<T>::C C;
+  C* c0 = (C*)smem;
+  C* c1 = c0 + nrdim;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(g + i);
+  __syncthreads();
+  T akv2 = BC<T>::cv(akd * akd);   // akval**2 (mlegs_spectfm_diff.f90:144)
+  for (int rep = 0; rep < cnt; ++rep) {
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+      C acc; acc.x = 0; acc.y = 0;
+      if (op == 0) {
+        const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
+        if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+        if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
+      } else {
+        const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          int j = i - 2 + c;
+          if (j < 0 || j >= nn) continue;
+          T v = BC<T>::cv(b[c]);
+          if (c == 2 && op == 2) v = v - akv2;
+          acc.x += v * c0[j].x;
+          acc.y += v * c0[j].y;
+        }
+      }
+      c1[i] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(g + i, c0[i]);
+  __syncthreads();
+}
+
+// grid (k, m).  The mixed form (T = float) still applies the m = 0 columns in FP64: they hold the
+// axisymmetric mean flow, and their radial sums cancel toward the axis.
 template <typename T>
 __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__ bd2, const double* __restrict__ bxx,
                              const double* __restrict__ ak, double* __restrict__ lnp, const double* __restrict__ lognorm,
                              int op, int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim,
                              double ell) {
-  typedef typename BC<T>::C C;
   extern __shared__ __align__(16) unsigned char band_smem[];
-  C* c0 = (C*)band_smem;
-  C* c1 = c0 + nrdim;
   int m = blockIdx.y, k = blockIdx.x;
   int nn = max(min(nrc, nrc - m), 0);
   int cnt = k_count(k, nzc, nzcu, nzdim);
@@ -59,37 +98,8 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
   double lnin = 0.0;
   if (lnblk) lnin = *lnp;
   if (m < npc && nn > 0 && cnt > 0) {
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(g + i);
-    __syncthreads();
-    double akd = ak[k];
-    T akv2 = BC<T>::cv(akd * akd);   // akval**2 (mlegs_spectfm_diff.f90:144)
-    for (int rep = 0; rep < cnt; ++rep) {
-      for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-        C acc; acc.x = 0; acc.y = 0;
-        if (op == 0) {
-          const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
-          if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
-          if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
-        } else {
-          const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
-#pragma unroll
-          for (int c = 0; c < 5; ++c) {
-            int j = i - 2 + c;
-            if (j < 0 || j >= nn) continue;
-            T v = BC<T>::cv(b[c]);
-            if (c == 2 && op == 2) v = v - akv2;
-            acc.x += v * c0[j].x;
-            acc.y += v * c0[j].y;
-          }
-        }
-        c1[i] = acc;
-      }
-      __syncthreads();
-      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
-      __syncthreads();
-    }
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(g + i, c0[i]);
-    __syncthreads();
+    if (m == 0) band_col<double>(g, bd2, bxx, ak[k], op, m, ne, nn, cnt, band_smem, nrdim);
+    else band_col<T>(g, bd2, bxx, ak[k], op, m, ne, nn, cnt, band_smem, nrdim);
   }
   if (lnblk && threadIdx.x == 0) {
     // the log-term contributions land on e(1..3,1,1) whether or not the column was active
@@ -111,7 +121,7 @@ int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
   dim3 grid(G.nzdim, std::max(c.npc, 1));
   kt_begin(2);
   if (G.precision == MLG_MIXED) {
-    size_t sm = 2ull * G.nrdim * sizeof(float2);
+    size_t sm = 2ull * G.nrdim * sizeof(double2);   // the m = 0 columns run in FP64
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_band_apply<float><<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
                                                      c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);

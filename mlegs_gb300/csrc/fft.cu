@@ -13,8 +13,7 @@
 // the FP32 transform and added (in FP64) to every output sample.  A vortex field is dominated by its
 // axisymmetric, axially uniform mean flow; without this the FP32 rounding of that mean (relative
 // 2^-24 of an O(1) value) would land on every other wavenumber, where the perturbation lives.  The
-// φ lines all get it (their DC is the m = 0 coefficient); of the z lines only those of the m = 0
-// plane (their DC is the (m = 0, k = 0) coefficient) do.
+// φ lines all get it (their DC is the m = 0 coefficient).  The z lines of the m = 0 plane run in FP64.
 //
 // Layout: a field is (nrdim, npdim, nzdim) with r fastest.  Both transforms run along a strided
 // dimension; a CTA takes TR consecutive r (the contiguous batch, so every global access is a run of
@@ -127,68 +126,26 @@ template <typename T> __device__ __forceinline__ void st(double2* p, typename CT
 template <> __device__ __forceinline__ void st<double>(double2* p, double2 v) { *p = v; }
 template <> __device__ __forceinline__ void st<float>(double2* p, float2 v) { st_c32(p, v); }
 
-// z FFT of columns (r, m): points at stride nrdim*npdim.  Lines of the first dc_m m-columns carry
-// their DC in FP64 (mixed form only; dc_m = 0 for the plain form).
+// z FFT of columns (r, m): points at stride nrdim*npdim; the grid covers m = m0, m0+1, ...
 template <typename T>
 __global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
-                       const typename TW<T>::t* __restrict__ tw, int sgn, T scale, double scale_d, double inv_l,
-                       int dc_m) {
+                       const typename TW<T>::t* __restrict__ tw, int sgn, T scale, int m0) {
   typedef typename CT<T>::t C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* s0 = (C*)smem_raw;
   C* s1 = s0 + (size_t)L * TR;
   int tr = threadIdx.x, tt = threadIdx.y, TT = blockDim.y;
   int r = blockIdx.x * TR + tr;
-  int m = blockIdx.y;
+  int m = blockIdx.y + m0;
   bool ok = r < nrdim;
   size_t pstride = (size_t)nrdim * npdim;
   double2* base = e + r + (size_t)nrdim * m;
-  bool dc = m < dc_m;                      // uniform over the CTA
-  double2 dcv = make_double2(0.0, 0.0);    // forward: sum of the line; backward: its k = 0 input
-  double2 mu = make_double2(0.0, 0.0);
-  if (dc) {
-    if (sgn < 0) {
-      double2* red = (double2*)(s1 + (size_t)L * TR);
-      double2 part = make_double2(0.0, 0.0);
-      if (ok)
-        for (int pt = tt; pt < L; pt += TT) { double2 v = base[pt * pstride]; part.x += v.x; part.y += v.y; }
-      red[tt * TR + tr] = part;
-      __syncthreads();
-      for (int q = 0; q < TT; ++q) { dcv.x += red[q * TR + tr].x; dcv.y += red[q * TR + tr].y; }
-      mu = make_double2(dcv.x * inv_l, dcv.y * inv_l);
-    } else if (ok) {
-      dcv = base[0];
-    }
-  }
-  for (int pt = tt; pt < L; pt += TT) {
-    C v = mk<T>(0, 0);
-    if (ok) {
-      if (dc) {
-        double2 d = base[pt * pstride];
-        if (sgn < 0) { d.x -= mu.x; d.y -= mu.y; }
-        else if (pt == 0) d = make_double2(0.0, 0.0);
-        v = mk<T>((T)d2f_fast(d.x), (T)d2f_fast(d.y));
-      } else {
-        v = ld<T>(base + pt * pstride);
-      }
-    }
-    s0[pt * TR + tr] = v;
-  }
+  for (int pt = tt; pt < L; pt += TT) s0[pt * TR + tr] = ok ? ld<T>(base + pt * pstride) : mk<T>(0, 0);
   __syncthreads();
   C* res;
   stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, sgn);
-  if (!ok) return;
-  double2 dcs = make_double2(dcv.x * scale_d, dcv.y * scale_d);
-  for (int pt = tt; pt < L; pt += TT) {
-    C y = c_scale(res[pt * TR + tr], (T)scale);
-    if (dc) {
-      double2 o = make_double2(f2d_fast((float)y.x), f2d_fast((float)y.y));
-      if (sgn > 0 || pt == 0) { o.x += dcs.x; o.y += dcs.y; }
-      base[pt * pstride] = o;
-    } else {
-      st<T>(base + pt * pstride, y);
-    }
-  }
+  if (ok)
+    for (int pt = tt; pt < L; pt += TT) st<T>(base + pt * pstride, c_scale(res[pt * TR + tr], (T)scale));
 }
 
 // φ forward: packed reals -> X_0..X_{L} (L = np/2) scaled 1/np, in place.  Mixed form: X_0 from the
@@ -318,31 +275,36 @@ static int set_smem(const void* fn, size_t bytes) {
 }
 
 template <typename T>
-static int vfft_t(cd* e, int dir, double scale) {
+static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max) {
   int L = G.nz;
-  if (L <= 1) return 0;
-  int TR = pick_tr(L, sizeof(typename CT<T>::t));
+  if (L <= 1 || nm <= 0) return 0;
+  int TR = std::min(pick_tr(L, sizeof(typename CT<T>::t)), tr_max);
   int TT = std::max(1, std::min(256 / TR, L / 2));
-  constexpr bool DC = std::is_same<T, float>::value;
-  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t) + (DC ? (size_t)TT * TR * sizeof(double2) : 0);
+  size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
-  dim3 grid(cdiv(G.nrdim, TR), G.npdim), blk(TR, TT);
-  kt_begin(1);
-  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, scale,
-                                          1.0 / L, DC ? 1 : 0);
+  dim3 grid(cdiv(G.nrdim, TR), nm), blk(TR, TT);
+  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
   MLG_LAUNCH();
+  return 0;
+}
+
+// plain form: FP64.  Mixed form: m >= 1 in FP32; the m = 0 lines (the axisymmetric part, with the mean
+// flow in its k = 0 coefficient) in FP64, in small CTAs so that they spread over the SMs.
+static int vfft_any(cd* e, int dir, double scale) {
+  kt_begin(1);
+  if (G.precision == MLG_MIXED) {
+    MLG_TRY(vfft_t<float>(e, dir, scale, 1, G.npdim - 1, 32));
+    MLG_TRY(vfft_t<double>(e, dir, scale, 0, 1, 2));
+  } else {
+    MLG_TRY(vfft_t<double>(e, dir, scale, 0, G.npdim, 32));
+  }
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;
 }
 
-int launch_vfft_buf(cd* e, int dir) {
-  double scale = dir < 0 ? 1.0 / G.nz : 1.0;
-  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir, scale) : vfft_t<double>(e, dir, scale);
-}
+int launch_vfft_buf(cd* e, int dir) { return vfft_any(e, dir, dir < 0 ? 1.0 / G.nz : 1.0); }
 // sum_j x_j exp(dir 2 pi i jk/nz) * scale, any direction and scale (the adjoint's FFTs)
-int launch_vfft_scaled(cd* e, int dir, double scale) {
-  return G.precision == MLG_MIXED ? vfft_t<float>(e, dir, scale) : vfft_t<double>(e, dir, scale);
-}
+int launch_vfft_scaled(cd* e, int dir, double scale) { return vfft_any(e, dir, scale); }
 int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
 
 template <typename T>

@@ -783,13 +783,8 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
   up.set_space("PFF");
   k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
   MLG_LAUNCH();
-  {
-    // u_z enters chi through an inverse horizontal Laplacian, which lifts rounding of the strong
-    // high-wavenumber part of u_z into the weak low modes; its two FFTs stay FP64 in every form
-    PrecisionScope fp64(MLG_PLAIN_FP64);
-    MLG_TRY(op_trans(uz, "PFP"));
-    if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
-  }
+  MLG_TRY(op_trans(uz, "PFP"));
+  if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
   uz.set_space("PFF");
   // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331); psi%ln was set above from calcat1
   MLG_TRY(launch_zero(psi.e));

@@ -9,34 +9,110 @@
 //   vec2tp projection (:1402-1438), five contractions against the V, D, T matrices with the
 //     eomul / oemul parity folds (:2067-2145), combined into psi and chi.
 // Each CTA owns one m, one parity of rows and one tile of z columns; the folded input (f(i) +- f(nr-1-i))
-// is formed while staging the K-chunk in shared memory.  The plain form accumulates in FP64 (DFMA),
-// the mixed form in FP32.
+// is formed while staging the K-chunk in shared memory.  The plain form accumulates in FP64 (DFMA).
+// The mixed form runs m >= 1 on the tensor cores (tc_radial.cu) or in FP32 and the m = 0 plane in
+// double-float (below): the m = 0 plane carries the axisymmetric mean flow, and its radial functions do
+// not vanish on the axis, so regular fields such as r d/dr(chi) reach zero there only by cancellation
+// of their radial sums, which the 1/r of the velocity components then magnifies (about 40x at the
+// innermost collocation point of a 192-point grid).
 #include "common.cuh"
 
 namespace mlg {
 
+// ---- double-float: an unevaluated sum h + l of two FP32 values (about 44 significant bits), every
+// operation on the FP32 pipe through error-free transformations (Knuth's two-sum, Dekker/Kahan's FMA
+// product error; Dekker 1971, Hida-Li-Bailey 2001).  GB300 issues about 2 FP64 FMAs per clock per SM
+// against 128 FP32 FMAs, so the work that needs more than FP32 in the mixed form runs in double-float.
+// The intrinsics (__fadd_rn, ...) are never contracted into FMAs, which the transformations rely on.
+struct dfl {
+  float h, l;
+  dfl() = default;
+  __device__ __forceinline__ dfl(int v) : h((float)v), l(0.f) {}   // small integers are exact
+  __device__ __forceinline__ dfl(float a, float b) : h(a), l(b) {}
+  __device__ __forceinline__ explicit dfl(double x);
+};
+__device__ __forceinline__ dfl df_quick(float a, float b) {   // |a| >= |b|
+  float s = __fadd_rn(a, b);
+  return dfl(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  float s = __fadd_rn(a.h, b.h), v = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+  return df_quick(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.h, -a.l); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return df_quick(p, e);
+}
+struct dfl2 { dfl x, y; };
+
+// multiply-accumulate in the kernel's arithmetic
+__device__ __forceinline__ double tmac(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float tmac(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ dfl tmac(dfl a, dfl b, dfl c) { return a * b + c; }
+
 template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 t; };
 template <> struct V2<float> { typedef float2 t; };
+template <> struct V2<dfl> { typedef dfl2 t; };
+
+// x = hi + lo with hi the 24-bit truncation of x and lo the next bits rounded to FP32 (about 47 bits
+// in all), split on the integer pipe; values below 2^-126 (and their lo below 2^-75) flush to zero
+__device__ __forceinline__ float2 d2ff(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  unsigned sign = hi & 0x80000000u;
+  int e = (int)((hi >> 20) & 0x7FFu);
+  int e32 = e - 1023 + 127;
+  if (e == 0x7FF) return make_float2(__uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u)), 0.f);
+  if (e32 <= 0) return make_float2(__uint_as_float(sign), 0.f);
+  if (e32 >= 255) return make_float2(__uint_as_float(sign | 0x7F800000u), 0.f);
+  float h = __uint_as_float(sign | ((unsigned)e32 << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+  int el = e - 1075 + 127;   // exponent of the unit of the 29 remaining bits
+  float l = 0.f;
+  if (el > 0) {
+    l = __uint2float_rn(lo & 0x1FFFFFFFu) * __uint_as_float((unsigned)el << 23);
+    if (sign) l = -l;
+  }
+  return make_float2(h, l);
+}
+__device__ __forceinline__ dfl::dfl(double x) { float2 v = d2ff(x); h = v.x; l = v.y; }
 
 // field loads / stores: FP64 as is for the plain form; for the mixed form the conversions run on
 // the integer pipe (d2f_fast / f2d_fast), keeping these kernels off GB300's narrow FP64 pipe
 template <typename T> __device__ __forceinline__ typename V2<T>::t ldc(const double2* p);
 template <> __device__ __forceinline__ double2 ldc<double>(const double2* p) { return *p; }
 template <> __device__ __forceinline__ float2 ldc<float>(const double2* p) { return ld_c32(p); }
+template <> __device__ __forceinline__ dfl2 ldc<dfl>(const double2* p) {
+  double2 v = *p;
+  dfl2 r; r.x = dfl(v.x); r.y = dfl(v.y); return r;
+}
 template <typename T> __device__ __forceinline__ double2 to_d2(T re, T im);
 template <> __device__ __forceinline__ double2 to_d2<double>(double re, double im) { return make_double2(re, im); }
 template <> __device__ __forceinline__ double2 to_d2<float>(float re, float im) {
   return make_double2(f2d_fast(re), f2d_fast(im));
 }
+template <> __device__ __forceinline__ double2 to_d2<dfl>(dfl re, dfl im) {
+  return make_double2(f2d_fast(re.h) + f2d_fast(re.l), f2d_fast(im.h) + f2d_fast(im.l));
+}
 template <typename T> __device__ __forceinline__ T wsel(const double* w, const float* w32, int i);
 template <> __device__ __forceinline__ double wsel<double>(const double* w, const float* w32, int i) { (void)w32; return w[i]; }
 template <> __device__ __forceinline__ float wsel<float>(const double* w, const float* w32, int i) { (void)w; return w32[i]; }
+template <> __device__ __forceinline__ dfl wsel<dfl>(const double* w, const float* w32, int i) { (void)w32; return dfl(w[i]); }
+// table entries: stored as T (FP64 or FP32); double-float reads the FP64 table and splits it
+template <typename T> struct TabT { typedef T t; };
+template <> struct TabT<dfl> { typedef double t; };
+template <typename T> __device__ __forceinline__ T tab(const typename TabT<T>::t* p, size_t o) { return (T)p[o]; }
 
 // forward: grid (ztiles, 2*ttiles, npc); block (ZT/ZPT, MT/MPT)
 template <typename T, int MT, int ZT, int KC, int MPT, int ZPT>
 __global__ void __launch_bounds__((MT / MPT) * (ZT / ZPT))
-k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T* __restrict__ pf,
+k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const typename TabT<T>::t* __restrict__ pf,
              const double* __restrict__ w, const float* __restrict__ w32, int nr, int nrh, int ne, int nrdim, int npdim,
              int nzdim, int nrc) {
   typedef typename V2<T>::t C;
@@ -62,7 +138,7 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       int ii = idx % KC, tt = idx / KC;
       int j = 2 * (t0 + tt) + par, i = i0 + ii;
       T v = 0;
-      if (j < nn && i < nrh) v = pf[i + (size_t)nrh * (j + (size_t)ne * m)];
+      if (j < nn && i < nrh) v = tab<T>(pf, i + (size_t)nrh * (j + (size_t)ne * m));
       As[ii][tt] = v;
     }
     // B chunk: folded columns (f(i) +- f(nr-1-i)) * w(i)
@@ -92,8 +168,8 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       for (int a = 0; a < MPT; ++a)
 #pragma unroll
         for (int b = 0; b < ZPT; ++b) {
-          acc_r[a][b] = fma(av[a], bv[b].x, acc_r[a][b]);
-          acc_i[a][b] = fma(av[a], bv[b].y, acc_i[a][b]);
+          acc_r[a][b] = tmac(av[a], bv[b].x, acc_r[a][b]);
+          acc_i[a][b] = tmac(av[a], bv[b].y, acc_i[a][b]);
         }
     }
     __syncthreads();
@@ -113,7 +189,7 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
 // backward: grid (ztiles, itiles, npc); each thread owns IPT rows i and ZPT columns and both parities
 template <typename T, int IT, int ZT, int KC, int IPT, int ZPT>
 __global__ void __launch_bounds__((IT / IPT) * (ZT / ZPT))
-k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T* __restrict__ pf,
+k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const typename TabT<T>::t* __restrict__ pf,
              const double* __restrict__ lnx, const double* __restrict__ lnp, int add_ln, int nr, int nrh, int ne,
              int nrdim, int npdim, int nzdim, int nrc) {
   typedef typename V2<T>::t C;
@@ -137,8 +213,8 @@ k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       int i = i0 + ii, je = 2 * (t0 + tt), jo = je + 1;
       T ve = 0, vo = 0;
       if (i < nrh) {
-        if (je < nn) ve = pf[i + (size_t)nrh * (je + (size_t)ne * m)];
-        if (jo < nn) vo = pf[i + (size_t)nrh * (jo + (size_t)ne * m)];
+        if (je < nn) ve = tab<T>(pf, i + (size_t)nrh * (je + (size_t)ne * m));
+        if (jo < nn) vo = tab<T>(pf, i + (size_t)nrh * (jo + (size_t)ne * m));
       }
       Ae[tt][ii] = ve; Ao[tt][ii] = vo;
     }
@@ -162,10 +238,10 @@ k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
       for (int a = 0; a < IPT; ++a)
 #pragma unroll
         for (int b = 0; b < ZPT; ++b) {
-          er[a][b] = fma(ae[a], be[b].x, er[a][b]);
-          ei[a][b] = fma(ae[a], be[b].y, ei[a][b]);
-          orr[a][b] = fma(ao[a], bo[b].x, orr[a][b]);
-          oi[a][b] = fma(ao[a], bo[b].y, oi[a][b]);
+          er[a][b] = tmac(ae[a], be[b].x, er[a][b]);
+          ei[a][b] = tmac(ae[a], be[b].y, ei[a][b]);
+          orr[a][b] = tmac(ao[a], bo[b].x, orr[a][b]);
+          oi[a][b] = tmac(ao[a], bo[b].y, oi[a][b]);
         }
     }
     __syncthreads();
@@ -196,8 +272,8 @@ k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const T*
 template <typename T, int MT, int ZT, int KC, int ZPT>
 __global__ void __launch_bounds__(MT * (ZT / ZPT))
 k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
-         double2* __restrict__ psi, double2* __restrict__ chi, const T* __restrict__ tV, const T* __restrict__ tD,
-         const T* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
+         double2* __restrict__ psi, double2* __restrict__ chi, const typename TabT<T>::t* __restrict__ tV,
+         const typename TabT<T>::t* __restrict__ tD, const typename TabT<T>::t* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
          int nzdim, int nrc, int nzc, int nzcu) {
   typedef typename V2<T>::t C;
   __shared__ T Av[KC][MT + 1], Ad[KC][MT + 1], At[KC][MT + 1];
@@ -223,7 +299,7 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
       T v = 0, d = 0, t = 0;
       if (j < nn && i < nrh) {
         size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
-        v = tV[o]; d = tD[o]; t = tT[o];
+        v = tab<T>(tV, o); d = tab<T>(tD, o); t = tab<T>(tT, o);
       }
       Av[ii][tt] = v; Ad[ii][tt] = d; At[ii][tt] = t;
     }
@@ -253,11 +329,11 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
       for (int b = 0; b < ZPT; ++b) {
         int zz = tx + b * (ZT / ZPT);
         C rs = Brs[ii][zz], ro = Bro[ii][zz], ps = Bps[ii][zz], po = Bpo[ii][zz], zs = Bzs[ii][zz];
-        a1[b].x = fma(v, rs.x, a1[b].x); a1[b].y = fma(v, rs.y, a1[b].y);   // V.F_s(ur)
-        a2[b].x = fma(d, po.x, a2[b].x); a2[b].y = fma(d, po.y, a2[b].y);   // D.F_o(up)
-        a3[b].x = fma(d, ro.x, a3[b].x); a3[b].y = fma(d, ro.y, a3[b].y);   // D.F_o(ur)
-        a4[b].x = fma(v, ps.x, a4[b].x); a4[b].y = fma(v, ps.y, a4[b].y);   // V.F_s(up)
-        a5[b].x = fma(t, zs.x, a5[b].x); a5[b].y = fma(t, zs.y, a5[b].y);   // T.F_s(uz)
+        a1[b].x = tmac(v, rs.x, a1[b].x); a1[b].y = tmac(v, rs.y, a1[b].y);   // V.F_s(ur)
+        a2[b].x = tmac(d, po.x, a2[b].x); a2[b].y = tmac(d, po.y, a2[b].y);   // D.F_o(up)
+        a3[b].x = tmac(d, ro.x, a3[b].x); a3[b].y = tmac(d, ro.y, a3[b].y);   // D.F_o(ur)
+        a4[b].x = tmac(v, ps.x, a4[b].x); a4[b].y = tmac(v, ps.y, a4[b].y);   // V.F_s(up)
+        a5[b].x = tmac(t, zs.x, a5[b].x); a5[b].y = tmac(t, zs.y, a5[b].y);   // T.F_s(uz)
       }
     }
     __syncthreads();
@@ -288,27 +364,6 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
 }
 
 // ---- mixed-form projection ------------------------------------------------------------------------
-// x = hi + lo with hi the 24-bit truncation of x and lo the next bits rounded to FP32 (about 47 bits
-// in all), split on the integer pipe; values below 2^-126 (and their lo below 2^-75) flush to zero
-__device__ __forceinline__ float2 d2ff(double x) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  unsigned sign = hi & 0x80000000u;
-  int e = (int)((hi >> 20) & 0x7FFu);
-  int e32 = e - 1023 + 127;
-  if (e == 0x7FF) return make_float2(__uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u)), 0.f);
-  if (e32 <= 0) return make_float2(__uint_as_float(sign), 0.f);
-  if (e32 >= 255) return make_float2(__uint_as_float(sign | 0x7F800000u), 0.f);
-  float h = __uint_as_float(sign | ((unsigned)e32 << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
-  int el = e - 1075 + 127;   // exponent of the unit of the 29 remaining bits
-  float l = 0.f;
-  if (el > 0) {
-    l = __uint2float_rn(lo & 0x1FFFFFFFu) * __uint_as_float((unsigned)el << 23);
-    if (sign) l = -l;
-  }
-  return make_float2(h, l);
-}
-
 // (ah + al) + (bh + bl) renormalised (Knuth two-sum on the high parts)
 __device__ __forceinline__ float2 df_add(float ah, float al, float bh, float bl) {
   float s = ah + bh, v = s - ah;
@@ -339,12 +394,12 @@ k_vec2tp_mixed(const double2* __restrict__ ur, const double2* __restrict__ up, c
                double2* __restrict__ psi, double2* __restrict__ chi, const float* __restrict__ tV,
                const float* __restrict__ tD, const float* __restrict__ tTh, const float* __restrict__ tTl,
                const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc,
-               int nzc, int nzcu) {
+               int nzc, int nzcu, int m0) {
   constexpr int RT = MT / MPT;   // row threads
   constexpr int CT = ZT / ZPT;   // column threads
   __shared__ float Av[KC][MT + 1], Ad[KC][MT + 1], Ath[KC][MT + 1], Atl[KC][MT + 1];
   __shared__ float2 Brs[KC][ZT], Bro[KC][ZT], Bps[KC][ZT], Bpo[KC][ZT], Bzh[KC][ZT], Bzl[KC][ZT];
-  int m = blockIdx.z;
+  int m = blockIdx.z + m0;
   int par = blockIdx.y & 1;
   int t0 = (blockIdx.y >> 1) * MT;
   int nn = max(min(nrc, nrc - m), 0);
@@ -459,6 +514,28 @@ static double fwd_flops(int nrc, int npc) {
   return f;
 }
 
+// the m = 0 plane of the mixed form in double-float: small tiles (about 190 CTAs at 192x128x128), one
+// output per thread
+static int m0_rtrans_fwd(const cd* in, cd* out, int nrc) {
+  constexpr int MT = 16, ZT = 8, KC = 16;
+  int nn = std::max(nrc, 0);
+  if (nn == 0) return 0;
+  dim3 grid(cdiv(G.nzdim, ZT), 2 * cdiv((nn + 1) / 2, MT), 1), blk(ZT, MT);
+  k_rtrans_fwd<dfl, MT, ZT, KC, 1, 1><<<grid, blk, 0, G.stream>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim,
+                                                                 G.npdim, G.nzdim, nrc);
+  MLG_LAUNCH();
+  return 0;
+}
+static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln) {
+  constexpr int IT = 16, ZT = 4, KC = 16;
+  if (nrc <= 0) return 0;
+  dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), 1), blk(ZT, IT);
+  k_rtrans_bwd<dfl, IT, ZT, KC, 1, 1><<<grid, blk, 0, G.stream>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
+                                                                 G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
+  MLG_LAUNCH();
+  return 0;
+}
+
 int launch_rtrans_fwd(Scalar& s) {
   int nrc, npc;
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_forward"));
@@ -468,7 +545,8 @@ int launch_rtrans_fwd(Scalar& s) {
   kt_begin(KT_RFWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
-      MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));   // tensor cores, split BF16 (tc_radial.cu); counts its launch
+      MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));   // m >= 1: tensor cores, split BF16 (tc_radial.cu)
+      MLG_TRY(m0_rtrans_fwd(s.e, out, nrc));         // m = 0: double-float
     } else {
       constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
       int tt = cdiv((nrc + 1) / 2, MT);
@@ -493,7 +571,8 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
-      MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));   // tensor cores, split BF16 (tc_radial.cu)
+      MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));   // m >= 1: tensor cores, split BF16
+      MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln));         // m = 0: double-float
     } else {
       constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
       dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
@@ -518,12 +597,20 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
   if (G.precision == MLG_MIXED) {
+    // m >= 1 in FP32 (with the u_z term in double-float), m = 0 in double-float
     constexpr int MMT = 32, MMPT = 2;
     int mtt = cdiv((nrc + 1) / 2, MMT);
-    dim3 mgrid(cdiv(G.nzdim, ZT), 2 * mtt, npc), mblk(ZT / ZPT, MMT / MMPT);
-    k_vec2tp_mixed<MMT, ZT, KC, MMPT, ZPT><<<mgrid, mblk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV32, G.tD32, G.tT32,
-                                                                         G.tT32lo, G.ak, G.nr, G.nrh, G.ne, G.nrdim,
-                                                                         G.npdim, G.nzdim, nrc, nzc, nzcu);
+    if (npc > 1) {
+      dim3 mgrid(cdiv(G.nzdim, ZT), 2 * mtt, npc - 1), mblk(ZT / ZPT, MMT / MMPT);
+      k_vec2tp_mixed<MMT, ZT, KC, MMPT, ZPT><<<mgrid, mblk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV32, G.tD32, G.tT32,
+                                                                           G.tT32lo, G.ak, G.nr, G.nrh, G.ne, G.nrdim,
+                                                                           G.npdim, G.nzdim, nrc, nzc, nzcu, 1);
+      MLG_LAUNCH();
+    }
+    constexpr int DMT = 16, DZT = 8;
+    dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
+    k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
+                                                                 G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
   } else
     k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
                                                                    G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);

@@ -28,11 +28,9 @@
 // Every wait is bounded (about a second of clock); a timeout sets the library's status flag, and the
 // CTA still releases its TMEM.
 //
-// The m = 0 plane: the columns (m = 0, z) of a vortex field all carry the axisymmetric, axially uniform
-// mean flow, O(1) against an O(1e-4) perturbation.  Transformed in FP32 at every z, its rounding would
-// differ from z to z and so land on every k != 0.  The mean over z of the plane is therefore taken
-// out (in FP64) before the FP32 operands are formed, transformed on its own in FP64 (one column), and
-// added back to every z column of the output.
+// The m = 0 plane is not done here: the mixed form contracts it in double-float (radial.cu), since
+// it carries the axisymmetric mean flow and its radial sums cancel toward the axis.  The grid starts
+// at m = m0.
 #include "common.cuh"
 #include <cstdint>
 
@@ -224,12 +222,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
                                                           const uint16_t* __restrict__ img, const float* __restrict__ w32,
                                                           const double* __restrict__ lnx, const double* __restrict__ lnp,
                                                           int add_ln, int nr, int nrh, int nrdim, int npdim, int nzdim,
-                                                          int nrc, int nmt, int nkc, const double2* __restrict__ zmean,
-                                                          int* __restrict__ status) {
+                                                          int nrc, int nmt, int nkc, int m0, int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(tc_smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int z0 = blockIdx.x * TC_NZ, mt = blockIdx.y, m = blockIdx.z;
+  const int z0 = blockIdx.x * TC_NZ, mt = blockIdx.y, m = blockIdx.z + m0;
   const int nn = max(min(nrc, nrc - m), 0);
   if (MODE == 0 && 2 * (mt * 128) >= nn) return;   // no rows of either parity in this tile
   if (MODE == 1 && (nn == 0 || mt * 128 >= nrh)) return;
@@ -255,25 +252,18 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
   const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * min(z, nzdim - 1));
   float2 ra[8], rb[8];
   float wv[8];
-  const bool sub = (m == 0) && (zmean != nullptr);   // uniform over the CTA
-  // field value at row i of this column, minus the plane's z-mean on the m = 0 plane (FP64)
-  auto ldr = [&](int i) -> float2 {
-    if (!sub) return ld_c32(col + i);
-    double2 v = col[i], u = zmean[i];
-    return make_float2(d2f_fast(v.x - u.x), d2f_fast(v.y - u.y));
-  };
   auto fetch = [&](int kc) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       int k = kc * TC_KC + kg * 8 + q;
       ra[q] = make_float2(0.f, 0.f); rb[q] = make_float2(0.f, 0.f); wv[q] = 0.f;
       if (MODE == 0) {
-        if (k < nrh && z < nzdim) { ra[q] = ldr(k); rb[q] = ldr(nr - 1 - k); wv[q] = w32[k]; }
+        if (k < nrh && z < nzdim) { ra[q] = ld_c32(col + k); rb[q] = ld_c32(col + nr - 1 - k); wv[q] = w32[k]; }
       } else {
         int je = 2 * k, jo = 2 * k + 1;
         if (z < nzdim) {
-          if (je < nn) ra[q] = ldr(je);
-          if (jo < nn) rb[q] = ldr(jo);
+          if (je < nn) ra[q] = ld_c32(col + je);
+          if (jo < nn) rb[q] = ld_c32(col + jo);
         }
       }
     }
@@ -378,83 +368,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
 }
 
 // ------------------------------------------------------------------------------------------------
-// the m = 0 plane's mean over z: zm(i) = (1/nz) sum_z in(i, 0, z), i < nrows (FP64).
-// block (32 rows, 8 z groups), grid over row tiles
-__global__ void __launch_bounds__(256) k_zmean0(const double2* __restrict__ in, double2* __restrict__ zm, int nrows,
-                                                int nrdim, int npdim, int nzdim, double inv_nz) {
-  __shared__ double2 red[8][32];
-  int i = blockIdx.x * 32 + threadIdx.x;
-  double2 s = make_double2(0.0, 0.0);
-  if (i < nrows)
-    for (int z = threadIdx.y; z < nzdim; z += 8) {
-      double2 v = in[i + (size_t)nrdim * npdim * z];
-      s.x += v.x; s.y += v.y;
-    }
-  red[threadIdx.y][threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.y == 0 && i < nrows) {
-    double2 t = make_double2(0.0, 0.0);
-    for (int q = 0; q < 8; ++q) { t.x += red[q][threadIdx.x].x; t.y += red[q][threadIdx.x].y; }
-    zm[i] = make_double2(t.x * inv_nz, t.y * inv_nz);
-  }
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// forward transform of the mean column in FP64 (rtrans_forward of one column), added to every z:
-// out(n, 0, z) += sum_{i < nrh} pf(i, n, 0) (zm(i) +- zm(nr-1-i)) w(i), '+' for even n.  One warp per n.
-__global__ void __launch_bounds__(128) k_dc0_fwd(const double2* __restrict__ zm, double2* __restrict__ out,
-                                                 const double* __restrict__ pf, const double* __restrict__ w, int nr,
-                                                 int nrh, int nrdim, int npdim, int nzdim, int nn) {
-  int n = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (n >= nn) return;
-  double sg = (n & 1) ? -1.0 : 1.0, cr = 0.0, ci = 0.0;
-  for (int i = lane; i < nrh; i += 32) {
-    double a = pf[i + (size_t)nrh * n] * w[i];
-    double2 u = zm[i], v = zm[nr - 1 - i];
-    cr = fma(a, u.x + sg * v.x, cr);
-    ci = fma(a, u.y + sg * v.y, ci);
-  }
-  cr = warp_sum(cr);
-  ci = warp_sum(ci);
-  for (int z = lane; z < nzdim; z += 32) {
-    double2* o = out + n + (size_t)nrdim * npdim * z;
-    double2 v = *o;
-    *o = make_double2(v.x + cr, v.y + ci);
-  }
-}
-
-// backward transform of the mean column in FP64 (rtrans_backward of one column), added to every z:
-// be(i) = sum_{n even} pf(i, n, 0) zm(n), bo(i) = sum_{n odd} ...; out(i) += be + bo, out(nr-1-i) += be - bo.
-// One warp per radial point pair i < nrh.
-__global__ void __launch_bounds__(128) k_dc0_bwd(const double2* __restrict__ zm, double2* __restrict__ out,
-                                                 const double* __restrict__ pf, int nr, int nrh, int nrdim, int npdim,
-                                                 int nzdim, int nn) {
-  int i = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i >= nrh) return;
-  double er = 0.0, ei = 0.0, orr = 0.0, oi = 0.0;
-  for (int n = lane; n < nn; n += 32) {
-    double a = pf[i + (size_t)nrh * n];
-    double2 c = zm[n];
-    if (n & 1) { orr = fma(a, c.x, orr); oi = fma(a, c.y, oi); }
-    else { er = fma(a, c.x, er); ei = fma(a, c.y, ei); }
-  }
-  er = warp_sum(er); ei = warp_sum(ei); orr = warp_sum(orr); oi = warp_sum(oi);
-  for (int z = lane; z < nzdim; z += 32) {
-    double2* o = out + (size_t)nrdim * npdim * z;
-    double2 p = o[i], q = o[nr - 1 - i];
-    o[i] = make_double2(p.x + er + orr, p.y + ei + oi);
-    o[nr - 1 - i] = make_double2(q.x + er - orr, q.y + ei - oi);
-  }
-}
-
-static double2* g_zmean = nullptr;
-static size_t g_zmean_n = 0;
-
 // ------------------------------------------------------------------------------------------------
 struct TcImg {
   uint16_t* p = nullptr;
@@ -468,9 +381,6 @@ void tc_free() {
     if (t.p) dfree(t.p, t.bytes);
     t = TcImg();
   }
-  if (g_zmean) dfree(g_zmean, g_zmean_n * sizeof(double2));
-  g_zmean = nullptr;
-  g_zmean_n = 0;
 }
 
 // forward (mode 0) / backward (mode 1) contraction on the tensor cores; out zeroed by the caller
@@ -492,40 +402,20 @@ static int tc_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, const do
   size_t sm = sizeof(TcSmem) + 1024;
   dim3 grid(cdiv(G.nzdim, TC_NZ), nmt, npc);
   int* st = (int*)(G.dscal + DS_FLAG + 1) + 1;
-  // the m = 0 plane's z-mean (rows read by the transform: nr physical points forward, nn(0) = nrc
-  // coefficients backward), lifted out of the FP32 operands when the plane has more than one z
-  const int nn0 = std::max(nrc, 0);
-  const int zrows = (mode == 0) ? G.nr : nn0;
-  const bool lift = G.nzdim > 1 && nn0 > 0;
-  if (lift) {
-    if (g_zmean_n < (size_t)G.nrdim) {
-      if (g_zmean) dfree(g_zmean, g_zmean_n * sizeof(double2));
-      g_zmean = nullptr;
-      g_zmean_n = 0;
-      MLG_TRY(dmalloc((void**)&g_zmean, (size_t)G.nrdim * sizeof(double2)));
-      g_zmean_n = G.nrdim;
-    }
-    k_zmean0<<<cdiv(zrows, 32), dim3(32, 8), 0, G.stream>>>(in, g_zmean, zrows, G.nrdim, G.npdim, G.nzdim, 1.0 / G.nzdim);
-    MLG_LAUNCH();
-  }
-  const double2* zm = lift ? g_zmean : nullptr;
+  // m >= 1 only: the m = 0 plane is contracted in double-float by the caller
+  const int m0 = 1;
+  if (npc <= m0) return 0;
+  grid.z = npc - m0;
   if (mode == 0) {
     MLG_CUDA(cudaFuncSetAttribute(k_tc_rtrans<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_tc_rtrans<0><<<grid, TC_THREADS, sm, G.stream>>>(in, out, im.p, G.w32, G.lnx, lnp, 0, G.nr, G.nrh, G.nrdim, G.npdim,
-                                                       G.nzdim, nrc, nmt, nkc, zm, st);
+                                                       G.nzdim, nrc, nmt, nkc, m0, st);
   } else {
     MLG_CUDA(cudaFuncSetAttribute(k_tc_rtrans<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_tc_rtrans<1><<<grid, TC_THREADS, sm, G.stream>>>(in, out, im.p, G.w32, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
-                                                       G.nrdim, G.npdim, G.nzdim, nrc, nmt, nkc, zm, st);
+                                                       G.nrdim, G.npdim, G.nzdim, nrc, nmt, nkc, m0, st);
   }
   MLG_LAUNCH();
-  if (lift) {
-    if (mode == 0)
-      k_dc0_fwd<<<cdiv(nn0, 4), 128, 0, G.stream>>>(g_zmean, out, G.pf, G.w, G.nr, G.nrh, G.nrdim, G.npdim, G.nzdim, nn0);
-    else
-      k_dc0_bwd<<<cdiv(G.nrh, 4), 128, 0, G.stream>>>(g_zmean, out, G.pf, G.nr, G.nrh, G.nrdim, G.npdim, G.nzdim, nn0);
-    MLG_LAUNCH();
-  }
   return 0;
 }
 

@@ -269,3 +269,34 @@ def test_mixed_vector_fields(mixed_pair):
     k.vec2tp(*gin, *gq); o.vec2tp(*ov, *oq)
     for i in range(2):
         compare(gq[i], oq[i], 1e-5, ln_tol=1.0, what=f"{name} mixed vec2tp {i}")
+
+
+def test_mixed_vortex_steps_within_1e6_of_fp64():
+    """The mixed form against the FP64 form over 20 vortex steps at 192x128x128 (q = 4 Batchelor
+    vortex, Re = 1e4, dt = 1e-3, SVV on, perturbation 1e-4 on |m| <= 4, |k| <= 8): every field of the
+    state within 1e-6 relative.  The FP64 form itself matches the oracle to 1e-11 (test_vortex_steps)."""
+    from mlegs_gb300 import vortex
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    from mlegs_gb300.params import make_params
+    p = make_params(nr=192, np=128, nz=128, nrchop=192, npchop=65, nzchop=65, ell=4.0, visc=1.0e-4)
+    k = Kit(p)
+    st = vortex.VortexState(k)
+    pert = (fields.spectral_noise(p, k.dims, 1001, amp=1e-4, decay=0.3, m_max=4, k_max=8),
+            fields.spectral_noise(p, k.dims, 1002, amp=1e-4, decay=0.3, m_max=4, k_max=8))
+    vortex.qvort_init(k, st, q=4.0, uz_b=0.0, pert=pert)
+    vortex.bootstrap(k, st, 1e-3)
+    snap = {n: getattr(st, n).get() for n in st.names}
+    out = {}
+    for mode in (PLAIN_FP64, MIXED):
+        k.set_precision(mode)
+        for n, (e, ln, sp, _) in snap.items():
+            getattr(st, n).set(e, ln, sp)
+        st.gains = [0.0, 0.0]
+        k.vortex_run(*st.args(), 1e-3, 20, st.gains)
+        out[mode] = {n: getattr(st, n).get() for n in ("psi", "chi", "nlpsi", "nlchi", "psi_p", "chi_p")}
+    k.close()
+    for n in out[MIXED]:
+        a, b = out[MIXED][n], out[PLAIN_FP64][n]
+        err = np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])
+        assert err < 1e-6, f"mixed {n} after 20 steps: {err:.3e} relative to FP64"
+        assert abs(a[1] - b[1]) <= 1e-6 * max(1.0, abs(b[1])), f"mixed {n} ln: {a[1]} vs {b[1]}"
