@@ -172,6 +172,39 @@ def run_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def ke_spectrum(kit, st_fields, dims, xw):
+    """Kinetic-energy spectrum E(m, k) of the velocity of (psi, chi), computed from the FP64 tp2vec
+    (PPP samples downloaded) with numpy FFTs in phi and z and the radial quadrature of the volume
+    integral: E(m, k) = 1/2 sum_i w_i r_i^2/(1 - x_i^2) 2 pi zlen c_m |u_hat(i, m, k)|^2, c_m = 2 for
+    0 < m < np/2.  Sum over (m, k) = the kinetic energy."""
+    from mlegs_gb300.kit import PLAIN_FP64
+    x, w, r = xw
+    nr = len(x)
+    p = kit.params
+    kit.set_precision(PLAIN_FP64)
+    psi = kit.scalar(*st_fields["psi"][:3])
+    chi = kit.scalar(*st_fields["chi"][:3])
+    v = [kit.scalar(np.zeros(dims, complex, order="F"), 0.0, "PPP") for _ in range(3)]
+    kit.tp2vec(psi, chi, *v)
+    W = w * r ** 2 / (1.0 - x ** 2) * 2.0 * np.pi * p.zlen
+    E = 0.0
+    for s in v:
+        e = s.e[:nr, : p.np // 2, :]
+        f = np.empty((nr, p.np, dims[2]))
+        f[:, 0::2, :] = e.real
+        f[:, 1::2, :] = e.imag
+        F = np.fft.fft(np.fft.rfft(f, axis=1) / p.np, axis=2) / dims[2]
+        cm = np.full(F.shape[1], 2.0)
+        cm[0] = 1.0
+        if p.np % 2 == 0:
+            cm[-1] = 1.0
+        E = E + 0.5 * np.einsum("i,imk->mk", W, np.abs(F) ** 2) * cm[:, None]
+        s.free()
+    for s in (psi, chi):
+        s.free()
+    return E
+
+
 def snapshot(st):
     return {n: getattr(st, n).get() for n in st.names}
 
@@ -234,19 +267,32 @@ def run_ours(args, rank, world, local, pg):
         ms_mixed = max_over_ranks(pg, ms_mixed)
         value = job_steps_per_s(world, args.steps, ms_mixed)
 
-        # plain FP64 over the same steps, and the error of mixed against it
+        # plain FP64 over the same steps
         k_cmp = min(args.steps, 20)
         ms_plain, _, _ = timed(PLAIN_FP64, k_cmp, 2)
         plain_sps = k_cmp / (ms_plain / 1e3)
-        errs = {}
+        # accuracy: both forms over the same accuracy_steps from the same state; per-field relative L2
+        # of mixed against FP64 at the end, and the kinetic-energy spectrum error
+        finals = {}
         for mode in (PLAIN_FP64, MIXED):
             kit.set_precision(mode)
             restore(st, snap0)
             st.gains = [0.0, 0.0]
-            kit.vortex_run(*st.args(), DT, k_cmp, st.gains)
+            kit.vortex_run(*st.args(), DT, args.accuracy_steps, st.gains)
             kit.sync()
-            errs[mode] = {n: getattr(st, n).e for n in ("psi", "chi", "nlpsi", "nlchi")}
-        err = {n: rel_l2(errs[MIXED][n], errs[PLAIN_FP64][n]) for n in errs[MIXED]}
+            finals[mode] = {n: getattr(st, n).get() for n in ("psi", "chi", "nlpsi", "nlchi")}
+        err = {n: rel_l2(finals[MIXED][n][0], finals[PLAIN_FP64][n][0]) for n in finals[MIXED]}
+        xw = (kit.kit_get("x"), kit.kit_get("w"), kit.kit_get("r"))
+        E64 = ke_spectrum(kit, finals[PLAIN_FP64], kit.dims, xw)
+        E32 = ke_spectrum(kit, finals[MIXED], kit.dims, xw)
+        big = E64 > 1e-12 * E64.max()
+        pert = np.ones_like(E64, dtype=bool)
+        pert[0, 0] = False
+        spec = {"max_rel_err": float(np.max(np.abs(E32 - E64)[big] / E64[big])),
+                "rel_l2": rel_l2(E32, E64),
+                "perturbation_max_rel_err": float(np.max(np.abs(E32 - E64)[big & pert] / E64[big & pert])),
+                "modes_compared": int(big.sum()), "floor": "E > 1e-12 max E",
+                "ke_total": float(E64.sum()), "ke_perturbation": float(E64[pert].sum())}
 
         # kernel classes timed launch by launch (CUDA events on the library's stream)
         kit.set_precision(MIXED)
@@ -314,7 +360,8 @@ def run_ours(args, rank, world, local, pg):
         "config": config_dict(),
         "fp64_plain": {"value": plain_sps, "unit": "steps/s", "steps": k_cmp,
                        "mixed_speedup": value / world / plain_sps},
-        "mixed_vs_fp64_rel_l2_after_steps": err,
+        "mixed_vs_fp64": {"steps": args.accuracy_steps, "rel_l2": err, "ke_spectrum": spec,
+                          "note": "FP64 form = the oracle to 1e-11 (GPU parity tests)"},
         "kit_init_s": t_init,
         "gpu_launches": int(launches),
         "gpu_launches_per_step": launches / args.steps,
@@ -376,6 +423,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
     args = ap.parse_args()

@@ -89,6 +89,10 @@ struct Ctx {
   long long launches = 0;     // kernels launched by the library since mlg_init
   KTimer kt;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // side stream for work that runs beside the work stream (the mixed form's m = 0 plane), forked and
+  // joined with events so that callers only ever see the work stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 extern Ctx G;
 
@@ -101,6 +105,11 @@ void dfree(void* p, size_t bytes);
 cd* get_buf();
 void put_buf(cd* b);
 int pool_reserve(int n);
+
+// side stream: fork makes it wait for everything enqueued on the work stream so far; join makes the
+// work stream wait for everything enqueued on it so far
+int side_fork();
+int side_join();
 
 // kernel timing helpers
 void kt_begin(int kind);

@@ -275,7 +275,7 @@ static int set_smem(const void* fn, size_t bytes) {
 }
 
 template <typename T>
-static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max) {
+static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max, cudaStream_t stream) {
   int L = G.nz;
   if (L <= 1 || nm <= 0) return 0;
   int TR = std::min(pick_tr(L, sizeof(typename CT<T>::t)), tr_max);
@@ -283,7 +283,7 @@ static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max) {
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), nm), blk(TR, TT);
-  k_vfft<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
+  k_vfft<T><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
   MLG_LAUNCH();
   return 0;
 }
@@ -293,10 +293,12 @@ static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max) {
 static int vfft_any(cd* e, int dir, double scale) {
   kt_begin(1);
   if (G.precision == MLG_MIXED) {
-    MLG_TRY(vfft_t<float>(e, dir, scale, 1, G.npdim - 1, 32));
-    MLG_TRY(vfft_t<double>(e, dir, scale, 0, 1, 2));
+    MLG_TRY(side_fork());
+    MLG_TRY(vfft_t<double>(e, dir, scale, 0, 1, 2, G.side));
+    MLG_TRY(vfft_t<float>(e, dir, scale, 1, G.npdim - 1, 32, G.stream));
+    MLG_TRY(side_join());
   } else {
-    MLG_TRY(vfft_t<double>(e, dir, scale, 0, G.npdim, 32));
+    MLG_TRY(vfft_t<double>(e, dir, scale, 0, G.npdim, 32, G.stream));
   }
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;

@@ -58,6 +58,17 @@ int pool_reserve(int n) {
   return 0;
 }
 
+int side_fork() {
+  MLG_CUDA(cudaEventRecord(G.ev_fork, G.stream));
+  MLG_CUDA(cudaStreamWaitEvent(G.side, G.ev_fork, 0));
+  return 0;
+}
+int side_join() {
+  MLG_CUDA(cudaEventRecord(G.ev_join, G.side));
+  MLG_CUDA(cudaStreamWaitEvent(G.stream, G.ev_join, 0));
+  return 0;
+}
+
 void kt_begin(int kind) {
   if (!G.kt.on) return;
   (void)kind;
@@ -911,6 +922,11 @@ const char* mlg_last_error(void) { return g_err.c_str(); }
 int mlg_init(const mlg_params* p) {
   if (!p) return set_error(MLG_EHANDLE, "mlg_init: null parameters");
   if (!G.ev0) { cudaEventCreate(&G.ev0); cudaEventCreate(&G.ev1); }
+  if (!G.side) {
+    MLG_CUDA(cudaStreamCreateWithFlags(&G.side, cudaStreamNonBlocking));
+    MLG_CUDA(cudaEventCreateWithFlags(&G.ev_fork, cudaEventDisableTiming));
+    MLG_CUDA(cudaEventCreateWithFlags(&G.ev_join, cudaEventDisableTiming));
+  }
   int rc = kit_build(p);
   if (rc) return rc;
   G.n_slots = 4096;
@@ -931,10 +947,11 @@ int mlg_finalize(void) {
                   G.tV32, G.tD32, G.tT32, G.tT32lo, G.tw_p, G.tw_z, G.tw_pr, G.tw_p32, G.tw_z32, G.tw_pr32, G.ln_slots, G.dscal, G.band_ws};
   for (void* a : arrs) if (a) cudaFree(a);
   cudaStream_t st = G.stream;
-  cudaEvent_t e0 = G.ev0, e1 = G.ev1;
+  cudaEvent_t e0 = G.ev0, e1 = G.ev1, ef = G.ev_fork, ej = G.ev_join;
+  cudaStream_t side = G.side;
   G = Ctx();
   G.stream = st;
-  G.ev0 = e0; G.ev1 = e1;
+  G.ev0 = e0; G.ev1 = e1; G.ev_fork = ef; G.ev_join = ej; G.side = side;
   return 0;
 }
 

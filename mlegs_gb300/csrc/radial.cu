@@ -516,21 +516,21 @@ static double fwd_flops(int nrc, int npc) {
 
 // the m = 0 plane of the mixed form in double-float: small tiles (about 190 CTAs at 192x128x128), one
 // output per thread
-static int m0_rtrans_fwd(const cd* in, cd* out, int nrc) {
+static int m0_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
   constexpr int MT = 16, ZT = 8, KC = 16;
   int nn = std::max(nrc, 0);
   if (nn == 0) return 0;
   dim3 grid(cdiv(G.nzdim, ZT), 2 * cdiv((nn + 1) / 2, MT), 1), blk(ZT, MT);
-  k_rtrans_fwd<dfl, MT, ZT, KC, 1, 1><<<grid, blk, 0, G.stream>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim,
+  k_rtrans_fwd<dfl, MT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim,
                                                                  G.npdim, G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
-static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln) {
+static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln, cudaStream_t st) {
   constexpr int IT = 16, ZT = 4, KC = 16;
   if (nrc <= 0) return 0;
   dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), 1), blk(ZT, IT);
-  k_rtrans_bwd<dfl, IT, ZT, KC, 1, 1><<<grid, blk, 0, G.stream>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
+  k_rtrans_bwd<dfl, IT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
                                                                  G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
@@ -545,8 +545,10 @@ int launch_rtrans_fwd(Scalar& s) {
   kt_begin(KT_RFWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
-      MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));   // m >= 1: tensor cores, split BF16 (tc_radial.cu)
-      MLG_TRY(m0_rtrans_fwd(s.e, out, nrc));         // m = 0: double-float
+      MLG_TRY(side_fork());
+      MLG_TRY(m0_rtrans_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
+      MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: tensor cores, split BF16 (tc_radial.cu)
+      MLG_TRY(side_join());
     } else {
       constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
       int tt = cdiv((nrc + 1) / 2, MT);
@@ -571,8 +573,10 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
-      MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));   // m >= 1: tensor cores, split BF16
-      MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln));         // m = 0: double-float
+      MLG_TRY(side_fork());
+      MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln, G.side));   // m = 0: double-float, beside
+      MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));      // m >= 1: tensor cores, split BF16
+      MLG_TRY(side_join());
     } else {
       constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
       dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
@@ -597,7 +601,13 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
   if (G.precision == MLG_MIXED) {
-    // m >= 1 in FP32 (with the u_z term in double-float), m = 0 in double-float
+    // m >= 1 in FP32 (with the u_z term in double-float), m = 0 in double-float beside it
+    MLG_TRY(side_fork());
+    constexpr int DMT = 16, DZT = 8;
+    dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
+    k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
+                                                               G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+    MLG_LAUNCH();
     constexpr int MMT = 32, MMPT = 2;
     int mtt = cdiv((nrc + 1) / 2, MMT);
     if (npc > 1) {
@@ -607,10 +617,9 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
                                                                            G.npdim, G.nzdim, nrc, nzc, nzcu, 1);
       MLG_LAUNCH();
     }
-    constexpr int DMT = 16, DZT = 8;
-    dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
-    k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
-                                                                 G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+    MLG_TRY(side_join());
+    kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
+    return 0;
   } else
     k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
                                                                    G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
