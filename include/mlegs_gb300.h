@@ -177,7 +177,9 @@ int mlg_vortex_run(mlg_scalar psi, mlg_scalar chi, mlg_scalar nlpsi, mlg_scalar 
  * (psi0, chi0) [psi <- psi0, nl <- advection_rhs, nl_p <- nl, then mlg_vortex_step nsteps times],
  * u' the velocity without the (m = 0, k = 0) column and ln, W the volume quadrature weights
  * w_i r_i^2/(1-x_i^2) (2 pi/np)(zlen/nz).  The forward state is kept every k_ckpt steps and each
- * segment recomputed on the way back.  grad_psi/grad_chi NULL: J only.  psi0, chi0 unchanged. */
+ * segment recomputed on the way back.  The gradient is with respect to the active coefficients (those
+ * that chop and dealias keep, which is where the step keeps its state); it is zero elsewhere.
+ * grad_psi/grad_chi NULL: J only.  psi0, chi0 unchanged. */
 int mlg_adjoint_run(mlg_scalar psi0, mlg_scalar chi0, mlg_scalar uz, double dt, int nsteps, int k_ckpt,
                     mlg_scalar grad_psi, mlg_scalar grad_chi, double* J);
 /* One step: state = (psi, chi, nlpsi, nlchi, nlpsi_p, nlchi_p) at the step's start (unchanged);

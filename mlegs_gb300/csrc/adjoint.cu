@@ -700,7 +700,11 @@ static int startup(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, Sc
 }
 
 // J and, if seeds are given, (psi_bar, chi_bar) = dJ/d(psi, chi)
+// J and its gradient run in FP64 in every form: the volume weights grow like r^2 toward the outer
+// collocation points (about 3e5 at 128 points), and the transposed transforms sum them against the
+// oscillating top-degree functions with cancellation that FP32 does not resolve.
 static int energy(const Scalar& psi, const Scalar& chi, double* J, Scalar* psib, Scalar* chib) {
+  PrecisionScope fp64(MLG_PLAIN_FP64);
   TMP(p); TMP(c);
   MLG_TRY(assign(p, psi)); MLG_TRY(assign(c, chi));
   k_drop_mean<<<1, 256, 0, G.stream>>>(p.e, p.ln, G.nrdim); MLG_LAUNCH();
@@ -749,6 +753,21 @@ static int copy_state(Scalar* const d[6], Scalar* const s[6]) {
 }
 
 // the gradient of J(T) w.r.t. (psi0, chi0) through nsteps steps, the state kept every k_ckpt steps
+// The state of the step sequence lives in the active subspace: psi and chi are chopped and dealiased
+// at every step boundary (the step ends with dealias, and the start-up's advection_rhs dealiases
+// psi0, chi0 in place), nl and nl_p are chopped and dealiased by advection_rhs, and no operator of
+// the step writes outside it.  The chopped coefficients are not degrees of freedom, but the step
+// does read three of them per column (the vector reconstruction runs with a chop offset of 3), and
+// with SVV off their influence grows by orders of magnitude per step.  The gradient is therefore
+// the one of J restricted to the active subspace: the adjoint state is projected onto it (chop,
+// dealias) at every step boundary, which is the exact transpose of the step restricted to that
+// invariant subspace.
+static int project_active(Scalar& s) {
+  set_fff0(s);
+  MLG_TRY(op_chop(s));
+  return op_dealias(s);
+}
+
 int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, double dt, int nsteps, int k_ckpt, Scalar* gpsi,
                 Scalar* gchi, double* J) {
   MLG_TRY(adjoint_supported());
@@ -783,6 +802,7 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
   if (ad.rc) { cleanup(); return ad.rc; }
   rc = energy(*cur.p[0], *cur.p[1], J, ad.p[0], ad.p[1]);
   for (int i = 2; i < 6 && !rc; ++i) { rc = launch_zero(ad.p[i]->e); if (!rc) rc = launch_set_ln(ad.p[i]->ln, 0.0); set_fff0(*ad.p[i]); }
+  for (int i = 0; i < 2 && !rc; ++i) rc = project_active(*ad.p[i]);
   // backward sweep, segment by segment: recompute the end-of-step states, then step back
   std::vector<State*> seg;
   for (int c = (int)ck.size() - 1; c >= 0 && !rc; --c) {
@@ -799,7 +819,10 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
       rc = forward_step(cur.p, uzb, dt);
       if (!rc) rc = copy_state(seg[q]->p, cur.p);
     }
-    for (int q = len - 1; q >= 0 && !rc; --q) rc = step_T(seg[q]->p, uzb, dt, ad.p);
+    for (int q = len - 1; q >= 0 && !rc; --q) {
+      rc = step_T(seg[q]->p, uzb, dt, ad.p);
+      for (int i = 0; i < 6 && !rc; ++i) rc = project_active(*ad.p[i]);
+    }
   }
   for (State* t : seg) delete t;
   if (!rc) {
@@ -810,10 +833,11 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
     if (!rc) rc = advection_T(psi0, chi0, uzb, *ad.p[2], *ad.p[3], nb, cb2);
     if (!rc) rc = lincomb(*gpsi, {{ad.p[0], 1.0}, {&nb, 1.0}}, {{ad.p[0], 1.0}, {&nb, 1.0}});
     if (!rc) rc = lincomb(*gchi, {{ad.p[1], 1.0}, {&cb2, 1.0}}, {{ad.p[1], 1.0}, {&cb2, 1.0}});
-    // the startup's psi <- psi0 passes through advection_rhs's in-place dealias
-    if (!rc) rc = op_dealias(*gpsi);
-    if (!rc) rc = op_dealias(*gchi);
+    // the startup's psi <- psi0 passes through advection_rhs's in-place dealias; the gradient is
+    // the one with respect to the active coefficients
     set_fff0(*gpsi); set_fff0(*gchi);
+    if (!rc) rc = project_active(*gpsi);
+    if (!rc) rc = project_active(*gchi);
   }
   cleanup();
   return rc;
