@@ -159,6 +159,8 @@ struct SolveArgs {
   int skip_root;        // substitution: leave the (0,0) column to the bordered solve
   int transpose;        // factor / solve A^T (kinds 0 and 1): the adjoint's systems
   int no_ln;            // substitution: skip the log-term handling of the (0,0) column
+  double2* e2 = nullptr;  // substitution: a second field with the same matrices (paired solve), or null
+  double* lnp2 = nullptr;
 };
 
 // entry (i, j) (0-based) of D(m,k) = D0(m) - ak^2 I for an n x n truncation
@@ -501,23 +503,38 @@ __device__ __forceinline__ void cpa16(void* sdst, const void* gsrc, bool pred) {
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// forward and back substitution with the cached factors (gbtrs 'N', NRHS = 1), in place on the
-// column.  One warp = 32 systems; factor rows and right-hand-side values are staged into shared
+// forward and back substitution with the cached factors (gbtrs 'N', one or two right-hand sides), in
+// place on the column.  One warp = 32 systems; factor rows and right-hand-side values are staged into shared
 // memory SST groups ahead of use by cp.async, so DRAM latency overlaps the recurrences.
 constexpr int SGR = 8, SST = 3, SNU = FKL + FKU;
+template <int NR>
 struct SubstSmem {
   double f[SST][SGR][SNU + 1][64];   // fwd: l1, l2, pivot; bwd: 1/U(j,j), U(j,j+1..j+4)
-  double v[SST][SGR][64];            // fwd: entering right-hand side; bwd: y(j)
+  double v[NR][SST][SGR][64];        // fwd: entering right-hand side; bwd: y(j)
 };
+
+// ihelm's pre-solve log-term handling of one field (:818-824): so%ln = s%ln/alpha, the log terms on
+// e(1..3, 1, 1)
+__device__ __forceinline__ void subst_root_pre(const SolveArgs& a, double2* g, double* lnp) {
+  double e2 = a.ell * a.ell;
+  double lno = *lnp / a.alpha;
+  *lnp = lno;
+  g[0].x -= 4.0 / 3.0 / e2 / exp(a.lognorm[0]) * lno;
+  g[1].x += 2.0 / 1.0 / e2 / exp(a.lognorm[1]) * lno;
+  g[2].x -= 2.0 / 3.0 / e2 / exp(a.lognorm[2]) * lno;
+}
 
 // The matrices are real, so the real and imaginary parts of a right-hand side are two independent
 // real systems with the same factors: block = 64 threads, threads 0-31 take the real parts of 32
 // consecutive systems and threads 32-63 the imaginary parts (twice the warps in flight for the
-// serial recurrences).  Only the real-part thread of system (0,0) touches ln and the log terms,
+// serial recurrences).  NR = 2 solves two fields with the same matrices (the psi and chi solves of
+// a vortex step) in one pass: the factors are staged once for both and every thread runs two
+// independent recurrences.  Only the real-part thread of system (0,0) touches ln and the log terms,
 // which all act on real parts.
+template <int NR>
 __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __restrict__ fac) {
   extern __shared__ __align__(16) unsigned char subst_smem[];
-  SubstSmem& sm = *reinterpret_cast<SubstSmem*>(subst_smem);
+  SubstSmem<NR>& sm = *reinterpret_cast<SubstSmem<NR>*>(subst_smem);
   int th = threadIdx.x;
   int comp = th >> 5;
   int sys = blockIdx.x * 32 + (th & 31);
@@ -527,17 +544,17 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
   int nn = max(min(a.nrc, a.nrc - m), 0);
   bool root = valid && (m == 0 && k == 0);
   if (root && a.skip_root) cnt = 0;
-  if (root && comp == 0 && a.kind == 0 && !a.skip_root && !a.no_ln) {   // ihelm: so%ln = s%ln/alpha, log terms (:818-824)
-    double e2 = a.ell * a.ell;
-    double lno = *a.lnp / a.alpha;
-    *a.lnp = lno;
-    double2* g = a.e;
-    g[0].x -= 4.0 / 3.0 / e2 / exp(a.lognorm[0]) * lno;
-    g[1].x += 2.0 / 1.0 / e2 / exp(a.lognorm[1]) * lno;
-    g[2].x -= 2.0 / 3.0 / e2 / exp(a.lognorm[2]) * lno;
+  double2* ev[2] = {a.e, a.e2};
+  double* lv[2] = {a.lnp, a.lnp2};
+  if (root && comp == 0 && a.kind == 0 && !a.skip_root && !a.no_ln) {
+#pragma unroll
+    for (int q = 0; q < NR; ++q) subst_root_pre(a, ev[q], lv[q]);
   }
   if (!valid || m >= a.npc || nn < 1) cnt = 0;
-  double* x = reinterpret_cast<double*>(a.e + (size_t)a.nrdim * (m + (size_t)a.npdim * k)) + comp;  // stride 2
+  double* x[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q)
+    x[q] = reinterpret_cast<double*>(ev[q] + (size_t)a.nrdim * (m + (size_t)a.npdim * k)) + comp;  // stride 2
   const size_t ns = a.nsys;
   int nnw = (cnt > 0) ? nn : 0;
   for (int o = 16; o; o >>= 1) nnw = max(nnw, __shfl_xor_sync(0xffffffffu, nnw, o));
@@ -558,12 +575,15 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
         for (int t = 0; t <= FKL; ++t) cpa8(&sm.f[st][u][t][th], ok ? f + t * ns : dummy, ok);
         int jn = jr + 1 + FKL;
         bool okx = act && jn < nn;
-        cpa8(&sm.v[st][u][th], okx ? (const void*)(x + 2 * jn) : (const void*)dummy, okx);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) cpa8(&sm.v[q][st][u][th], okx ? (const void*)(x[q] + 2 * jn) : (const void*)dummy, okx);
       }
     };
-    double r[FKL + 1];
+    double r[NR][FKL + 1];
 #pragma unroll
-    for (int t = 0; t <= FKL; ++t) r[t] = (act && t < nn) ? x[2 * t] : 0.0;
+    for (int q = 0; q < NR; ++q)
+#pragma unroll
+      for (int t = 0; t <= FKL; ++t) r[q][t] = (act && t < nn) ? x[q][2 * t] : 0.0;
     for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_f(g); cpa_commit(); }
     for (int g = 0; g < ng; ++g) {
       if (g + SST - 1 < ng) issue_f(g + SST - 1);
@@ -577,13 +597,23 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
         double pv = sm.f[st][u][FKL][th];
 #pragma unroll
         for (int t = 1; t <= FKL; ++t)
-          if (pv == (double)t) { double q = r[0]; r[0] = r[t]; r[t] = q; }
+          if (pv == (double)t) {
 #pragma unroll
-        for (int t = 1; t <= FKL; ++t) r[t] -= sm.f[st][u][t - 1][th] * r[0];
-        x[2 * jr] = r[0];
+            for (int q = 0; q < NR; ++q) { double w = r[q][0]; r[q][0] = r[q][t]; r[q][t] = w; }
+          }
 #pragma unroll
-        for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
-        r[FKL] = sm.v[st][u][th];
+        for (int t = 1; t <= FKL; ++t) {
+          double l = sm.f[st][u][t - 1][th];
+#pragma unroll
+          for (int q = 0; q < NR; ++q) r[q][t] -= l * r[q][0];
+        }
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+          x[q][2 * jr] = r[q][0];
+#pragma unroll
+          for (int t = 0; t < FKL; ++t) r[q][t] = r[q][t + 1];
+          r[q][FKL] = sm.v[q][st][u][th];
+        }
       }
     }
     cpa_wait<0>();
@@ -597,12 +627,15 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
         const double* f = fac + (size_t)max(jr, 0) * FSL * ns + sys;
 #pragma unroll
         for (int c = 0; c <= SNU; ++c) cpa8(&sm.f[st][u][c][th], ok ? f + (FKL + 1 + c) * ns : dummy, ok);
-        cpa8(&sm.v[st][u][th], ok ? (const void*)(x + 2 * jr) : (const void*)dummy, ok);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) cpa8(&sm.v[q][st][u][th], ok ? (const void*)(x[q] + 2 * jr) : (const void*)dummy, ok);
       }
     };
-    double xs[SNU];
+    double xs[NR][SNU];
 #pragma unroll
-    for (int c = 0; c < SNU; ++c) xs[c] = 0.0;
+    for (int q = 0; q < NR; ++q)
+#pragma unroll
+      for (int c = 0; c < SNU; ++c) xs[q][c] = 0.0;
     for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_b(g); cpa_commit(); }
     for (int g = 0; g < ng; ++g) {
       if (g + SST - 1 < ng) issue_b(g + SST - 1);
@@ -613,20 +646,28 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
       for (int u = 0; u < SGR; ++u) {
         int jr = nn - 1 - (g * SGR + u);
         if (!act || jr < 0) break;
-        // y - U(j,j+1..j+4) . x(j+1..j+4), summed as a tree to shorten the dependency chain
-        double p1 = sm.f[st][u][1][th] * xs[0] + sm.f[st][u][2][th] * xs[1];
-        double p2 = sm.f[st][u][3][th] * xs[2] + sm.f[st][u][4][th] * xs[3];
-        double xj = (sm.v[st][u][th] - (p1 + p2)) * sm.f[st][u][0][th];
-        x[2 * jr] = xj;
+        double f0 = sm.f[st][u][0][th], f1 = sm.f[st][u][1][th], f2 = sm.f[st][u][2][th];
+        double f3 = sm.f[st][u][3][th], f4 = sm.f[st][u][4][th];
 #pragma unroll
-        for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
-        xs[0] = xj;
+        for (int q = 0; q < NR; ++q) {
+          // y - U(j,j+1..j+4) . x(j+1..j+4), summed as a tree to shorten the dependency chain
+          double p1 = f1 * xs[q][0] + f2 * xs[q][1];
+          double p2 = f3 * xs[q][2] + f4 * xs[q][3];
+          double xj = (sm.v[q][st][u][th] - (p1 + p2)) * f0;
+          x[q][2 * jr] = xj;
+#pragma unroll
+          for (int c = SNU - 1; c >= 1; --c) xs[q][c] = xs[q][c - 1];
+          xs[q][0] = xj;
+        }
       }
     }
     cpa_wait<0>();
     __threadfence_block();
   }
-  if (root && comp == 0 && a.kind == 1 && !a.skip_root && !a.no_ln && cnt > 0) *a.lnp = x[0] * exp(a.lognorm[0]);
+  if (root && comp == 0 && a.kind == 1 && !a.skip_root && !a.no_ln && cnt > 0) {
+#pragma unroll
+    for (int q = 0; q < NR; ++q) *lv[q] = x[q][0] * exp(a.lognorm[0]);
+  }
 }
 
 // the bordered (0,0) system of idel2_preln (KL = 3), single thread, after the batch
@@ -842,9 +883,9 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
       MLG_LAUNCH();
       return 0;
     }));
-    size_t smb = sizeof(SubstSmem);
-    MLG_CUDA(cudaFuncSetAttribute(k_band_subst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-    k_band_subst<<<cdiv(nsys, 32), 64, smb, G.stream>>>(b, fac);
+    size_t smb = sizeof(SubstSmem<1>);
+    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    k_band_subst<1><<<cdiv(nsys, 32), 64, smb, G.stream>>>(b, fac);
     MLG_LAUNCH();
     if (kind == 2) {
       k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
@@ -856,6 +897,34 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
 }
 
 // ------------------------------------------------------------------------------------------------
+// ihelm of two fields with the same chop window and alpha in one substitution pass (the psi and chi
+// solves of a vortex step): the factors are read once for both.  Results are those of two ihelm calls.
+int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  int npc = std::max(c.npc, 1);
+  size_t nsys = (size_t)npc * G.nzdim;
+  SolveArgs a;
+  a.e = s1.e; a.ws = G.band_ws; a.lnp = s1.ln; a.bd2 = G.bd2; a.ak = G.ak; a.lognorm = G.lognorm;
+  a.status = (int*)(G.dscal + DS_FLAG + 1);
+  a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
+  a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = 0.0; a.ell = G.ell; a.preln = 0.0;
+  a.kind = 0; a.power = 0; a.skip_root = 0; a.transpose = 0; a.no_ln = 0;
+  a.e2 = s2.e; a.lnp2 = s2.ln;
+  kt_begin(2);
+  double* fac = nullptr;
+  MLG_TRY(lu_cache_get(0, alpha, c, nsys, &fac, [&](double* buf) -> int {
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    MLG_LAUNCH();
+    return 0;
+  }));
+  size_t smb = sizeof(SubstSmem<2>);
+  MLG_CUDA(cudaFuncSetAttribute(k_band_subst<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+  k_band_subst<2><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
+  MLG_LAUNCH();
+  kt_end(2, 4.0 * G.fsize * 16);
+  return 0;
+}
+
 // transposes for the adjoint (FP64 in both forms)
 
 // k_band_apply^T: x <- B^T x per active column (cnt times, as the forward), rows >= nn and inactive
@@ -941,9 +1010,9 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
     MLG_LAUNCH();
     return 0;
   }));
-  size_t smb = sizeof(SubstSmem);
-  MLG_CUDA(cudaFuncSetAttribute(k_band_subst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-  k_band_subst<<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
+  size_t smb = sizeof(SubstSmem<1>);
+  MLG_CUDA(cudaFuncSetAttribute(k_band_subst<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+  k_band_subst<1><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
   MLG_LAUNCH();
   kt_end(2, 2.0 * G.fsize * 16);
   return 0;

@@ -4,6 +4,7 @@
 // field arithmetic runs in the kernels of this file, fft.cu, radial.cu and banded.cu.  The log-term
 // coefficient ln of every field lives in device memory, so no step needs a host round trip.
 #include "common.cuh"
+#include <tuple>
 #include <cmath>
 #include <mutex>
 #include <algorithm>
@@ -757,6 +758,47 @@ int op_abcn(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, double dt) {
   return 0;
 }
 
+// abcn of the two fields of a vortex step, (psi, psi_p, nlpsi, nlpsi_p) and (chi, ...): the same
+// operations as two abcn calls, with the two Helmholtz solves (same alpha, same chop window) done in
+// one substitution pass
+static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar& t, Scalar& t_p, Scalar& ml,
+                        Scalar& ml_p, double dt) {
+  if (G.P.hyperpow != 0) {
+    MLG_TRY(op_abcn(s, s_p, nl, nl_p, dt));
+    return op_abcn(t, t_p, ml, ml_p, dt);
+  }
+  if (!fff4(s, nl) || !fff4(s_p, nl_p) || !fff4(t, ml) || !fff4(t_p, ml_p))
+    return set_error(MLG_ESPACE, "fefe: all input scalars must be in FFF for time stepping");
+  if (G.P.visc < 5.0e-14)
+    return set_error(MLG_EINVISCID, "abcn: inviscid case and no linear term in rhs. semi-implicit time adv is impossible");
+  double a = -2.0 / (dt * G.P.visc);
+  if (std::fabs(a) < 5.0e-14) return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
+  for (auto q : {std::make_tuple(&s, &nl, &nl_p), std::make_tuple(&t, &ml, &ml_p)}) {
+    Scalar& x = *std::get<0>(q);
+    Scalar& n = *std::get<1>(q);
+    Scalar& np_ = *std::get<2>(q);
+    TMP(svis);
+    MLG_TRY(assign(svis, x));
+    MLG_TRY(lterm(svis));
+    MLG_TRY(lincomb(x, {{&x, 1.0}, {&n, 1.5 * dt}, {&np_, -.5 * dt}, {&svis, dt / 2.0}},
+                    {{&x, 1.0}, {&n, 1.5 * dt}, {&np_, -.5 * dt}, {&svis, dt / 2.0}}, a));
+  }
+  ChopIdx c1, c2;
+  MLG_TRY(chop_index(s, c1));
+  MLG_TRY(chop_index(t, c2));
+  if (c1.nrc == c2.nrc && c1.npc == c2.npc && c1.nzc == c2.nzc && c1.nzcu == c2.nzcu) {
+    MLG_TRY(launch_ihelm_pair(s, t, c1, a));
+  } else {
+    MLG_TRY(launch_band_solve(s, 0, c1, a, 0.0, 0.0, 0));
+    MLG_TRY(launch_band_solve(t, 0, c2, a, 0.0, 0.0, 0));
+  }
+  MLG_TRY(assign(s_p, s));
+  MLG_TRY(assign(nl_p, nl));
+  MLG_TRY(assign(t_p, t));
+  MLG_TRY(assign(ml_p, ml));
+  return 0;
+}
+
 // ------------------------------------------------------------------------------------------------
 // vector fields (:1264-1560)
 int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
@@ -887,8 +929,7 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
                        Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev) {
   for (Scalar* q : {&psi, &chi, &nlpsi, &nlchi, &psip, &chip, &nlpsip, &nlchip}) MLG_TRY(op_trans(*q, "FFF"));
-  MLG_TRY(op_abcn(psi, psip, nlpsi, nlpsip, dt));
-  MLG_TRY(op_abcn(chi, chip, nlchi, nlchip, dt));
+  MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt));
   MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
   MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
   MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));

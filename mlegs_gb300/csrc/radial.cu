@@ -274,11 +274,11 @@ __global__ void __launch_bounds__(MT * (ZT / ZPT))
 k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
          double2* __restrict__ psi, double2* __restrict__ chi, const typename TabT<T>::t* __restrict__ tV,
          const typename TabT<T>::t* __restrict__ tD, const typename TabT<T>::t* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
-         int nzdim, int nrc, int nzc, int nzcu) {
+         int nzdim, int nrc, int nzc, int nzcu, int m0) {
   typedef typename V2<T>::t C;
   __shared__ T Av[KC][MT + 1], Ad[KC][MT + 1], At[KC][MT + 1];
   __shared__ C Brs[KC][ZT], Bro[KC][ZT], Bps[KC][ZT], Bpo[KC][ZT], Bzs[KC][ZT];
-  int m = blockIdx.z;
+  int m = blockIdx.z + m0;
   int par = blockIdx.y & 1;
   int t0 = (blockIdx.y >> 1) * MT;
   int nn = max(min(nrc, nrc - m), 0);
@@ -606,7 +606,7 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
     constexpr int DMT = 16, DZT = 8;
     dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
     k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
-                                                               G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+                                                               G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
     MLG_LAUNCH();
     constexpr int MMT = 32, MMPT = 2;
     int mtt = cdiv((nrc + 1) / 2, MMT);
@@ -622,7 +622,7 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
     return 0;
   } else
     k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
-                                                                   G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
+                                                                   G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
   MLG_LAUNCH();
   kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
   return 0;
