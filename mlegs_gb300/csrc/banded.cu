@@ -116,6 +116,134 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
   }
 }
 
+// The right-hand side of abcn (mlegs_scalar_ops.f90:1200-1262) with hyperpow = 0, fused:
+//   svis = s; svis = del2(svis) (band rows, with the log terms of (0,0)); svis = visc*svis;
+//   s = a*(s + 1.5 dt nl - 0.5 dt nl_p + dt/2 svis)   (e and ln; svis%ln = 0 after del2)
+// One CTA per (m, k) column of the whole array, the same operations and order as the copy, band
+// apply, scale and four-term combination it replaces.  The mixed form runs the m >= 1 stencils in FP32.
+template <typename T>
+__global__ void k_abcn_rhs(double2* __restrict__ e, const double2* __restrict__ nl, const double2* __restrict__ nlp,
+                           double* __restrict__ lnp, const double* __restrict__ lnnl, const double* __restrict__ lnnlp,
+                           const double* __restrict__ bd2, const double* __restrict__ ak, const double* __restrict__ lognorm,
+                           int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell,
+                           double visc, double c1, double c2, double c3, double post) {
+  extern __shared__ __align__(16) unsigned char rhs_smem[];
+  double2* sv = (double2*)rhs_smem;               // svis of the column (FP64)
+  int m = blockIdx.y, k = blockIdx.x;
+  int nn = max(min(nrc, nrc - m), 0);
+  int cnt = k_count(k, nzc, nzcu, nzdim);
+  size_t off = (size_t)nrdim * (m + (size_t)npdim * k);
+  double2* g = e + off;
+  bool lnblk = (m == 0 && k == 0);
+  double lnin = lnblk ? *lnp : 0.0;
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) sv[i] = g[i];
+  __syncthreads();
+  if (m < npc && nn > 0 && cnt > 0) {
+    if (m == 0) {
+      double2* c0 = sv;
+      double2* c1b = sv + nrdim;
+      double akv2 = ak[k] * ak[k];
+      for (int rep = 0; rep < cnt; ++rep) {
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          double2 acc; acc.x = 0; acc.y = 0;
+          const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            int j = i - 2 + c;
+            if (j < 0 || j >= nn) continue;
+            double v = b[c];
+            if (c == 2) v = v - akv2;
+            acc.x += v * c0[j].x;
+            acc.y += v * c0[j].y;
+          }
+          c1b[i] = acc;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
+        __syncthreads();
+      }
+    } else {
+      typedef typename BC<T>::C C;
+      C* c0 = (C*)(sv + 2 * nrdim);
+      C* c1b = c0 + nrdim;
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(sv + i);
+      __syncthreads();
+      T akv2 = BC<T>::cv(ak[k] * ak[k]);
+      for (int rep = 0; rep < cnt; ++rep) {
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          C acc; acc.x = 0; acc.y = 0;
+          const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            int j = i - 2 + c;
+            if (j < 0 || j >= nn) continue;
+            T v = BC<T>::cv(b[c]);
+            if (c == 2) v = v - akv2;
+            acc.x += v * c0[j].x;
+            acc.y += v * c0[j].y;
+          }
+          c1b[i] = acc;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
+        __syncthreads();
+      }
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(sv + i, c0[i]);
+    }
+    __syncthreads();
+  }
+  if (lnblk && threadIdx.x == 0) {   // the log terms of del2 (:561-566) on svis(1..3, 1, 1)
+    double e2 = ell * ell;
+    sv[0].x += 4.0 / 3.0 / e2 / exp(lognorm[0]) * lnin;
+    sv[1].x -= 2.0 / 1.0 / e2 / exp(lognorm[1]) * lnin;
+    sv[2].x += 2.0 / 3.0 / e2 / exp(lognorm[2]) * lnin;
+  }
+  __syncthreads();
+  const double2* n0 = nl + off;
+  const double2* n1 = nlp + off;
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
+    double2 x = g[i], a1 = n0[i], a2 = n1[i], s3 = sv[i];
+    s3 = make_double2(0.0 + visc * s3.x, 0.0 + visc * s3.y);   // svis = visc*svis
+    double2 acc = make_double2(0, 0);
+    acc.x += 1.0 * x.x; acc.y += 1.0 * x.y;
+    acc.x += c1 * a1.x; acc.y += c1 * a1.y;
+    acc.x += c2 * a2.x; acc.y += c2 * a2.y;
+    acc.x += c3 * s3.x; acc.y += c3 * s3.y;
+    g[i] = make_double2(post * acc.x, post * acc.y);
+  }
+  if (lnblk && threadIdx.x == 0) {
+    double l = 0.0;
+    l += 1.0 * lnin;
+    l += c1 * *lnnl;
+    l += c2 * *lnnlp;
+    l += c3 * 0.0;
+    *lnp = post * l;
+  }
+}
+
+int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, double a) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  dim3 grid(G.nzdim, G.npdim);
+  size_t sm = 2ull * G.nrdim * sizeof(double2) + 2ull * G.nrdim * sizeof(double2);
+  kt_begin(2);
+  if (G.precision == MLG_MIXED) {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_abcn_rhs<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_abcn_rhs<float><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, G.bd2, G.ak, G.lognorm, G.nrdim,
+                                                   G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell, G.P.visc,
+                                                   1.5 * dt, -.5 * dt, dt / 2.0, a);
+  } else {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_abcn_rhs<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_abcn_rhs<double><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, G.bd2, G.ak, G.lognorm, G.nrdim,
+                                                    G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell, G.P.visc,
+                                                    1.5 * dt, -.5 * dt, dt / 2.0, a);
+  }
+  MLG_LAUNCH();
+  kt_end(2, 5.0 * G.fsize * 16);
+  return 0;
+}
+
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   dim3 grid(G.nzdim, std::max(c.npc, 1));

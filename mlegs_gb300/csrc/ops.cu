@@ -4,7 +4,6 @@
 // field arithmetic runs in the kernels of this file, fft.cu, radial.cu and banded.cu.  The log-term
 // coefficient ln of every field lives in device memory, so no step needs a host round trip.
 #include "common.cuh"
-#include <tuple>
 #include <cmath>
 #include <mutex>
 #include <algorithm>
@@ -773,16 +772,8 @@ static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar
     return set_error(MLG_EINVISCID, "abcn: inviscid case and no linear term in rhs. semi-implicit time adv is impossible");
   double a = -2.0 / (dt * G.P.visc);
   if (std::fabs(a) < 5.0e-14) return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
-  for (auto q : {std::make_tuple(&s, &nl, &nl_p), std::make_tuple(&t, &ml, &ml_p)}) {
-    Scalar& x = *std::get<0>(q);
-    Scalar& n = *std::get<1>(q);
-    Scalar& np_ = *std::get<2>(q);
-    TMP(svis);
-    MLG_TRY(assign(svis, x));
-    MLG_TRY(lterm(svis));
-    MLG_TRY(lincomb(x, {{&x, 1.0}, {&n, 1.5 * dt}, {&np_, -.5 * dt}, {&svis, dt / 2.0}},
-                    {{&x, 1.0}, {&n, 1.5 * dt}, {&np_, -.5 * dt}, {&svis, dt / 2.0}}, a));
-  }
+  MLG_TRY(launch_abcn_rhs(s, nl, nl_p, dt, a));
+  MLG_TRY(launch_abcn_rhs(t, ml, ml_p, dt, a));
   ChopIdx c1, c2;
   MLG_TRY(chop_index(s, c1));
   MLG_TRY(chop_index(t, c2));
