@@ -257,6 +257,243 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Power-of-two lengths 16..256: two passes through registers.  L = R1 * R2, n = n2 + R2 n1,
+// k = k1 + R1 k2:  X_k = sum_n2 w_L^(n2 k1) [sum_n1 x_n w_R1^(n1 k1)] w_R2^(n2 k2).
+// A CTA holds TRL lines (consecutive r: every global access is a run of TRL*16 bytes) and R2 threads
+// per line; pass 1: each thread loads R1 points of its line and does the R1-point DFT in registers,
+// multiplies by w_L^(n2 k1) and stores to shared memory [k1][n2][line]; pass 2: each thread does
+// R1/R2 DFTs of R2 points and writes the results.  Every element is read and written once in HBM and
+// once in shared memory, with compile-time index arithmetic.
+
+// cos and sin of 2 pi j / 16 (j mod 16)
+__host__ __device__ constexpr double cos16(int j) {
+  return (j & 15) == 0 ? 1.0 : (j & 15) == 1 ? 0.92387953251128675613 : (j & 15) == 2 ? 0.70710678118654752440
+       : (j & 15) == 3 ? 0.38268343236508977173 : (j & 15) == 4 ? 0.0 : (j & 15) == 5 ? -0.38268343236508977173
+       : (j & 15) == 6 ? -0.70710678118654752440 : (j & 15) == 7 ? -0.92387953251128675613 : (j & 15) == 8 ? -1.0
+       : (j & 15) == 9 ? -0.92387953251128675613 : (j & 15) == 10 ? -0.70710678118654752440
+       : (j & 15) == 11 ? -0.38268343236508977173 : (j & 15) == 12 ? 0.0 : (j & 15) == 13 ? 0.38268343236508977173
+       : (j & 15) == 14 ? 0.70710678118654752440 : 0.92387953251128675613;
+}
+__host__ __device__ constexpr double sin16(int j) { return cos16(j - 4); }
+
+// v * exp(SGN 2 pi i j / 16)
+template <typename T, int SGN>
+__device__ __forceinline__ typename CT<T>::t tw16(typename CT<T>::t v, int j) {
+  typedef typename CT<T>::t C;
+  j &= 15;
+  if (j == 0) return v;
+  if (j == 8) { C r; r.x = -v.x; r.y = -v.y; return r; }
+  if (j == 4) return c_muli(v, SGN);
+  if (j == 12) return c_muli(v, -SGN);
+  C w; w.x = (T)cos16(j); w.y = (T)(SGN * sin16(j));
+  return c_mul(v, w);
+}
+
+__host__ __device__ constexpr int bitrev(int i, int n) {   // bit reversal of i in log2(n) bits
+  int r = 0;
+  for (int b = 1; b < n; b <<= 1) { r = (r << 1) | (i & 1); i >>= 1; }
+  return r;
+}
+
+// in-register DFT of N <= 16 points, sign SGN: radix-2 decimation in frequency, fully unrolled, so
+// every register index is a compile-time constant; the result comes out in bit-reversed order,
+// a[i] = X_bitrev(i), and the callers fold the reversal into their memory addresses
+template <typename T, int N, int SGN>
+__device__ __forceinline__ void dft_reg(typename CT<T>::t* a) {
+  typedef typename CT<T>::t C;
+#pragma unroll
+  for (int len = N; len >= 2; len >>= 1) {
+#pragma unroll
+    for (int i = 0; i < N; i += len) {
+#pragma unroll
+      for (int k = 0; k < len / 2; ++k) {
+        C u = a[i + k], v = a[i + k + len / 2];
+        a[i + k] = c_add(u, v);
+        a[i + k + len / 2] = tw16<T, SGN>(c_sub(u, v), k * (16 / len));
+      }
+    }
+  }
+}
+
+template <int L> struct Split;            // L = R1 * R2, R1 >= R2, R1 <= 16
+template <> struct Split<16> { static constexpr int R1 = 4, R2 = 4; };
+template <> struct Split<32> { static constexpr int R1 = 8, R2 = 4; };
+template <> struct Split<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct Split<128> { static constexpr int R1 = 16, R2 = 8; };
+template <> struct Split<256> { static constexpr int R1 = 16, R2 = 16; };
+
+// the two passes on a CTA's lines; a[] holds the R1 inputs of this thread (n1 order); on return
+// b[q][i] holds X_(k1 + R1 bitrev(i)) for k1 = w*(R1/R2) + q
+template <typename T, int L, int SGN, int TRL>
+__device__ __forceinline__ void fft2pass(typename CT<T>::t* a, typename CT<T>::t (*b)[Split<L>::R2],
+                                         typename CT<T>::t* S, const typename TW<T>::t* __restrict__ tw, int w,
+                                         int lane) {
+  constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
+  dft_reg<T, R1, SGN>(a);
+#pragma unroll
+  for (int i = 0; i < R1; ++i) {
+    const int k1 = bitrev(i, R1);
+    typename CT<T>::t v = a[i];
+    if (k1) v = c_mul(v, load_tw<T>(tw, (w * k1) & (L - 1), SGN));
+    S[(k1 * R2 + w) * TRL + lane] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    int k1 = w * Q + q;
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) b[q][n2] = S[(k1 * R2 + n2) * TRL + lane];
+    dft_reg<T, R2, SGN>(b[q]);
+  }
+}
+
+// z FFT: lines (r, m) for m = m0 + blockIdx.y, points at stride nrdim*npdim
+template <typename T, int L, int SGN, int TRL>
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restrict__ e, int nrdim, int npdim,
+                                                              const typename TW<T>::t* __restrict__ tw, T scale, int m0) {
+  typedef typename CT<T>::t C;
+  constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = (C*)smem_raw;
+  int lane = threadIdx.x, w = threadIdx.y;
+  int r = blockIdx.x * TRL + lane;
+  int m = blockIdx.y + m0;
+  bool ok = r < nrdim;
+  size_t ps = (size_t)nrdim * npdim;
+  double2* base = e + r + (size_t)nrdim * m;
+  C a[R1];
+#pragma unroll
+  for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * ps) : mk<T>(0, 0);
+  C b[Q][R2];
+  fft2pass<T, L, SGN, TRL>(a, b, S, tw, w, lane);
+  if (!ok) return;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    int k1 = w * Q + q;
+#pragma unroll
+    for (int i = 0; i < R2; ++i) st<T>(base + (size_t)(k1 + R1 * bitrev(i, R2)) * ps, c_scale(b[q][i], scale));
+  }
+}
+
+// φ forward: packed reals -> X_0..X_L scaled, in place (lines (r, z)); mixed form: X_0 from the FP64
+// sum of the row, the FP32 transform on the samples minus their FP64 mean
+template <typename T, int L, int TRL>
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __restrict__ e, int nrdim, int npdim,
+                                                                  const typename TW<T>::t* __restrict__ tw,
+                                                                  const typename TW<T>::t* __restrict__ twr, T scale,
+                                                                  double scale_d, double inv_np) {
+  typedef typename CT<T>::t C;
+  constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
+  constexpr bool DC = std::is_same<T, float>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = (C*)smem_raw;
+  double* red = (double*)(smem_raw + (size_t)L * TRL * sizeof(C));
+  int lane = threadIdx.x, w = threadIdx.y;
+  int r = blockIdx.x * TRL + lane;
+  int z = blockIdx.y;
+  bool ok = r < nrdim;
+  double2* base = e + r + (size_t)nrdim * npdim * z;
+  C a[R1];
+  double sum = 0.0;
+  if (DC) {
+    double2 d[R1];
+    double part = 0.0;
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) {
+      d[n1] = ok ? base[(size_t)(w + R2 * n1) * nrdim] : make_double2(0.0, 0.0);
+      part += d[n1].x + d[n1].y;
+    }
+    red[w * TRL + lane] = part;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < R2; ++q) sum += red[q * TRL + lane];
+    double mu = sum * inv_np;
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>((T)d2f_fast(d[n1].x - mu), (T)d2f_fast(d[n1].y - mu));
+  } else {
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * nrdim) : mk<T>(0, 0);
+  }
+  C b[Q][R2];
+  fft2pass<T, L, -1, TRL>(a, b, S, tw, w, lane);
+  __syncthreads();   // every thread has read its pass-2 inputs: S can take the spectrum
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    int k1 = w * Q + q;
+#pragma unroll
+    for (int i = 0; i < R2; ++i) S[(k1 * R2 + bitrev(i, R2)) * TRL + lane] = b[q][i];   // Z_(k1 + R1 k2)
+  }
+  __syncthreads();
+  if (!ok) return;
+  auto Z = [&](int k) -> C { return S[((k % R1) * R2 + k / R1) * TRL + lane]; };
+  for (int k = w; k <= L; k += R2) {
+    C zk = Z(k & (L - 1));
+    C zc = Z((L - k) & (L - 1));
+    zc.y = -zc.y;
+    C fe = c_scale(c_add(zk, zc), (T)0.5);
+    C fo = c_muli(c_scale(c_sub(zk, zc), (T)0.5), -1);   // (zk - zc)/(2i)
+    typename TW<T>::t wd = twr[k];
+    C x = c_scale(c_add(fe, c_mul(mk<T>(wd.x, wd.y), fo)), scale);
+    if (DC && k == 0) base[0] = make_double2(f2d_fast((float)x.x) + sum * scale_d, f2d_fast((float)x.y));
+    else st<T>(base + (size_t)k * nrdim, x);
+  }
+}
+
+// φ backward: X_0..X_L -> packed reals (unnormalised), slot L <- np X_L, in place; mixed form: Re X_0
+// left out of the FP32 transform and added to every sample in FP64
+template <typename T, int L, int TRL>
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __restrict__ e, int nrdim, int npdim,
+                                                                  const typename TW<T>::t* __restrict__ tw,
+                                                                  const typename TW<T>::t* __restrict__ twr, double np_d) {
+  typedef typename CT<T>::t C;
+  constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
+  constexpr bool DC = std::is_same<T, float>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = (C*)smem_raw;
+  int lane = threadIdx.x, w = threadIdx.y;
+  int r = blockIdx.x * TRL + lane;
+  int z = blockIdx.y;
+  bool ok = r < nrdim;
+  double2* base = e + r + (size_t)nrdim * npdim * z;
+  double2 nyq = make_double2(0, 0);
+  double dc = 0.0;
+  if (ok && w == 0) nyq = base[(size_t)L * nrdim];
+  if (DC && ok) dc = base[0].x;
+  C a[R1];
+#pragma unroll
+  for (int n1 = 0; n1 < R1; ++n1) {
+    int k = w + R2 * n1;
+    C v = mk<T>(0, 0);
+    if (ok) {
+      C xk = ld<T>(base + (size_t)k * nrdim);
+      C xc = ld<T>(base + (size_t)(L - k) * nrdim);
+      if (k == 0) { xk.y = 0; xc.y = 0; if (DC) xk.x = 0; }
+      xc.y = -xc.y;
+      C g = c_add(xk, xc);
+      typename TW<T>::t wd = twr[k];
+      C h = c_mul(c_sub(xk, xc), mk<T>(wd.x, -wd.y));   // exp(+2 pi i k / np)
+      v = c_add(g, c_muli(h, 1));
+    }
+    a[n1] = v;
+  }
+  C b[Q][R2];
+  fft2pass<T, L, +1, TRL>(a, b, S, tw, w, lane);
+  if (!ok) return;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    int k1 = w * Q + q;
+#pragma unroll
+    for (int i = 0; i < R2; ++i) {
+      C y = b[q][i];
+      double2* o = base + (size_t)(k1 + R1 * bitrev(i, R2)) * nrdim;
+      if (DC) *o = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+      else st<T>(o, y);
+    }
+  }
+  if (w == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
+}
+
 template <typename T> const typename TW<T>::t* tw_of(const double2* d, const float2* f);
 template <> const double2* tw_of<double>(const double2* d, const float2* f) { (void)f; return d; }
 template <> const float2* tw_of<float>(const double2* d, const float2* f) { (void)d; return f; }
@@ -274,10 +511,37 @@ static int set_smem(const void* fn, size_t bytes) {
   return 0;
 }
 
+template <typename T, int L, int SGN, int TRL>
+static int zfft2_launch(cd* e, double scale, int m0, int nm, cudaStream_t stream) {
+  size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t);
+  MLG_TRY(set_smem<T>((const void*)k_zfft2<T, L, SGN, TRL>, sm));
+  dim3 grid(cdiv(G.nrdim, TRL), nm), blk(TRL, Split<L>::R2);
+  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0);
+  MLG_LAUNCH();
+  return 0;
+}
+template <typename T, int L, int TRL>
+static int zfft2_dir(cd* e, int dir, double scale, int m0, int nm, cudaStream_t stream) {
+  return dir < 0 ? zfft2_launch<T, L, -1, TRL>(e, scale, m0, nm, stream) : zfft2_launch<T, L, +1, TRL>(e, scale, m0, nm, stream);
+}
+template <typename T, int TRL>
+static int zfft2_any(cd* e, int dir, double scale, int m0, int nm, cudaStream_t stream) {
+  switch (G.nz) {
+    case 16: return zfft2_dir<T, 16, TRL>(e, dir, scale, m0, nm, stream);
+    case 32: return zfft2_dir<T, 32, TRL>(e, dir, scale, m0, nm, stream);
+    case 64: return zfft2_dir<T, 64, TRL>(e, dir, scale, m0, nm, stream);
+    case 128: return zfft2_dir<T, 128, TRL>(e, dir, scale, m0, nm, stream);
+    case 256: return zfft2_dir<T, 256, TRL>(e, dir, scale, m0, nm, stream);
+  }
+  return -1;
+}
+static bool pow2_fast(int L) { return L == 16 || L == 32 || L == 64 || L == 128 || L == 256; }
+
 template <typename T>
 static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max, cudaStream_t stream) {
   int L = G.nz;
   if (L <= 1 || nm <= 0) return 0;
+  if (pow2_fast(L)) return tr_max >= 32 ? zfft2_any<T, 32>(e, dir, scale, m0, nm, stream) : zfft2_any<T, 8>(e, dir, scale, m0, nm, stream);
   int TR = std::min(pick_tr(L, sizeof(typename CT<T>::t)), tr_max);
   int TT = std::max(1, std::min(256 / TR, L / 2));
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
@@ -309,16 +573,46 @@ int launch_vfft_buf(cd* e, int dir) { return vfft_any(e, dir, dir < 0 ? 1.0 / G.
 int launch_vfft_scaled(cd* e, int dir, double scale) { return vfft_any(e, dir, scale); }
 int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
 
+template <typename T, int L>
+static int pfft2_launch(cd* e, int dir, double scale) {
+  constexpr int TRL = 32;
+  constexpr bool DC = std::is_same<T, float>::value;
+  size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t) + (DC && dir < 0 ? (size_t)Split<L>::R2 * TRL * sizeof(double) : 0);
+  dim3 grid(cdiv(G.nrdim, TRL), G.nzdim), blk(TRL, Split<L>::R2);
+  if (dir < 0) {
+    MLG_TRY(set_smem<T>((const void*)k_pfft_fwd2<T, L, TRL>, sm));
+    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np);
+  } else {
+    MLG_TRY(set_smem<T>((const void*)k_pfft_bwd2<T, L, TRL>, sm));
+    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np);
+  }
+  MLG_LAUNCH();
+  return 0;
+}
+
 template <typename T>
 static int hfft_t(cd* e, int dir, double scale) {
   int L = G.nph;
   if (G.np <= 1) return 0;
+  kt_begin(1);
+  if (pow2_fast(L)) {
+    switch (L) {
+      case 16: MLG_TRY((pfft2_launch<T, 16>(e, dir, scale))); break;
+      case 32: MLG_TRY((pfft2_launch<T, 32>(e, dir, scale))); break;
+      case 64: MLG_TRY((pfft2_launch<T, 64>(e, dir, scale))); break;
+      case 128: MLG_TRY((pfft2_launch<T, 128>(e, dir, scale))); break;
+      case 256: MLG_TRY((pfft2_launch<T, 256>(e, dir, scale))); break;
+    }
+    kt_end(1, 2.0 * G.fsize * 16);
+    return 0;
+  }
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
   int TT = std::max(1, std::min(256 / TR, std::max(L / 2, 1)));
   constexpr bool DC = std::is_same<T, float>::value;
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t) + (DC ? (size_t)TT * TR * sizeof(double) : 0);
   dim3 grid(cdiv(G.nrdim, TR), G.nzdim), blk(TR, TT);
-  kt_begin(1);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
     k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
