@@ -394,7 +394,142 @@ def run_ours(args, rank, world, local, pg):
         o.close()
     if not args.no_adjoint and world == 1:
         line["adjoint"] = adjoint_case(args)
+    if not args.no_sweep and world == 1:
+        line["transform_sweep"] = transform_sweep(args)
+    if args.large and world == 1:
+        line["large"] = large_case(args)
     print(json.dumps(line), flush=True)
+
+
+SWEEP_WORKLOAD = dict(nr=256, np=256, nz=256, nrchop=256, npchop=129, nzchop=129, ell=4.0)
+SWEEP_TRIPS, SWEEP_ORACLE_TRIPS = 50, 1
+
+
+def transform_sweep(args):
+    """Transform-only sweep, 256 x 256 x 256, ELL = 4, full chops: spectral coefficients with uniform
+    phase and magnitude exp(-0.05(n+|m|+|k|)) (seeded, Hermitian at m = 0), 50 forward+backward round
+    trips FFF -> PPP -> FFF in each form, timed with CUDA events.  Errors: each form against the FP64
+    oracle after one round trip (coefficients and the physical field), and mixed against FP64 after
+    50 round trips."""
+    from mlegs_gb300 import fields
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    from mlegs_gb300.params import make_params
+    import torch
+    p = make_params(**SWEEP_WORKLOAD)
+    kit = Kit(p, stream=torch.cuda.current_stream().cuda_stream)
+    c0 = fields.spectral_noise(p, kit.dims, 7, amp=1.0, decay=0.05)
+    out = {"workload": "256^3 ELL=4 full chops, |c| = exp(-0.05(n+|m|+|k|)), FFF->PPP->FFF round trips",
+           "field_MB": float(np.prod(kit.dims) * 16 / 1e6)}
+    res = {}
+    for mode, tag in ((PLAIN_FP64, "fp64"), (MIXED, "mixed")):
+        kit.set_precision(mode)
+        s = kit.scalar(c0, 0.0, "FFF")
+        kit.trans(s, "PPP")
+        phys1 = s.e
+        kit.trans(s, "FFF")
+        one = s.e
+        for _ in range(2):
+            kit.trans(s, "PPP"); kit.trans(s, "FFF")
+        s.set(c0, 0.0, "FFF")
+        kit.sync()
+        stream = torch.cuda.current_stream()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(SWEEP_TRIPS):
+            kit.trans(s, "PPP"); kit.trans(s, "FFF")
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        res[tag] = (phys1, one, s.e)
+        out[tag] = {"round_trips_per_s": SWEEP_TRIPS / (ms / 1e3), "ms_per_round_trip": ms / SWEEP_TRIPS}
+        s.free()
+    kit.close()
+    mixed50, fp6450 = res["mixed"][2], res["fp64"][2]
+    out["mixed"]["vs_fp64_after_50"] = {"rel_l2": rel_l2(mixed50, fp6450),
+                                        "max_rel": float(np.max(np.abs(mixed50 - fp6450)) / np.max(np.abs(fp6450)))}
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["round_trips_per_s"] / out["fp64"]["round_trips_per_s"]
+    if not args.no_cpu_baseline:
+        from oracle.oracle import Oracle
+        o = Oracle(p, threads=os.cpu_count() or 1)
+        so = o.scalar(c0, 0.0, "FFF")
+        o.trans(so, "PPP")
+        ophys = so.get()[0]
+        o.trans(so, "FFF")
+        oone = so.get()[0]
+        o.close()
+        for tag in ("fp64", "mixed"):
+            ph, one, _ = res[tag]
+            out[tag]["vs_oracle_one_trip"] = {
+                "physical_rel_l2": rel_l2(ph, ophys), "physical_max_rel": float(np.max(np.abs(ph - ophys)) / np.max(np.abs(ophys))),
+                "coeff_rel_l2": rel_l2(one, oone), "coeff_max_rel": float(np.max(np.abs(one - oone)) / np.max(np.abs(oone)))}
+    return out
+
+
+LARGE_WORKLOAD = dict(nr=512, np=512, nz=256, nrchop=512, npchop=257, nzchop=129, ell=6.0, visc=5.0e-5)
+LARGE_DT, LARGE_Q, LARGE_STEPS, LARGE_ADJ_STEPS, LARGE_CKPT = 5.0e-4, 2.0, 200, 100, 20
+
+
+def large_case(args):
+    """512 x 512 x 256, ELL = 6, Batchelor q = 2 vortex, Re = 2e4, dt = 5e-4: 200 mixed steps (SVV on,
+    the reference default) timed and compared with the FP64 form over the same steps; then the adjoint
+    (SVV off, which it requires) over 100 steps with checkpoints every 20.  Reports steps/s, the error
+    against FP64 and the memory high-water mark."""
+    from mlegs_gb300 import fields, vortex
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    from mlegs_gb300.params import make_params
+    import torch
+    out = {"workload": "NR=512 NP=512 NZ=256 ELL=6 q=2 Re=2e4 dt=5e-4, perturbation 1e-4 |m|<=4 |k|<=8"}
+    p = make_params(**LARGE_WORKLOAD)
+    kit = Kit(p, stream=torch.cuda.current_stream().cuda_stream)
+    st = vortex.VortexState(kit)
+    pert = (fields.spectral_noise(p, kit.dims, 5001, amp=PERT, decay=0.3, m_max=4, k_max=8),
+            fields.spectral_noise(p, kit.dims, 5002, amp=PERT, decay=0.3, m_max=4, k_max=8))
+    vortex.qvort_init(kit, st, q=LARGE_Q, uz_b=0.0, pert=pert)
+    kit.set_precision(MIXED)
+    vortex.bootstrap(kit, st, LARGE_DT)
+    kit.sync()
+    snap = snapshot(st)
+    fin = {}
+    for mode, tag in ((MIXED, "mixed"), (PLAIN_FP64, "fp64")):
+        kit.set_precision(mode)
+        restore(st, snap)
+        st.gains = [0.0, 0.0]
+        kit.vortex_run(*st.args(), LARGE_DT, 3, st.gains)
+        restore(st, snap)
+        st.gains = [0.0, 0.0]
+        kit.sync()
+        stream = torch.cuda.current_stream()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        kit.vortex_run(*st.args(), LARGE_DT, LARGE_STEPS, st.gains)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        fin[tag] = {n: getattr(st, n).e for n in ("psi", "chi", "nlpsi", "nlchi")}
+        out[tag] = {"steps": LARGE_STEPS, "steps_per_s": LARGE_STEPS / (ms / 1e3), "ms_per_step": ms / LARGE_STEPS}
+    out["mixed"]["rel_l2_vs_fp64"] = {n: rel_l2(fin["mixed"][n], fin["fp64"][n]) for n in fin["mixed"]}
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["mem_high_water_MB_forward"] = kit.mem_high_water() / 1e6
+    kit.close()
+    # the adjoint, SVV off
+    p2 = make_params(**dict(LARGE_WORKLOAD, is_svv=0))
+    kit = Kit(p2, precision=MIXED, stream=torch.cuda.current_stream().cuda_stream)
+    st = vortex.VortexState(kit)
+    vortex.qvort_init(kit, st, q=LARGE_Q, uz_b=0.0, pert=pert)
+    t0 = time.perf_counter()
+    J = kit.adjoint_run(st.psi, st.chi, st.uz, LARGE_DT, LARGE_ADJ_STEPS, LARGE_CKPT)
+    t_fwd = time.perf_counter() - t0
+    gp, gc = kit.scalar(), kit.scalar()
+    t0 = time.perf_counter()
+    kit.adjoint_run(st.psi, st.chi, st.uz, LARGE_DT, LARGE_ADJ_STEPS, LARGE_CKPT, gp, gc)
+    t_adj = time.perf_counter() - t0
+    g = gp.e
+    out["adjoint_mixed"] = {"steps": LARGE_ADJ_STEPS, "checkpoint": LARGE_CKPT, "J": J, "forward_s": t_fwd,
+                            "adjoint_run_s": t_adj, "sweep_over_forward": (t_adj - t_fwd) / t_fwd,
+                            "gradient_finite": bool(np.all(np.isfinite(g))), "svv": "off"}
+    out["mem_high_water_MB"] = kit.mem_high_water() / 1e6
+    kit.close()
+    return out
 
 
 ADJ_WORKLOAD = dict(nr=128, np=64, nz=64, nrchop=128, npchop=33, nzchop=33, ell=4.0, visc=2.0e-4, is_svv=0)
@@ -511,6 +646,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--large", action="store_true", help="also the 512x512x256 case (several minutes)")
     ap.add_argument("--adjoint-dirs", type=int, default=8)
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
