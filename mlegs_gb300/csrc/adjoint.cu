@@ -20,6 +20,7 @@
 // W_i = w_i r_i^2 / (1 - x_i^2) * (2 pi / np) * (zlen / nz) the quadrature of the volume integral
 // r dr dphi dz over the mapped Gauss-Legendre points (dr/dx = r / (1 - x^2)).
 #include "common.cuh"
+#include "dfloat.cuh"
 #include <cmath>
 #include <vector>
 
@@ -225,27 +226,29 @@ __global__ void k_vecprod_T(double2* __restrict__ vbr, double2* __restrict__ vbp
 // F_s_bar(up) = m k S4, F_o_bar(up) = -S2, F_s_bar(uz) = -S5, unfolded as
 // u_bar_i += F_s_bar + F_o_bar, u_bar_{nr-1-i} += s (F_s_bar - F_o_bar).
 // One CTA per (m, z tile, i tile); each thread one (i, z) pair; rows staged in shared memory.
-template <int IT, int ZT, int KC>
+template <typename T, int IT, int ZT, int KC>
 __global__ void __launch_bounds__(IT * ZT / 2)
 k_vec2tp_T(const double2* __restrict__ psib, const double2* __restrict__ chib, double2* __restrict__ urb,
-           double2* __restrict__ upb, double2* __restrict__ uzb, const double* __restrict__ tV, const double* __restrict__ tD,
-           const double* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim,
-           int nzdim, int nrc, int nzc, int nzcu) {
-  __shared__ double Vs[KC][IT + 1], Ds[KC][IT + 1], Ts[KC][IT + 1];
-  __shared__ double2 Ps[KC][ZT], Cs[KC][ZT];
-  int m = blockIdx.z;
+           double2* __restrict__ upb, double2* __restrict__ uzb, const typename TabT<T>::t* __restrict__ tV,
+           const typename TabT<T>::t* __restrict__ tD, const typename TabT<T>::t* __restrict__ tT,
+           const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc, int nzc,
+           int nzcu, int m0) {
+  typedef typename V2<T>::t C;
+  __shared__ T Vs[KC][IT + 1], Ds[KC][IT + 1], Ts[KC][IT + 1];
+  __shared__ C Ps[KC][ZT], Cs[KC][ZT];
+  int m = blockIdx.z + m0;
   int i0 = blockIdx.y * IT, z0 = blockIdx.x * ZT;
   int nn = max(min(nrc, nrc - m), 0);
   int tz = threadIdx.x % ZT, ti = threadIdx.x / ZT;   // ZT columns x (IT/2) rows of threads
   constexpr int NT = IT * ZT / 2;
   // two i per thread: ti and ti + IT/2
-  double2 S[2][2][5];
+  C S[2][2][5];
 #pragma unroll
   for (int a = 0; a < 2; ++a)
 #pragma unroll
     for (int p = 0; p < 2; ++p)
 #pragma unroll
-      for (int q = 0; q < 5; ++q) S[a][p][q] = make_double2(0.0, 0.0);
+      for (int q = 0; q < 5; ++q) { S[a][p][q].x = 0; S[a][p][q].y = 0; }
   int z = z0 + tz;
   int kk = z + 1;
   bool zact = z < nzdim && (kk <= nzc || kk >= nzcu);
@@ -253,20 +256,21 @@ k_vec2tp_T(const double2* __restrict__ psib, const double2* __restrict__ chib, d
     for (int idx = threadIdx.x; idx < KC * IT; idx += NT) {
       int jj = idx / IT, ii = idx % IT;
       int j = j0 + jj, i = i0 + ii;
-      double v = 0.0, d = 0.0, t = 0.0;
+      T v = 0, d = 0, t = 0;
       if (j < nn && i < nrh) {
         size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
-        v = tV[o]; d = tD[o]; t = tT[o];
+        v = tab<T>(tV, o); d = tab<T>(tD, o); t = tab<T>(tT, o);
       }
       Vs[jj][ii] = v; Ds[jj][ii] = d; Ts[jj][ii] = t;
     }
     for (int idx = threadIdx.x; idx < KC * ZT; idx += NT) {
       int jj = idx / ZT, zz = idx % ZT;
       int j = j0 + jj, zg = z0 + zz;
-      double2 pv = make_double2(0.0, 0.0), cv = pv;
+      C pv, cv;
+      pv.x = 0; pv.y = 0; cv = pv;
       if (j < nn && zg < nzdim) {
         size_t o = j + (size_t)nrdim * (m + (size_t)npdim * zg);
-        pv = psib[o]; cv = chib[o];
+        pv = ldc<T>(psib + o); cv = ldc<T>(chib + o);
       }
       Ps[jj][zz] = pv; Cs[jj][zz] = cv;
     }
@@ -274,47 +278,49 @@ k_vec2tp_T(const double2* __restrict__ psib, const double2* __restrict__ chib, d
 #pragma unroll 4
     for (int jj = 0; jj < KC; ++jj) {
       int p = (j0 + jj) & 1;
-      double2 pv = Ps[jj][tz], cv = Cs[jj][tz];
+      C pv = Ps[jj][tz], cv = Cs[jj][tz];
 #pragma unroll
       for (int a = 0; a < 2; ++a) {
         int ii = ti + a * (IT / 2);
-        double v = Vs[jj][ii], d = Ds[jj][ii], t = Ts[jj][ii];
-        S[a][p][0].x += v * pv.x; S[a][p][0].y += v * pv.y;
-        S[a][p][1].x += d * pv.x; S[a][p][1].y += d * pv.y;
-        S[a][p][2].x += d * cv.x; S[a][p][2].y += d * cv.y;
-        S[a][p][3].x += v * cv.x; S[a][p][3].y += v * cv.y;
-        S[a][p][4].x += t * cv.x; S[a][p][4].y += t * cv.y;
+        T v = Vs[jj][ii], d = Ds[jj][ii], t = Ts[jj][ii];
+        S[a][p][0].x = tmac(v, pv.x, S[a][p][0].x); S[a][p][0].y = tmac(v, pv.y, S[a][p][0].y);
+        S[a][p][1].x = tmac(d, pv.x, S[a][p][1].x); S[a][p][1].y = tmac(d, pv.y, S[a][p][1].y);
+        S[a][p][2].x = tmac(d, cv.x, S[a][p][2].x); S[a][p][2].y = tmac(d, cv.y, S[a][p][2].y);
+        S[a][p][3].x = tmac(v, cv.x, S[a][p][3].x); S[a][p][3].y = tmac(v, cv.y, S[a][p][3].y);
+        S[a][p][4].x = tmac(t, cv.x, S[a][p][4].x); S[a][p][4].y = tmac(t, cv.y, S[a][p][4].y);
       }
     }
     __syncthreads();
   }
   if (!zact) return;
-  double kv = ak[z], mv = (double)m;
+  T kv = (T)ak[z], mv = (T)m;
   size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
     int i = i0 + ti + a * (IT / 2);
     if (i >= nrh) continue;
-    double2 r_lo = make_double2(0, 0), r_hi = r_lo, p_lo = r_lo, p_hi = r_lo, z_lo = r_lo, z_hi = r_lo;
+    C r_lo, r_hi, p_lo, p_hi, z_lo, z_hi;
+    r_lo.x = 0; r_lo.y = 0; r_hi = r_lo; p_lo = r_lo; p_hi = r_lo; z_lo = r_lo; z_hi = r_lo;
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
-      double s = p ? -1.0 : 1.0;
-      double2 S1 = S[a][p][0], S2 = S[a][p][1], S3 = S[a][p][2], S4 = S[a][p][3], S5 = S[a][p][4];
-      double2 fs_r = make_double2(-mv * S1.y, mv * S1.x);    // i m S1
-      double2 fo_r = make_double2(kv * S3.y, -kv * S3.x);    // -i k S3
-      double2 fs_p = make_double2(mv * kv * S4.x, mv * kv * S4.y);
-      double2 fo_p = make_double2(-S2.x, -S2.y);
-      double2 fs_z = make_double2(-S5.x, -S5.y);
-      r_lo.x += fs_r.x + fo_r.x; r_lo.y += fs_r.y + fo_r.y;
-      r_hi.x += s * (fs_r.x - fo_r.x); r_hi.y += s * (fs_r.y - fo_r.y);
-      p_lo.x += fs_p.x + fo_p.x; p_lo.y += fs_p.y + fo_p.y;
-      p_hi.x += s * (fs_p.x - fo_p.x); p_hi.y += s * (fs_p.y - fo_p.y);
-      z_lo.x += fs_z.x; z_lo.y += fs_z.y;
-      z_hi.x += s * fs_z.x; z_hi.y += s * fs_z.y;
+      T sg = p ? (T)-1 : (T)1;
+      C S1 = S[a][p][0], S2 = S[a][p][1], S3 = S[a][p][2], S4 = S[a][p][3], S5 = S[a][p][4];
+      C fs_r, fo_r, fs_p, fo_p, fs_z;
+      fs_r.x = -mv * S1.y; fs_r.y = mv * S1.x;              // i m S1
+      fo_r.x = kv * S3.y; fo_r.y = -kv * S3.x;              // -i k S3
+      fs_p.x = mv * kv * S4.x; fs_p.y = mv * kv * S4.y;
+      fo_p.x = -S2.x; fo_p.y = -S2.y;
+      fs_z.x = -S5.x; fs_z.y = -S5.y;
+      r_lo.x = r_lo.x + (fs_r.x + fo_r.x); r_lo.y = r_lo.y + (fs_r.y + fo_r.y);
+      r_hi.x = r_hi.x + sg * (fs_r.x - fo_r.x); r_hi.y = r_hi.y + sg * (fs_r.y - fo_r.y);
+      p_lo.x = p_lo.x + (fs_p.x + fo_p.x); p_lo.y = p_lo.y + (fs_p.y + fo_p.y);
+      p_hi.x = p_hi.x + sg * (fs_p.x - fo_p.x); p_hi.y = p_hi.y + sg * (fs_p.y - fo_p.y);
+      z_lo.x = z_lo.x + fs_z.x; z_lo.y = z_lo.y + fs_z.y;
+      z_hi.x = z_hi.x + sg * fs_z.x; z_hi.y = z_hi.y + sg * fs_z.y;
     }
-    urb[base + i] = r_lo; urb[base + nr - 1 - i] = r_hi;
-    upb[base + i] = p_lo; upb[base + nr - 1 - i] = p_hi;
-    uzb[base + i] = z_lo; uzb[base + nr - 1 - i] = z_hi;
+    urb[base + i] = to_d2<T>(r_lo.x, r_lo.y); urb[base + nr - 1 - i] = to_d2<T>(r_hi.x, r_hi.y);
+    upb[base + i] = to_d2<T>(p_lo.x, p_lo.y); upb[base + nr - 1 - i] = to_d2<T>(p_hi.x, p_hi.y);
+    uzb[base + i] = to_d2<T>(z_lo.x, z_lo.y); uzb[base + nr - 1 - i] = to_d2<T>(z_hi.x, z_hi.y);
   }
 }
 
@@ -553,12 +559,31 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
     int nrc = G.nrchop + 3, npc = G.npchop;
     if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
     constexpr int IT = 32, ZT = 16, KC = 16;
-    dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc);
     kt_begin(KT_V2TP);
-    k_vec2tp_T<IT, ZT, KC><<<grid, IT * ZT / 2, 0, G.stream>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV, G.tD, G.tT, G.ak, G.nr,
-                                                               G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, G.chopzl,
-                                                               G.chopzu);
-    MLG_LAUNCH();
+    if (G.precision == MLG_MIXED) {
+      // as the forward: m >= 1 in FP32, the m = 0 plane in double-float beside it
+      MLG_TRY(side_fork());
+      constexpr int DIT = 16, DZT = 8;
+      dim3 dgrid(cdiv(G.nzdim, DZT), cdiv(G.nrh, DIT), 1);
+      k_vec2tp_T<dfl, DIT, DZT, KC><<<dgrid, DIT * DZT / 2, 0, G.side>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV, G.tD, G.tT,
+                                                                         G.ak, G.nr, G.nrh, G.ne, G.nrdim, G.npdim,
+                                                                         G.nzdim, nrc, G.chopzl, G.chopzu, 0);
+      MLG_LAUNCH();
+      if (npc > 1) {
+        dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc - 1);
+        k_vec2tp_T<float, IT, ZT, KC><<<grid, IT * ZT / 2, 0, G.stream>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV32, G.tD32,
+                                                                          G.tT32, G.ak, G.nr, G.nrh, G.ne, G.nrdim,
+                                                                          G.npdim, G.nzdim, nrc, G.chopzl, G.chopzu, 1);
+        MLG_LAUNCH();
+      }
+      MLG_TRY(side_join());
+    } else {
+      dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc);
+      k_vec2tp_T<double, IT, ZT, KC><<<grid, IT * ZT / 2, 0, G.stream>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV, G.tD, G.tT,
+                                                                         G.ak, G.nr, G.nrh, G.ne, G.nrdim, G.npdim,
+                                                                         G.nzdim, nrc, G.chopzl, G.chopzu, 0);
+      MLG_LAUNCH();
+    }
     kt_end(KT_V2TP, 0.0);
   }
   for (Scalar* q : {&ur, &up, &uz}) { q->set_space("PFF"); q->off[0] = q->off[1] = q->off[2] = 0; }
