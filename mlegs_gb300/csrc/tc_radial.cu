@@ -13,7 +13,7 @@
 // A_par(i, t) = pf(i, 2t+par, m) and B_par(t, n) = c(2t+par, m, z); the epilogue forms
 // f(i) = D_0 + D_1 and f(nr-1-i) = D_0 - D_1 (and adds the log term at m = 0).
 //
-// Engine: one CTA per (m, 128-row tile, 32 complex z columns), 128 threads, 72 KiB of shared memory
+// Engine: one CTA per (m, 128-row tile, 32 complex z columns), 256 threads, 72 KiB of shared memory
 // (three CTAs per SM).
 //  * The table operand is split and laid out at kit init in the UMMA canonical no-swizzle K-major
 //    layout (8x8 BF16 core matrices, 16-byte rows) per (m, row tile, K chunk): one K chunk of both
@@ -32,106 +32,10 @@
 // it carries the axisymmetric mean flow and its radial sums cancel toward the axis.  The grid starts
 // at m = m0.
 #include "common.cuh"
+#include "tc_common.cuh"
 #include <cstdint>
 
 namespace mlg {
-
-// ------------------------------------------------------------------------------------------------
-// PTX wrappers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait (~1 s of SM clock); false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-  long long t0 = clock64();
-  while (!mbar_try_wait(bar, phase))
-    if (clock64() - t0 > 2000000000LL) return false;
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(dst)), "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-
-// 32 TMEM lanes x 16 consecutive 32-bit columns into each thread (lane = thread of the warp)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// shared-memory matrix descriptor: no swizzle, K-major; LBO = byte distance between the two core
-// matrices adjacent in K, SBO = byte distance between core matrices adjacent in M/N
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
-         (1ull << 46);
-}
-// instruction descriptor: kind::f16 with BF16 A and B, FP32 D, both K-major
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// BF16 split of an FP32 value (round to nearest even on the integer pipe)
-__device__ __forceinline__ uint16_t bf16_rn(float x) {
-  uint32_t u = __float_as_uint(x);
-  u += 0x7FFFu + ((u >> 16) & 1u);
-  return (uint16_t)(u >> 16);
-}
-__device__ __forceinline__ float bf16_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
-__device__ __forceinline__ void split3(float x, uint16_t& s0, uint16_t& s1, uint16_t& s2) {
-  s0 = bf16_rn(x);
-  float r = x - bf16_f(s0);
-  s1 = bf16_rn(r);
-  r = r - bf16_f(s1);
-  s2 = bf16_rn(r);
-}
 
 // canonical layout of one operand tile of R rows x KC columns (BF16): byte offset of (row, k)
 constexpr int TC_KC = 32;                       // K chunk
@@ -143,7 +47,8 @@ __host__ __device__ constexpr int tc_off(int row, int k) {
 constexpr int TC_TILE_BYTES = 128 * TC_KC * 2;  // 8 KiB: 128 rows x 32 BF16 (table tiles, M = 128)
 constexpr int TC_NZ = 32;                       // complex z columns per CTA (N = 64)
 constexpr int TC_BTILE_BYTES = 2 * TC_NZ * TC_KC * 2;   // 4 KiB: 64 rows x 32 BF16 (field tiles)
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;   // 8 warps: the operand staging is split in two halves, the epilogue in
+                                  // two column halves of the four TMEM lane quarters
 
 // ------------------------------------------------------------------------------------------------
 // table images, split and laid out once per kit: for (m, row tile, K chunk): [par 2][split 3][tile]
@@ -246,8 +151,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
   const uint32_t tmem = sm.tmem;
   bool ok = true;
   const uint8_t* img_m = (const uint8_t*)img + ((size_t)m * nmt + mt) * nkc * (size_t)(6 * TC_TILE_BYTES);
-  // staging item of this thread: z column zz and K group kg (8 consecutive K indices)
-  const int zz = tid % TC_NZ, kg = tid / TC_NZ;
+  // staging item of this thread: z column zz, K group kg (8 consecutive K indices) and half: the row
+  // parity it writes (forward: the fold sign, backward: the parity of the rows it reads)
+  const int zz = tid % TC_NZ, kg = (tid / TC_NZ) & 3, half = tid / (4 * TC_NZ);
   const int z = z0 + zz;
   const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * min(z, nzdim - 1));
   float2 ra[8], rb[8];
@@ -260,11 +166,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
       if (MODE == 0) {
         if (k < nrh && z < nzdim) { ra[q] = ld_c32(col + k); rb[q] = ld_c32(col + nr - 1 - k); wv[q] = w32[k]; }
       } else {
-        int je = 2 * k, jo = 2 * k + 1;
-        if (z < nzdim) {
-          if (je < nn) ra[q] = ld_c32(col + je);
-          if (jo < nn) rb[q] = ld_c32(col + jo);
-        }
+        int j = 2 * k + half;
+        if (z < nzdim && j < nn) ra[q] = ld_c32(col + j);
       }
     }
   };
@@ -277,31 +180,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
     {
       float v[8];
       if (MODE == 0) {
+        const float sg = half ? -1.f : 1.f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x + rb[q].x) * wv[q];
-        store_split8(sm.b, 0, 2 * zz, kg, v);
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x + sg * rb[q].x) * wv[q];
+        store_split8(sm.b, half, 2 * zz, kg, v);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y + rb[q].y) * wv[q];
-        store_split8(sm.b, 0, 2 * zz + 1, kg, v);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x - rb[q].x) * wv[q];
-        store_split8(sm.b, 1, 2 * zz, kg, v);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y - rb[q].y) * wv[q];
-        store_split8(sm.b, 1, 2 * zz + 1, kg, v);
+        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y + sg * rb[q].y) * wv[q];
+        store_split8(sm.b, half, 2 * zz + 1, kg, v);
       } else {
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = ra[q].x;
-        store_split8(sm.b, 0, 2 * zz, kg, v);
+        store_split8(sm.b, half, 2 * zz, kg, v);
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = ra[q].y;
-        store_split8(sm.b, 0, 2 * zz + 1, kg, v);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = rb[q].x;
-        store_split8(sm.b, 1, 2 * zz, kg, v);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = rb[q].y;
-        store_split8(sm.b, 1, 2 * zz + 1, kg, v);
+        store_split8(sm.b, half, 2 * zz + 1, kg, v);
       }
     }
     fence_async_smem();
@@ -318,16 +210,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
     __syncthreads();
   }
   tc_fence_after();
+  // warp w reads TMEM lanes 32 (w % 4) .. +31 and the column half w / 4 of each accumulator
+  const int lq = warp & 3, ch = warp >> 2;
+  constexpr int CBH = (2 * TC_NZ) / 32;   // 16-column blocks per column half
   if (MODE == 0) {
-    // warp w holds rows t = mt*128 + 32w + lane of both parities
-    const int t = mt * 128 + warp * 32 + lane;
+    // lane quarter lq holds rows t = mt*128 + 32 lq + lane of both parities
+    const int t = mt * 128 + lq * 32 + lane;
 #pragma unroll
     for (int par = 0; par < 2; ++par) {
       int j = 2 * t + par;
 #pragma unroll
-      for (int cb = 0; cb < (2 * TC_NZ) / 16; ++cb) {
+      for (int cbi = 0; cbi < CBH; ++cbi) {
+        const int cb = ch * CBH + cbi;
         float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + par * (2 * TC_NZ) + cb * 16, v);
+        tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + par * (2 * TC_NZ) + cb * 16, v);
         if (j < nn) {
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
@@ -339,14 +235,16 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
       }
     }
   } else {
-    // warp w holds radial points i = mt*128 + 32w + lane: f(i) = be + bo, f(nr-1-i) = be - bo
-    const int i = mt * 128 + warp * 32 + lane;
-    double lnv = (add_ln && m == 0) ? *lnp : 0.0;
+    // lane quarter lq holds radial points i = mt*128 + 32 lq + lane: f(i) = be + bo, f(nr-1-i) = be - bo
+    const int i = mt * 128 + lq * 32 + lane;
+    const bool addl = add_ln && m == 0;
+    const double lnv = addl ? *lnp : 0.0;
 #pragma unroll
-    for (int cb = 0; cb < (2 * TC_NZ) / 16; ++cb) {
+    for (int cbi = 0; cbi < CBH; ++cbi) {
+      const int cb = ch * CBH + cbi;
       float ve[16], vo[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 0 * (2 * TC_NZ) + cb * 16, ve);
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 1 * (2 * TC_NZ) + cb * 16, vo);
+      tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + 0 * (2 * TC_NZ) + cb * 16, ve);
+      tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + 1 * (2 * TC_NZ) + cb * 16, vo);
       if (i < nrh) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
@@ -355,7 +253,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
           size_t b0 = (size_t)nrdim * (m + (size_t)npdim * zo);
           double2 p = make_double2(f2d_fast(ve[2 * q] + vo[2 * q]), f2d_fast(ve[2 * q + 1] + vo[2 * q + 1]));
           double2 qq = make_double2(f2d_fast(ve[2 * q] - vo[2 * q]), f2d_fast(ve[2 * q + 1] - vo[2 * q + 1]));
-          if (lnv != 0.0) { p.x += lnv * lnx[i]; qq.x += lnv * lnx[nr - 1 - i]; }
+          if (addl) { p.x += lnv * lnx[i]; qq.x += lnv * lnx[nr - 1 - i]; }
           out[b0 + i] = p;
           out[b0 + nr - 1 - i] = qq;
         }
