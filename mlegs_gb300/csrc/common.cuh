@@ -64,12 +64,11 @@ struct Ctx {
   bool svv_q_ready = false;
   double *lognorm = nullptr;   // (ne, npchop)
   double *pf = nullptr;        // (nrh, ne, npchop): P_L^m(x_i) normalised, reference layout
-  float *pf32 = nullptr;       // FP32 copy of pf for the mixed form
   double *at0 = nullptr, *at1 = nullptr;   // (nrchop)
   double *bd2 = nullptr;       // del2 bands without the -k^2 term: (5, ne, npchop)
   double *bxx = nullptr;       // xxdx bands: (3, ne+1, npchop)
   double *tV = nullptr, *tD = nullptr, *tT = nullptr;   // vec2tp matrices (nrh, ne, npchop)
-  float *tV32 = nullptr, *tD32 = nullptr, *tT32 = nullptr, *tT32lo = nullptr;   // tT32lo: tT - tT32
+  float *tV32 = nullptr, *tD32 = nullptr, *tT32 = nullptr;   // FP32 copies (the mixed form's adjoint)
   double2 *tw_p = nullptr, *tw_z = nullptr;  // FFT twiddles exp(-2 pi i k/L): L = np/2 (phi), nz (z)
   double2 *tw_pr = nullptr;    // real-FFT post-processing twiddles exp(-2 pi i k/np), k < np/2+1
   float2 *tw_p32 = nullptr, *tw_z32 = nullptr, *tw_pr32 = nullptr;   // FP32 copies for the mixed form
@@ -135,6 +134,8 @@ void tc_free();
 int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc);
 int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln);
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
+int pv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc);
+void pv_free();
 
 // pointwise
 int launch_zero(cd* e);

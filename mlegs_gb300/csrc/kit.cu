@@ -201,11 +201,6 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, si
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
 }
-// the FP32 rounding of what k_to_f32 left out: a = b + lo to about 48 bits
-__global__ void k_to_f32lo(const double* __restrict__ a, float* __restrict__ lo, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    lo[i] = (float)(a[i] - (double)(float)a[i]);
-}
 
 // ------------------------------------------------------------------------------------------------
 // host-side FP64 pieces, same operation order as the reference
@@ -361,16 +356,12 @@ int kit_build(const mlg_params* P) {
   MLG_LAUNCH();
 
   // FP32 copies for the mixed form
-  MLG_TRY(dmalloc((void**)&G.pf32, npf * sizeof(float)));
   MLG_TRY(dmalloc((void**)&G.tV32, npf * sizeof(float)));
   MLG_TRY(dmalloc((void**)&G.tD32, npf * sizeof(float)));
   MLG_TRY(dmalloc((void**)&G.tT32, npf * sizeof(float)));
-  k_to_f32<<<256, 256, 0, G.stream>>>(G.pf, G.pf32, npf); MLG_LAUNCH();
   k_to_f32<<<256, 256, 0, G.stream>>>(G.tV, G.tV32, npf); MLG_LAUNCH();
   k_to_f32<<<256, 256, 0, G.stream>>>(G.tD, G.tD32, npf); MLG_LAUNCH();
   k_to_f32<<<256, 256, 0, G.stream>>>(G.tT, G.tT32, npf); MLG_LAUNCH();
-  MLG_TRY(dmalloc((void**)&G.tT32lo, npf * sizeof(float)));
-  k_to_f32lo<<<256, 256, 0, G.stream>>>(G.tT, G.tT32lo, npf); MLG_LAUNCH();
 
   // FFT twiddles, exp(-2 pi i k / L) as in FFTE's SETTBL0 (fft235.f:205-217)
   auto twid = [](int L, int count) {

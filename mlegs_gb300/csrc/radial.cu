@@ -274,142 +274,6 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
   }
 }
 
-// ---- mixed-form projection ------------------------------------------------------------------------
-// (ah + al) + (bh + bl) renormalised (Knuth two-sum on the high parts)
-__device__ __forceinline__ float2 df_add(float ah, float al, float bh, float bl) {
-  float s = ah + bh, v = s - ah;
-  float e = (ah - (s - v)) + (bh - v);
-  e += al + bl;
-  float h = s + e;
-  return make_float2(h, e - (h - s));
-}
-
-// acc += (th + tl) * (zh + zl): exact product of the high parts (fma), cross terms, two-sum
-__device__ __forceinline__ void df_mac(float& acch, float& accl, float th, float tl, float zh, float zl) {
-  float p = th * zh;
-  float e = fmaf(th, zh, -p);
-  e = fmaf(th, zl, e);
-  e = fmaf(tl, zh, e);
-  float s = acch + p, v = s - acch;
-  accl += ((acch - (s - v)) + (p - v)) + e;
-  acch = s;
-}
-
-// The mixed form of the vec2tp contraction.  V.F_s(ur), D.F_o(up), D.F_o(ur), V.F_s(up) run in FP32;
-// T.F_s(uz) runs in double-float: chi is finished by an inverse horizontal Laplacian that lifts the
-// rounding of this term (relative to the largest u_z) into chi's weak low modes, which FP32
-// accumulation over the radial points cannot resolve.  Each thread holds MPT rows x ZPT columns.
-template <int MT, int ZT, int KC, int MPT, int ZPT>
-__global__ void __launch_bounds__((MT / MPT) * (ZT / ZPT))
-k_vec2tp_mixed(const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
-               double2* __restrict__ psi, double2* __restrict__ chi, const float* __restrict__ tV,
-               const float* __restrict__ tD, const float* __restrict__ tTh, const float* __restrict__ tTl,
-               const double* __restrict__ ak, int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc,
-               int nzc, int nzcu, int m0) {
-  constexpr int RT = MT / MPT;   // row threads
-  constexpr int CT = ZT / ZPT;   // column threads
-  __shared__ float Av[KC][MT + 1], Ad[KC][MT + 1], Ath[KC][MT + 1], Atl[KC][MT + 1];
-  __shared__ float2 Brs[KC][ZT], Bro[KC][ZT], Bps[KC][ZT], Bpo[KC][ZT], Bzh[KC][ZT], Bzl[KC][ZT];
-  int m = blockIdx.z + m0;
-  int par = blockIdx.y & 1;
-  int t0 = (blockIdx.y >> 1) * MT;
-  int nn = max(min(nrc, nrc - m), 0);
-  if (2 * t0 + par >= nn) return;
-  int z0 = blockIdx.x * ZT;
-  int tx = threadIdx.x, ty = threadIdx.y;
-  int tid = ty * CT + tx;
-  constexpr int NTHR = RT * CT;
-  float2 a1[MPT][ZPT], a2[MPT][ZPT], a3[MPT][ZPT], a4[MPT][ZPT], ch[MPT][ZPT], cl[MPT][ZPT];
-#pragma unroll
-  for (int q = 0; q < MPT; ++q)
-#pragma unroll
-    for (int b = 0; b < ZPT; ++b) {
-      a1[q][b] = a2[q][b] = a3[q][b] = a4[q][b] = ch[q][b] = cl[q][b] = make_float2(0.f, 0.f);
-    }
-  const float ss = par ? -1.f : 1.f;   // own-parity fold sign
-  for (int i0 = 0; i0 < nrh; i0 += KC) {
-    for (int idx = tid; idx < KC * MT; idx += NTHR) {
-      int ii = idx % KC, tt = idx / KC;
-      int j = 2 * (t0 + tt) + par, i = i0 + ii;
-      float v = 0.f, d = 0.f, th = 0.f, tl = 0.f;
-      if (j < nn && i < nrh) {
-        size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
-        v = tV[o]; d = tD[o]; th = tTh[o]; tl = tTl[o];
-      }
-      Av[ii][tt] = v; Ad[ii][tt] = d; Ath[ii][tt] = th; Atl[ii][tt] = tl;
-    }
-    for (int idx = tid; idx < KC * ZT; idx += NTHR) {
-      int ii = idx % KC, zz = idx / KC;
-      int i = i0 + ii, z = z0 + zz;
-      float2 rs = make_float2(0.f, 0.f), ro = rs, ps = rs, po = rs, zh = rs, zl = rs;
-      if (i < nrh && z < nzdim) {
-        size_t base = (size_t)nrdim * (m + (size_t)npdim * z);
-        float2 a = ld_c32(ur + base + i), b = ld_c32(ur + base + nr - 1 - i);
-        rs = make_float2(a.x + ss * b.x, a.y + ss * b.y);
-        ro = make_float2(a.x - ss * b.x, a.y - ss * b.y);
-        a = ld_c32(up + base + i); b = ld_c32(up + base + nr - 1 - i);
-        ps = make_float2(a.x + ss * b.x, a.y + ss * b.y);
-        po = make_float2(a.x - ss * b.x, a.y - ss * b.y);
-        double2 za = uz[base + i], zb = uz[base + nr - 1 - i];
-        float2 xa = d2ff(za.x), xb = d2ff(zb.x), ya = d2ff(za.y), yb = d2ff(zb.y);
-        float2 sx = df_add(xa.x, xa.y, ss * xb.x, ss * xb.y), sy = df_add(ya.x, ya.y, ss * yb.x, ss * yb.y);
-        zh = make_float2(sx.x, sy.x);
-        zl = make_float2(sx.y, sy.y);
-      }
-      Brs[ii][zz] = rs; Bro[ii][zz] = ro; Bps[ii][zz] = ps; Bpo[ii][zz] = po; Bzh[ii][zz] = zh; Bzl[ii][zz] = zl;
-    }
-    __syncthreads();
-#pragma unroll 2
-    for (int ii = 0; ii < KC; ++ii) {
-      float v[MPT], d[MPT], th[MPT], tl[MPT];
-#pragma unroll
-      for (int q = 0; q < MPT; ++q) {
-        v[q] = Av[ii][ty + q * RT]; d[q] = Ad[ii][ty + q * RT]; th[q] = Ath[ii][ty + q * RT]; tl[q] = Atl[ii][ty + q * RT];
-      }
-#pragma unroll
-      for (int b = 0; b < ZPT; ++b) {
-        int zz = tx + b * CT;
-        float2 rs = Brs[ii][zz], ro = Bro[ii][zz], ps = Bps[ii][zz], po = Bpo[ii][zz], zh = Bzh[ii][zz], zl = Bzl[ii][zz];
-#pragma unroll
-        for (int q = 0; q < MPT; ++q) {
-          a1[q][b].x = fmaf(v[q], rs.x, a1[q][b].x); a1[q][b].y = fmaf(v[q], rs.y, a1[q][b].y);   // V.F_s(ur)
-          a2[q][b].x = fmaf(d[q], po.x, a2[q][b].x); a2[q][b].y = fmaf(d[q], po.y, a2[q][b].y);   // D.F_o(up)
-          a3[q][b].x = fmaf(d[q], ro.x, a3[q][b].x); a3[q][b].y = fmaf(d[q], ro.y, a3[q][b].y);   // D.F_o(ur)
-          a4[q][b].x = fmaf(v[q], ps.x, a4[q][b].x); a4[q][b].y = fmaf(v[q], ps.y, a4[q][b].y);   // V.F_s(up)
-          df_mac(ch[q][b].x, cl[q][b].x, th[q], tl[q], zh.x, zl.x);                                // T.F_s(uz)
-          df_mac(ch[q][b].y, cl[q][b].y, th[q], tl[q], zh.y, zl.y);
-        }
-      }
-    }
-    __syncthreads();
-  }
-  float mv = (float)m;
-#pragma unroll
-  for (int q = 0; q < MPT; ++q) {
-    int j = 2 * (t0 + ty + q * RT) + par;
-    if (j >= nn) continue;
-#pragma unroll
-    for (int b = 0; b < ZPT; ++b) {
-      int z = z0 + tx + b * CT;
-      if (z >= nzdim) continue;
-      int kk = z + 1;
-      if (!(kk <= nzc || kk >= nzcu)) continue;
-      float kv = d2f_fast(ak[z]);
-      float w1x = m ? a1[q][b].x : 0.f, w1y = m ? a1[q][b].y : 0.f;
-      // psi = -i*mv*w1 - w2
-      double2 p = make_double2(f2d_fast(mv * w1y - a2[q][b].x), f2d_fast(-mv * w1x - a2[q][b].y));
-      float v2x = m ? a4[q][b].x : 0.f, v2y = m ? a4[q][b].y : 0.f;
-      // chi = i*kv*w1' + mv*kv*w2' - c, the double-float c subtracted in FP64
-      float gx = -kv * a3[q][b].y + mv * kv * v2x, gy = kv * a3[q][b].x + mv * kv * v2y;
-      double2 c = make_double2(f2d_fast(gx) - (f2d_fast(ch[q][b].x) + f2d_fast(cl[q][b].x)),
-                               f2d_fast(gy) - (f2d_fast(ch[q][b].y) + f2d_fast(cl[q][b].y)));
-      size_t o = j + (size_t)nrdim * (m + (size_t)npdim * z);
-      psi[o] = p;
-      chi[o] = c;
-    }
-  }
-}
-
 static int rtrans_check(const Scalar& s, int& nrc, int& npc, const char* who) {
   nrc = G.nrchop + s.off[0];
   npc = G.npchop + s.off[1];
@@ -512,22 +376,15 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
   if (G.precision == MLG_MIXED) {
-    // m >= 1 in FP32 (with the u_z term in double-float), m = 0 in double-float beside it
+    // m >= 1 on the tensor cores (split BF16, the u_z term in exact digit slices), m = 0 in
+    // double-float beside it
     MLG_TRY(side_fork());
     constexpr int DMT = 16, DZT = 8;
     dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
     k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
                                                                G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
     MLG_LAUNCH();
-    constexpr int MMT = 32, MMPT = 2;
-    int mtt = cdiv((nrc + 1) / 2, MMT);
-    if (npc > 1) {
-      dim3 mgrid(cdiv(G.nzdim, ZT), 2 * mtt, npc - 1), mblk(ZT / ZPT, MMT / MMPT);
-      k_vec2tp_mixed<MMT, ZT, KC, MMPT, ZPT><<<mgrid, mblk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV32, G.tD32, G.tT32,
-                                                                           G.tT32lo, G.ak, G.nr, G.nrh, G.ne, G.nrdim,
-                                                                           G.npdim, G.nzdim, nrc, nzc, nzcu, 1);
-      MLG_LAUNCH();
-    }
+    MLG_TRY(pv_contract(ur, up, uz, psi, chi, nrc, npc));   // m >= 1: tensor cores (tc_vec2tp.cu)
     MLG_TRY(side_join());
     kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
     return 0;
