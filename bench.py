@@ -300,7 +300,7 @@ def run_ours(args, rank, world, local, pg):
         kit.kernel_timing(True)
         kit.vortex_run(*st.args(), DT, 2, st.gains)
         kt = {name: kit.kernel_timing_read(i) for i, name in
-              enumerate(["radial_fwd", "fft", "banded", "radial_bwd", "vec2tp"])}
+              enumerate(["radial_fwd", "fft", "banded", "radial_bwd", "vec2tp", "solve"])}
         kit.kernel_timing(False)
         kit.sync()
 
@@ -337,22 +337,46 @@ def run_ours(args, rank, world, local, pg):
     except Exception:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # dominant kernel class by time per step
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    # the dominant kernel class by time per step; its algorithmic work per launch is what the library
+    # counts for it (bytes: each field read and written once, tables / factors read once)
     dom = max(kt, key=lambda n: kt[n][0])
     d_ms, d_n, d_work = kt[dom]
     avg_ms = d_ms / max(d_n, 1)
-    # algorithmic bytes per launch of the radial contractions (mixed form): FP64 field columns in and
-    # out once, FP32 tables once (forward: nr rows x npc columns in, sum nn rows out; backward the
-    # reverse; vec2tp: three fields in, two out, three tables)
-    nrh, nz, fb = 96, 128, 16
-    sum_nn = sum(max(min(192, 192 - m), 0) for m in range(65))
-    sum_nn3 = sum(max(min(195, 195 - m), 0) for m in range(65))
-    alg = {"radial_fwd": 192 * 65 * nz * fb + sum_nn * nz * fb + sum_nn * nrh * 4,
-           "radial_bwd": 192 * 65 * nz * fb + sum_nn * nz * fb + sum_nn * nrh * 4,
-           "vec2tp": 3 * 192 * 65 * nz * fb + 2 * sum_nn3 * nz * fb + 3 * sum_nn3 * nrh * 4,
-           "fft": 2 * 195 * 65 * 128 * fb, "banded": 2 * 195 * 65 * 128 * fb}
-    bytes_launch = alg[dom]
+    sum_nn = sum(max(192 - m, 0) for m in range(65))
+    flop_class_bytes = {   # the contraction classes count flops; their algorithmic bytes per launch
+        "radial_fwd": 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2,
+        "radial_bwd": 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2,
+        "vec2tp": 3 * 192 * 65 * 128 * 16 + 2 * (sum_nn + 3 * 65) * 128 * 16 + 12 * sum_nn * 96 * 2}
+    bytes_launch = flop_class_bytes.get(dom, d_work / max(d_n, 1))
     achieved_gbs = bytes_launch / (avg_ms * 1e-3) / 1e9
+    # DRAM traffic per launch of the class's largest kernel from one ncu capture at this workload
+    # (dram__bytes_read.sum + dram__bytes_write.sum), and what limits it
+    ncu = {"solve": {"kernel": "k_band_subst<2> (psi and chi Helmholtz substitutions)", "traffic": 157.33e6,
+                     "algorithmic_bytes": 2.0 * 2 * 195 * 65 * 128 * 16 + 192 * 8 * 65 * 128 * 8,
+                     "limit": "FP64 pipe 48.8% busy (ncu), 5% of warps active: serial recurrences, ~2 FP64 FMA/clk/SM "
+                              "on GB300; the solves stay FP64 in both forms"}}
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+            "frac": achieved_gbs / hbm, "traffic": ncu.get(dom, {}).get("traffic"),
+            "avg_launch_us": 1e3 * avg_ms, "launches_per_step": d_n / 2,
+            "algorithmic_bytes_per_launch": bytes_launch,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    if dom in ncu:
+        roof["ncu_kernel"] = ncu[dom]["kernel"]
+        roof["limit"] = ncu[dom]["limit"]
+    # the tensor-core Legendre transforms (backward, m >= 1 on tcgen05 plus the m = 0 plane beside it):
+    # algorithmic flops 4 sum_m nn(m) nrh nz per launch against the bf16 peak
+    r_ms, r_n, r_flops = kt["radial_bwd"]
+    r_avg = r_ms / max(r_n, 1)
+    r_tf = (r_flops / max(r_n, 1)) / (r_avg * 1e-3) / 1e12
+    r_bytes = 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2
+    roof_tc = {"bound": "tensor", "kernel": "radial_bwd (k_tc_rtrans<1>, split BF16 on tcgen05)", "achieved": r_tf,
+               "peak": bf16, "unit": "TFLOP/s", "frac": r_tf / bf16, "avg_launch_us": 1e3 * r_avg,
+               "bf16_products_per_mac": 6, "algorithmic_flops_per_launch": r_flops / max(r_n, 1),
+               "hbm_view": {"algorithmic_bytes_per_launch": r_bytes,
+                            "achieved_gbs": r_bytes / (r_avg * 1e-3) / 1e9,
+                            "frac": r_bytes / (r_avg * 1e-3) / 1e9 / hbm},
+               "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"}
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -365,10 +389,8 @@ def run_ours(args, rank, world, local, pg):
         "kit_init_s": t_init,
         "gpu_launches": int(launches),
         "gpu_launches_per_step": launches / args.steps,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm, "traffic": None, "avg_launch_us": 1e3 * avg_ms,
-                     "launches_per_step": d_n / 2, "algorithmic_bytes_per_launch": bytes_launch,
-                     "work_per_launch": d_work / max(d_n, 1), "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "roofline": roof,
+        "roofline_tensor": roof_tc,
         "kernel_classes_ms_per_step": {n: v[0] / 2 for n, v in kt.items()},
         "kernel_classes_launches_per_step": {n: v[1] / 2 for n, v in kt.items()},
         "clocks": ck,

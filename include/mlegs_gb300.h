@@ -198,9 +198,11 @@ int mlg_adj_advection(mlg_scalar psi, mlg_scalar chi, mlg_scalar uz, mlg_scalar 
                       mlg_scalar psi_bar, mlg_scalar chi_bar);
 
 /* ---- kernel timing (CUDA events around each launch of one kernel class) ----------------- */
-/* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators and solves,
- *       3 = backward radial contraction, 4 = vec2tp projection contraction.  work = flops for the
- *       contractions, bytes moved for the others. */
+/* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators (applies and the
+ *       fused abcn right-hand side), 3 = backward radial contraction, 4 = vec2tp projection
+ *       contraction, 5 = banded solves (substitutions with cached factors).  work = flops for the
+ *       contractions, algorithmic bytes (each field read and written once, tables and factors read
+ *       once) for the others. */
 int mlg_kernel_timing(int enable);
 int mlg_kernel_timing_read(int kind, double* total_ms, long long* launches, double* flops_or_bytes);
 

@@ -971,6 +971,14 @@ static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsys, d
 }
 
 // kind as in SolveArgs; the band scratch grows to fit (kl, ku)
+// algorithmic bytes of one substitution pass over nrhs fields: each field read and written once, the
+// cached factors (FSL doubles per row and system) read once
+static double solve_bytes(int nrhs, const ChopIdx& c) {
+  double nsys = (double)std::max(c.npc, 1) * G.nzdim;
+  double rows = std::max(std::min(c.nrc, G.nrdim), 1);
+  return 2.0 * nrhs * G.fsize * 16 + rows * FSL * nsys * 8;
+}
+
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   int kl = 2, ku = 2;
@@ -994,7 +1002,7 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
   a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
   a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = beta; a.ell = G.ell; a.preln = preln;
   a.kind = kind; a.power = power; a.skip_root = 0; a.transpose = 0; a.no_ln = 0;
-  kt_begin(2);
+  kt_begin(KT_SOLVE);
   if (kind == 3) {
     k_band_solve<<<cdiv(nsys, 64), 64, 0, G.stream>>>(a);
     MLG_LAUNCH();
@@ -1020,7 +1028,7 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
       MLG_LAUNCH();
     }
   }
-  kt_end(2, 2.0 * G.fsize * 16);
+  kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
 }
 
@@ -1038,7 +1046,7 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = 0.0; a.ell = G.ell; a.preln = 0.0;
   a.kind = 0; a.power = 0; a.skip_root = 0; a.transpose = 0; a.no_ln = 0;
   a.e2 = s2.e; a.lnp2 = s2.ln;
-  kt_begin(2);
+  kt_begin(KT_SOLVE);
   double* fac = nullptr;
   MLG_TRY(lu_cache_get(0, alpha, c, nsys, &fac, [&](double* buf) -> int {
     k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
@@ -1049,7 +1057,7 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   MLG_CUDA(cudaFuncSetAttribute(k_band_subst<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
   k_band_subst<2><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
   MLG_LAUNCH();
-  kt_end(2, 4.0 * G.fsize * 16);
+  kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
 }
 
@@ -1131,7 +1139,7 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
   a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = 0.0; a.ell = G.ell; a.preln = 0.0;
   a.kind = kind; a.power = 0; a.skip_root = 0; a.transpose = 1; a.no_ln = 1;
-  kt_begin(2);
+  kt_begin(KT_SOLVE);
   double* fac = nullptr;
   MLG_TRY(lu_cache_get(kind + 8, alpha, c, nsys, &fac, [&](double* buf) -> int {
     k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
@@ -1142,7 +1150,7 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   MLG_CUDA(cudaFuncSetAttribute(k_band_subst<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
   k_band_subst<1><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
   MLG_LAUNCH();
-  kt_end(2, 2.0 * G.fsize * 16);
+  kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
 }
 

@@ -40,12 +40,12 @@ struct Scalar {
 struct ChopIdx { int nrc, npc, nzc, nzcu; };
 
 // kernel-time accounting per kernel class (mlg_kernel_timing)
-enum { KT_RFWD = 0, KT_FFT = 1, KT_BAND = 2, KT_RBWD = 3, KT_V2TP = 4, KT_N = 5 };
+enum { KT_RFWD = 0, KT_FFT = 1, KT_BAND = 2, KT_RBWD = 3, KT_V2TP = 4, KT_SOLVE = 5, KT_N = 6 };
 struct KTimer {
   bool on = false;
-  double ms[KT_N] = {0, 0, 0, 0, 0};
-  long long n[KT_N] = {0, 0, 0, 0, 0};
-  double work[KT_N] = {0, 0, 0, 0, 0};
+  double ms[KT_N] = {0, 0, 0, 0, 0, 0};
+  long long n[KT_N] = {0, 0, 0, 0, 0, 0};
+  double work[KT_N] = {0, 0, 0, 0, 0, 0};
 };
 
 struct Ctx {

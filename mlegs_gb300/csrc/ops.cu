@@ -1217,7 +1217,7 @@ int mlg_kernel_timing(int enable) {
   return 0;
 }
 int mlg_kernel_timing_read(int kind, double* ms, long long* n, double* work) {
-  if (kind < 0 || kind >= KT_N) return set_error(MLG_EPARAM, "mlg_kernel_timing_read: kind 0..4");
+  if (kind < 0 || kind >= KT_N) return set_error(MLG_EPARAM, "mlg_kernel_timing_read: kind 0..5");
   if (ms) *ms = G.kt.ms[kind];
   if (n) *n = G.kt.n[kind];
   if (work) *work = G.kt.work[kind];
