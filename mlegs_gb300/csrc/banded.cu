@@ -602,8 +602,9 @@ __global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restr
     }
     f[FKL * ns] = (double)p;
     f[(FKL + 1) * ns] = rp;
+    // U(j, j+c) / U(j, j): the back substitution then has one dependent FMA per row
 #pragma unroll
-    for (int c = 1; c < WC; ++c) f[(FKL + 1 + c) * ns] = W[0][c];
+    for (int c = 1; c < WC; ++c) f[(FKL + 1 + c) * ns] = W[0][c] * rp;
 #pragma unroll
     for (int t = 0; t < FKL; ++t) {
 #pragma unroll
@@ -635,9 +636,10 @@ template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.a
 // place on the column.  One warp = 32 systems; factor rows and right-hand-side values are staged into shared
 // memory SST groups ahead of use by cp.async, so DRAM latency overlaps the recurrences.
 constexpr int SGR = 8, SST = 3, SNU = FKL + FKU;
+static_assert(FKL == 2, "the substitution compares the pivot index by the high words of 1.0 and 2.0");
 template <int NR>
 struct SubstSmem {
-  double f[SST][SGR][SNU + 1][64];   // fwd: l1, l2, pivot; bwd: 1/U(j,j), U(j,j+1..j+4)
+  double f[SST][SGR][SNU + 1][64];   // fwd: l1, l2, pivot; bwd: 1/U(j,j), U(j,j+1..j+4)/U(j,j)
   double v[NR][SST][SGR][64];        // fwd: entering right-hand side; bwd: y(j)
 };
 
@@ -722,10 +724,11 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
       for (int u = 0; u < SGR; ++u) {
         int jr = g * SGR + u;
         if (!act || jr >= nn) break;
-        double pv = sm.f[st][u][FKL][th];
+        // the pivot row index p (0..FKL), stored as a double: compared by its high word, off the FP64 pipe
+        const int ph = __double2hiint(sm.f[st][u][FKL][th]);
 #pragma unroll
         for (int t = 1; t <= FKL; ++t)
-          if (pv == (double)t) {
+          if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) {
 #pragma unroll
             for (int q = 0; q < NR; ++q) { double w = r[q][0]; r[q][0] = r[q][t]; r[q][t] = w; }
           }
@@ -774,14 +777,13 @@ __global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __
       for (int u = 0; u < SGR; ++u) {
         int jr = nn - 1 - (g * SGR + u);
         if (!act || jr < 0) break;
-        double f0 = sm.f[st][u][0][th], f1 = sm.f[st][u][1][th], f2 = sm.f[st][u][2][th];
-        double f3 = sm.f[st][u][3][th], f4 = sm.f[st][u][4][th];
+        double f0 = sm.f[st][u][0][th], g1 = sm.f[st][u][1][th], g2 = sm.f[st][u][2][th];
+        double g3 = sm.f[st][u][3][th], g4 = sm.f[st][u][4][th];
 #pragma unroll
         for (int q = 0; q < NR; ++q) {
-          // y - U(j,j+1..j+4) . x(j+1..j+4), summed as a tree to shorten the dependency chain
-          double p1 = f1 * xs[q][0] + f2 * xs[q][1];
-          double p2 = f3 * xs[q][2] + f4 * xs[q][3];
-          double xj = (sm.v[q][st][u][th] - (p1 + p2)) * f0;
+          // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
+          double t = fma(-g4, xs[q][3], fma(-g3, xs[q][2], fma(-g2, xs[q][1], sm.v[q][st][u][th] * f0)));
+          double xj = fma(-g1, xs[q][0], t);
           x[q][2 * jr] = xj;
 #pragma unroll
           for (int c = SNU - 1; c >= 1; --c) xs[q][c] = xs[q][c - 1];
