@@ -90,18 +90,12 @@ struct TcSmem {
 
 // store the 8 values of one K group of one field row (n) as the three BF16 splits
 __device__ __forceinline__ void store_split8(uint8_t* b, int par, int n, int kg, const float* v) {
-  uint16_t h[3][8];
+  uint32_t w[4][3];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) split3(v[q], h[0][q], h[1][q], h[2][q]);
+  for (int q = 0; q < 4; ++q) split3x2(v[2 * q], v[2 * q + 1], w[q]);
 #pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    uint4 u;
-    u.x = (uint32_t)h[s][0] | ((uint32_t)h[s][1] << 16);
-    u.y = (uint32_t)h[s][2] | ((uint32_t)h[s][3] << 16);
-    u.z = (uint32_t)h[s][4] | ((uint32_t)h[s][5] << 16);
-    u.w = (uint32_t)h[s][6] | ((uint32_t)h[s][7] << 16);
-    *(uint4*)(b + (par * 3 + s) * TC_BTILE_BYTES + tc_off(n, kg * 8)) = u;
-  }
+  for (int s = 0; s < 3; ++s)
+    *(uint4*)(b + (par * 3 + s) * TC_BTILE_BYTES + tc_off(n, kg * 8)) = make_uint4(w[0][s], w[1][s], w[2][s], w[3][s]);
 }
 
 // the two-parity bf16x3 MMA group of one K chunk: D_par += A_par * B_par, six split products

@@ -22,11 +22,11 @@
 // With NS = 6 digits of w = 7 bits (6 when nr/2 > 173, keeping the orders exact) the term carries
 // 42 (36) bits.
 //
-// Engine: one CTA per (m, parity, 128-row tile, 16 complex z columns), 128 threads (warp = role in
-// the staging: ur, up, Re uz, Im uz), 66 KiB of shared memory and 256 TMEM columns.  Per K chunk of
+// Engine: one CTA per (m, parity, 128-row tile, 8 complex z columns), 128 threads (warp = role in
+// the staging: ur, up, Re uz, Im uz), 57 KiB of shared memory and 128 TMEM columns.  Per K chunk of
 // 16 radial points the table tiles (V, D splits and T digits, laid out at kit init in the UMMA
 // canonical K-major layout) arrive by one bulk copy on an mbarrier; the threads fold and split the
-// field operand; one thread issues 53 tcgen05.mma (M = 128, N = 32, K = 16).  Every wait is bounded.
+// field operand; one thread issues 53 tcgen05.mma (M = 128, N = 16, K = 16).  Every wait is bounded.
 #include "common.cuh"
 #include "tc_common.cuh"
 #include <cstdint>
@@ -34,7 +34,7 @@
 namespace mlg {
 
 constexpr int PV_KC = 16;                  // K chunk (radial points): one MMA K step
-constexpr int PV_NZ = 16;                  // complex z columns per CTA
+constexpr int PV_NZ = 8;                   // complex z columns per CTA
 constexpr int PV_N = 2 * PV_NZ;            // real columns (N of the MMA)
 constexpr int PV_NS = 6;                   // digits of the T term
 constexpr int PV_THREADS = 128;
@@ -44,10 +44,12 @@ __host__ __device__ constexpr int pv_off(int row, int k) {
   return (row >> 3) * PV_SBO + (k >> 3) * PV_LBO + (row & 7) * 16 + (k & 7) * 2;
 }
 constexpr int PV_ATILE = 128 * PV_KC * 2;  // 4 KiB
-constexpr int PV_BTILE = PV_N * PV_KC * 2; // 1 KiB
+constexpr int PV_BTILE = PV_N * PV_KC * 2; // 512 B
 constexpr int PV_NA = 6 + PV_NS;           // A tiles per chunk: V s0..2, D s0..2, T digits 0..5
 constexpr int PV_NB = 12 + PV_NS;          // B tiles: psi1 (3), psi2 (3), chi1 (3), chi2 (3), uz digits
-constexpr int PV_TMEM_COLS = 256;          // psi, chi, then the NS digit orders, N columns each
+constexpr int PV_TMEM_COLS = 128;          // psi, chi, then the NS digit orders, N columns each
+static_assert((2 + PV_NS) * PV_N <= PV_TMEM_COLS, "TMEM columns");
+constexpr int PV_KQ = PV_KC * PV_NZ / 32;  // consecutive K per staging item: 32 items per warp
 
 // the NS signed w-bit digits of x / 2^fexp (|x| < 2^fexp), most significant first, by integer ops
 __device__ __forceinline__ void pv_digits(double x, int fexp, int w, int* d) {
@@ -147,20 +149,14 @@ struct PvSmem {
   uint32_t tmem;
 };
 
-// 8 consecutive K of one B row as three BF16 splits into tiles t0, t0+1, t0+2
-__device__ __forceinline__ void pv_store_split8(uint8_t* b, int t0, int n, int kg, const float* v) {
-  uint16_t h[3][8];
+// PV_KQ consecutive K of one B row as three BF16 splits into tiles t0, t0+1, t0+2
+__device__ __forceinline__ void pv_store_split(uint8_t* b, int t0, int n, int kg, const float* v) {
+  static_assert(PV_KQ == 4, "staging items of 4 K");
+  uint32_t w[2][3];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) split3(v[q], h[0][q], h[1][q], h[2][q]);
+  for (int q = 0; q < 2; ++q) split3x2(v[2 * q], v[2 * q + 1], w[q]);
 #pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    uint4 u;
-    u.x = (uint32_t)h[s][0] | ((uint32_t)h[s][1] << 16);
-    u.y = (uint32_t)h[s][2] | ((uint32_t)h[s][3] << 16);
-    u.z = (uint32_t)h[s][4] | ((uint32_t)h[s][5] << 16);
-    u.w = (uint32_t)h[s][6] | ((uint32_t)h[s][7] << 16);
-    *(uint4*)(b + (t0 + s) * PV_BTILE + pv_off(n, kg * 8)) = u;
-  }
+  for (int s = 0; s < 3; ++s) *(uint2*)(b + (t0 + s) * PV_BTILE + pv_off(n, kg * PV_KQ)) = make_uint2(w[0][s], w[1][s]);
 }
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
@@ -236,16 +232,16 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
   }
   const uint32_t tmem = sm.tmem;
   // staging role of this warp: 0 ur, 1 up, 2 Re uz, 3 Im uz; lane: z column zz, K group kg (8 K)
-  const int role = warp, zz = lane & (PV_NZ - 1), kg = lane >> 4;
+  const int role = warp, zz = lane % PV_NZ, kg = lane / PV_NZ;
   const int z = z0 + zz;
   const bool zok = z < nzdim;
   const size_t cbase = (size_t)nrdim * (m + (size_t)npdim * (zok ? z : 0));
-  float2 fa[8], fb[8];   // roles 0, 1: the two halves of ur / up (FP32)
-  double da[8], db[8];   // roles 2, 3: the two halves of the uz component (FP64)
+  float2 fa[PV_KQ], fb[PV_KQ];   // roles 0, 1: the two halves of ur / up (FP32)
+  double da[PV_KQ], db[PV_KQ];   // roles 2, 3: the two halves of the uz component (FP64)
   auto fetch = [&](int kc) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      int i = kc * PV_KC + kg * 8 + q;
+    for (int q = 0; q < PV_KQ; ++q) {
+      int i = kc * PV_KC + kg * PV_KQ + q;
       bool ok = zok && i < nrh;
       if (role < 2) {
         const double2* src = role == 0 ? ur : up;
@@ -268,9 +264,9 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
       bulk_g2s(sm.a, img_b + (size_t)kc * (PV_NA * PV_ATILE), PV_NA * PV_ATILE, &sm.bar_a);
     }
     if (role < 2) {
-      float v0[8], v1[8], v2[8], v3[8];
+      float v0[PV_KQ], v1[PV_KQ], v2[PV_KQ], v3[PV_KQ];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
+      for (int q = 0; q < PV_KQ; ++q) {
         float2 fs = make_float2(fa[q].x + ss * fb[q].x, fa[q].y + ss * fb[q].y);
         float2 fo = make_float2(fa[q].x - ss * fb[q].x, fa[q].y - ss * fb[q].y);
         if (role == 0) {   // psi1 = -i F_s(ur): columns (re, im) = (Im, -Re); chi1 = i F_o(ur): (-Im, Re)
@@ -282,31 +278,26 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
         }
       }
       const int tp = role == 0 ? 0 : 3, tc = role == 0 ? 6 : 9;
-      pv_store_split8(sm.b, tp, 2 * zz, kg, v0);
-      pv_store_split8(sm.b, tp, 2 * zz + 1, kg, v1);
-      pv_store_split8(sm.b, tc, 2 * zz, kg, v2);
-      pv_store_split8(sm.b, tc, 2 * zz + 1, kg, v3);
+      pv_store_split(sm.b, tp, 2 * zz, kg, v0);
+      pv_store_split(sm.b, tp, 2 * zz + 1, kg, v1);
+      pv_store_split(sm.b, tc, 2 * zz, kg, v2);
+      pv_store_split(sm.b, tc, 2 * zz + 1, kg, v3);
     } else {
       const int n = 2 * zz + (role - 2);
       const int fe = sm.fexp[n];
-      uint16_t h[PV_NS][8];
+      uint32_t h[PV_NS][PV_KQ];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
+      for (int q = 0; q < PV_KQ; ++q) {
         double f = ss > 0.f ? da[q] + db[q] : da[q] - db[q];   // F_s(uz), FP64
         int dg[PV_NS];
         pv_digits(f, fe, w, dg);
 #pragma unroll
-        for (int s = 0; s < PV_NS; ++s) h[s][q] = bf16_rn((float)dg[s]);
+        for (int s = 0; s < PV_NS; ++s) h[s][q] = bf16_small_int(dg[s]);
       }
 #pragma unroll
-      for (int s = 0; s < PV_NS; ++s) {
-        uint4 u;
-        u.x = (uint32_t)h[s][0] | ((uint32_t)h[s][1] << 16);
-        u.y = (uint32_t)h[s][2] | ((uint32_t)h[s][3] << 16);
-        u.z = (uint32_t)h[s][4] | ((uint32_t)h[s][5] << 16);
-        u.w = (uint32_t)h[s][6] | ((uint32_t)h[s][7] << 16);
-        *(uint4*)(sm.b + (12 + s) * PV_BTILE + pv_off(n, kg * 8)) = u;
-      }
+      for (int s = 0; s < PV_NS; ++s)
+        *(uint2*)(sm.b + (12 + s) * PV_BTILE + pv_off(n, kg * PV_KQ)) =
+            make_uint2(h[s][0] | (h[s][1] << 16), h[s][2] | (h[s][3] << 16));
     }
     fence_async_smem();
     __syncthreads();
