@@ -244,6 +244,130 @@ int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, 
   return 0;
 }
 
+// dst = scale * band(src), out of place: the same values as copying src to dst, applying the band
+// operator in place and multiplying dst by scale (dst%ln = 0), in one pass over every column
+template <typename T>
+__global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __restrict__ src, const double* __restrict__ lnsrc,
+                                double* __restrict__ lndst, const double* __restrict__ bd2, const double* __restrict__ bxx,
+                                const double* __restrict__ ak, const double* __restrict__ lognorm, int op, int nrdim, int npdim,
+                                int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell, double scale) {
+  extern __shared__ __align__(16) unsigned char bat_smem[];
+  double2* sv = (double2*)bat_smem;   // the column, then its band product on the active rows (FP64)
+  int m = blockIdx.y, k = blockIdx.x;
+  int nn = max(min(nrc, nrc - m), 0);
+  int cnt = k_count(k, nzc, nzcu, nzdim);
+  size_t off = (size_t)nrdim * (m + (size_t)npdim * k);
+  bool lnblk = (m == 0 && k == 0);
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) sv[i] = src[off + i];
+  __syncthreads();
+  if (m < npc && nn > 0 && cnt > 0) {
+    if (m == 0) {
+      double2* c0 = sv;
+      double2* c1 = sv + nrdim;
+      double akv2 = ak[k] * ak[k];
+      for (int rep = 0; rep < cnt; ++rep) {
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          double2 acc; acc.x = 0; acc.y = 0;
+          if (op == 0) {
+            const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
+            if (i - 1 >= 0) { double v = b[0]; acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+            if (i + 1 < nn) { double v = b[2]; acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
+          } else {
+            const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+              int j = i - 2 + c;
+              if (j < 0 || j >= nn) continue;
+              double v = b[c];
+              if (c == 2 && op == 2) v = v - akv2;
+              acc.x += v * c0[j].x;
+              acc.y += v * c0[j].y;
+            }
+          }
+          c1[i] = acc;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
+        __syncthreads();
+      }
+    } else {
+      typedef typename BC<T>::C C;
+      C* c0 = (C*)(sv + 2 * nrdim);
+      C* c1 = c0 + nrdim;
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(sv + i);
+      __syncthreads();
+      T akv2 = BC<T>::cv(ak[k] * ak[k]);
+      for (int rep = 0; rep < cnt; ++rep) {
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          C acc; acc.x = 0; acc.y = 0;
+          if (op == 0) {
+            const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
+            if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+            if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
+          } else {
+            const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+              int j = i - 2 + c;
+              if (j < 0 || j >= nn) continue;
+              T v = BC<T>::cv(b[c]);
+              if (c == 2 && op == 2) v = v - akv2;
+              acc.x += v * c0[j].x;
+              acc.y += v * c0[j].y;
+            }
+          }
+          c1[i] = acc;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
+        __syncthreads();
+      }
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(sv + i, c0[i]);
+    }
+    __syncthreads();
+  }
+  if (lnblk && threadIdx.x == 0) {
+    double lnin = *lnsrc;
+    double e2 = ell * ell;
+    if (op == 0) {   // (:452-456)
+      sv[0].x += 1.0 / exp(lognorm[0]) * lnin;
+      sv[1].x += 1.0 / exp(lognorm[1]) * lnin;
+    } else {         // (:506-511, :561-566)
+      sv[0].x += 4.0 / 3.0 / e2 / exp(lognorm[0]) * lnin;
+      sv[1].x -= 2.0 / 1.0 / e2 / exp(lognorm[1]) * lnin;
+      sv[2].x += 2.0 / 3.0 / e2 / exp(lognorm[2]) * lnin;
+    }
+    *lndst = 0.0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
+    double2 v = sv[i];
+    if (scale != 1.0) v = make_double2(0.0 + scale * v.x, 0.0 + scale * v.y);
+    dst[off + i] = v;
+  }
+}
+
+int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  dim3 grid(G.nzdim, G.npdim);
+  size_t sm = 4ull * G.nrdim * sizeof(double2);
+  kt_begin(KT_BAND);
+  if (G.precision == MLG_MIXED) {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply_to<float><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, G.bd2, G.bxx, G.ak, G.lognorm, op,
+                                                        G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
+                                                        scale);
+  } else {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply_to<double><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, G.bd2, G.bxx, G.ak, G.lognorm, op,
+                                                         G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
+                                                         scale);
+  }
+  MLG_LAUNCH();
+  kt_end(KT_BAND, 2.0 * G.fsize * 16);
+  return 0;
+}
+
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   dim3 grid(G.nzdim, std::max(c.npc, 1));

@@ -121,6 +121,7 @@ int chop_index(const Scalar& s, ChopIdx& c);
 int kit_build(const mlg_params* p);
 int kit_free();
 int launch_hfft(Scalar& s, int dir);             // dir -1 forward (1/np), +1 backward
+int launch_hfft_rs(Scalar& s, int dir, const double* rs);   // with the rows times rs (before fwd / after bwd)
 int launch_vfft(Scalar& s, int dir);             // dir -1 forward (1/nz), +1 backward
 int launch_vfft_buf(cd* e, int dir);
 int launch_vfft_scaled(cd* e, int dir, double scale);
@@ -182,6 +183,7 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
                        Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
+int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale);
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
 int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha);

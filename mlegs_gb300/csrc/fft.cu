@@ -153,7 +153,7 @@ __global__ void k_vfft(double2* __restrict__ e, int nrdim, int npdim, int L, int
 template <typename T>
 __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
                            const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, T scale,
-                           double scale_d, double inv_np) {
+                           double scale_d, double inv_np, const double* __restrict__ rs, int nrs) {
   typedef typename CT<T>::t C;
   constexpr bool DC = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -164,12 +164,13 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   int z = blockIdx.y;
   bool ok = r < nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
+  const double rv = (rs != nullptr && ok && r < nrs) ? rs[r] : 1.0;   // scale_r of the input row
   double sum = 0.0, mu = 0.0;
   if (DC) {
     double* red = (double*)(s1 + (size_t)L * TR);
     double part = 0.0;
     if (ok)
-      for (int pt = tt; pt < L; pt += TT) { double2 v = base[(size_t)pt * nrdim]; part += v.x + v.y; }
+      for (int pt = tt; pt < L; pt += TT) { double2 v = base[(size_t)pt * nrdim]; part += v.x * rv + v.y * rv; }
     red[tt * TR + tr] = part;
     __syncthreads();
     for (int q = 0; q < TT; ++q) sum += red[q * TR + tr];
@@ -180,9 +181,10 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
     if (ok) {
       if (DC) {
         double2 d = base[(size_t)pt * nrdim];
-        v = mk<T>((T)d2f_fast(d.x - mu), (T)d2f_fast(d.y - mu));
+        v = mk<T>((T)d2f_fast(d.x * rv - mu), (T)d2f_fast(d.y * rv - mu));
       } else {
-        v = ld<T>(base + (size_t)pt * nrdim);
+        double2 d = base[(size_t)pt * nrdim];
+        v = mk<T>((T)(d.x * rv), (T)(d.y * rv));
       }
     }
     s0[pt * TR + tr] = v;
@@ -212,7 +214,8 @@ __global__ void k_hfft_fwd(double2* __restrict__ e, int nrdim, int npdim, int L,
 // form: Re X_0 is left out of the FP32 FFT and added to every sample in FP64.
 template <typename T>
 __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L, int TR,
-                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, double np_d) {
+                           const typename TW<T>::t* __restrict__ tw, const typename TW<T>::t* __restrict__ twr, double np_d,
+                           const double* __restrict__ rs, int nrs) {
   typedef typename CT<T>::t C;
   constexpr bool DC = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -246,15 +249,15 @@ __global__ void k_hfft_bwd(double2* __restrict__ e, int nrdim, int npdim, int L,
   C* res;
   stockham<T>(s0, s1, &res, L, TR, tr, tt, TT, tw, +1);
   if (!ok) return;
+  const double rv = (rs != nullptr && r < nrs) ? rs[r] : 1.0;   // scale_r of the output row
   for (int pt = tt; pt < L; pt += TT) {
-    if (DC) {
-      C y = res[pt * TR + tr];
-      base[(size_t)pt * nrdim] = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
-    } else {
-      st<T>(base + (size_t)pt * nrdim, res[pt * TR + tr]);
-    }
+    C y = res[pt * TR + tr];
+    double2 v;
+    if (DC) v = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+    else v = make_double2((double)y.x, (double)y.y);
+    base[(size_t)pt * nrdim] = make_double2(v.x * rv, v.y * rv);
   }
-  if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
+  if (tt == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d * rv, nyq.y * np_d * rv);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -382,7 +385,8 @@ template <typename T, int L, int TRL>
 __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __restrict__ e, int nrdim, int npdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
                                                                   const typename TW<T>::t* __restrict__ twr, T scale,
-                                                                  double scale_d, double inv_np) {
+                                                                  double scale_d, double inv_np,
+                                                                  const double* __restrict__ rs, int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
   constexpr bool DC = std::is_same<T, float>::value;
@@ -394,6 +398,8 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
   int z = blockIdx.y;
   bool ok = r < nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
+  const bool rsc = rs != nullptr && ok && r < nrs;   // the row's samples times rs[r] first (scale_r)
+  const double rv = rsc ? rs[r] : 1.0;
   C a[R1];
   double sum = 0.0;
   if (DC) {
@@ -402,6 +408,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       d[n1] = ok ? base[(size_t)(w + R2 * n1) * nrdim] : make_double2(0.0, 0.0);
+      if (rsc) { d[n1].x *= rv; d[n1].y *= rv; }
       part += d[n1].x + d[n1].y;
     }
     red[w * TRL + lane] = part;
@@ -413,7 +420,14 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
     for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>((T)d2f_fast(d[n1].x - mu), (T)d2f_fast(d[n1].y - mu));
   } else {
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * nrdim) : mk<T>(0, 0);
+    for (int n1 = 0; n1 < R1; ++n1) {
+      if (rsc) {
+        double2 d = base[(size_t)(w + R2 * n1) * nrdim];
+        a[n1] = mk<T>((T)(d.x * rv), (T)(d.y * rv));
+      } else {
+        a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * nrdim) : mk<T>(0, 0);
+      }
+    }
   }
   C b[Q][R2];
   fft2pass<T, L, -1, TRL>(a, b, S, tw, w, lane);
@@ -445,7 +459,8 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
 template <typename T, int L, int TRL>
 __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __restrict__ e, int nrdim, int npdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
-                                                                  const typename TW<T>::t* __restrict__ twr, double np_d) {
+                                                                  const typename TW<T>::t* __restrict__ twr, double np_d,
+                                                                  const double* __restrict__ rs, int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
   constexpr bool DC = std::is_same<T, float>::value;
@@ -480,6 +495,8 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __res
   C b[Q][R2];
   fft2pass<T, L, +1, TRL>(a, b, S, tw, w, lane);
   if (!ok) return;
+  const bool rsc = rs != nullptr && r < nrs;   // every slot of the row times rs[r] last (scale_r)
+  const double rv = rsc ? rs[r] : 1.0;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     int k1 = w * Q + q;
@@ -487,11 +504,18 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __res
     for (int i = 0; i < R2; ++i) {
       C y = b[q][i];
       double2* o = base + (size_t)(k1 + R1 * bitrev(i, R2)) * nrdim;
-      if (DC) *o = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
-      else st<T>(o, y);
+      double2 v;
+      if (DC) v = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+      else v = make_double2((double)y.x, (double)y.y);
+      if (rsc) { v.x *= rv; v.y *= rv; }
+      *o = v;
     }
   }
-  if (w == 0) base[(size_t)L * nrdim] = make_double2(nyq.x * np_d, nyq.y * np_d);
+  if (w == 0) {
+    double2 v = make_double2(nyq.x * np_d, nyq.y * np_d);
+    if (rsc) { v.x *= rv; v.y *= rv; }
+    base[(size_t)L * nrdim] = v;
+  }
 }
 
 template <typename T> const typename TW<T>::t* tw_of(const double2* d, const float2* f);
@@ -574,7 +598,7 @@ int launch_vfft_scaled(cd* e, int dir, double scale) { return vfft_any(e, dir, s
 int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
 
 template <typename T, int L>
-static int pfft2_launch(cd* e, int dir, double scale) {
+static int pfft2_launch(cd* e, int dir, double scale, const double* rs) {
   constexpr int TRL = 32;
   constexpr bool DC = std::is_same<T, float>::value;
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t) + (DC && dir < 0 ? (size_t)Split<L>::R2 * TRL * sizeof(double) : 0);
@@ -582,28 +606,29 @@ static int pfft2_launch(cd* e, int dir, double scale) {
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_pfft_fwd2<T, L, TRL>, sm));
     k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np);
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np, rs,
+                                                        G.nr);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_pfft_bwd2<T, L, TRL>, sm));
     k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np);
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, rs, G.nr);
   }
   MLG_LAUNCH();
   return 0;
 }
 
 template <typename T>
-static int hfft_t(cd* e, int dir, double scale) {
+static int hfft_t(cd* e, int dir, double scale, const double* rs = nullptr) {
   int L = G.nph;
   if (G.np <= 1) return 0;
   kt_begin(1);
   if (pow2_fast(L)) {
     switch (L) {
-      case 16: MLG_TRY((pfft2_launch<T, 16>(e, dir, scale))); break;
-      case 32: MLG_TRY((pfft2_launch<T, 32>(e, dir, scale))); break;
-      case 64: MLG_TRY((pfft2_launch<T, 64>(e, dir, scale))); break;
-      case 128: MLG_TRY((pfft2_launch<T, 128>(e, dir, scale))); break;
-      case 256: MLG_TRY((pfft2_launch<T, 256>(e, dir, scale))); break;
+      case 16: MLG_TRY((pfft2_launch<T, 16>(e, dir, scale, rs))); break;
+      case 32: MLG_TRY((pfft2_launch<T, 32>(e, dir, scale, rs))); break;
+      case 64: MLG_TRY((pfft2_launch<T, 64>(e, dir, scale, rs))); break;
+      case 128: MLG_TRY((pfft2_launch<T, 128>(e, dir, scale, rs))); break;
+      case 256: MLG_TRY((pfft2_launch<T, 256>(e, dir, scale, rs))); break;
     }
     kt_end(1, 2.0 * G.fsize * 16);
     return 0;
@@ -617,22 +642,25 @@ static int hfft_t(cd* e, int dir, double scale) {
     MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
     k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
                                                 tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale,
-                                                scale, 1.0 / G.np);
+                                                scale, 1.0 / G.np, rs, G.nr);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
     k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np);
+                                                tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, rs, G.nr);
   }
   MLG_LAUNCH();
   kt_end(1, 2.0 * G.fsize * 16);
   return 0;
 }
 
-int launch_hfft(Scalar& s, int dir) {
+int launch_hfft(Scalar& s, int dir) { return launch_hfft_rs(s, dir, nullptr); }
+// with rs: the rows i < nr of the field times rs[i] before the forward transform / after the
+// backward one (scale_r folded into the transform)
+int launch_hfft_rs(Scalar& s, int dir, const double* rs) {
   if (G.npchop + s.off[1] > G.npdim)
     return set_error(MLG_ECHOP, dir < 0 ? "horizontal_fft_forward: chopping in p too large"
                                         : "horizontal_fft_fbackard: chopping in p too large");
-  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir, 1.0 / G.np) : hfft_t<double>(s.e, dir, 1.0 / G.np);
+  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir, 1.0 / G.np, rs) : hfft_t<double>(s.e, dir, 1.0 / G.np, rs);
 }
 // the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs)
 int launch_hfft_fwd_scaled(cd* e, double scale) {

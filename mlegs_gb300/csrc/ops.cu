@@ -206,9 +206,11 @@ __global__ void k_scale_r(double2* __restrict__ e, const double* __restrict__ r,
 }
 
 // vecprod (mlegs_scalar_ops.f90:1264-1306) on the packed reals; everything else zero
+// v x u on the packed samples; vzb (optional): a field added to vz first (the background axial flow of
+// advection_rhs, vortical_flow_3d.f90:371, with the rounding of that separate addition)
 __global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, double2* __restrict__ vz,
                           const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
-                          int nr, int nph, int nrdim, int npdim, int nzdim) {
+                          const double2* __restrict__ vzb, int nr, int nph, int nrdim, int npdim, int nzdim) {
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
@@ -216,6 +218,7 @@ __global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, do
     double2 o1 = make_double2(0, 0), o2 = o1, o3 = o1;
     if (i < nr && m < nph) {
       double2 A1 = vr[idx], A2 = vp[idx], A3 = vz[idx], B1 = ur[idx], B2 = up[idx], B3 = uz[idx];
+      if (vzb) { double2 b = vzb[idx]; A3 = make_double2(A3.x + b.x, A3.y + b.y); }
       o1 = make_double2(A2.x * B3.x - A3.x * B2.x, A2.y * B3.y - A3.y * B2.y);
       o2 = make_double2(A3.x * B1.x - A1.x * B3.x, A3.y * B1.y - A1.y * B3.y);
       o3 = make_double2(A1.x * B2.x - A2.x * B1.x, A1.y * B2.y - A2.y * B1.y);
@@ -792,13 +795,18 @@ static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar
 
 // ------------------------------------------------------------------------------------------------
 // vector fields (:1264-1560)
-int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
+static int vecprod_bg(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz,
+                      const Scalar* vzb) {
   for (const Scalar* q : {(const Scalar*)&vr, (const Scalar*)&vp, (const Scalar*)&vz, &ur, &up, &uz})
     if (!q->is("PPP")) return set_error(MLG_ESPACE, "vector_product: to compute v x u, all inputs must be in PPP");
-  k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
+  k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, vzb ? vzb->e : nullptr, G.nr,
+                                                 G.np / 2, G.nrdim, G.npdim, G.nzdim);
   MLG_LAUNCH();
   for (Scalar* q : {&vr, &vp, &vz}) { MLG_TRY(launch_set_ln(q->ln, 0.0)); q->off[0] = q->off[1] = q->off[2] = 0; }
   return 0;
+}
+int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
+  return vecprod_bg(vr, vp, vz, ur, up, uz, nullptr);
 }
 
 int scale_r(Scalar& s, int mode) {
@@ -809,16 +817,17 @@ int scale_r(Scalar& s, int mode) {
 }
 
 
-int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi) {
-  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
-  if (!psi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
-  if (!chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: chi must be in FFF");
-  TMP(ur); TMP(up); TMP(uz);
-  MLG_TRY(assign(ur, vr)); MLG_TRY(assign(up, vp)); MLG_TRY(assign(uz, vz));
-  MLG_TRY(scale_r(ur, 0)); MLG_TRY(scale_r(up, 0));
-  MLG_TRY(op_trans(ur, "PFP"));
+// vector_projection on (ur, up, uz) PPP fields that it may overwrite (the caller's copies or its own
+// temporaries): r*ur, r*up enter the φ transforms (scale_r folded into them)
+static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& chi) {
+  if (G.np > 1) MLG_TRY(launch_hfft_rs(ur, -1, G.r));
+  else MLG_TRY(scale_r(ur, 0));
+  ur.set_space("PFP");
   if (G.nz > 1) MLG_TRY(vfft_checked(ur, -1));
   ur.set_space("PFF");
+  if (G.np > 1) MLG_TRY(launch_hfft_rs(up, -1, G.r));
+  else MLG_TRY(scale_r(up, 0));
+  up.set_space("PFP");
   MLG_TRY(op_trans(up, "FFF"));
   MLG_TRY(calcat_dev(up, G.at1, false));
   k_set_ln_from_calc<<<1, 32, 0, G.stream>>>(psi.ln, (const double2*)(G.dscal + DS_CALC), -1.0 / 2.0);
@@ -843,6 +852,20 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
   return 0;
 }
 
+static int vec2tp_check(const Scalar& vr, const Scalar& vp, const Scalar& vz, const Scalar& psi, const Scalar& chi) {
+  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
+  if (!psi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
+  if (!chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: chi must be in FFF");
+  return 0;
+}
+
+int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi) {
+  MLG_TRY(vec2tp_check(vr, vp, vz, psi, chi));
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(assign(ur, vr)); MLG_TRY(assign(up, vp)); MLG_TRY(assign(uz, vz));
+  return vec2tp_core(ur, up, uz, psi, chi);
+}
+
 // combination step of vector_reconstruction (:1488-1502)
 __global__ void k_tp2vec_mix(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
                              const double2* __restrict__ uz, const double* __restrict__ ak, int nrdim, int npdim, int nzdim,
@@ -864,39 +887,56 @@ __global__ void k_tp2vec_mix(double2* __restrict__ ur, double2* __restrict__ up,
   }
 }
 
-int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scalar& vz) {
-  if (!psi.is("FFF") || !chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
-  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
-  TMP(ur); TMP(up); TMP(uz);
-  MLG_TRY(assign(ur, chi)); ur.off[0] = 3; ur.off[1] = ur.off[2] = 0;
-  MLG_TRY(assign(up, psi)); up.off[0] = 3; up.off[1] = up.off[2] = 0;
-  MLG_TRY(assign(uz, chi)); uz.off[0] = 3; uz.off[1] = uz.off[2] = 0;
+// vector_reconstruction into (ur, up, uz), none of them aliasing psi or chi: they are the workspace
+// (the same steps as copying chi / psi into temporaries and the temporaries into the outputs)
+static int tp2vec_into(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
+  for (Scalar* q : {&ur, &up, &uz}) { q->set_space("FFF"); q->off[0] = 3; q->off[1] = q->off[2] = 0; }
   ChopIdx c;
   MLG_TRY(chop_index(ur, c));
-  MLG_TRY(op_band(ur, 0));
-  MLG_TRY(op_band(up, 0));
-  k_tp2vec_mix<<<nblk(G.fsize), 256, 0, G.stream>>>(ur.e, up.e, psi.e, uz.e, G.ak, G.nrdim, G.npdim, G.nzdim, c.nrc, c.npc,
+  MLG_TRY(launch_band_apply_to(ur, chi, 0, c, 1.0));    // r d/dr chi
+  MLG_TRY(launch_band_apply_to(up, psi, 0, c, 1.0));    // r d/dr psi
+  k_tp2vec_mix<<<nblk(G.fsize), 256, 0, G.stream>>>(ur.e, up.e, psi.e, chi.e, G.ak, G.nrdim, G.npdim, G.nzdim, c.nrc, c.npc,
                                                      c.nzc, c.nzcu);
   MLG_LAUNCH();
   ur.off[0] = 0; up.off[0] = 0;
   MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
-  MLG_TRY(op_trans(ur, "PPP")); MLG_TRY(op_trans(up, "PPP"));
-  MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
-  MLG_TRY(op_band(uz, 1));
-  MLG_TRY(lincomb(uz, {{&uz, -1.0}}, {}, 1.0, false));
+  // to PPP, the last φ transform dividing by r (scale_r folded into it)
+  for (Scalar* q : {&ur, &up}) {
+    MLG_TRY(op_trans(*q, "PFP"));
+    if (G.np > 1) MLG_TRY(launch_hfft_rs(*q, +1, G.rinv));
+    else MLG_TRY(scale_r(*q, 1));
+    q->set_space("PPP");
+  }
+  MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0));   // -del2h chi
   uz.off[0] = 0;
   MLG_TRY(op_chop(uz));
   MLG_TRY(op_trans(uz, "PPP"));
+  return 0;
+}
+
+static bool aliases(const Scalar& a, const Scalar& b) { return a.e == b.e; }
+
+int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scalar& vz) {
+  if (!psi.is("FFF") || !chi.is("FFF")) return set_error(MLG_ESPACE, "vector_projection: psi must be in FFF");
+  if (!vr.is("PPP") || !vp.is("PPP") || !vz.is("PPP")) return set_error(MLG_ESPACE, "vector_projection: vr must be in PPP");
+  bool alias = false;
+  for (const Scalar* o : {&vr, &vp, &vz})
+    for (const Scalar* i : {&psi, &chi}) alias = alias || aliases(*o, *i);
+  alias = alias || aliases(vr, vp) || aliases(vr, vz) || aliases(vp, vz);
+  if (!alias) return tp2vec_into(psi, chi, vr, vp, vz);
+  TMP(ur); TMP(up); TMP(uz);
+  MLG_TRY(tp2vec_into(psi, chi, ur, up, uz));
   MLG_TRY(assign(vr, ur)); MLG_TRY(assign(vp, up)); MLG_TRY(assign(vz, uz));
   return 0;
 }
 
 int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, Scalar& wz) {
   TMP(md);
-  MLG_TRY(assign(md, chi));
   md.set_space("FFF");
-  MLG_TRY(op_band(md, 2));
-  MLG_TRY(lincomb(md, {{&md, -1.0}}, {}, 1.0, false));
+  md.off[0] = chi.off[0]; md.off[1] = chi.off[1]; md.off[2] = chi.off[2];
+  ChopIdx c;
+  MLG_TRY(chop_index(md, c));
+  MLG_TRY(launch_band_apply_to(md, chi, 2, c, -1.0));   // md = -del2 chi
   return op_tp2vec(md, psi, wr, wp, wz);
 }
 
@@ -906,11 +946,11 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
     return set_error(MLG_ESPACE, "advection_rhs: psi, chi, nlpsi, nlchi must be in FFF and uz in PPP");
   MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
   TMP(vr); TMP(vp); TMP(vz); TMP(wr); TMP(wp); TMP(wz);
-  MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
-  MLG_TRY(lincomb(vz, {{&vz, 1.0}, {&uz, 1.0}}, {}, 1.0, false));
+  for (Scalar* q : {&vr, &vp, &vz, &wr, &wp, &wz}) q->set_space("PPP");
+  MLG_TRY(tp2vec_into(psi, chi, vr, vp, vz));
   MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
-  MLG_TRY(op_vecprod(vr, vp, vz, wr, wp, wz));
-  MLG_TRY(op_vec2tp(vr, vp, vz, nlpsi, nlchi));
+  MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz));   // (vz + uz) with the background flow
+  MLG_TRY(vec2tp_core(vr, vp, vz, nlpsi, nlchi));
   MLG_TRY(launch_set_ln(nlpsi.ln, 0.0)); MLG_TRY(launch_set_ln(nlchi.ln, 0.0));
   MLG_TRY(op_dealias(nlpsi)); MLG_TRY(op_dealias(nlchi));
   return 0;
