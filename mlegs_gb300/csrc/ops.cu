@@ -240,22 +240,26 @@ __device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, doubl
   double kv = (gk >= 1 && gk <= nak) ? fabs(ak[k]) : 0.0;
   return fmin(1.0, kv / kmax);
 }
+// per block: the energy of the head and of the tail (q >= cutoff) of the spectrum (:112-117).  The q
+// are in [0, 1], so q >= cutoff is compared on the FP64 bit patterns; the sums stay FP64.
 __global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ qt,
-                           double cutoff, double* __restrict__ partial) {
+                           unsigned long long cbits, double* __restrict__ partial) {
   __shared__ double s0[256], s1[256];
+  const unsigned long long* qb = reinterpret_cast<const unsigned long long*>(qt);
   size_t n = (size_t)nrdim * npdim * nzdim;
-  double tot = 0, tail = 0;
+  double head = 0, tail = 0;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
     int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
     int k = (int)(idx / (unsigned)(nrdim * npdim));
     double2 v = e[idx];
     double a2 = v.x * v.x + v.y * v.y;
-    tot += a2;
-    double q = fmin(1.0, fmax(qt[i], fmax(qt[nrdim + m], qt[nrdim + npdim + k])));
-    if (q >= cutoff) tail += a2;
+    unsigned long long b = qb[i], bm = qb[nrdim + m], bk = qb[nrdim + npdim + k];
+    b = b > bm ? b : bm;
+    b = b > bk ? b : bk;
+    if (b >= cbits) tail += a2; else head += a2;
   }
-  s0[threadIdx.x] = tot; s1[threadIdx.x] = tail;
+  s0[threadIdx.x] = head; s1[threadIdx.x] = tail;
   __syncthreads();
   for (int o = blockDim.x / 2; o; o >>= 1) {
     if (threadIdx.x < o) { s0[threadIdx.x] += s0[threadIdx.x + o]; s1[threadIdx.x] += s1[threadIdx.x + o]; }
@@ -263,33 +267,44 @@ __global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, 
   }
   if (threadIdx.x == 0) { partial[2 * blockIdx.x] = s0[0]; partial[2 * blockIdx.x + 1] = s1[0]; }
 }
-// gain relaxation and strength (:119-126); st[0] = strength (0: nothing to do); then the 1-D factor
-// tables ft[0..nrdim) (n), ft[nrdim..+npdim) (m), ft[..+nzdim) (k): exp(-s*shape^8) where q > cutoff, 1 elsewhere
-__global__ void k_svv_gain(const double* __restrict__ partial, int nb, double* __restrict__ gain, double* __restrict__ st,
-                           double target, double relax, double strength_max, double* __restrict__ ft, int nrdim, int npdim,
-                           int nzdim, int nrchop, int np, double kmax, const double* __restrict__ ak, double cutoff) {
+// gain relaxation and strength (:119-126) and the 1-D factor tables ft[0..nrdim) (n), ft[nrdim..+npdim)
+// (m), ft[..+nzdim) (k): exp(-s*shape^8) where q > cutoff, 1 elsewhere.  Every block reduces the
+// partial sums (a tree over its threads) and fills its share of the tables; block 0 stores the
+// strength in st[0] and the new gain in st[1] (copied to the gain by k_svv_apply: no block may see
+// a half-updated gain)
+__global__ void k_svv_gain(const double* __restrict__ partial, int nb, const double* __restrict__ gain,
+                           double* __restrict__ st, double target, double relax, double strength_max,
+                           double* __restrict__ ft, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
+                           const double* __restrict__ ak, double cutoff) {
+  __shared__ double r0[256], r1[256];
   __shared__ double str;
+  double h = 0, t = 0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) { h += partial[2 * b]; t += partial[2 * b + 1]; }
+  r0[threadIdx.x] = h; r1[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if (threadIdx.x < o) { r0[threadIdx.x] += r0[threadIdx.x + o]; r1[threadIdx.x] += r1[threadIdx.x + o]; }
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    double tot = 0, tail = 0;
-    for (int b = 0; b < nb; ++b) { tot += partial[2 * b]; tail += partial[2 * b + 1]; }
-    double sv = 0.0;
+    double tail = r1[0], tot = r0[0] + tail;
+    double g = *gain, sv = 0.0;
     if (tot > 2.2250738585072014e-308) {
       double ratio = tail / tot;
       double fb = fmin(fmax(ratio / target - 1.0, 0.0), 1.0);
       double rl = fmin(fmax(relax, 0.0), 1.0);
-      double g = (1.0 - rl) * (*gain) + rl * fb;
-      *gain = g;
+      g = (1.0 - rl) * g + rl * fb;
       sv = fmin(fmax(strength_max, 0.0) * g, 1.0);
     }
-    st[0] = sv;
+    if (blockIdx.x == 0) { st[0] = sv; st[1] = g; }
     str = sv;
   }
   __syncthreads();
   double sv = str;
   int ntot = nrdim + npdim + nzdim;
-  for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-    double q = (t < nrdim) ? svv_qr(t, nrchop) : (t < nrdim + npdim) ? svv_qp(t - nrdim, np)
-                                                                       : svv_qz(t - nrdim - npdim, ak, nzdim, kmax);
+  for (int tt = blockIdx.x * blockDim.x + threadIdx.x; tt < ntot; tt += gridDim.x * blockDim.x) {
+    double q = (tt < nrdim) ? svv_qr(tt, nrchop) : (tt < nrdim + npdim) ? svv_qp(tt - nrdim, np)
+                                                                          : svv_qz(tt - nrdim - npdim, ak, nzdim, kmax);
     q = fmin(1.0, q);
     double f = 1.0;
     if (sv > 0.0 && q > cutoff) {
@@ -297,7 +312,7 @@ __global__ void k_svv_gain(const double* __restrict__ partial, int nb, double* _
       double s2 = shape * shape, s4 = s2 * s2;
       f = exp(-sv * (s4 * s4));
     }
-    ft[t] = f;
+    ft[tt] = f;
   }
 }
 // q_r, q_p, q_z of every row, azimuthal slot and axial slot (:96-110), filled once
@@ -309,7 +324,8 @@ __global__ void k_svv_qtab(double* __restrict__ qt, int nrdim, int npdim, int nz
                                                                  : svv_qz(t - nrdim - npdim, ak, nzdim, kmax);
 }
 __global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ st,
-                            const double* __restrict__ ft) {
+                            const double* __restrict__ ft, double* __restrict__ gain) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *gain = st[1];
   if (st[0] <= 0.0) return;
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
@@ -546,12 +562,16 @@ int op_svv_filter_dev(Scalar& s, double* gain_dev) {
     MLG_LAUNCH();
     G.svv_q_ready = true;
   }
-  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, qt, cutoff, partial);
+  unsigned long long cbits = 0;
+  std::memcpy(&cbits, &cutoff, sizeof(cbits));
+  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, qt, cbits, partial);
   MLG_LAUNCH();
-  k_svv_gain<<<1, 256, 0, G.stream>>>(partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength,
-                                      ft, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak, cutoff);
+  const int ntab = G.nrdim + G.npdim + G.nzdim;
+  k_svv_gain<<<std::max(1, std::min(8, cdiv(ntab, 64))), 256, 0, G.stream>>>(
+      partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength, ft, G.nrdim, G.npdim, G.nzdim,
+      G.nrchop, G.np, kmax, G.ak, cutoff);
   MLG_LAUNCH();
-  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.dscal + DS_SUM0, ft);
+  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.dscal + DS_SUM0, ft, gain_dev);
   MLG_LAUNCH();
   return 0;
 }
