@@ -497,6 +497,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __res
   if (!ok) return;
   const bool rsc = rs != nullptr && r < nrs;   // every slot of the row times rs[r] last (scale_r)
   const double rv = rsc ? rs[r] : 1.0;
+  const double dcr = dc * rv;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     int k1 = w * Q + q;
@@ -505,9 +506,14 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __res
       C y = b[q][i];
       double2* o = base + (size_t)(k1 + R1 * bitrev(i, R2)) * nrdim;
       double2 v;
-      if (DC) v = make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
-      else v = make_double2((double)y.x, (double)y.y);
-      if (rsc) { v.x *= rv; v.y *= rv; }
+      if (DC) {
+        // (y + dc) rv as one FMA per component
+        v = rsc ? make_double2(fma(f2d_fast((float)y.x), rv, dcr), fma(f2d_fast((float)y.y), rv, dcr))
+                : make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+      } else {
+        v = make_double2((double)y.x, (double)y.y);
+        if (rsc) { v.x *= rv; v.y *= rv; }
+      }
       *o = v;
     }
   }

@@ -301,12 +301,53 @@ static int m0_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
   MLG_LAUNCH();
   return 0;
 }
+// the m = 0 plane of the backward transform in double-float: one warp per (radial point pair i, column
+// z), the lanes splitting the sums over the rows of each parity and reducing them by shuffles (the
+// plane is 1/50 of the work: spread over every SM it stays shorter than the tensor-core kernel beside it)
+__device__ __forceinline__ dfl df_shfl_xor(dfl v, int o) {
+  return dfl(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
+}
+__global__ void __launch_bounds__(256) k_m0_bwd_df(const double2* __restrict__ in, double2* __restrict__ out,
+                                                   const double* __restrict__ pf, const double* __restrict__ lnx,
+                                                   const double* __restrict__ lnp, int add_ln, int nr, int nrh, int nrdim,
+                                                   int npdim, int nzdim, int nn) {
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int i = wid % nrh, z = wid / nrh;
+  if (z >= nzdim) return;
+  const double2* col = in + (size_t)nrdim * npdim * z;
+  dfl er = 0, ei = 0, orr = 0, oi = 0;
+  const int nt = (nn + 1) / 2;
+  for (int t = lane; t < nt; t += 32) {
+    int je = 2 * t, jo = je + 1;
+    dfl ae(pf[i + (size_t)nrh * je]);
+    dfl2 ce = ldc<dfl>(col + je);
+    er = tmac(ae, ce.x, er); ei = tmac(ae, ce.y, ei);
+    if (jo < nn) {
+      dfl ao(pf[i + (size_t)nrh * jo]);
+      dfl2 co = ldc<dfl>(col + jo);
+      orr = tmac(ao, co.x, orr); oi = tmac(ao, co.y, oi);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    er = er + df_shfl_xor(er, o); ei = ei + df_shfl_xor(ei, o);
+    orr = orr + df_shfl_xor(orr, o); oi = oi + df_shfl_xor(oi, o);
+  }
+  if (lane == 0) {
+    double2* base = out + (size_t)nrdim * npdim * z;
+    double2 p = to_d2<dfl>(er + orr, ei + oi);
+    double2 q = to_d2<dfl>(er - orr, ei - oi);
+    if (add_ln) { double lnv = *lnp; p.x += lnv * lnx[i]; q.x += lnv * lnx[nr - 1 - i]; }
+    base[i] = p;
+    base[nr - 1 - i] = q;
+  }
+}
+
 static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln, cudaStream_t st) {
-  constexpr int IT = 16, ZT = 4, KC = 16;
   if (nrc <= 0) return 0;
-  dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), 1), blk(ZT, IT);
-  k_rtrans_bwd<dfl, IT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
-                                                                 G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
+  const int warps = G.nrh * G.nzdim;
+  k_m0_bwd_df<<<cdiv(warps, 8), 256, 0, st>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh, G.nrdim, G.npdim,
+                                              G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
