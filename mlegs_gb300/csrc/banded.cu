@@ -12,10 +12,12 @@
 // Every per-(m,k) loop of the reference visits k = 1..nzc and then k = nzcu..nzdim; when nzc == nzcu
 // (nzchop = nz/2+1) the shared slot is processed twice, and so it is here.
 #include "common.cuh"
+#include "dfloat.cuh"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 namespace mlg {
 
@@ -405,6 +407,7 @@ struct SolveArgs {
   int* status;
   int nrdim, npdim, ne, nrc, npc, nzc, nzcu, nzdim;
   int nsys;             // npc * nzdim
+  int nsp = 0;          // the factor image's system stride: nsys rounded up to 32
   double alpha, beta, ell, preln;
   int kind;             // 0 ihelm, 1 idel2_proln, 2 idel2_preln, 3 ihelmp
   int power;
@@ -692,7 +695,7 @@ __global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restr
   double alpha = (a.kind == 0) ? a.alpha : 0.0;
   double e2 = a.ell * a.ell;
   constexpr int WC = FKL + FKU + 1;
-  const size_t ns = a.nsys;
+  const size_t ns = a.nsp;
   double W[FKL + 1][WC];
 #pragma unroll
   for (int t = 0; t <= FKL; ++t)
@@ -753,18 +756,27 @@ __device__ __forceinline__ void cpa16(void* sdst, const void* gsrc, bool pred) {
   int sz = pred ? 16 : 0;
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
 }
+// 16 bytes through L2 only: for rows that other threads of the block have just stored
+__device__ __forceinline__ void cpa16cg(void* sdst, const void* gsrc, bool pred) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
+  int sz = pred ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
+}
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // forward and back substitution with the cached factors (gbtrs 'N', one or two right-hand sides), in
 // place on the column.  One warp = 32 systems; factor rows and right-hand-side values are staged into shared
 // memory SST groups ahead of use by cp.async, so DRAM latency overlaps the recurrences.
-constexpr int SGR = 8, SST = 3, SNU = FKL + FKU;
+constexpr int SGR = 8, SST = 4, SNU = FKL + FKU, SFS = SNU + 1;
 static_assert(FKL == 2, "the substitution compares the pivot index by the high words of 1.0 and 2.0");
 template <int NR>
 struct SubstSmem {
-  double f[SST][SGR][SNU + 1][64];   // fwd: l1, l2, pivot; bwd: 1/U(j,j), U(j,j+1..j+4)/U(j,j)
-  double v[NR][SST][SGR][64];        // fwd: entering right-hand side; bwd: y(j)
+  double f[SST][SFS][SGR][32];   // factor rows by group: [slot][row in group][system]
+  double2 v[NR][SST][SGR][32];   // field rows by group: fwd the entering rows, bwd y(j)
+  double2 o[NR][2][SGR][32];     // outgoing rows by group parity: fwd y(j), bwd x(j)
+  long long off[32];             // the block's systems: column offset, active rows, passes
+  int nn[32], cnt[32];
 };
 
 // ihelm's pre-solve log-term handling of one field (:818-824): so%ln = s%ln/alpha, the log terms on
@@ -779,149 +791,204 @@ __device__ __forceinline__ void subst_root_pre(const SolveArgs& a, double2* g, d
 }
 
 // The matrices are real, so the real and imaginary parts of a right-hand side are two independent
-// real systems with the same factors: block = 64 threads, threads 0-31 take the real parts of 32
-// consecutive systems and threads 32-63 the imaginary parts (twice the warps in flight for the
-// serial recurrences).  NR = 2 solves two fields with the same matrices (the psi and chi solves of
-// a vortex step) in one pass: the factors are staged once for both and every thread runs two
-// independent recurrences.  Only the real-part thread of system (0,0) touches ln and the log terms,
-// which all act on real parts.
-template <int NR>
-__global__ void __launch_bounds__(64) k_band_subst(SolveArgs a, const double* __restrict__ fac) {
+// real systems with the same factors.  A block takes 32 consecutive systems (m, k) and has 64*NR
+// threads: one per system, part (real / imaginary) and field (NR = 2 solves the psi and chi fields of
+// a vortex step with the same matrices).  The systems' serial recurrences are all the parallelism
+// there is (a few warps per SM), so the kernel is built to issue few instructions per row: the
+// factors and field rows are staged by groups of SGR rows with 16-byte copies shared by the whole
+// block (the factors laid out [row][slot][system], a field's rows 128-byte runs per system), the
+// outgoing rows go back the same way, and the rows are walked by absolute index with no early exit
+// (rows past a system's own count are computed on whatever was staged and never stored; in the
+// backward pass they keep the recurrence at zero until the system's last row).  Only the real-part
+// thread of system (0,0) touches ln and the log terms, which all act on real parts.
+// The substitution's arithmetic: FP64 (DF = false), or double-float for the mixed form (DF = true):
+// the factors come from their float-pair image (hi in the low word, lo in the high word of each
+// 8-byte slot; the pivot slot stays a double), the forward pass keeps y(j) in the field's slot as a
+// float pair, and the backward pass writes x(j) = hi + lo as a double (exact: at most 49 bits).
+// About 15 FP32 instructions per multiply-subtract against one FP64 FMA that holds the SM
+// sub-partition's FP64 pipe for 64 cycles per warp: the systems are too few to hide that.
+template <bool DF> struct SubstT { typedef double R; };
+template <> struct SubstT<true> { typedef dfl R; };
+__device__ __forceinline__ dfl df_unpack(double b) { return dfl(__int_as_float(__double2loint(b)), __int_as_float(__double2hiint(b))); }
+__device__ __forceinline__ double df_pack(dfl v) { return __hiloint2double(__float_as_int(v.l), __float_as_int(v.h)); }
+// a - b*c with b*c's error terms carried unnormalised into the two-sum of the high parts
+__device__ __forceinline__ dfl df_fnma(dfl b, dfl c, dfl a) {
+  float p = __fmul_rn(-b.h, c.h);
+  float e = __fmaf_rn(-b.h, c.h, -p);
+  e = __fmaf_rn(-b.h, c.l, e);
+  e = __fmaf_rn(-b.l, c.h, e);
+  float s = __fadd_rn(a.h, p), v = __fsub_rn(s, a.h);
+  float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(p, v));
+  return df_quick(s, __fadd_rn(err, __fadd_rn(e, a.l)));
+}
+__device__ __forceinline__ double sb_fnma(double b, double c, double a) { return fma(-b, c, a); }
+__device__ __forceinline__ dfl sb_fnma(dfl b, dfl c, dfl a) { return df_fnma(b, c, a); }
+template <bool DF> __device__ __forceinline__ typename SubstT<DF>::R sb_in(double v);     // a field value
+template <> __device__ __forceinline__ double sb_in<false>(double v) { return v; }
+template <> __device__ __forceinline__ dfl sb_in<true>(double v) { return dfl(v); }
+template <bool DF> __device__ __forceinline__ typename SubstT<DF>::R sb_slot(double v);   // a factor or y slot
+template <> __device__ __forceinline__ double sb_slot<false>(double v) { return v; }
+template <> __device__ __forceinline__ dfl sb_slot<true>(double v) { return df_unpack(v); }
+__device__ __forceinline__ double sb_y(double v) { return v; }
+__device__ __forceinline__ double sb_y(dfl v) { return df_pack(v); }
+__device__ __forceinline__ double sb_x(double v) { return v; }
+__device__ __forceinline__ double sb_x(dfl v) { return f2d_fast(v.h) + f2d_fast(v.l); }
+
+template <int NR, bool DF>
+__global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const double* __restrict__ fac) {
+  typedef typename SubstT<DF>::R R;
+  constexpr int NT = 64 * NR;
   extern __shared__ __align__(16) unsigned char subst_smem[];
   SubstSmem<NR>& sm = *reinterpret_cast<SubstSmem<NR>*>(subst_smem);
-  int th = threadIdx.x;
-  int comp = th >> 5;
-  int sys = blockIdx.x * 32 + (th & 31);
-  bool valid = sys < a.nsys;
-  int m = valid ? sys / a.nzdim : 0, k = valid ? sys % a.nzdim : 0;
-  int cnt = valid ? k_count(k, a.nzc, a.nzcu, a.nzdim) : 0;
-  int nn = max(min(a.nrc, a.nrc - m), 0);
-  bool root = valid && (m == 0 && k == 0);
-  if (root && a.skip_root) cnt = 0;
-  double2* ev[2] = {a.e, a.e2};
-  double* lv[2] = {a.lnp, a.lnp2};
-  if (root && comp == 0 && a.kind == 0 && !a.skip_root && !a.no_ln) {
-#pragma unroll
-    for (int q = 0; q < NR; ++q) subst_root_pre(a, ev[q], lv[q]);
-  }
-  if (!valid || m >= a.npc || nn < 1) cnt = 0;
-  double* x[NR];
-#pragma unroll
-  for (int q = 0; q < NR; ++q)
-    x[q] = reinterpret_cast<double*>(ev[q] + (size_t)a.nrdim * (m + (size_t)a.npdim * k)) + comp;  // stride 2
-  const size_t ns = a.nsys;
+  const int th = threadIdx.x, q = th >> 6, comp = (th >> 5) & 1, lane = th & 31;
+  const size_t nsp = a.nsp;
+  const int sys0 = blockIdx.x * 32, sys = sys0 + lane;
+  double2* ev = q == 0 ? a.e : a.e2;
+  double* lv = q == 0 ? a.lnp : a.lnp2;
+  auto sys_info = [&](int s, int& nn, int& cnt, size_t& off) {
+    bool valid = s < a.nsys;
+    int m = valid ? s / a.nzdim : 0, k = valid ? s % a.nzdim : 0;
+    cnt = valid ? k_count(k, a.nzc, a.nzcu, a.nzdim) : 0;
+    nn = max(min(a.nrc, a.nrc - m), 0);
+    if (valid && m == 0 && k == 0 && a.skip_root) cnt = 0;
+    if (!valid || m >= a.npc || nn < 1) cnt = 0;
+    off = (size_t)a.nrdim * (m + (size_t)a.npdim * k);
+  };
+  int nn, cnt;
+  size_t off;
+  sys_info(sys, nn, cnt, off);
+  if (th < 32) { sm.nn[th] = nn; sm.cnt[th] = cnt; sm.off[th] = (long long)off; }
+  const bool root = sys < a.nsys && off == 0;
+  if (root && comp == 0 && a.kind == 0 && !a.skip_root && !a.no_ln) subst_root_pre(a, ev, lv);
+  double* x = reinterpret_cast<double*>(ev + off) + comp;   // stride 2
+  // every warp holds the same 32 systems: warp-wide maxima are block-wide
   int nnw = (cnt > 0) ? nn : 0;
   for (int o = 16; o; o >>= 1) nnw = max(nnw, __shfl_xor_sync(0xffffffffu, nnw, o));
   int cntw = cnt;
   for (int o = 16; o; o >>= 1) cntw = max(cntw, __shfl_xor_sync(0xffffffffu, cntw, o));
-  int ng = (nnw + SGR - 1) / SGR;
-  const double* dummy = fac;
+  const int ng = (nnw + SGR - 1) / SGR;
+  const double* dummy = fac;   // a 256-byte aligned address for the zero-size copies
+  __syncthreads();             // the system table
+  // the block's field rows of a group: chunk c = th + i*NT -> field c/256, system (c%256)/8, row in
+  // group c%8 (eight consecutive threads copy one system's 128-byte run); each thread's four chunks
+  // keep their system for the whole kernel
+  constexpr int NCH = NR * 256 / NT;   // 4
+  double2* cbase[NCH];
+  int cnn[NCH], ccnt[NCH];
+  const int cu = th & 7;
+#pragma unroll
+  for (int i = 0; i < NCH; ++i) {
+    const int c = th + i * NT, qq = c >> 8, sl = (c >> 3) & 31;
+    cbase[i] = (qq == 0 ? a.e : a.e2) + sm.off[sl];
+    cnn[i] = sm.nn[sl];
+    ccnt[i] = sm.cnt[sl];
+  }
+  auto stage_rows = [&](int g, int rep, bool bwd) {
+    const int st = g % SST;
+#pragma unroll
+    for (int i = 0; i < NCH; ++i) {
+      const int c = th + i * NT, qq = c >> 8, sl = (c >> 3) & 31;
+      const int j = bwd ? nnw - 1 - (g * SGR + cu) : g * SGR + cu + 1 + FKL;
+      const bool ok = rep < ccnt[i] && j >= 0 && j < cnn[i];
+      cpa16cg(&sm.v[qq][st][cu][sl], ok ? (const void*)(cbase[i] + j) : (const void*)dummy, ok);
+    }
+  };
+  auto write_out = [&](int g, int rep, bool bwd) {
+#pragma unroll
+    for (int i = 0; i < NCH; ++i) {
+      const int c = th + i * NT, qq = c >> 8, sl = (c >> 3) & 31;
+      const int j = bwd ? nnw - 1 - (g * SGR + cu) : g * SGR + cu;
+      if (rep < ccnt[i] && j >= 0 && j < cnn[i]) cbase[i][j] = sm.o[qq][g & 1][cu][sl];
+    }
+  };
+  // the factor rows of group g: NSL slots from S0 of rows j(u), 256 bytes per (row, slot), 16 per copy
+  const double* fbase = fac + sys0 + 2 * (th & 15);
+  auto stage_fac_t = [&](auto bwdc, int g) {
+    constexpr bool BWD = decltype(bwdc)::value;
+    constexpr int NSL = BWD ? SNU + 1 : FKL + 1, S0 = BWD ? FKL + 1 : 0;
+    const int st = g % SST;
+#pragma unroll
+    for (int c = th; c < SGR * NSL * 16; c += NT) {
+      const int pr = c >> 4;
+      const int u = pr / NSL, t = pr - u * NSL;
+      const int j = BWD ? nnw - 1 - (g * SGR + u) : g * SGR + u;
+      const bool ok = j >= 0 && j < nnw;
+      cpa16cg(&sm.f[st][t][u][2 * (th & 15)], ok ? (const void*)(fbase + ((size_t)j * FSL + S0 + t) * nsp) : (const void*)dummy, ok);
+    }
+  };
+  auto stage_fac = [&](int g, bool bwd) {
+    if (bwd) stage_fac_t(std::integral_constant<bool, true>(), g);
+    else stage_fac_t(std::integral_constant<bool, false>(), g);
+  };
   for (int rep = 0; rep < cntw; ++rep) {
-    bool act = rep < cnt;
-    auto issue_f = [&](int g) {
-      int st = g % SST;
+    // ---- forward: L y = P b, y(j) into the field's slot of row j ----
+    R r[FKL + 1];
 #pragma unroll
-      for (int u = 0; u < SGR; ++u) {
-        int jr = g * SGR + u;
-        bool ok = act && jr < nn;
-        const double* f = fac + (size_t)jr * FSL * ns + sys;
-#pragma unroll
-        for (int t = 0; t <= FKL; ++t) cpa8(&sm.f[st][u][t][th], ok ? f + t * ns : dummy, ok);
-        int jn = jr + 1 + FKL;
-        bool okx = act && jn < nn;
-#pragma unroll
-        for (int q = 0; q < NR; ++q) cpa8(&sm.v[q][st][u][th], okx ? (const void*)(x[q] + 2 * jn) : (const void*)dummy, okx);
-      }
-    };
-    double r[NR][FKL + 1];
-#pragma unroll
-    for (int q = 0; q < NR; ++q)
-#pragma unroll
-      for (int t = 0; t <= FKL; ++t) r[q][t] = (act && t < nn) ? x[q][2 * t] : 0.0;
-    for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_f(g); cpa_commit(); }
+    for (int t = 0; t <= FKL; ++t) r[t] = sb_in<DF>((rep < cnt && t < nn) ? __ldcg(x + 2 * t) : 0.0);
+    for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, false); stage_rows(g, rep, false); } cpa_commit(); }
     for (int g = 0; g < ng; ++g) {
-      if (g + SST - 1 < ng) issue_f(g + SST - 1);
+      cpa_wait<SST - 2>();
+      __syncthreads();   // group g staged; group g-1 computed; stage (g-1)%SST free
+      if (g + SST - 1 < ng) { stage_fac(g + SST - 1, false); stage_rows(g + SST - 1, rep, false); }
       cpa_commit();
-      cpa_wait<SST - 1>();
-      int st = g % SST;
+      if (g > 0) write_out(g - 1, rep, false);
+      const int st = g % SST;
 #pragma unroll
       for (int u = 0; u < SGR; ++u) {
-        int jr = g * SGR + u;
-        if (!act || jr >= nn) break;
         // the pivot row index p (0..FKL), stored as a double: compared by its high word, off the FP64 pipe
-        const int ph = __double2hiint(sm.f[st][u][FKL][th]);
+        const int ph = __double2hiint(sm.f[st][FKL][u][lane]);
 #pragma unroll
         for (int t = 1; t <= FKL; ++t)
-          if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) {
+          if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) { R w = r[0]; r[0] = r[t]; r[t] = w; }
 #pragma unroll
-            for (int q = 0; q < NR; ++q) { double w = r[q][0]; r[q][0] = r[q][t]; r[q][t] = w; }
-          }
+        for (int t = 1; t <= FKL; ++t) r[t] = sb_fnma(sb_slot<DF>(sm.f[st][t - 1][u][lane]), r[0], r[t]);
+        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = sb_y(r[0]);
 #pragma unroll
-        for (int t = 1; t <= FKL; ++t) {
-          double l = sm.f[st][u][t - 1][th];
-#pragma unroll
-          for (int q = 0; q < NR; ++q) r[q][t] -= l * r[q][0];
-        }
-#pragma unroll
-        for (int q = 0; q < NR; ++q) {
-          x[q][2 * jr] = r[q][0];
-#pragma unroll
-          for (int t = 0; t < FKL; ++t) r[q][t] = r[q][t + 1];
-          r[q][FKL] = sm.v[q][st][u][th];
-        }
+        for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
+        r[FKL] = sb_in<DF>(reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp]);
       }
     }
     cpa_wait<0>();
-    __threadfence_block();   // the y(j) just stored are read back below by this thread's cp.async
-    auto issue_b = [&](int g) {
-      int st = g % SST;
-#pragma unroll
-      for (int u = 0; u < SGR; ++u) {
-        int jr = nn - 1 - (g * SGR + u);
-        bool ok = act && jr >= 0;
-        const double* f = fac + (size_t)max(jr, 0) * FSL * ns + sys;
-#pragma unroll
-        for (int c = 0; c <= SNU; ++c) cpa8(&sm.f[st][u][c][th], ok ? f + (FKL + 1 + c) * ns : dummy, ok);
-#pragma unroll
-        for (int q = 0; q < NR; ++q) cpa8(&sm.v[q][st][u][th], ok ? (const void*)(x[q] + 2 * jr) : (const void*)dummy, ok);
-      }
-    };
-    double xs[NR][SNU];
-#pragma unroll
-    for (int q = 0; q < NR; ++q)
-#pragma unroll
-      for (int c = 0; c < SNU; ++c) xs[q][c] = 0.0;
-    for (int g = 0; g < SST - 1; ++g) { if (g < ng) issue_b(g); cpa_commit(); }
-    for (int g = 0; g < ng; ++g) {
-      if (g + SST - 1 < ng) issue_b(g + SST - 1);
-      cpa_commit();
-      cpa_wait<SST - 1>();
-      int st = g % SST;
-#pragma unroll
-      for (int u = 0; u < SGR; ++u) {
-        int jr = nn - 1 - (g * SGR + u);
-        if (!act || jr < 0) break;
-        double f0 = sm.f[st][u][0][th], g1 = sm.f[st][u][1][th], g2 = sm.f[st][u][2][th];
-        double g3 = sm.f[st][u][3][th], g4 = sm.f[st][u][4][th];
-#pragma unroll
-        for (int q = 0; q < NR; ++q) {
-          // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
-          double t = fma(-g4, xs[q][3], fma(-g3, xs[q][2], fma(-g2, xs[q][1], sm.v[q][st][u][th] * f0)));
-          double xj = fma(-g1, xs[q][0], t);
-          x[q][2 * jr] = xj;
-#pragma unroll
-          for (int c = SNU - 1; c >= 1; --c) xs[q][c] = xs[q][c - 1];
-          xs[q][0] = xj;
-        }
-      }
-    }
-    cpa_wait<0>();
+    __syncthreads();
+    if (ng > 0) write_out(ng - 1, rep, false);
     __threadfence_block();
-  }
-  if (root && comp == 0 && a.kind == 1 && !a.skip_root && !a.no_ln && cnt > 0) {
+    __syncthreads();   // y(j) in the fields, read back below by other threads' copies
+    // ---- backward: U x = y from row nnw-1 down; a system joins at its own last row ----
+    R xs[SNU];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) *lv[q] = x[q][0] * exp(a.lognorm[0]);
+    for (int c = 0; c < SNU; ++c) xs[c] = sb_in<DF>(0.0);
+    for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, true); stage_rows(g, rep, true); } cpa_commit(); }
+    for (int g = 0; g < ng; ++g) {
+      cpa_wait<SST - 2>();
+      __syncthreads();
+      if (g + SST - 1 < ng) { stage_fac(g + SST - 1, true); stage_rows(g + SST - 1, rep, true); }
+      cpa_commit();
+      if (g > 0) write_out(g - 1, rep, true);
+      const int st = g % SST;
+#pragma unroll
+      for (int u = 0; u < SGR; ++u) {
+        const int j = nnw - 1 - (g * SGR + u);
+        R f0 = sb_slot<DF>(sm.f[st][0][u][lane]), g1 = sb_slot<DF>(sm.f[st][1][u][lane]);
+        R g2 = sb_slot<DF>(sm.f[st][2][u][lane]), g3 = sb_slot<DF>(sm.f[st][3][u][lane]);
+        R g4 = sb_slot<DF>(sm.f[st][4][u][lane]);
+        // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
+        R yj = sb_slot<DF>(reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp]);
+        R t = sb_fnma(g4, xs[3], sb_fnma(g3, xs[2], sb_fnma(g2, xs[1], yj * f0)));
+        R xj = sb_fnma(g1, xs[0], t);
+        if (j >= nn) xj = sb_in<DF>(0.0);
+        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = sb_x(xj);
+#pragma unroll
+        for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
+        xs[0] = xj;
+      }
+    }
+    cpa_wait<0>();
+    __syncthreads();
+    if (ng > 0) write_out(ng - 1, rep, true);
+    __threadfence_block();
+    __syncthreads();   // x complete before the next pass (or the log-term read below)
   }
+  if (root && comp == 0 && a.kind == 1 && !a.skip_root && !a.no_ln && cnt > 0) *lv = __ldcg(x) * exp(a.lognorm[0]);
 }
 
 // the bordered (0,0) system of idel2_preln (KL = 3), single thread, after the batch
@@ -1061,38 +1128,104 @@ int ihelm_noalloc(void* e_dev, double* ln, double alpha) {
 }
 
 // LRU cache of factor sets, keyed by (kind, alpha, chop window)
+// the float-pair image of a factor set for the double-float substitution: slot by slot hi + lo of
+// each FP64 factor (the pivot slot copied as is).  A factor outside [1e-30, 1e30] in magnitude (or
+// not finite) would lose digits or overflow in FP32's exponent range: it is counted in *bad, and
+// such a factor set keeps the FP64 substitution.
+__global__ void k_fac_split(const double* __restrict__ fac, double* __restrict__ out, size_t n, size_t ns,
+                            int* __restrict__ bad) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = fac[i];
+    if ((int)((i / ns) % FSL) == FKL) { out[i] = v; continue; }
+    double av = fabs(v);
+    if (!(av <= 1e30) || (av != 0.0 && av < 1e-30)) atomicAdd(bad, 1);
+    out[i] = df_pack(dfl(v));
+  }
+}
+
 struct LUEntry {
   int kind; double alpha; int nrc, npc, nzc, nzcu; double* buf; size_t bytes; unsigned long long used;
+  double* buf32;   // the float-pair image (mixed form), made on first use
+  int df_ok;       // -1 not yet checked, 0 FP64 only, 1 the image is usable
 };
 static std::vector<LUEntry> g_lu;
 static unsigned long long g_lu_clock = 0;
 static const size_t LU_MAX_ENTRIES = 4;
 
+static void lu_entry_free(LUEntry& e) {
+  dfree(e.buf, e.bytes);
+  if (e.buf32) dfree(e.buf32, e.bytes);
+  e.buf32 = nullptr;
+}
+
 void lu_cache_clear() {
-  for (auto& e : g_lu) dfree(e.buf, e.bytes);
+  for (auto& e : g_lu) lu_entry_free(e);
   g_lu.clear();
 }
 
+// the float-pair image of e for the mixed form (made and range-checked once; one host read of the
+// check when it is made), or nullptr when the factors need FP64
+static int lu_df_image(LUEntry& e, size_t nsp, double** out32) {
+  *out32 = nullptr;
+  if (e.df_ok == 0) return 0;
+  if (e.df_ok < 0) {
+    MLG_TRY(dmalloc((void**)&e.buf32, e.bytes));
+    int* bad = (int*)(G.dscal + DS_FLAG + 2);
+    MLG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), G.stream));
+    size_t n = e.bytes / sizeof(double);
+    k_fac_split<<<std::max(1, std::min(cdiv(n, 256), 152 * 16)), 256, 0, G.stream>>>(e.buf, e.buf32, n, nsp, bad);
+    MLG_LAUNCH();
+    int hbad = 0;
+    MLG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, G.stream));
+    MLG_CUDA(cudaStreamSynchronize(G.stream));
+    e.df_ok = hbad == 0 ? 1 : 0;
+    if (!e.df_ok) { dfree(e.buf32, e.bytes); e.buf32 = nullptr; return 0; }
+  }
+  *out32 = e.buf32;
+  return 0;
+}
+
+// the cached factors of (kind, alpha, chop window), made by factor() on a miss; with out32, also
+// their float-pair image when the mixed form can use it (nullptr otherwise)
 template <class F>
-static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsys, double** out, F factor) {
+static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, double** out, F factor,
+                        double** out32 = nullptr) {
+  if (out32) *out32 = nullptr;
   for (auto& e : g_lu)
     if (e.kind == kind && e.alpha == alpha && e.nrc == c.nrc && e.npc == c.npc && e.nzc == c.nzc && e.nzcu == c.nzcu) {
       e.used = ++g_lu_clock;
       *out = e.buf;
+      if (out32) MLG_TRY(lu_df_image(e, nsp, out32));
       return 0;
     }
   int nnmax = std::max(std::min(c.nrc, G.nrdim), 1);
-  size_t bytes = (size_t)nnmax * FSL * nsys * sizeof(double);
+  size_t bytes = (size_t)nnmax * FSL * nsp * sizeof(double);
   if (g_lu.size() >= LU_MAX_ENTRIES) {
     auto it = std::min_element(g_lu.begin(), g_lu.end(), [](const LUEntry& x, const LUEntry& y) { return x.used < y.used; });
-    dfree(it->buf, it->bytes);
+    lu_entry_free(*it);
     g_lu.erase(it);
   }
-  LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock};
+  LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock, nullptr, -1};
   MLG_TRY(dmalloc((void**)&e.buf, bytes));
   MLG_TRY(factor(e.buf));
   g_lu.push_back(e);
   *out = e.buf;
+  if (out32) MLG_TRY(lu_df_image(g_lu.back(), nsp, out32));
+  return 0;
+}
+
+// the substitution launch: double-float from the float-pair image when there is one, else FP64
+template <int NR>
+static int launch_subst(const SolveArgs& a, const double* fac, const double* fac32, size_t nsys) {
+  size_t smb = sizeof(SubstSmem<NR>);
+  if (fac32) {
+    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<NR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    k_band_subst<NR, true><<<cdiv(nsys, 32), 64 * NR, smb, G.stream>>>(a, fac32);
+  } else {
+    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<NR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    k_band_subst<NR, false><<<cdiv(nsys, 32), 64 * NR, smb, G.stream>>>(a, fac);
+  }
+  MLG_LAUNCH();
   return 0;
 }
 
@@ -1140,15 +1273,14 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
     SolveArgs b = a;
     b.kind = fkind;
     b.skip_root = (kind == 2) ? 1 : 0;
-    MLG_TRY(lu_cache_get(fkind, alpha, c, nsys, &fac, [&](double* buf) -> int {
+    double* fac32 = nullptr;
+    b.nsp = (int)((nsys + 31) / 32 * 32);
+    MLG_TRY(lu_cache_get(fkind, alpha, c, (size_t)b.nsp, &fac, [&](double* buf) -> int {
       k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(b, buf);
       MLG_LAUNCH();
       return 0;
-    }));
-    size_t smb = sizeof(SubstSmem<1>);
-    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-    k_band_subst<1><<<cdiv(nsys, 32), 64, smb, G.stream>>>(b, fac);
-    MLG_LAUNCH();
+    }, G.precision == MLG_MIXED ? &fac32 : nullptr));
+    MLG_TRY(launch_subst<1>(b, fac, fac32, nsys));
     if (kind == 2) {
       k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
       MLG_LAUNCH();
@@ -1174,15 +1306,14 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   a.e2 = s2.e; a.lnp2 = s2.ln;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  MLG_TRY(lu_cache_get(0, alpha, c, nsys, &fac, [&](double* buf) -> int {
+  double* fac32 = nullptr;
+  a.nsp = (int)((nsys + 31) / 32 * 32);
+  MLG_TRY(lu_cache_get(0, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
     MLG_LAUNCH();
     return 0;
-  }));
-  size_t smb = sizeof(SubstSmem<2>);
-  MLG_CUDA(cudaFuncSetAttribute(k_band_subst<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-  k_band_subst<2><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
-  MLG_LAUNCH();
+  }, G.precision == MLG_MIXED ? &fac32 : nullptr));
+  MLG_TRY(launch_subst<2>(a, fac, fac32, nsys));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
 }
@@ -1267,15 +1398,13 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   a.kind = kind; a.power = 0; a.skip_root = 0; a.transpose = 1; a.no_ln = 1;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  MLG_TRY(lu_cache_get(kind + 8, alpha, c, nsys, &fac, [&](double* buf) -> int {
+  a.nsp = (int)((nsys + 31) / 32 * 32);
+  MLG_TRY(lu_cache_get(kind + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
     MLG_LAUNCH();
     return 0;
   }));
-  size_t smb = sizeof(SubstSmem<1>);
-  MLG_CUDA(cudaFuncSetAttribute(k_band_subst<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-  k_band_subst<1><<<cdiv(nsys, 32), 64, smb, G.stream>>>(a, fac);
-  MLG_LAUNCH();
+  MLG_TRY(launch_subst<1>(a, fac, nullptr, nsys));
   kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
 }

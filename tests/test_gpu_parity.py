@@ -304,3 +304,29 @@ def test_mixed_vortex_steps_within_1e6_of_fp64():
         tol = 5e-6 if n.startswith("nl") else 1e-6
         assert err < tol, f"mixed {n} after 20 steps: {err:.3e} relative to FP64"
         assert abs(a[1] - b[1]) <= 1e-6 * max(1.0, abs(b[1])), f"mixed {n} ln: {a[1]} vs {b[1]}"
+
+
+@pytest.mark.parametrize("op", ["idel2_pro", "idel2_pre", "ihelm", "abcn"])
+def test_mixed_solves_double_float(mixed_pair, op):
+    """The mixed form's banded substitutions run in double-float (FP32 pairs, about 47 bits) from the
+    cached FP64 factors: held to 1e-10 of the FP64 oracle (1e-9 for the Poisson solves, whose
+    condition number is ~1e4), far inside the 2e-6 of the FP32 transforms."""
+    name, k, o = mixed_pair
+    p = k.params
+    c = fff_input(p, k.dims, 121)
+    for ln in ((0.0,) if op == "abcn" else (0.0, 0.7)):
+        if op == "abcn":
+            g = [k.scalar(fff_input(p, k.dims, 122 + i, 1.0 if i < 2 else 0.1), 0.1 * i, "FFF") for i in range(4)]
+            r = [o.scalar(*x.get()[:3]) for x in g]
+            k.abcn(*g, 1e-3); o.abcn(*r, 1e-3)
+            for i in range(4):
+                compare(g[i], r[i], 1e-10, what=f"{name} mixed abcn arg{i} ln={ln}")
+            continue
+        gs, os_ = both(k, o, c, ln, "FFF")
+        if op == "idel2_pro":
+            k.idel2(gs); o.idel2(os_)
+        elif op == "idel2_pre":
+            k.idel2(gs, 0.25); o.idel2(os_, 0.25)
+        else:
+            k.ihelm(gs, -3.5e3); o.ihelm(os_, -3.5e3)
+        compare(gs, os_, 1e-9 if op.startswith("idel2") else 1e-10, what=f"{name} mixed {op} ln={ln}")
