@@ -43,32 +43,47 @@ template <> struct BC<float> {
   static __device__ __forceinline__ void st(double2* p, C v) { st_c32(p, v); }
   static __device__ __forceinline__ float cv(double v) { return d2f_fast(v); }
 };
+// the band tables in T: FP64 as built, or their FP32 copies (made once with the kit)
+struct BandTabs {
+  const double *bd2, *bxx, *ak;
+  const float *bd2f, *bxxf, *ak2f;
+};
+template <typename T> __device__ __forceinline__ T btab(const double* d, const float* f, size_t i);
+template <> __device__ __forceinline__ double btab<double>(const double* d, const float* f, size_t i) { (void)f; return d[i]; }
+template <> __device__ __forceinline__ float btab<float>(const double* d, const float* f, size_t i) { (void)d; return f[i]; }
+template <typename T> __device__ __forceinline__ T bakv2(const BandTabs& t, int k);   // akval**2 (mlegs_spectfm_diff.f90:144)
+template <> __device__ __forceinline__ double bakv2<double>(const BandTabs& t, int k) { return t.ak[k] * t.ak[k]; }
+template <> __device__ __forceinline__ float bakv2<float>(const BandTabs& t, int k) { return t.ak2f[k]; }
+// -v exactly, by the sign bits (off the FP64 pipe)
+__device__ __forceinline__ double2 neg_d2(double2 v) {
+  return make_double2(__hiloint2double(__double2hiint(v.x) ^ (int)0x80000000, __double2loint(v.x)),
+                      __hiloint2double(__double2hiint(v.y) ^ (int)0x80000000, __double2loint(v.y)));
+}
 
 // one (m, k) column of nn rows, applied cnt times in place through shared memory
 template <typename T>
-__device__ __forceinline__ void band_col(double2* __restrict__ g, const double* __restrict__ bd2,
-                                         const double* __restrict__ bxx, double akd, int op, int m, int ne, int nn,
-                                         int cnt, unsigned char* smem, int nrdim) {
+__device__ __forceinline__ void band_col(double2* __restrict__ g, const BandTabs& tb, int k, int op, int m, int ne,
+                                         int nn, int cnt, unsigned char* smem, int nrdim) {
   typedef typename BC<T>::C C;
   C* c0 = (C*)smem;
   C* c1 = c0 + nrdim;
   for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(g + i);
   __syncthreads();
-  T akv2 = BC<T>::cv(akd * akd);   // akval**2 (mlegs_spectfm_diff.f90:144)
+  const T akv2 = bakv2<T>(tb, k);
   for (int rep = 0; rep < cnt; ++rep) {
     for (int i = threadIdx.x; i < nn; i += blockDim.x) {
       C acc; acc.x = 0; acc.y = 0;
       if (op == 0) {
-        const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
-        if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
-        if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
+        const size_t b = 3 * ((size_t)i + (size_t)ne * m);
+        if (i - 1 >= 0) { T v = btab<T>(tb.bxx, tb.bxxf, b); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+        if (i + 1 < nn) { T v = btab<T>(tb.bxx, tb.bxxf, b + 2); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
       } else {
-        const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+        const size_t b = 5 * ((size_t)i + (size_t)ne * m);
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
           int j = i - 2 + c;
           if (j < 0 || j >= nn) continue;
-          T v = BC<T>::cv(b[c]);
+          T v = btab<T>(tb.bd2, tb.bd2f, b + c);
           if (c == 2 && op == 2) v = v - akv2;
           acc.x += v * c0[j].x;
           acc.y += v * c0[j].y;
@@ -87,8 +102,7 @@ __device__ __forceinline__ void band_col(double2* __restrict__ g, const double* 
 // grid (k, m).  The mixed form (T = float) still applies the m = 0 columns in FP64: they hold the
 // axisymmetric mean flow, and their radial sums cancel toward the axis.
 template <typename T>
-__global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__ bd2, const double* __restrict__ bxx,
-                             const double* __restrict__ ak, double* __restrict__ lnp, const double* __restrict__ lognorm,
+__global__ void k_band_apply(double2* __restrict__ e, BandTabs tb, double* __restrict__ lnp, const double* __restrict__ lognorm,
                              int op, int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim,
                              double ell) {
   extern __shared__ __align__(16) unsigned char band_smem[];
@@ -100,8 +114,8 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
   double lnin = 0.0;
   if (lnblk) lnin = *lnp;
   if (m < npc && nn > 0 && cnt > 0) {
-    if (m == 0) band_col<double>(g, bd2, bxx, ak[k], op, m, ne, nn, cnt, band_smem, nrdim);
-    else band_col<T>(g, bd2, bxx, ak[k], op, m, ne, nn, cnt, band_smem, nrdim);
+    if (m == 0) band_col<double>(g, tb, k, op, m, ne, nn, cnt, band_smem, nrdim);
+    else band_col<T>(g, tb, k, op, m, ne, nn, cnt, band_smem, nrdim);
   }
   if (lnblk && threadIdx.x == 0) {
     // the log-term contributions land on e(1..3,1,1) whether or not the column was active
@@ -126,7 +140,7 @@ __global__ void k_band_apply(double2* __restrict__ e, const double* __restrict__
 template <typename T>
 __global__ void k_abcn_rhs(double2* __restrict__ e, const double2* __restrict__ nl, const double2* __restrict__ nlp,
                            double* __restrict__ lnp, const double* __restrict__ lnnl, const double* __restrict__ lnnlp,
-                           const double* __restrict__ bd2, const double* __restrict__ ak, const double* __restrict__ lognorm,
+                           BandTabs tb, const double* __restrict__ lognorm,
                            int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell,
                            double visc, double c1, double c2, double c3, double post) {
   extern __shared__ __align__(16) unsigned char rhs_smem[];
@@ -136,63 +150,78 @@ __global__ void k_abcn_rhs(double2* __restrict__ e, const double2* __restrict__ 
   int cnt = k_count(k, nzc, nzcu, nzdim);
   size_t off = (size_t)nrdim * (m + (size_t)npdim * k);
   double2* g = e + off;
+  const double2* n0 = nl + off;
+  const double2* n1 = nlp + off;
+  const bool act = m < npc && nn > 0 && cnt > 0;
+  if (m > 0 && sizeof(T) == sizeof(float)) {
+    // the mixed form's m >= 1 columns: the increment 1.5 dt nl - 0.5 dt nl_p + dt/2 visc del2(s) summed
+    // in FP32 (its terms carry the FP32 contractions' rounding already), added to the FP64 state
+    typedef float2 C;
+    C* c0 = (C*)rhs_smem;
+    C* c1b = c0 + nrdim;
+    if (act) {
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = ld_c32(g + i);
+      __syncthreads();
+      const float akv2 = tb.ak2f[k];
+      for (int rep = 0; rep < cnt; ++rep) {
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          C acc; acc.x = 0; acc.y = 0;
+          const float* b = tb.bd2f + 5 * ((size_t)i + (size_t)ne * m);
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            int j = i - 2 + c;
+            if (j < 0 || j >= nn) continue;
+            float v = b[c];
+            if (c == 2) v = v - akv2;
+            acc.x += v * c0[j].x;
+            acc.y += v * c0[j].y;
+          }
+          c1b[i] = acc;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
+        __syncthreads();
+      }
+    }
+    const float f1 = d2f_fast(c1), f2 = d2f_fast(c2), f3 = d2f_fast(c3 * visc);
+    for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
+      double2 x = g[i];
+      float2 a1 = ld_c32(n0 + i), a2 = ld_c32(n1 + i);
+      float2 s3 = (act && i < nn) ? c0[i] : make_float2(d2f_fast(x.x), d2f_fast(x.y));
+      float dx = f1 * a1.x, dy = f1 * a1.y;
+      dx = fmaf(f2, a2.x, dx); dy = fmaf(f2, a2.y, dy);
+      dx = fmaf(f3, s3.x, dx); dy = fmaf(f3, s3.y, dy);
+      g[i] = make_double2(post * (x.x + f2d_fast(dx)), post * (x.y + f2d_fast(dy)));
+    }
+    return;
+  }
   bool lnblk = (m == 0 && k == 0);
   double lnin = lnblk ? *lnp : 0.0;
   for (int i = threadIdx.x; i < nrdim; i += blockDim.x) sv[i] = g[i];
   __syncthreads();
-  if (m < npc && nn > 0 && cnt > 0) {
-    if (m == 0) {
-      double2* c0 = sv;
-      double2* c1b = sv + nrdim;
-      double akv2 = ak[k] * ak[k];
-      for (int rep = 0; rep < cnt; ++rep) {
-        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-          double2 acc; acc.x = 0; acc.y = 0;
-          const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+  if (act) {
+    double2* c0 = sv;
+    double2* c1b = sv + nrdim;
+    double akv2 = tb.ak[k] * tb.ak[k];
+    for (int rep = 0; rep < cnt; ++rep) {
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+        double2 acc; acc.x = 0; acc.y = 0;
+        const double* b = tb.bd2 + 5 * ((size_t)i + (size_t)ne * m);
 #pragma unroll
-          for (int c = 0; c < 5; ++c) {
-            int j = i - 2 + c;
-            if (j < 0 || j >= nn) continue;
-            double v = b[c];
-            if (c == 2) v = v - akv2;
-            acc.x += v * c0[j].x;
-            acc.y += v * c0[j].y;
-          }
-          c1b[i] = acc;
+        for (int c = 0; c < 5; ++c) {
+          int j = i - 2 + c;
+          if (j < 0 || j >= nn) continue;
+          double v = b[c];
+          if (c == 2) v = v - akv2;
+          acc.x += v * c0[j].x;
+          acc.y += v * c0[j].y;
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
-        __syncthreads();
+        c1b[i] = acc;
       }
-    } else {
-      typedef typename BC<T>::C C;
-      C* c0 = (C*)(sv + 2 * nrdim);
-      C* c1b = c0 + nrdim;
-      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(sv + i);
       __syncthreads();
-      T akv2 = BC<T>::cv(ak[k] * ak[k]);
-      for (int rep = 0; rep < cnt; ++rep) {
-        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-          C acc; acc.x = 0; acc.y = 0;
-          const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
-#pragma unroll
-          for (int c = 0; c < 5; ++c) {
-            int j = i - 2 + c;
-            if (j < 0 || j >= nn) continue;
-            T v = BC<T>::cv(b[c]);
-            if (c == 2) v = v - akv2;
-            acc.x += v * c0[j].x;
-            acc.y += v * c0[j].y;
-          }
-          c1b[i] = acc;
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
-        __syncthreads();
-      }
-      for (int i = threadIdx.x; i < nn; i += blockDim.x) BC<T>::st(sv + i, c0[i]);
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1b[i];
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (lnblk && threadIdx.x == 0) {   // the log terms of del2 (:561-566) on svis(1..3, 1, 1)
     double e2 = ell * ell;
@@ -201,8 +230,6 @@ __global__ void k_abcn_rhs(double2* __restrict__ e, const double2* __restrict__ 
     sv[2].x += 2.0 / 3.0 / e2 / exp(lognorm[2]) * lnin;
   }
   __syncthreads();
-  const double2* n0 = nl + off;
-  const double2* n1 = nlp + off;
   for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
     double2 x = g[i], a1 = n0[i], a2 = n1[i], s3 = sv[i];
     s3 = make_double2(0.0 + visc * s3.x, 0.0 + visc * s3.y);   // svis = visc*svis
@@ -223,21 +250,23 @@ __global__ void k_abcn_rhs(double2* __restrict__ e, const double2* __restrict__ 
   }
 }
 
+static BandTabs band_tabs() { return BandTabs{G.bd2, G.bxx, G.ak, G.bd2f, G.bxxf, G.ak2f}; }
+
 int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, double a) {
   ChopIdx c;
   MLG_TRY(chop_index(s, c));
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   dim3 grid(G.nzdim, G.npdim);
-  size_t sm = 2ull * G.nrdim * sizeof(double2) + 2ull * G.nrdim * sizeof(double2);
+  size_t sm = 2ull * G.nrdim * sizeof(double2);
   kt_begin(2);
   if (G.precision == MLG_MIXED) {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_abcn_rhs<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_abcn_rhs<float><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, G.bd2, G.ak, G.lognorm, G.nrdim,
+    k_abcn_rhs<float><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, band_tabs(), G.lognorm, G.nrdim,
                                                    G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell, G.P.visc,
                                                    1.5 * dt, -.5 * dt, dt / 2.0, a);
   } else {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_abcn_rhs<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_abcn_rhs<double><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, G.bd2, G.ak, G.lognorm, G.nrdim,
+    k_abcn_rhs<double><<<grid, 128, sm, G.stream>>>(s.e, nl.e, nl_p.e, s.ln, nl.ln, nl_p.ln, band_tabs(), G.lognorm, G.nrdim,
                                                     G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell, G.P.visc,
                                                     1.5 * dt, -.5 * dt, dt / 2.0, a);
   }
@@ -250,9 +279,9 @@ int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, 
 // operator in place and multiplying dst by scale (dst%ln = 0), in one pass over every column
 template <typename T>
 __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __restrict__ src, const double* __restrict__ lnsrc,
-                                double* __restrict__ lndst, const double* __restrict__ bd2, const double* __restrict__ bxx,
-                                const double* __restrict__ ak, const double* __restrict__ lognorm, int op, int nrdim, int npdim,
-                                int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell, double scale) {
+                                double* __restrict__ lndst, BandTabs tb, const double* __restrict__ lognorm, int op,
+                                int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell,
+                                double scale, int smode) {
   extern __shared__ __align__(16) unsigned char bat_smem[];
   double2* sv = (double2*)bat_smem;   // the column, then its band product on the active rows (FP64)
   int m = blockIdx.y, k = blockIdx.x;
@@ -266,16 +295,16 @@ __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __rest
     if (m == 0) {
       double2* c0 = sv;
       double2* c1 = sv + nrdim;
-      double akv2 = ak[k] * ak[k];
+      double akv2 = tb.ak[k] * tb.ak[k];
       for (int rep = 0; rep < cnt; ++rep) {
         for (int i = threadIdx.x; i < nn; i += blockDim.x) {
           double2 acc; acc.x = 0; acc.y = 0;
           if (op == 0) {
-            const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
+            const double* b = tb.bxx + 3 * ((size_t)i + (size_t)ne * m);
             if (i - 1 >= 0) { double v = b[0]; acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
             if (i + 1 < nn) { double v = b[2]; acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
           } else {
-            const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+            const double* b = tb.bd2 + 5 * ((size_t)i + (size_t)ne * m);
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
               int j = i - 2 + c;
@@ -298,21 +327,21 @@ __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __rest
       C* c1 = c0 + nrdim;
       for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = BC<T>::ld(sv + i);
       __syncthreads();
-      T akv2 = BC<T>::cv(ak[k] * ak[k]);
+      const T akv2 = bakv2<T>(tb, k);
       for (int rep = 0; rep < cnt; ++rep) {
         for (int i = threadIdx.x; i < nn; i += blockDim.x) {
           C acc; acc.x = 0; acc.y = 0;
           if (op == 0) {
-            const double* b = bxx + 3 * ((size_t)i + (size_t)ne * m);
-            if (i - 1 >= 0) { T v = BC<T>::cv(b[0]); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
-            if (i + 1 < nn) { T v = BC<T>::cv(b[2]); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
+            const size_t b = 3 * ((size_t)i + (size_t)ne * m);
+            if (i - 1 >= 0) { T v = btab<T>(tb.bxx, tb.bxxf, b); acc.x += v * c0[i - 1].x; acc.y += v * c0[i - 1].y; }
+            if (i + 1 < nn) { T v = btab<T>(tb.bxx, tb.bxxf, b + 2); acc.x += v * c0[i + 1].x; acc.y += v * c0[i + 1].y; }
           } else {
-            const double* b = bd2 + 5 * ((size_t)i + (size_t)ne * m);
+            const size_t b = 5 * ((size_t)i + (size_t)ne * m);
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
               int j = i - 2 + c;
               if (j < 0 || j >= nn) continue;
-              T v = BC<T>::cv(b[c]);
+              T v = btab<T>(tb.bd2, tb.bd2f, b + c);
               if (c == 2 && op == 2) v = v - akv2;
               acc.x += v * c0[j].x;
               acc.y += v * c0[j].y;
@@ -344,26 +373,28 @@ __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __rest
   __syncthreads();
   for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
     double2 v = sv[i];
-    if (scale != 1.0) v = make_double2(0.0 + scale * v.x, 0.0 + scale * v.y);
+    if (smode == 1) v = neg_d2(v);
+    else if (smode == 2) v = make_double2(0.0 + scale * v.x, 0.0 + scale * v.y);
     dst[off + i] = v;
   }
 }
 
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  const int smode = scale == 1.0 ? 0 : scale == -1.0 ? 1 : 2;   // identity, exact negation, FP64 product
   dim3 grid(G.nzdim, G.npdim);
   size_t sm = 4ull * G.nrdim * sizeof(double2);
   kt_begin(KT_BAND);
   if (G.precision == MLG_MIXED) {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply_to<float><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, G.bd2, G.bxx, G.ak, G.lognorm, op,
+    k_band_apply_to<float><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                         G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
-                                                        scale);
+                                                        scale, smode);
   } else {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply_to<double><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, G.bd2, G.bxx, G.ak, G.lognorm, op,
+    k_band_apply_to<double><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                          G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
-                                                         scale);
+                                                         scale, smode);
   }
   MLG_LAUNCH();
   kt_end(KT_BAND, 2.0 * G.fsize * 16);
@@ -377,12 +408,12 @@ int launch_band_apply(Scalar& s, int op, const ChopIdx& c) {
   if (G.precision == MLG_MIXED) {
     size_t sm = 2ull * G.nrdim * sizeof(double2);   // the m = 0 columns run in FP64
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply<float><<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+    k_band_apply<float><<<grid, 128, sm, G.stream>>>(s.e, band_tabs(), s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
                                                      c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
   } else {
     size_t sm = 2ull * G.nrdim * sizeof(double2);
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply<double><<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+    k_band_apply<double><<<grid, 128, sm, G.stream>>>(s.e, band_tabs(), s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
                                                       c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
   }
   MLG_LAUNCH();

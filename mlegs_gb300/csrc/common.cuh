@@ -67,6 +67,7 @@ struct Ctx {
   double *at0 = nullptr, *at1 = nullptr;   // (nrchop)
   double *bd2 = nullptr;       // del2 bands without the -k^2 term: (5, ne, npchop)
   double *bxx = nullptr;       // xxdx bands: (3, ne+1, npchop)
+  float *bd2f = nullptr, *bxxf = nullptr, *ak2f = nullptr;   // FP32 bands and ak^2 (the mixed form's m >= 1 stencils)
   double *tV = nullptr, *tD = nullptr, *tT = nullptr;   // vec2tp matrices (nrh, ne, npchop)
   float *tV32 = nullptr, *tD32 = nullptr, *tT32 = nullptr;   // FP32 copies (the mixed form's adjoint)
   double2 *tw_p = nullptr, *tw_z = nullptr;  // FFT twiddles exp(-2 pi i k/L): L = np/2 (phi), nz (z)

@@ -318,6 +318,9 @@ int kit_build(const mlg_params* P) {
   std::vector<float> w32(nr);
   for (int i = 0; i < nr; ++i) w32[i] = (float)w[i];
   MLG_TRY(upload(&G.w32, w32));
+  std::vector<float> ak2f(nz);
+  for (int i = 0; i < nz; ++i) ak2f[i] = (float)(ak[i] * ak[i]);
+  MLG_TRY(upload(&G.ak2f, ak2f));
   MLG_TRY(upload(&G.x, x)); MLG_TRY(upload(&G.w, w)); MLG_TRY(upload(&G.r, r)); MLG_TRY(upload(&G.rinv, rinv));
   MLG_TRY(upload(&G.lnx, lnx)); MLG_TRY(upload(&G.ak, ak)); MLG_TRY(upload(&G.lognorm, lognorm));
   double* d_logfact = nullptr;
@@ -346,6 +349,10 @@ int kit_build(const mlg_params* P) {
   MLG_TRY(dmalloc((void**)&G.bxx, (size_t)3 * G.ne * G.npchop * sizeof(double)));
   k_bands<<<dim3(cdiv(G.ne, 64), G.npchop), 64, 0, G.stream>>>(G.ne, G.npchop, G.ell, G.lognorm, G.bd2, G.bxx);
   MLG_LAUNCH();
+  MLG_TRY(dmalloc((void**)&G.bd2f, (size_t)5 * G.ne * G.npchop * sizeof(float)));
+  MLG_TRY(dmalloc((void**)&G.bxxf, (size_t)3 * G.ne * G.npchop * sizeof(float)));
+  k_to_f32<<<256, 256, 0, G.stream>>>(G.bd2, G.bd2f, (size_t)5 * G.ne * G.npchop); MLG_LAUNCH();
+  k_to_f32<<<256, 256, 0, G.stream>>>(G.bxx, G.bxxf, (size_t)3 * G.ne * G.npchop); MLG_LAUNCH();
 
   // vec2tp matrices
   MLG_TRY(dmalloc((void**)&G.tV, npf * sizeof(double)));
