@@ -379,6 +379,110 @@ __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __rest
   }
 }
 
+// ------------------------------------------------------------------------------------------------
+// (ur, up) of vector_reconstruction (mlegs_scalar_ops.f90:1455-1502: ur = r d/dr chi, up = r d/dr psi,
+// then ur = i m psi + i kv ur, up = -up - m kv chi on the active window) per (m, k) column in one pass: the
+// two xxdx stencils run side by side in shared memory, the mix follows, and the rows outside the
+// window keep the band products' copies of their inputs (with the log terms of (0,0)); ln(ur) =
+// ln(up) = 0.  U = double for m = 0 (and the plain form), float for the mixed form's m >= 1.
+template <typename U>
+__device__ __forceinline__ void uv_col(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
+                                       const double2* __restrict__ chi, double lnp, double lnc, const BandTabs& tb,
+                                       const double* __restrict__ lognorm, int nrdim, int ne, int nn, int cnt, bool act,
+                                       int m, int k, bool lnblk, unsigned char* smem) {
+  typedef typename BC<U>::C C;
+  C* a0 = (C*)smem;
+  C* a1 = a0 + nrdim;
+  C* b0 = a1 + nrdim;
+  C* b1 = b0 + nrdim;
+  if (act) {
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) { a0[i] = BC<U>::ld(chi + i); b0[i] = BC<U>::ld(psi + i); }
+    __syncthreads();
+    for (int rep = 0; rep < cnt; ++rep) {
+      for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+        C sa, sb;
+        sa.x = 0; sa.y = 0; sb.x = 0; sb.y = 0;
+        const size_t b = 3 * ((size_t)i + (size_t)ne * m);
+        if (i - 1 >= 0) {
+          U v = btab<U>(tb.bxx, tb.bxxf, b);
+          sa.x += v * a0[i - 1].x; sa.y += v * a0[i - 1].y;
+          sb.x += v * b0[i - 1].x; sb.y += v * b0[i - 1].y;
+        }
+        if (i + 1 < nn) {
+          U v = btab<U>(tb.bxx, tb.bxxf, b + 2);
+          sa.x += v * a0[i + 1].x; sa.y += v * a0[i + 1].y;
+          sb.x += v * b0[i + 1].x; sb.y += v * b0[i + 1].y;
+        }
+        a1[i] = sa;
+        b1[i] = sb;
+      }
+      __syncthreads();
+      C* t = a0; a0 = a1; a1 = t;
+      t = b0; b0 = b1; b1 = t;
+    }
+  }
+  const double kv = tb.ak[k], mv = (double)m;
+  for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
+    const double2 c = chi[i], p = psi[i];
+    const bool in = act && i < nn;
+    double2 av = c, bv = p;
+    if (in) { BC<U>::st(&av, a0[i]); BC<U>::st(&bv, b0[i]); }
+    if (lnblk && i < 2) {   // r d/dr of the log terms (mlegs_scalar_ops.f90:452-456)
+      av.x += 1.0 / exp(lognorm[i]) * lnc;
+      bv.x += 1.0 / exp(lognorm[i]) * lnp;
+    }
+    if (!in) { ur[i] = av; up[i] = bv; continue; }
+    if (sizeof(U) == sizeof(double)) {
+      ur[i] = make_double2(-mv * p.y - kv * av.y, mv * p.x + kv * av.x);
+      up[i] = make_double2(-bv.x - mv * kv * c.x, -bv.y - mv * kv * c.y);
+    } else {
+      const float mf = (float)m, kf = d2f_fast(kv), mk = d2f_fast(mv * kv);
+      const C af = a0[i], bf = b0[i];
+      const float2 pf = ld_c32(psi + i), cf = ld_c32(chi + i);
+      st_c32(ur + i, make_float2(-mf * pf.y - kf * (float)af.y, mf * pf.x + kf * (float)af.x));
+      st_c32(up + i, make_float2(-(float)bf.x - mk * cf.x, -(float)bf.y - mk * cf.y));
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_tp2vec_uv(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
+                            const double2* __restrict__ chi, const double* __restrict__ lnpsi,
+                            const double* __restrict__ lnchi, double* __restrict__ lnur, double* __restrict__ lnup,
+                            BandTabs tb, const double* __restrict__ lognorm, int nrdim, int npdim, int ne, int nrc,
+                            int npc, int nzc, int nzcu, int nzdim) {
+  extern __shared__ __align__(16) unsigned char uv_smem[];
+  const int m = blockIdx.y, k = blockIdx.x;
+  const int nn = max(min(nrc, nrc - m), 0);
+  const int cnt = k_count(k, nzc, nzcu, nzdim);
+  const size_t off = (size_t)nrdim * (m + (size_t)npdim * k);
+  const bool lnblk = m == 0 && k == 0;
+  const double lnp = lnblk ? *lnpsi : 0.0, lnc = lnblk ? *lnchi : 0.0;
+  const bool act = m < npc && nn > 0 && cnt > 0;
+  if (m == 0) uv_col<double>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, uv_smem);
+  else uv_col<T>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, uv_smem);
+  if (lnblk && threadIdx.x == 0) { *lnur = 0.0; *lnup = 0.0; }
+}
+
+int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  dim3 grid(G.nzdim, G.npdim);
+  size_t sm = 4ull * G.nrdim * sizeof(double2);
+  kt_begin(KT_BAND);
+  if (G.precision == MLG_MIXED) {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_tp2vec_uv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_tp2vec_uv<float><<<grid, 128, sm, G.stream>>>(ur.e, up.e, psi.e, chi.e, psi.ln, chi.ln, ur.ln, up.ln, band_tabs(),
+                                                    G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim);
+  } else {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_tp2vec_uv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_tp2vec_uv<double><<<grid, 128, sm, G.stream>>>(ur.e, up.e, psi.e, chi.e, psi.ln, chi.ln, ur.ln, up.ln, band_tabs(),
+                                                     G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim);
+  }
+  MLG_LAUNCH();
+  kt_end(KT_BAND, 4.0 * G.fsize * 16);
+  return 0;
+}
+
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   const int smode = scale == 1.0 ? 0 : scale == -1.0 ? 1 : 2;   // identity, exact negation, FP64 product

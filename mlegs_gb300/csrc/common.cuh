@@ -185,6 +185,7 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
                        Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale);
+int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c);
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
 int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha);

@@ -105,25 +105,23 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 // pointwise kernels
 
 // chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
-__global__ void k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int mode, int f0, int f1, int f2,
-                       int nrc, int npc, int nzc, int nzcu, int pcut, int zcut, int zupper, int np_gt1, int nz_gt1) {
-  size_t n = (size_t)nrdim * npdim * nzdim;
-  GRID_STRIDE(idx, n) {
-    int i = (int)(idx % (unsigned)nrdim);
-    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
-    int k = (int)(idx / (unsigned)(nrdim * npdim));
-    bool z = false;
-    if (mode == 0) {
-      int nrcs = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
-      if (f0 && i >= nrcs) z = true;
-      if (f1 && m >= npc) z = true;
-      if (f2 && nzc < nzcu && (k + 1) >= nzc + 1 && (k + 1) <= nzcu - 1) z = true;
-    } else {
-      if (np_gt1 && f1 && (m + 1) > pcut) z = true;
-      if (nz_gt1 && f2 && (k + 1) > zcut && (k + 1) < zupper) z = true;
-    }
-    if (z) e[idx] = make_double2(0.0, 0.0);
+// one warp per (m, k) column (8 per block): the column's first zeroed row is worked out once, and
+// only the zeroed rows are written (a column that keeps all its rows touches no memory)
+__global__ void __launch_bounds__(256) k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int mode, int f0,
+                                              int f1, int f2, int nrc, int npc, int nzc, int nzcu, int pcut, int zcut,
+                                              int zupper, int np_gt1, int nz_gt1) {
+  const int col = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (col >= npdim * nzdim) return;
+  const int m = col % npdim, k = col / npdim;
+  int zf = nrdim;   // rows [zf, nrdim) become zero
+  if (mode == 0) {
+    if ((f1 && m >= npc) || (f2 && nzc < nzcu && (k + 1) >= nzc + 1 && (k + 1) <= nzcu - 1)) zf = 0;
+    else if (f0) zf = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
+  } else {
+    if ((np_gt1 && f1 && (m + 1) > pcut) || (nz_gt1 && f2 && (k + 1) > zcut && (k + 1) < zupper)) zf = 0;
   }
+  double2* g = e + (size_t)nrdim * col;
+  for (int i = zf + lane; i < nrdim; i += 32) g[i] = make_double2(0.0, 0.0);
 }
 
 // e(:nr, 1, :) += sgn * ln * lnx (trans :193-195, :219-221)
@@ -522,7 +520,7 @@ int op_trans(Scalar& s, const char* space) {
 int op_chop(Scalar& s) {
   ChopIdx c;
   MLG_TRY(chop_index(s, c));
-  k_mask<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F',
+  k_mask<<<cdiv((long long)G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F',
                                               s.space[2] == 'F', c.nrc, c.npc, c.nzc, c.nzcu, 0, 0, 0, 0, 0);
   MLG_LAUNCH();
   return 0;
@@ -530,7 +528,7 @@ int op_chop(Scalar& s) {
 
 int op_dealias(Scalar& s) {
   int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
-  k_mask<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F',
+  k_mask<<<cdiv((long long)G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F',
                                               0, 0, 0, 0, pcut, zcut, zupper, G.np > 1, G.nz > 1);
   MLG_LAUNCH();
   return 0;
@@ -886,38 +884,13 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
   return vec2tp_core(ur, up, uz, psi, chi);
 }
 
-// combination step of vector_reconstruction (:1488-1502)
-__global__ void k_tp2vec_mix(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
-                             const double2* __restrict__ uz, const double* __restrict__ ak, int nrdim, int npdim, int nzdim,
-                             int nrc, int npc, int nzc, int nzcu) {
-  size_t n = (size_t)nrdim * npdim * nzdim;
-  GRID_STRIDE(idx, n) {
-    int i = (int)(idx % (unsigned)nrdim);
-    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
-    int k = (int)(idx / (unsigned)(nrdim * npdim));
-    if (m >= npc) continue;
-    int nn = max(min(nrc, nrc - m), 0);
-    int kk = k + 1;
-    if (i >= nn || !(kk <= nzc || kk >= nzcu)) continue;
-    double kv = ak[k], mv = (double)m;
-    double2 p = psi[idx], a = ur[idx], b = up[idx], c = uz[idx];
-    // ur = i*mv*psi + i*kv*ur; up = -up - mv*kv*uz
-    ur[idx] = make_double2(-mv * p.y - kv * a.y, mv * p.x + kv * a.x);
-    up[idx] = make_double2(-b.x - mv * kv * c.x, -b.y - mv * kv * c.y);
-  }
-}
-
 // vector_reconstruction into (ur, up, uz), none of them aliasing psi or chi: they are the workspace
 // (the same steps as copying chi / psi into temporaries and the temporaries into the outputs)
 static int tp2vec_into(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
   for (Scalar* q : {&ur, &up, &uz}) { q->set_space("FFF"); q->off[0] = 3; q->off[1] = q->off[2] = 0; }
   ChopIdx c;
   MLG_TRY(chop_index(ur, c));
-  MLG_TRY(launch_band_apply_to(ur, chi, 0, c, 1.0));    // r d/dr chi
-  MLG_TRY(launch_band_apply_to(up, psi, 0, c, 1.0));    // r d/dr psi
-  k_tp2vec_mix<<<nblk(G.fsize), 256, 0, G.stream>>>(ur.e, up.e, psi.e, chi.e, G.ak, G.nrdim, G.npdim, G.nzdim, c.nrc, c.npc,
-                                                     c.nzc, c.nzcu);
-  MLG_LAUNCH();
+  MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c));       // r d/dr chi, r d/dr psi and their mix
   ur.off[0] = 0; up.off[0] = 0;
   MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
   // to PPP, the last φ transform dividing by r (scale_r folded into it)
