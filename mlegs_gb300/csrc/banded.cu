@@ -12,7 +12,6 @@
 // Every per-(m,k) loop of the reference visits k = 1..nzc and then k = nzcu..nzdim; when nzc == nzcu
 // (nzchop = nz/2+1) the shared slot is processed twice, and so it is here.
 #include "common.cuh"
-#include "dfloat.cuh"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -879,19 +878,8 @@ __global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restr
   }
 }
 
-// cp.async helpers (each thread copies only the words it later reads itself, so a wait_group on
-// the thread is enough and no block barrier is needed)
-__device__ __forceinline__ void cpa8(void* sdst, const void* gsrc, bool pred) {
-  unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
-  int sz = pred ? 8 : 0;   // src-size 0 fills the destination with zeros
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
-}
-__device__ __forceinline__ void cpa16(void* sdst, const void* gsrc, bool pred) {
-  unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
-  int sz = pred ? 16 : 0;
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(sz));
-}
-// 16 bytes through L2 only: for rows that other threads of the block have just stored
+// cp.async helpers: 16 bytes through L2 only (the staged rows include rows that other threads of the
+// block have just stored; a zero source size fills the destination with zeros)
 __device__ __forceinline__ void cpa16cg(void* sdst, const void* gsrc, bool pred) {
   unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
   int sz = pred ? 16 : 0;
@@ -936,42 +924,9 @@ __device__ __forceinline__ void subst_root_pre(const SolveArgs& a, double2* g, d
 // (rows past a system's own count are computed on whatever was staged and never stored; in the
 // backward pass they keep the recurrence at zero until the system's last row).  Only the real-part
 // thread of system (0,0) touches ln and the log terms, which all act on real parts.
-// The substitution's arithmetic: FP64 (DF = false), or double-float for the mixed form (DF = true):
-// the factors come from their float-pair image (hi in the low word, lo in the high word of each
-// 8-byte slot; the pivot slot stays a double), the forward pass keeps y(j) in the field's slot as a
-// float pair, and the backward pass writes x(j) = hi + lo as a double (exact: at most 49 bits).
-// About 15 FP32 instructions per multiply-subtract against one FP64 FMA that holds the SM
-// sub-partition's FP64 pipe for 64 cycles per warp: the systems are too few to hide that.
-template <bool DF> struct SubstT { typedef double R; };
-template <> struct SubstT<true> { typedef dfl R; };
-__device__ __forceinline__ dfl df_unpack(double b) { return dfl(__int_as_float(__double2loint(b)), __int_as_float(__double2hiint(b))); }
-__device__ __forceinline__ double df_pack(dfl v) { return __hiloint2double(__float_as_int(v.l), __float_as_int(v.h)); }
-// a - b*c with b*c's error terms carried unnormalised into the two-sum of the high parts
-__device__ __forceinline__ dfl df_fnma(dfl b, dfl c, dfl a) {
-  float p = __fmul_rn(-b.h, c.h);
-  float e = __fmaf_rn(-b.h, c.h, -p);
-  e = __fmaf_rn(-b.h, c.l, e);
-  e = __fmaf_rn(-b.l, c.h, e);
-  float s = __fadd_rn(a.h, p), v = __fsub_rn(s, a.h);
-  float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(p, v));
-  return df_quick(s, __fadd_rn(err, __fadd_rn(e, a.l)));
-}
-__device__ __forceinline__ double sb_fnma(double b, double c, double a) { return fma(-b, c, a); }
-__device__ __forceinline__ dfl sb_fnma(dfl b, dfl c, dfl a) { return df_fnma(b, c, a); }
-template <bool DF> __device__ __forceinline__ typename SubstT<DF>::R sb_in(double v);     // a field value
-template <> __device__ __forceinline__ double sb_in<false>(double v) { return v; }
-template <> __device__ __forceinline__ dfl sb_in<true>(double v) { return dfl(v); }
-template <bool DF> __device__ __forceinline__ typename SubstT<DF>::R sb_slot(double v);   // a factor or y slot
-template <> __device__ __forceinline__ double sb_slot<false>(double v) { return v; }
-template <> __device__ __forceinline__ dfl sb_slot<true>(double v) { return df_unpack(v); }
-__device__ __forceinline__ double sb_y(double v) { return v; }
-__device__ __forceinline__ double sb_y(dfl v) { return df_pack(v); }
-__device__ __forceinline__ double sb_x(double v) { return v; }
-__device__ __forceinline__ double sb_x(dfl v) { return f2d_fast(v.h) + f2d_fast(v.l); }
-
-template <int NR, bool DF>
+template <int NR>
 __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const double* __restrict__ fac) {
-  typedef typename SubstT<DF>::R R;
+  typedef double R;
   constexpr int NT = 64 * NR;
   extern __shared__ __align__(16) unsigned char subst_smem[];
   SubstSmem<NR>& sm = *reinterpret_cast<SubstSmem<NR>*>(subst_smem);
@@ -1059,7 +1014,7 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
     // ---- forward: L y = P b, y(j) into the field's slot of row j ----
     R r[FKL + 1];
 #pragma unroll
-    for (int t = 0; t <= FKL; ++t) r[t] = sb_in<DF>((rep < cnt && t < nn) ? __ldcg(x + 2 * t) : 0.0);
+    for (int t = 0; t <= FKL; ++t) r[t] = ((rep < cnt && t < nn) ? __ldcg(x + 2 * t) : 0.0);
     for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, false); stage_rows(g, rep, false); } cpa_commit(); }
     for (int g = 0; g < ng; ++g) {
       cpa_wait<SST - 2>();
@@ -1076,11 +1031,11 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
         for (int t = 1; t <= FKL; ++t)
           if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) { R w = r[0]; r[0] = r[t]; r[t] = w; }
 #pragma unroll
-        for (int t = 1; t <= FKL; ++t) r[t] = sb_fnma(sb_slot<DF>(sm.f[st][t - 1][u][lane]), r[0], r[t]);
-        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = sb_y(r[0]);
+        for (int t = 1; t <= FKL; ++t) r[t] = fma(-sm.f[st][t - 1][u][lane], r[0], r[t]);
+        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = r[0];
 #pragma unroll
         for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
-        r[FKL] = sb_in<DF>(reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp]);
+        r[FKL] = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
       }
     }
     cpa_wait<0>();
@@ -1091,7 +1046,7 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
     // ---- backward: U x = y from row nnw-1 down; a system joins at its own last row ----
     R xs[SNU];
 #pragma unroll
-    for (int c = 0; c < SNU; ++c) xs[c] = sb_in<DF>(0.0);
+    for (int c = 0; c < SNU; ++c) xs[c] = 0.0;
     for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, true); stage_rows(g, rep, true); } cpa_commit(); }
     for (int g = 0; g < ng; ++g) {
       cpa_wait<SST - 2>();
@@ -1103,15 +1058,14 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
 #pragma unroll
       for (int u = 0; u < SGR; ++u) {
         const int j = nnw - 1 - (g * SGR + u);
-        R f0 = sb_slot<DF>(sm.f[st][0][u][lane]), g1 = sb_slot<DF>(sm.f[st][1][u][lane]);
-        R g2 = sb_slot<DF>(sm.f[st][2][u][lane]), g3 = sb_slot<DF>(sm.f[st][3][u][lane]);
-        R g4 = sb_slot<DF>(sm.f[st][4][u][lane]);
+        const R f0 = sm.f[st][0][u][lane], g1 = sm.f[st][1][u][lane], g2 = sm.f[st][2][u][lane];
+        const R g3 = sm.f[st][3][u][lane], g4 = sm.f[st][4][u][lane];
         // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
-        R yj = sb_slot<DF>(reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp]);
-        R t = sb_fnma(g4, xs[3], sb_fnma(g3, xs[2], sb_fnma(g2, xs[1], yj * f0)));
-        R xj = sb_fnma(g1, xs[0], t);
-        if (j >= nn) xj = sb_in<DF>(0.0);
-        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = sb_x(xj);
+        const R yj = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
+        const R t = fma(-g4, xs[3], fma(-g3, xs[2], fma(-g2, xs[1], yj * f0)));
+        R xj = fma(-g1, xs[0], t);
+        if (j >= nn) xj = 0.0;
+        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = xj;
 #pragma unroll
         for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
         xs[0] = xj;
@@ -1263,107 +1217,52 @@ int ihelm_noalloc(void* e_dev, double* ln, double alpha) {
 }
 
 // LRU cache of factor sets, keyed by (kind, alpha, chop window)
-// the float-pair image of a factor set for the double-float substitution: slot by slot hi + lo of
-// each FP64 factor (the pivot slot copied as is).  A factor outside [1e-30, 1e30] in magnitude (or
-// not finite) would lose digits or overflow in FP32's exponent range: it is counted in *bad, and
-// such a factor set keeps the FP64 substitution.
-__global__ void k_fac_split(const double* __restrict__ fac, double* __restrict__ out, size_t n, size_t ns,
-                            int* __restrict__ bad) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double v = fac[i];
-    if ((int)((i / ns) % FSL) == FKL) { out[i] = v; continue; }
-    double av = fabs(v);
-    if (!(av <= 1e30) || (av != 0.0 && av < 1e-30)) atomicAdd(bad, 1);
-    out[i] = df_pack(dfl(v));
-  }
-}
-
 struct LUEntry {
   int kind; double alpha; int nrc, npc, nzc, nzcu; double* buf; size_t bytes; unsigned long long used;
-  double* buf32;   // the float-pair image (mixed form), made on first use
-  int df_ok;       // -1 not yet checked, 0 FP64 only, 1 the image is usable
 };
 static std::vector<LUEntry> g_lu;
 static unsigned long long g_lu_clock = 0;
 static const size_t LU_MAX_ENTRIES = 4;
 
-static void lu_entry_free(LUEntry& e) {
-  dfree(e.buf, e.bytes);
-  if (e.buf32) dfree(e.buf32, e.bytes);
-  e.buf32 = nullptr;
-}
-
 void lu_cache_clear() {
-  for (auto& e : g_lu) lu_entry_free(e);
+  for (auto& e : g_lu) dfree(e.buf, e.bytes);
   g_lu.clear();
 }
 
-// the float-pair image of e for the mixed form (made and range-checked once; one host read of the
-// check when it is made), or nullptr when the factors need FP64
-static int lu_df_image(LUEntry& e, size_t nsp, double** out32) {
-  *out32 = nullptr;
-  if (e.df_ok == 0) return 0;
-  if (e.df_ok < 0) {
-    MLG_TRY(dmalloc((void**)&e.buf32, e.bytes));
-    int* bad = (int*)(G.dscal + DS_FLAG + 2);
-    MLG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), G.stream));
-    size_t n = e.bytes / sizeof(double);
-    k_fac_split<<<std::max(1, std::min(cdiv(n, 256), 152 * 16)), 256, 0, G.stream>>>(e.buf, e.buf32, n, nsp, bad);
-    MLG_LAUNCH();
-    int hbad = 0;
-    MLG_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, G.stream));
-    MLG_CUDA(cudaStreamSynchronize(G.stream));
-    e.df_ok = hbad == 0 ? 1 : 0;
-    if (!e.df_ok) { dfree(e.buf32, e.bytes); e.buf32 = nullptr; return 0; }
-  }
-  *out32 = e.buf32;
-  return 0;
-}
-
-// the cached factors of (kind, alpha, chop window), made by factor() on a miss; with out32, also
-// their float-pair image when the mixed form can use it (nullptr otherwise)
+// the cached factors of (kind, alpha, chop window), laid out [row][slot][system] with system stride
+// nsp, made by factor() on a miss
 template <class F>
-static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, double** out, F factor,
-                        double** out32 = nullptr) {
-  if (out32) *out32 = nullptr;
+static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, double** out, F factor) {
   for (auto& e : g_lu)
     if (e.kind == kind && e.alpha == alpha && e.nrc == c.nrc && e.npc == c.npc && e.nzc == c.nzc && e.nzcu == c.nzcu) {
       e.used = ++g_lu_clock;
       *out = e.buf;
-      if (out32) MLG_TRY(lu_df_image(e, nsp, out32));
       return 0;
     }
   int nnmax = std::max(std::min(c.nrc, G.nrdim), 1);
   size_t bytes = (size_t)nnmax * FSL * nsp * sizeof(double);
   if (g_lu.size() >= LU_MAX_ENTRIES) {
     auto it = std::min_element(g_lu.begin(), g_lu.end(), [](const LUEntry& x, const LUEntry& y) { return x.used < y.used; });
-    lu_entry_free(*it);
+    dfree(it->buf, it->bytes);
     g_lu.erase(it);
   }
-  LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock, nullptr, -1};
+  LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock};
   MLG_TRY(dmalloc((void**)&e.buf, bytes));
   MLG_TRY(factor(e.buf));
   g_lu.push_back(e);
   *out = e.buf;
-  if (out32) MLG_TRY(lu_df_image(g_lu.back(), nsp, out32));
   return 0;
 }
 
-// the substitution launch: double-float from the float-pair image when there is one, else FP64
+// the substitution launch: 64*NR threads per 32 systems
 template <int NR>
-static int launch_subst(const SolveArgs& a, const double* fac, const double* fac32, size_t nsys) {
+static int launch_subst(const SolveArgs& a, const double* fac, size_t nsys) {
   size_t smb = sizeof(SubstSmem<NR>);
-  if (fac32) {
-    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<NR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-    k_band_subst<NR, true><<<cdiv(nsys, 32), 64 * NR, smb, G.stream>>>(a, fac32);
-  } else {
-    MLG_CUDA(cudaFuncSetAttribute(k_band_subst<NR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-    k_band_subst<NR, false><<<cdiv(nsys, 32), 64 * NR, smb, G.stream>>>(a, fac);
-  }
+  MLG_CUDA(cudaFuncSetAttribute(k_band_subst<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+  k_band_subst<NR><<<cdiv(nsys, 32), 64 * NR, smb, G.stream>>>(a, fac);
   MLG_LAUNCH();
   return 0;
 }
-
 // kind as in SolveArgs; the band scratch grows to fit (kl, ku)
 // algorithmic bytes of one substitution pass over nrhs fields: each field read and written once, the
 // cached factors (FSL doubles per row and system) read once
@@ -1408,14 +1307,13 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
     SolveArgs b = a;
     b.kind = fkind;
     b.skip_root = (kind == 2) ? 1 : 0;
-    double* fac32 = nullptr;
     b.nsp = (int)((nsys + 31) / 32 * 32);
     MLG_TRY(lu_cache_get(fkind, alpha, c, (size_t)b.nsp, &fac, [&](double* buf) -> int {
       k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(b, buf);
       MLG_LAUNCH();
       return 0;
-    }, G.precision == MLG_MIXED ? &fac32 : nullptr));
-    MLG_TRY(launch_subst<1>(b, fac, fac32, nsys));
+    }));
+    MLG_TRY(launch_subst<1>(b, fac, nsys));
     if (kind == 2) {
       k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
       MLG_LAUNCH();
@@ -1441,14 +1339,13 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   a.e2 = s2.e; a.lnp2 = s2.ln;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  double* fac32 = nullptr;
   a.nsp = (int)((nsys + 31) / 32 * 32);
   MLG_TRY(lu_cache_get(0, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
     MLG_LAUNCH();
     return 0;
-  }, G.precision == MLG_MIXED ? &fac32 : nullptr));
-  MLG_TRY(launch_subst<2>(a, fac, fac32, nsys));
+  }));
+  MLG_TRY(launch_subst<2>(a, fac, nsys));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
 }
@@ -1539,7 +1436,7 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
     MLG_LAUNCH();
     return 0;
   }));
-  MLG_TRY(launch_subst<1>(a, fac, nullptr, nsys));
+  MLG_TRY(launch_subst<1>(a, fac, nsys));
   kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
 }

@@ -307,10 +307,10 @@ def test_mixed_vortex_steps_within_1e6_of_fp64():
 
 
 @pytest.mark.parametrize("op", ["idel2_pro", "idel2_pre", "ihelm", "abcn"])
-def test_mixed_solves_double_float(mixed_pair, op):
-    """The mixed form's banded substitutions run in double-float (FP32 pairs, about 47 bits) from the
-    cached FP64 factors: held to 1e-10 of the FP64 oracle (1e-9 for the Poisson solves, whose
-    condition number is ~1e4), far inside the 2e-6 of the FP32 transforms."""
+def test_mixed_solves_stay_fp64(mixed_pair, op):
+    """The mixed form keeps the banded solves in FP64 (only abcn's explicit increment is summed in
+    FP32 for m >= 1): held to 1e-10 of the FP64 oracle (1e-9 for the Poisson solves, whose condition
+    number is ~1e4), far inside the 2e-6 of the FP32 transforms."""
     name, k, o = mixed_pair
     p = k.params
     c = fff_input(p, k.dims, 121)
