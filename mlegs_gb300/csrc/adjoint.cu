@@ -85,23 +85,23 @@ __global__ void k_scale_tab(double2* __restrict__ e, const double* __restrict__ 
 }
 
 // *lnp += sgn * sum_{i < nr, z} lnx_i Re e(i, 0, z): the adjoint of e(:nr, 1, :) += ln * lnx
-__global__ void k_ln_dot(const double2* __restrict__ e, const double* __restrict__ lnx, int nr, int nrdim, int npdim,
-                         int nzdim, double* __restrict__ lnp, double sgn) {
-  __shared__ double red[256];
+__global__ void __launch_bounds__(1024) k_ln_dot(const double2* __restrict__ e, const double* __restrict__ lnx, int nr,
+                                                 int nrdim, int npdim, int nzdim, double* __restrict__ lnp, double sgn) {
+  __shared__ double red[32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double s = 0.0;
-  size_t n = (size_t)nr * nzdim;
-  for (size_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    int i = (int)(idx % (unsigned)nr);
-    int z = (int)(idx / (unsigned)nr);
-    s += lnx[i] * e[i + (size_t)nrdim * npdim * z].x;
+  for (int z = warp; z < nzdim; z += 32) {   // a warp per z line, its lanes over r (coalesced)
+    const double2* col = e + (size_t)nrdim * npdim * z;
+    for (int i = lane; i < nr; i += 32) s += lnx[i] * col[i].x;
   }
-  red[threadIdx.x] = s;
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
   __syncthreads();
-  for (int o = 128; o; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  if (warp == 0) {
+    s = red[lane];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) *lnp += sgn * s;
   }
-  if (threadIdx.x == 0) *lnp += sgn * red[0];
 }
 
 // zeroat1^T: the forward sets e(0,0,k) <- e(0,0,k) - sum_{n<nmax} at_n e(n,0,k) / at_0, so
@@ -324,6 +324,75 @@ k_vec2tp_T(const double2* __restrict__ psib, const double2* __restrict__ chib, d
   }
 }
 
+// The m = 0 plane of k_vec2tp_T in double-float: one warp per output pair (i, z), the lanes over the
+// row pairs (2t, 2t+1) -- the two parities.  With m = 0 the terms in S1 and S4 vanish, and the unfolded
+// outputs are F_o_bar(ur) = -i k S3, F_o_bar(up) = -S2, F_s_bar(uz) = -S5 per parity: six complex sums,
+// reduced by shuffles.
+__global__ void __launch_bounds__(256) k_m0_vec2tp_T_df(const double2* __restrict__ psib, const double2* __restrict__ chib,
+                                                        double2* __restrict__ urb, double2* __restrict__ upb,
+                                                        double2* __restrict__ uzb, const double* __restrict__ tD,
+                                                        const double* __restrict__ tT,
+                                                        const double* __restrict__ ak, int nr, int nrh, int nrdim,
+                                                        int npdim, int nzdim, int nn, int nzc, int nzcu) {
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int i = wid % nrh, z = wid / nrh;
+  if (z >= nzdim) return;
+  const int kk = z + 1;
+  if (!(kk <= nzc || kk >= nzcu)) return;
+  const size_t base = (size_t)nrdim * npdim * z;
+  dfl2 S[2][5];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 5; ++q) { S[p][q].x = 0; S[p][q].y = 0; }
+  for (int t = lane; 2 * t < nn; t += 32) {
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int j = 2 * t + p;
+      if (j >= nn) break;
+      const size_t o = i + (size_t)nrh * j;
+      // V enters only through S1 and S4, which m = 0 multiplies by zero
+      const dfl d(tD[o]), tt(tT[o]);
+      const dfl2 pv = ldc<dfl>(psib + base + j), cv = ldc<dfl>(chib + base + j);
+      S[p][1].x = tmac(d, pv.x, S[p][1].x); S[p][1].y = tmac(d, pv.y, S[p][1].y);
+      S[p][2].x = tmac(d, cv.x, S[p][2].x); S[p][2].y = tmac(d, cv.y, S[p][2].y);
+      S[p][4].x = tmac(tt, cv.x, S[p][4].x); S[p][4].y = tmac(tt, cv.y, S[p][4].y);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1)
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 1; q < 5; ++q) {
+        if (q == 3) continue;
+        S[p][q].x = S[p][q].x + df_shfl_xor(S[p][q].x, o);
+        S[p][q].y = S[p][q].y + df_shfl_xor(S[p][q].y, o);
+      }
+  if (lane != 0) return;
+  const dfl kv(ak[z]);
+  dfl2 r_lo, r_hi, p_lo, p_hi, z_lo, z_hi;
+  r_lo.x = 0; r_lo.y = 0; r_hi = r_lo; p_lo = r_lo; p_hi = r_lo; z_lo = r_lo; z_hi = r_lo;
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const dfl sg = p ? dfl(-1) : dfl(1);
+    const dfl2 S2 = S[p][1], S3 = S[p][2], S5 = S[p][4];
+    dfl2 fo_r, fo_p, fs_z;
+    fo_r.x = kv * S3.y; fo_r.y = -(kv * S3.x);   // -i k S3
+    fo_p.x = -S2.x; fo_p.y = -S2.y;
+    fs_z.x = -S5.x; fs_z.y = -S5.y;
+    r_lo.x = r_lo.x + fo_r.x; r_lo.y = r_lo.y + fo_r.y;
+    r_hi.x = r_hi.x + sg * (-fo_r.x); r_hi.y = r_hi.y + sg * (-fo_r.y);
+    p_lo.x = p_lo.x + fo_p.x; p_lo.y = p_lo.y + fo_p.y;
+    p_hi.x = p_hi.x + sg * (-fo_p.x); p_hi.y = p_hi.y + sg * (-fo_p.y);
+    z_lo.x = z_lo.x + fs_z.x; z_lo.y = z_lo.y + fs_z.y;
+    z_hi.x = z_hi.x + sg * fs_z.x; z_hi.y = z_hi.y + sg * fs_z.y;
+  }
+  urb[base + i] = to_d2<dfl>(r_lo.x, r_lo.y); urb[base + nr - 1 - i] = to_d2<dfl>(r_hi.x, r_hi.y);
+  upb[base + i] = to_d2<dfl>(p_lo.x, p_lo.y); upb[base + nr - 1 - i] = to_d2<dfl>(p_hi.x, p_hi.y);
+  uzb[base + i] = to_d2<dfl>(z_lo.x, z_lo.y); uzb[base + nr - 1 - i] = to_d2<dfl>(z_hi.x, z_hi.y);
+}
+
 // J = 1/2 sum W_i |u|^2 over i < nr, slots < np/2 (both packed reals), every z; u_bar = W u
 // (zero elsewhere); one partial sum per block
 __global__ void k_energy(double2* __restrict__ ubr, double2* __restrict__ ubp, double2* __restrict__ ubz,
@@ -407,7 +476,7 @@ static int scale_tab(Scalar& s, const double* tab, int inv) {
 }
 
 static int ln_dot(Scalar& s, double sgn) {
-  k_ln_dot<<<1, 256, 0, G.stream>>>(s.e, G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, s.ln, sgn);
+  k_ln_dot<<<1, 1024, 0, G.stream>>>(s.e, G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, s.ln, sgn);
   MLG_LAUNCH();
   return 0;
 }
@@ -481,6 +550,24 @@ int ihelm_T(Scalar& s, double alpha) {
   MLG_TRY(launch_band_solve_T(s, 0, c, alpha));
   k_ihelm_T_ln<<<1, 32, 0, G.stream>>>(s.e, s.ln, G.lognorm, G.ell, alpha);
   MLG_LAUNCH();
+  return 0;
+}
+
+// ihelm^T of two fields with the same alpha: one paired substitution when their chop windows agree
+static int ihelm_T_pair(Scalar& s1, Scalar& s2, double alpha) {
+  if (std::fabs(alpha) < 5.0e-14) return set_error(MLG_EALPHA, "ihelm: alpha equals to zero. Inversion of 0*identity is impossible");
+  ChopIdx c1, c2;
+  MLG_TRY(chop_index(s1, c1));
+  MLG_TRY(chop_index(s2, c2));
+  if (!(c1.nrc == c2.nrc && c1.npc == c2.npc && c1.nzc == c2.nzc && c1.nzcu == c2.nzcu)) {
+    MLG_TRY(ihelm_T(s1, alpha));
+    return ihelm_T(s2, alpha);
+  }
+  MLG_TRY(launch_band_solve_T_pair(s1, s2, c1, alpha));
+  for (Scalar* s : {&s1, &s2}) {
+    k_ihelm_T_ln<<<1, 32, 0, G.stream>>>(s->e, s->ln, G.lognorm, G.ell, alpha);
+    MLG_LAUNCH();
+  }
   return 0;
 }
 
@@ -563,11 +650,9 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
     if (G.precision == MLG_MIXED) {
       // as the forward: m >= 1 in FP32, the m = 0 plane in double-float beside it
       MLG_TRY(side_fork());
-      constexpr int DIT = 16, DZT = 8;
-      dim3 dgrid(cdiv(G.nzdim, DZT), cdiv(G.nrh, DIT), 1);
-      k_vec2tp_T<dfl, DIT, DZT, KC><<<dgrid, DIT * DZT / 2, 0, G.side>>>(pb.e, cb.e, ur.e, up.e, uz.e, G.tV, G.tD, G.tT,
-                                                                         G.ak, G.nr, G.nrh, G.ne, G.nrdim, G.npdim,
-                                                                         G.nzdim, nrc, G.chopzl, G.chopzu, 0);
+      k_m0_vec2tp_T_df<<<cdiv((long long)G.nrh * G.nzdim, 8), 256, 0, G.side>>>(
+          pb.e, cb.e, ur.e, up.e, uz.e, G.tD, G.tT, G.ak, G.nr, G.nrh, G.nrdim, G.npdim, G.nzdim,
+          std::max(nrc, 0), G.chopzl, G.chopzu);
       MLG_LAUNCH();
       if (npc > 1) {
         dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc - 1);
@@ -663,9 +748,18 @@ int advection_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const S
 
 // abcn^T (hyperpow = 0): sb holds the adjoint of the new s; on return sb holds the adjoint w.r.t.
 // the old s, and nlb, nlpb have received the adjoints w.r.t. nl and nl_p (added)
-static int abcn_T(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt) {
+static int abcn_T_rest(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt);
+// abcn^T of the psi and chi chains of a step: the two transposed Helmholtz solves in one pass, the
+// rest per field (the chains touch disjoint scalars, so the order between them is free)
+static int abcn_T_pair(Scalar& pb, Scalar& npb, Scalar& nppb, Scalar& cb, Scalar& ncb, Scalar& ncpb, double dt) {
   double a = -2.0 / (dt * G.P.visc);
-  MLG_TRY(ihelm_T(sb, a));
+  MLG_TRY(ihelm_T_pair(pb, cb, a));
+  MLG_TRY(abcn_T_rest(pb, npb, nppb, dt));
+  return abcn_T_rest(cb, ncb, ncpb, dt);
+}
+// abcn^T after its solve: the adjoints of nl and nl_p, and sb mapped to the old s
+static int abcn_T_rest(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt) {
+  double a = -2.0 / (dt * G.P.visc);
   MLG_TRY(lincomb(nlb, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}));
   MLG_TRY(lincomb(nlpb, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}));
   TMP(t);
@@ -703,8 +797,7 @@ static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* con
   MLG_TRY(assign(npb, nppb)); MLG_TRY(assign(ncb, ncpb));
   MLG_TRY(launch_zero(nppb.e)); MLG_TRY(launch_set_ln(nppb.ln, 0.0));
   MLG_TRY(launch_zero(ncpb.e)); MLG_TRY(launch_set_ln(ncpb.ln, 0.0));
-  MLG_TRY(abcn_T(pb, npb, nppb, dt));
-  MLG_TRY(abcn_T(cb, ncb, ncpb, dt));
+  MLG_TRY(abcn_T_pair(pb, npb, nppb, cb, ncb, ncpb, dt));
   for (int i = 0; i < 6; ++i) set_fff0(*ad[i]);
   return 0;
 }

@@ -1441,4 +1441,30 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   return 0;
 }
 
+// A^T x = b for kind 0 on two fields with the same chop window and alpha, in one substitution pass
+// (the psi and chi solves of the adjoint step); results are those of two launch_band_solve_T calls
+int launch_band_solve_T_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
+  if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
+  int npc = std::max(c.npc, 1);
+  size_t nsys = (size_t)npc * G.nzdim;
+  SolveArgs a;
+  a.e = s1.e; a.ws = G.band_ws; a.lnp = s1.ln; a.bd2 = G.bd2; a.ak = G.ak; a.lognorm = G.lognorm;
+  a.status = (int*)(G.dscal + DS_FLAG + 1);
+  a.nrdim = G.nrdim; a.npdim = G.npdim; a.ne = G.ne; a.nrc = c.nrc; a.npc = c.npc; a.nzc = c.nzc; a.nzcu = c.nzcu;
+  a.nzdim = G.nzdim; a.nsys = (int)nsys; a.alpha = alpha; a.beta = 0.0; a.ell = G.ell; a.preln = 0.0;
+  a.kind = 0; a.power = 0; a.skip_root = 0; a.transpose = 1; a.no_ln = 1;
+  a.e2 = s2.e; a.lnp2 = s2.ln;
+  kt_begin(KT_SOLVE);
+  double* fac = nullptr;
+  a.nsp = (int)((nsys + 31) / 32 * 32);
+  MLG_TRY(lu_cache_get(0 + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    MLG_LAUNCH();
+    return 0;
+  }));
+  MLG_TRY(launch_subst<2>(a, fac, nsys));
+  kt_end(KT_SOLVE, solve_bytes(2, c));
+  return 0;
+}
+
 }  // namespace mlg

@@ -189,6 +189,7 @@ int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& ch
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
 int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha);
+int launch_band_solve_T_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha);
 int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha);
 int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, double a);
 

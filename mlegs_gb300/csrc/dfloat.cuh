@@ -36,6 +36,9 @@ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
   return df_quick(p, e);
 }
 struct dfl2 { dfl x, y; };
+__device__ __forceinline__ dfl df_shfl_xor(dfl v, int o) {   // a butterfly step of a warp reduction
+  return dfl(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
+}
 
 // multiply-accumulate in the kernel's arithmetic
 __device__ __forceinline__ double tmac(double a, double b, double c) { return fma(a, b, c); }

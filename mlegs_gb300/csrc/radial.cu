@@ -304,9 +304,6 @@ static int m0_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
 // the m = 0 plane of the backward transform in double-float: one warp per (radial point pair i, column
 // z), the lanes splitting the sums over the rows of each parity and reducing them by shuffles (the
 // plane is 1/50 of the work: spread over every SM it stays shorter than the tensor-core kernel beside it)
-__device__ __forceinline__ dfl df_shfl_xor(dfl v, int o) {
-  return dfl(__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o));
-}
 __global__ void __launch_bounds__(256) k_m0_bwd_df(const double2* __restrict__ in, double2* __restrict__ out,
                                                    const double* __restrict__ pf, const double* __restrict__ lnx,
                                                    const double* __restrict__ lnp, int add_ln, int nr, int nrh, int nrdim,
