@@ -20,6 +20,7 @@
 // W_i = w_i r_i^2 / (1 - x_i^2) * (2 pi / np) * (zlen / nz) the quadrature of the volume integral
 // r dr dphi dz over the mapped Gauss-Legendre points (dr/dx = r / (1 - x^2)).
 #include "common.cuh"
+#include <cstring>
 #include "dfloat.cuh"
 #include <cmath>
 #include <vector>
@@ -705,7 +706,7 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
 // the nonlinear term around (psi, chi) (already dealiased, FFF): nl = dealias(vec2tp(v x w)), nl%ln = 0,
 // v = tp2vec(psi, chi) + (0, 0, uz), w = tp2curlvec(psi, chi).  (nlpsi_bar, nlchi_bar) -> (psi_bar, chi_bar)
 int nlcore_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scalar& nlpb, const Scalar& nlcb, Scalar& psib,
-             Scalar& chib) {
+             Scalar& chib, Scalar* const* vw_kept) {
   TMP(np_); TMP(nc_);
   MLG_TRY(assign(np_, nlpb)); MLG_TRY(assign(nc_, nlcb));
   set_fff0(np_); set_fff0(nc_);
@@ -713,11 +714,18 @@ int nlcore_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scal
   MLG_TRY(launch_set_ln(np_.ln, 0.0)); MLG_TRY(launch_set_ln(nc_.ln, 0.0));
   TMP(obr); TMP(obp); TMP(obz);
   MLG_TRY(vec2tp_T(np_, nc_, obr, obp, obz));
-  // the linearisation point: v and w of the forward
-  TMP(vr); TMP(vp); TMP(vz); TMP(wr); TMP(wp); TMP(wz);
-  MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
+  // the linearisation point: v and w of the forward, kept by the forward step (they are consumed
+  // here) or recomputed from (psi, chi)
+  TMP(vr_t); TMP(vp_t); TMP(vz_t); TMP(wr_t); TMP(wp_t); TMP(wz_t);
+  Scalar* vw[6] = {&vr_t, &vp_t, &vz_t, &wr_t, &wp_t, &wz_t};
+  if (vw_kept) for (int i = 0; i < 6; ++i) vw[i] = vw_kept[i];
+  Scalar &vr = *vw[0], &vp = *vw[1], &vz = *vw[2], &wr = *vw[3], &wp = *vw[4], &wz = *vw[5];
+  if (!vw_kept) {
+    for (Scalar* q : vw) q->set_space("PPP");
+    MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
+    MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
+  }
   MLG_TRY(lincomb(vz, {{&vz, 1.0}, {&uzb, 1.0}}, {}, 1.0, false));
-  MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
   TMP(vbr); TMP(vbp); TMP(vbz); TMP(wbr); TMP(wbp); TMP(wbz);
   k_vecprod_T<<<nblk(G.fsize), 256, 0, G.stream>>>(vbr.e, vbp.e, vbz.e, wbr.e, wbp.e, wbz.e, vr.e, vp.e, vz.e, wr.e, wp.e,
                                                     wz.e, obr.e, obp.e, obz.e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
@@ -741,7 +749,7 @@ int advection_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const S
   TMP(p3); TMP(c3);
   MLG_TRY(assign(p3, psi)); MLG_TRY(assign(c3, chi));
   MLG_TRY(op_dealias(p3)); MLG_TRY(op_dealias(c3));
-  MLG_TRY(nlcore_T(p3, c3, uzb, nlpb, nlcb, psib, chib));
+  MLG_TRY(nlcore_T(p3, c3, uzb, nlpb, nlcb, psib, chib, nullptr));
   MLG_TRY(op_dealias(psib)); MLG_TRY(op_dealias(chib));
   return 0;
 }
@@ -762,9 +770,10 @@ static int abcn_T_rest(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt) {
   double a = -2.0 / (dt * G.P.visc);
   MLG_TRY(lincomb(nlb, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}));
   MLG_TRY(lincomb(nlpb, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}));
-  TMP(t);
-  MLG_TRY(assign(t, sb));
-  MLG_TRY(lincomb(t, {{&t, G.P.visc * a * dt / 2.0}}, {}, 1.0, false));
+  TMP(t);   // t = (visc a dt/2) sb with sb's ln and tags, in one pass
+  std::memcpy(t.space, sb.space, 4);
+  for (int i = 0; i < 3; ++i) t.off[i] = sb.off[i];
+  MLG_TRY(lincomb(t, {{&sb, G.P.visc * a * dt / 2.0}}, {{&sb, 1.0}}));
   MLG_TRY(band_T(t, 2));   // t.e <- del2^T t.e; t.ln <- the log-term adjoint
   MLG_TRY(lincomb(sb, {{&sb, a}, {&t, 1.0}}, {{&sb, a}, {&t, 1.0}}));
   return 0;
@@ -780,12 +789,12 @@ static int adjoint_supported() {
 // One step backward.  st = (psi, chi, nlpsi, nlchi, nlpsi_p, nlchi_p) at the step's end (the point
 // its nonlinear term was evaluated at); ad = the adjoint of that state, replaced by the adjoint of
 // the state at the step's start.
-static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const ad[6]) {
+static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const ad[6], Scalar* const* vw) {
   Scalar& pb = *ad[0]; Scalar& cb = *ad[1];
   Scalar& npb = *ad[2]; Scalar& ncb = *ad[3];
   Scalar& nppb = *ad[4]; Scalar& ncpb = *ad[5];
   TMP(xp); TMP(xc);
-  MLG_TRY(nlcore_T(*st[0], *st[1], uzb, npb, ncb, xp, xc));
+  MLG_TRY(nlcore_T(*st[0], *st[1], uzb, npb, ncb, xp, xc, vw));
   MLG_TRY(lincomb(pb, {{&pb, 1.0}, {&xp, 1.0}}, {{&pb, 1.0}, {&xp, 1.0}}));
   MLG_TRY(lincomb(cb, {{&cb, 1.0}, {&xc, 1.0}}, {{&cb, 1.0}, {&xc, 1.0}}));
   for (Scalar* q : {&pb, &cb}) {
@@ -802,10 +811,11 @@ static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* con
   return 0;
 }
 
-static int forward_step(Scalar* const st[6], const Scalar& uzb, double dt) {
+// keep (optional): receives the step's velocity and vorticity for step_T
+static int forward_step(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const* keep = nullptr) {
   TMP(pp); TMP(cp);
   MLG_TRY(assign(pp, *st[0])); MLG_TRY(assign(cp, *st[1]));
-  return op_vortex_step_dev(*st[0], *st[1], *st[2], *st[3], pp, cp, *st[4], *st[5], uzb, dt, G.dscal + DS_GAIN0);
+  return op_vortex_step_dev(*st[0], *st[1], *st[2], *st[3], pp, cp, *st[4], *st[5], uzb, dt, G.dscal + DS_GAIN0, keep);
 }
 
 // startup from (psi0, chi0): psi <- dealias(psi0), nl <- advection_rhs, nl_p <- nl
@@ -921,8 +931,9 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
   rc = energy(*cur.p[0], *cur.p[1], J, ad.p[0], ad.p[1]);
   for (int i = 2; i < 6 && !rc; ++i) { rc = launch_zero(ad.p[i]->e); if (!rc) rc = launch_set_ln(ad.p[i]->ln, 0.0); set_fff0(*ad.p[i]); }
   for (int i = 0; i < 2 && !rc; ++i) rc = project_active(*ad.p[i]);
-  // backward sweep, segment by segment: recompute the end-of-step states, then step back
-  std::vector<State*> seg;
+  // backward sweep, segment by segment: recompute the end-of-step states (keeping each step's
+  // velocity and vorticity, the linearisation point of its nonlinear term), then step back
+  std::vector<State*> seg, segvw;
   for (int c = (int)ck.size() - 1; c >= 0 && !rc; --c) {
     int s0 = c * k_ckpt, s1 = std::min(nsteps, s0 + k_ckpt);
     int len = s1 - s0;
@@ -930,19 +941,23 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
       State* t = new State();
       if (t->rc) { rc = t->rc; delete t; break; }
       seg.push_back(t);
+      State* v = new State();
+      if (v->rc) { rc = v->rc; delete v; break; }
+      segvw.push_back(v);
     }
     if (rc) break;
     rc = copy_state(cur.p, ck[c]->p);
     for (int q = 0; q < len && !rc; ++q) {
-      rc = forward_step(cur.p, uzb, dt);
+      rc = forward_step(cur.p, uzb, dt, segvw[q]->p);
       if (!rc) rc = copy_state(seg[q]->p, cur.p);
     }
     for (int q = len - 1; q >= 0 && !rc; --q) {
-      rc = step_T(seg[q]->p, uzb, dt, ad.p);
+      rc = step_T(seg[q]->p, uzb, dt, ad.p, segvw[q]->p);
       for (int i = 0; i < 6 && !rc; ++i) rc = project_active(*ad.p[i]);
     }
   }
   for (State* t : seg) delete t;
+  for (State* t : segvw) delete t;
   if (!rc) {
     // through the startup: nl(0) = nl_p(0) = advection_rhs(psi0, chi0)
     TMP(nb); TMP(cb2);
@@ -965,9 +980,11 @@ int adjoint_step(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* cons
   MLG_TRY(adjoint_supported());
   State e;
   if (e.rc) return e.rc;
+  State vw;
+  if (vw.rc) return vw.rc;
   MLG_TRY(copy_state(e.p, st));
-  MLG_TRY(forward_step(e.p, uzb, dt));
-  return step_T(e.p, uzb, dt, ad);
+  MLG_TRY(forward_step(e.p, uzb, dt, vw.p));
+  return step_T(e.p, uzb, dt, ad, vw.p);
 }
 
 }  // namespace mlg

@@ -180,9 +180,12 @@ int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scal
 int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, Scalar& wz);
 int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz);
 int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi);
-int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz);
+// keep (optional): six scalars that receive the velocity and vorticity (vr, vp, vz, wr, wp, wz, in PPP,
+// vz without the background) the nonlinear term was formed from
+int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz,
+                     Scalar* const* keep = nullptr);
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
-                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev);
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep = nullptr);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale);
 int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c);

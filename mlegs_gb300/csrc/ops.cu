@@ -206,9 +206,9 @@ __global__ void k_scale_r(double2* __restrict__ e, const double* __restrict__ r,
 // vecprod (mlegs_scalar_ops.f90:1264-1306) on the packed reals; everything else zero
 // v x u on the packed samples; vzb (optional): a field added to vz first (the background axial flow of
 // advection_rhs, vortical_flow_3d.f90:371, with the rounding of that separate addition)
-__global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, double2* __restrict__ vz,
-                          const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
-                          const double2* __restrict__ vzb, int nr, int nph, int nrdim, int npdim, int nzdim) {
+__global__ void k_vecprod(double2* vr, double2* vp, double2* vz, const double2* __restrict__ ur,
+                          const double2* __restrict__ up, const double2* __restrict__ uz, const double2* __restrict__ vzb,
+                          double2* o_r, double2* o_p, double2* o_z, int nr, int nph, int nrdim, int npdim, int nzdim) {
   size_t n = (size_t)nrdim * npdim * nzdim;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
@@ -221,7 +221,7 @@ __global__ void k_vecprod(double2* __restrict__ vr, double2* __restrict__ vp, do
       o2 = make_double2(A3.x * B1.x - A1.x * B3.x, A3.y * B1.y - A1.y * B3.y);
       o3 = make_double2(A1.x * B2.x - A2.x * B1.x, A1.y * B2.y - A2.y * B1.y);
     }
-    vr[idx] = o1; vp[idx] = o2; vz[idx] = o3;
+    o_r[idx] = o1; o_p[idx] = o2; o_z[idx] = o3;   // in place when the outputs are (vr, vp, vz)
   }
 }
 
@@ -813,14 +813,17 @@ static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar
 
 // ------------------------------------------------------------------------------------------------
 // vector fields (:1264-1560)
+// (vr, vp, vz) x (ur, up, uz), vz plus the background vzb when given, into out (or in place)
 static int vecprod_bg(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz,
-                      const Scalar* vzb) {
+                      const Scalar* vzb, Scalar* const* out = nullptr) {
   for (const Scalar* q : {(const Scalar*)&vr, (const Scalar*)&vp, (const Scalar*)&vz, &ur, &up, &uz})
     if (!q->is("PPP")) return set_error(MLG_ESPACE, "vector_product: to compute v x u, all inputs must be in PPP");
-  k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, vzb ? vzb->e : nullptr, G.nr,
-                                                 G.np / 2, G.nrdim, G.npdim, G.nzdim);
+  Scalar* o[3] = {&vr, &vp, &vz};
+  if (out) for (int i = 0; i < 3; ++i) o[i] = out[i];
+  k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, vzb ? vzb->e : nullptr, o[0]->e,
+                                                 o[1]->e, o[2]->e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
   MLG_LAUNCH();
-  for (Scalar* q : {&vr, &vp, &vz}) { MLG_TRY(launch_set_ln(q->ln, 0.0)); q->off[0] = q->off[1] = q->off[2] = 0; }
+  for (Scalar* q : o) { MLG_TRY(launch_set_ln(q->ln, 0.0)); q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
   return 0;
 }
 int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
@@ -934,16 +937,21 @@ int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, 
 }
 
 // advection_rhs (vortical_flow_3d.f90:353-395)
-int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz) {
+int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz, Scalar* const* keep) {
   if (!psi.is("FFF") || !chi.is("FFF") || !nlpsi.is("FFF") || !nlchi.is("FFF") || !uz.is("PPP"))
     return set_error(MLG_ESPACE, "advection_rhs: psi, chi, nlpsi, nlchi must be in FFF and uz in PPP");
   MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
-  TMP(vr); TMP(vp); TMP(vz); TMP(wr); TMP(wp); TMP(wz);
-  for (Scalar* q : {&vr, &vp, &vz, &wr, &wp, &wz}) q->set_space("PPP");
+  TMP(vr_t); TMP(vp_t); TMP(vz_t); TMP(wr_t); TMP(wp_t); TMP(wz_t);
+  Scalar* vw[6] = {&vr_t, &vp_t, &vz_t, &wr_t, &wp_t, &wz_t};
+  if (keep) for (int i = 0; i < 6; ++i) vw[i] = keep[i];
+  for (Scalar* q : vw) q->set_space("PPP");
+  Scalar &vr = *vw[0], &vp = *vw[1], &vz = *vw[2], &wr = *vw[3], &wp = *vw[4], &wz = *vw[5];
   MLG_TRY(tp2vec_into(psi, chi, vr, vp, vz));
   MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
-  MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz));   // (vz + uz) with the background flow
-  MLG_TRY(vec2tp_core(vr, vp, vz, nlpsi, nlchi));
+  // (vz + uz) with the background flow; in place, or into the temporaries when v and w are kept
+  Scalar* prod[3] = {&vr_t, &vp_t, &vz_t};
+  MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz, keep ? prod : nullptr));
+  MLG_TRY(vec2tp_core(vr_t, vp_t, vz_t, nlpsi, nlchi));
   MLG_TRY(launch_set_ln(nlpsi.ln, 0.0)); MLG_TRY(launch_set_ln(nlchi.ln, 0.0));
   MLG_TRY(op_dealias(nlpsi)); MLG_TRY(op_dealias(nlchi));
   return 0;
@@ -951,13 +959,13 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
 
 // main-loop step (vortical_flow_3d.f90:168-180) with the gains in device memory
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
-                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev) {
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep) {
   for (Scalar* q : {&psi, &chi, &nlpsi, &nlchi, &psip, &chip, &nlpsip, &nlchip}) MLG_TRY(op_trans(*q, "FFF"));
   MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt));
   MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
   MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
   MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
-  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz));
+  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz, keep));
   k_finite<<<nblk(G.fsize), 256, 0, G.stream>>>(psi.e, chi.e, G.fsize, (int*)(G.dscal + DS_FLAG));
   MLG_LAUNCH();
   return 0;
