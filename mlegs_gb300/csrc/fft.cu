@@ -351,20 +351,22 @@ __device__ __forceinline__ void fft2pass(typename CT<T>::t* a, typename CT<T>::t
   }
 }
 
-// z FFT: lines (r, m) for m = m0 + blockIdx.y, points at stride nrdim*npdim
+// z FFT: the lines (r, m) of m in [m0, m0 + nm) taken flat, line r + nrdim*(m - m0) at offset
+// r + nrdim*m (so a block's lanes read one run of consecutive offsets and no block is left ragged at
+// the end of an m), points at stride nrdim*npdim
 template <typename T, int L, int SGN, int TRL>
 __global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restrict__ e, int nrdim, int npdim,
-                                                              const typename TW<T>::t* __restrict__ tw, T scale, int m0) {
+                                                              const typename TW<T>::t* __restrict__ tw, T scale, int m0,
+                                                              int nlines) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   int lane = threadIdx.x, w = threadIdx.y;
-  int r = blockIdx.x * TRL + lane;
-  int m = blockIdx.y + m0;
-  bool ok = r < nrdim;
+  const int line = blockIdx.x * TRL + lane;
+  bool ok = line < nlines;
   size_t ps = (size_t)nrdim * npdim;
-  double2* base = e + r + (size_t)nrdim * m;
+  double2* base = e + (size_t)nrdim * m0 + line;
   C a[R1];
 #pragma unroll
   for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * ps) : mk<T>(0, 0);
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restric
 // φ forward: packed reals -> X_0..X_L scaled, in place (lines (r, z)); mixed form: X_0 from the FP64
 // sum of the row, the FP32 transform on the samples minus their FP64 mean
 template <typename T, int L, int TRL>
-__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __restrict__ e, int nrdim, int npdim,
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __restrict__ e, int nrdim, int npdim, int nzdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
                                                                   const typename TW<T>::t* __restrict__ twr, T scale,
                                                                   double scale_d, double inv_np,
@@ -394,9 +396,9 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
   C* S = (C*)smem_raw;
   double* red = (double*)(smem_raw + (size_t)L * TRL * sizeof(C));
   int lane = threadIdx.x, w = threadIdx.y;
-  int r = blockIdx.x * TRL + lane;
-  int z = blockIdx.y;
-  bool ok = r < nrdim;
+  const int line = blockIdx.x * TRL + lane;   // the lines (r, z) taken flat: r + nrdim*z
+  bool ok = line < nrdim * nzdim;
+  const int r = line % nrdim, z = line / nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
   const bool rsc = rs != nullptr && ok && r < nrs;   // the row's samples times rs[r] first (scale_r)
   const double rv = rsc ? rs[r] : 1.0;
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
 // φ backward: X_0..X_L -> packed reals (unnormalised), slot L <- np X_L, in place; mixed form: Re X_0
 // left out of the FP32 transform and added to every sample in FP64
 template <typename T, int L, int TRL>
-__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __restrict__ e, int nrdim, int npdim,
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __restrict__ e, int nrdim, int npdim, int nzdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
                                                                   const typename TW<T>::t* __restrict__ twr, double np_d,
                                                                   const double* __restrict__ rs, int nrs) {
@@ -467,9 +469,9 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __res
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   int lane = threadIdx.x, w = threadIdx.y;
-  int r = blockIdx.x * TRL + lane;
-  int z = blockIdx.y;
-  bool ok = r < nrdim;
+  const int line = blockIdx.x * TRL + lane;   // the lines (r, z) taken flat: r + nrdim*z
+  bool ok = line < nrdim * nzdim;
+  const int r = line % nrdim, z = line / nrdim;
   double2* base = e + r + (size_t)nrdim * npdim * z;
   double2 nyq = make_double2(0, 0);
   double dc = 0.0;
@@ -545,8 +547,10 @@ template <typename T, int L, int SGN, int TRL>
 static int zfft2_launch(cd* e, double scale, int m0, int nm, cudaStream_t stream) {
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_zfft2<T, L, SGN, TRL>, sm));
-  dim3 grid(cdiv(G.nrdim, TRL), nm), blk(TRL, Split<L>::R2);
-  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0);
+  const int nlines = G.nrdim * nm;
+  dim3 grid(cdiv(nlines, TRL)), blk(TRL, Split<L>::R2);
+  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0,
+                                                     nlines);
   MLG_LAUNCH();
   return 0;
 }
@@ -608,15 +612,15 @@ static int pfft2_launch(cd* e, int dir, double scale, const double* rs) {
   constexpr int TRL = 32;
   constexpr bool DC = std::is_same<T, float>::value;
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t) + (DC && dir < 0 ? (size_t)Split<L>::R2 * TRL * sizeof(double) : 0);
-  dim3 grid(cdiv(G.nrdim, TRL), G.nzdim), blk(TRL, Split<L>::R2);
+  dim3 grid(cdiv((long long)G.nrdim * G.nzdim, TRL)), blk(TRL, Split<L>::R2);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_pfft_fwd2<T, L, TRL>, sm));
-    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
+    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
                                                         tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np, rs,
                                                         G.nr);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_pfft_bwd2<T, L, TRL>, sm));
-    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_p, G.tw_p32),
+    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
                                                         tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, rs, G.nr);
   }
   MLG_LAUNCH();
