@@ -128,6 +128,8 @@ int launch_vfft_buf(cd* e, int dir);
 int launch_vfft_scaled(cd* e, int dir, double scale);
 int launch_hfft_fwd_scaled(cd* e, double scale);
 int launch_hfft_bwd_buf(cd* e);
+int launch_vfft_multi(Scalar* const* s, int n, int dir);   // n <= 6 fields in one pass
+int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir);
 int launch_rtrans_fwd(Scalar& s);
 int launch_rtrans_bwd(Scalar& s, bool add_ln);
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx

@@ -351,11 +351,20 @@ __device__ __forceinline__ void fft2pass(typename CT<T>::t* a, typename CT<T>::t
   }
 }
 
+// a set of fields transformed by one launch (the components of a vector field, stage by stage): their
+// lines are taken flat, field after field, so that one launch has enough blocks to fill the GPU
+constexpr int FS_MAX = 6;
+struct FSet {
+  double2* e[FS_MAX];
+  const double* rs[FS_MAX];   // per field: the row scaling of the phi transforms, or null
+  int n;
+};
+
 // z FFT: the lines (r, m) of m in [m0, m0 + nm) taken flat, line r + nrdim*(m - m0) at offset
 // r + nrdim*m (so a block's lanes read one run of consecutive offsets and no block is left ragged at
 // the end of an m), points at stride nrdim*npdim
 template <typename T, int L, int SGN, int TRL>
-__global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restrict__ e, int nrdim, int npdim,
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(FSet fs, int nrdim, int npdim,
                                                               const typename TW<T>::t* __restrict__ tw, T scale, int m0,
                                                               int nlines) {
   typedef typename CT<T>::t C;
@@ -363,10 +372,11 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restric
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   int lane = threadIdx.x, w = threadIdx.y;
-  const int line = blockIdx.x * TRL + lane;
-  bool ok = line < nlines;
+  const int gl = blockIdx.x * TRL + lane;     // line over the set; nlines per field
+  const int f = gl / nlines, line = gl - f * nlines;
+  bool ok = f < fs.n;
   size_t ps = (size_t)nrdim * npdim;
-  double2* base = e + (size_t)nrdim * m0 + line;
+  double2* base = (ok ? fs.e[f] : fs.e[0]) + (size_t)nrdim * m0 + line;
   C a[R1];
 #pragma unroll
   for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * ps) : mk<T>(0, 0);
@@ -384,11 +394,10 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(double2* __restric
 // φ forward: packed reals -> X_0..X_L scaled, in place (lines (r, z)); mixed form: X_0 from the FP64
 // sum of the row, the FP32 transform on the samples minus their FP64 mean
 template <typename T, int L, int TRL>
-__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __restrict__ e, int nrdim, int npdim, int nzdim,
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int nrdim, int npdim, int nzdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
                                                                   const typename TW<T>::t* __restrict__ twr, T scale,
-                                                                  double scale_d, double inv_np,
-                                                                  const double* __restrict__ rs, int nrs) {
+                                                                  double scale_d, double inv_np, int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
   constexpr bool DC = std::is_same<T, float>::value;
@@ -396,10 +405,13 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
   C* S = (C*)smem_raw;
   double* red = (double*)(smem_raw + (size_t)L * TRL * sizeof(C));
   int lane = threadIdx.x, w = threadIdx.y;
-  const int line = blockIdx.x * TRL + lane;   // the lines (r, z) taken flat: r + nrdim*z
-  bool ok = line < nrdim * nzdim;
+  const int per = nrdim * nzdim;               // the lines (r, z) of a field taken flat: r + nrdim*z
+  const int gl = blockIdx.x * TRL + lane;
+  const int f = gl / per, line = gl - f * per;
+  bool ok = f < fs.n;
   const int r = line % nrdim, z = line / nrdim;
-  double2* base = e + r + (size_t)nrdim * npdim * z;
+  double2* base = (ok ? fs.e[f] : fs.e[0]) + r + (size_t)nrdim * npdim * z;
+  const double* rs = ok ? fs.rs[f] : nullptr;
   const bool rsc = rs != nullptr && ok && r < nrs;   // the row's samples times rs[r] first (scale_r)
   const double rv = rsc ? rs[r] : 1.0;
   C a[R1];
@@ -459,20 +471,23 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(double2* __res
 // φ backward: X_0..X_L -> packed reals (unnormalised), slot L <- np X_L, in place; mixed form: Re X_0
 // left out of the FP32 transform and added to every sample in FP64
 template <typename T, int L, int TRL>
-__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(double2* __restrict__ e, int nrdim, int npdim, int nzdim,
+__global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int nrdim, int npdim, int nzdim,
                                                                   const typename TW<T>::t* __restrict__ tw,
                                                                   const typename TW<T>::t* __restrict__ twr, double np_d,
-                                                                  const double* __restrict__ rs, int nrs) {
+                                                                  int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
   constexpr bool DC = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   int lane = threadIdx.x, w = threadIdx.y;
-  const int line = blockIdx.x * TRL + lane;   // the lines (r, z) taken flat: r + nrdim*z
-  bool ok = line < nrdim * nzdim;
+  const int per = nrdim * nzdim;               // the lines (r, z) of a field taken flat: r + nrdim*z
+  const int gl = blockIdx.x * TRL + lane;
+  const int f = gl / per, line = gl - f * per;
+  bool ok = f < fs.n;
   const int r = line % nrdim, z = line / nrdim;
-  double2* base = e + r + (size_t)nrdim * npdim * z;
+  double2* base = (ok ? fs.e[f] : fs.e[0]) + r + (size_t)nrdim * npdim * z;
+  const double* rs = ok ? fs.rs[f] : nullptr;
   double2 nyq = make_double2(0, 0);
   double dc = 0.0;
   if (ok && w == 0) nyq = base[(size_t)L * nrdim];
@@ -543,104 +558,119 @@ static int set_smem(const void* fn, size_t bytes) {
   return 0;
 }
 
+static FSet fset1(cd* e, const double* rs = nullptr) {
+  FSet fs{};
+  fs.e[0] = e; fs.rs[0] = rs; fs.n = 1;
+  return fs;
+}
+
 template <typename T, int L, int SGN, int TRL>
-static int zfft2_launch(cd* e, double scale, int m0, int nm, cudaStream_t stream) {
+static int zfft2_launch(const FSet& fs, double scale, int m0, int nm, cudaStream_t stream) {
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_zfft2<T, L, SGN, TRL>, sm));
   const int nlines = G.nrdim * nm;
-  dim3 grid(cdiv(nlines, TRL)), blk(TRL, Split<L>::R2);
-  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0,
+  dim3 grid(cdiv((long long)nlines * fs.n, TRL)), blk(TRL, Split<L>::R2);
+  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(fs, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0,
                                                      nlines);
   MLG_LAUNCH();
   return 0;
 }
 template <typename T, int L, int TRL>
-static int zfft2_dir(cd* e, int dir, double scale, int m0, int nm, cudaStream_t stream) {
-  return dir < 0 ? zfft2_launch<T, L, -1, TRL>(e, scale, m0, nm, stream) : zfft2_launch<T, L, +1, TRL>(e, scale, m0, nm, stream);
+static int zfft2_dir(const FSet& fs, int dir, double scale, int m0, int nm, cudaStream_t stream) {
+  return dir < 0 ? zfft2_launch<T, L, -1, TRL>(fs, scale, m0, nm, stream) : zfft2_launch<T, L, +1, TRL>(fs, scale, m0, nm, stream);
 }
 template <typename T, int TRL>
-static int zfft2_any(cd* e, int dir, double scale, int m0, int nm, cudaStream_t stream) {
+static int zfft2_any(const FSet& fs, int dir, double scale, int m0, int nm, cudaStream_t stream) {
   switch (G.nz) {
-    case 16: return zfft2_dir<T, 16, TRL>(e, dir, scale, m0, nm, stream);
-    case 32: return zfft2_dir<T, 32, TRL>(e, dir, scale, m0, nm, stream);
-    case 64: return zfft2_dir<T, 64, TRL>(e, dir, scale, m0, nm, stream);
-    case 128: return zfft2_dir<T, 128, TRL>(e, dir, scale, m0, nm, stream);
-    case 256: return zfft2_dir<T, 256, TRL>(e, dir, scale, m0, nm, stream);
+    case 16: return zfft2_dir<T, 16, TRL>(fs, dir, scale, m0, nm, stream);
+    case 32: return zfft2_dir<T, 32, TRL>(fs, dir, scale, m0, nm, stream);
+    case 64: return zfft2_dir<T, 64, TRL>(fs, dir, scale, m0, nm, stream);
+    case 128: return zfft2_dir<T, 128, TRL>(fs, dir, scale, m0, nm, stream);
+    case 256: return zfft2_dir<T, 256, TRL>(fs, dir, scale, m0, nm, stream);
   }
   return -1;
 }
 static bool pow2_fast(int L) { return L == 16 || L == 32 || L == 64 || L == 128 || L == 256; }
 
 template <typename T>
-static int vfft_t(cd* e, int dir, double scale, int m0, int nm, int tr_max, cudaStream_t stream) {
+static int vfft_t(const FSet& fs, int dir, double scale, int m0, int nm, int tr_max, cudaStream_t stream) {
   int L = G.nz;
   if (L <= 1 || nm <= 0) return 0;
-  if (pow2_fast(L)) return tr_max >= 32 ? zfft2_any<T, 32>(e, dir, scale, m0, nm, stream) : zfft2_any<T, 8>(e, dir, scale, m0, nm, stream);
+  if (pow2_fast(L)) return tr_max >= 32 ? zfft2_any<T, 32>(fs, dir, scale, m0, nm, stream) : zfft2_any<T, 8>(fs, dir, scale, m0, nm, stream);
   int TR = std::min(pick_tr(L, sizeof(typename CT<T>::t)), tr_max);
   int TT = std::max(1, std::min(256 / TR, L / 2));
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), nm), blk(TR, TT);
-  k_vfft<T><<<grid, blk, sm, stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
-  MLG_LAUNCH();
+  for (int f = 0; f < fs.n; ++f) {   // other lengths: the Stockham kernel, field by field
+    k_vfft<T><<<grid, blk, sm, stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
+    MLG_LAUNCH();
+  }
   return 0;
 }
 
 // plain form: FP64.  Mixed form: m >= 1 in FP32; the m = 0 lines (the axisymmetric part, with the mean
 // flow in its k = 0 coefficient) in FP64, in small CTAs so that they spread over the SMs.
-static int vfft_any(cd* e, int dir, double scale) {
+static int vfft_any(const FSet& fs, int dir, double scale) {
   kt_begin(1);
   if (G.precision == MLG_MIXED) {
     MLG_TRY(side_fork());
-    MLG_TRY(vfft_t<double>(e, dir, scale, 0, 1, 2, G.side));
-    MLG_TRY(vfft_t<float>(e, dir, scale, 1, G.npdim - 1, 32, G.stream));
+    MLG_TRY(vfft_t<double>(fs, dir, scale, 0, 1, 2, G.side));
+    MLG_TRY(vfft_t<float>(fs, dir, scale, 1, G.npdim - 1, 32, G.stream));
     MLG_TRY(side_join());
   } else {
-    MLG_TRY(vfft_t<double>(e, dir, scale, 0, G.npdim, 32, G.stream));
+    MLG_TRY(vfft_t<double>(fs, dir, scale, 0, G.npdim, 32, G.stream));
   }
-  kt_end(1, 2.0 * G.fsize * 16);
+  kt_end(1, 2.0 * fs.n * G.fsize * 16);
   return 0;
 }
 
-int launch_vfft_buf(cd* e, int dir) { return vfft_any(e, dir, dir < 0 ? 1.0 / G.nz : 1.0); }
+int launch_vfft_buf(cd* e, int dir) { return vfft_any(fset1(e), dir, dir < 0 ? 1.0 / G.nz : 1.0); }
 // sum_j x_j exp(dir 2 pi i jk/nz) * scale, any direction and scale (the adjoint's FFTs)
-int launch_vfft_scaled(cd* e, int dir, double scale) { return vfft_any(e, dir, scale); }
+int launch_vfft_scaled(cd* e, int dir, double scale) { return vfft_any(fset1(e), dir, scale); }
 int launch_vfft(Scalar& s, int dir) { return launch_vfft_buf(s.e, dir); }
+// the z transform of n fields in one pass (forward scaled by 1/nz)
+int launch_vfft_multi(Scalar* const* s, int n, int dir) {
+  if (n < 1 || n > FS_MAX) return set_error(MLG_EPARAM, "vertical_fft: 1 to 6 fields per batch");
+  FSet fs{};
+  for (int i = 0; i < n; ++i) { fs.e[i] = s[i]->e; fs.rs[i] = nullptr; }
+  fs.n = n;
+  return vfft_any(fs, dir, dir < 0 ? 1.0 / G.nz : 1.0);
+}
 
 template <typename T, int L>
-static int pfft2_launch(cd* e, int dir, double scale, const double* rs) {
+static int pfft2_launch(const FSet& fs, int dir, double scale) {
   constexpr int TRL = 32;
   constexpr bool DC = std::is_same<T, float>::value;
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t) + (DC && dir < 0 ? (size_t)Split<L>::R2 * TRL * sizeof(double) : 0);
-  dim3 grid(cdiv((long long)G.nrdim * G.nzdim, TRL)), blk(TRL, Split<L>::R2);
+  dim3 grid(cdiv((long long)G.nrdim * G.nzdim * fs.n, TRL)), blk(TRL, Split<L>::R2);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_pfft_fwd2<T, L, TRL>, sm));
-    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np, rs,
-                                                        G.nr);
+    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np, G.nr);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_pfft_bwd2<T, L, TRL>, sm));
-    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, rs, G.nr);
+    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
+                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, G.nr);
   }
   MLG_LAUNCH();
   return 0;
 }
 
 template <typename T>
-static int hfft_t(cd* e, int dir, double scale, const double* rs = nullptr) {
+static int hfft_t(const FSet& fs, int dir, double scale) {
   int L = G.nph;
   if (G.np <= 1) return 0;
   kt_begin(1);
   if (pow2_fast(L)) {
     switch (L) {
-      case 16: MLG_TRY((pfft2_launch<T, 16>(e, dir, scale, rs))); break;
-      case 32: MLG_TRY((pfft2_launch<T, 32>(e, dir, scale, rs))); break;
-      case 64: MLG_TRY((pfft2_launch<T, 64>(e, dir, scale, rs))); break;
-      case 128: MLG_TRY((pfft2_launch<T, 128>(e, dir, scale, rs))); break;
-      case 256: MLG_TRY((pfft2_launch<T, 256>(e, dir, scale, rs))); break;
+      case 16: MLG_TRY((pfft2_launch<T, 16>(fs, dir, scale))); break;
+      case 32: MLG_TRY((pfft2_launch<T, 32>(fs, dir, scale))); break;
+      case 64: MLG_TRY((pfft2_launch<T, 64>(fs, dir, scale))); break;
+      case 128: MLG_TRY((pfft2_launch<T, 128>(fs, dir, scale))); break;
+      case 256: MLG_TRY((pfft2_launch<T, 256>(fs, dir, scale))); break;
     }
-    kt_end(1, 2.0 * G.fsize * 16);
+    kt_end(1, 2.0 * fs.n * G.fsize * 16);
     return 0;
   }
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
@@ -648,18 +678,20 @@ static int hfft_t(cd* e, int dir, double scale, const double* rs = nullptr) {
   constexpr bool DC = std::is_same<T, float>::value;
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t) + (DC ? (size_t)TT * TR * sizeof(double) : 0);
   dim3 grid(cdiv(G.nrdim, TR), G.nzdim), blk(TR, TT);
-  if (dir < 0) {
-    MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
-    k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale,
-                                                scale, 1.0 / G.np, rs, G.nr);
-  } else {
-    MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
-    k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(e, G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, rs, G.nr);
+  if (dir < 0) MLG_TRY(set_smem<T>((const void*)k_hfft_fwd<T>, sm));
+  else MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
+  for (int f = 0; f < fs.n; ++f) {   // other lengths: the Stockham kernels, field by field
+    if (dir < 0) {
+      k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
+                                                  tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale,
+                                                  scale, 1.0 / G.np, fs.rs[f], G.nr);
+    } else {
+      k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
+                                                  tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, fs.rs[f], G.nr);
+    }
+    MLG_LAUNCH();
   }
-  MLG_LAUNCH();
-  kt_end(1, 2.0 * G.fsize * 16);
+  kt_end(1, 2.0 * fs.n * G.fsize * 16);
   return 0;
 }
 
@@ -667,18 +699,30 @@ int launch_hfft(Scalar& s, int dir) { return launch_hfft_rs(s, dir, nullptr); }
 // with rs: the rows i < nr of the field times rs[i] before the forward transform / after the
 // backward one (scale_r folded into the transform)
 int launch_hfft_rs(Scalar& s, int dir, const double* rs) {
-  if (G.npchop + s.off[1] > G.npdim)
-    return set_error(MLG_ECHOP, dir < 0 ? "horizontal_fft_forward: chopping in p too large"
-                                        : "horizontal_fft_fbackard: chopping in p too large");
-  return G.precision == MLG_MIXED ? hfft_t<float>(s.e, dir, 1.0 / G.np, rs) : hfft_t<double>(s.e, dir, 1.0 / G.np, rs);
+  Scalar* ps = &s;
+  return launch_hfft_multi(&ps, &rs, 1, dir);
+}
+// the phi transform of n fields in one pass, field i's rows times rs[i] (before the forward / after
+// the backward transform) where rs[i] is not null
+int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir) {
+  if (n < 1 || n > FS_MAX) return set_error(MLG_EPARAM, "horizontal_fft: 1 to 6 fields per batch");
+  FSet fs{};
+  for (int i = 0; i < n; ++i) {
+    if (G.npchop + s[i]->off[1] > G.npdim)
+      return set_error(MLG_ECHOP, dir < 0 ? "horizontal_fft_forward: chopping in p too large"
+                                          : "horizontal_fft_fbackard: chopping in p too large");
+    fs.e[i] = s[i]->e; fs.rs[i] = rs ? rs[i] : nullptr;
+  }
+  fs.n = n;
+  return G.precision == MLG_MIXED ? hfft_t<float>(fs, dir, 1.0 / G.np) : hfft_t<double>(fs, dir, 1.0 / G.np);
 }
 // the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs)
 int launch_hfft_fwd_scaled(cd* e, double scale) {
-  return G.precision == MLG_MIXED ? hfft_t<float>(e, -1, scale) : hfft_t<double>(e, -1, scale);
+  return G.precision == MLG_MIXED ? hfft_t<float>(fset1(e), -1, scale) : hfft_t<double>(fset1(e), -1, scale);
 }
 // the half-complex-to-real sum (unnormalised, Nyquist slot kept times np), on a raw buffer
 int launch_hfft_bwd_buf(cd* e) {
-  return G.precision == MLG_MIXED ? hfft_t<float>(e, +1, 1.0) : hfft_t<double>(e, +1, 1.0);
+  return G.precision == MLG_MIXED ? hfft_t<float>(fset1(e), +1, 1.0) : hfft_t<double>(fset1(e), +1, 1.0);
 }
 
 }  // namespace mlg

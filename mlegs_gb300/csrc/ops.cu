@@ -479,10 +479,14 @@ static int space_code(const char* sp) {
   return -1;
 }
 
-static int vfft_checked(Scalar& s, int dir) {
+static int vfft_check(const Scalar& s, int dir) {
   int nzc = G.chopzl + s.off[2], nzcu = G.chopzu - s.off[2];
   if (2 * s.off[2] > nzcu - nzc)
     return set_error(MLG_ECHOP, dir < 0 ? "vertical_fft_forward: chopping in z too large" : "vertical_fft_backward: chopping in z too large");
+  return 0;
+}
+static int vfft_checked(Scalar& s, int dir) {
+  MLG_TRY(vfft_check(s, dir));
   return launch_vfft(s, dir);
 }
 
@@ -841,15 +845,26 @@ int scale_r(Scalar& s, int mode) {
 // vector_projection on (ur, up, uz) PPP fields that it may overwrite (the caller's copies or its own
 // temporaries): r*ur, r*up enter the φ transforms (scale_r folded into them)
 static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& chi) {
-  if (G.np > 1) MLG_TRY(launch_hfft_rs(ur, -1, G.r));
-  else MLG_TRY(scale_r(ur, 0));
-  ur.set_space("PFP");
-  if (G.nz > 1) MLG_TRY(vfft_checked(ur, -1));
+  // the three components stage by stage, each stage one launch over the three: phi forward (ur and up
+  // times r first), then up's radial forward (op_trans's PFP -> FFP step), then z forward
+  Scalar* u3[3] = {&ur, &uz, &up};   // up last: its radial transform follows while it is in L2
+  if (G.nz > 1)
+    for (Scalar* q : u3) MLG_TRY(vfft_check(*q, -1));
+  if (G.np > 1) {
+    const double* rs[3] = {G.r, nullptr, G.r};
+    MLG_TRY(launch_hfft_multi(u3, rs, 3, -1));
+  } else {
+    MLG_TRY(scale_r(ur, 0));
+    MLG_TRY(scale_r(up, 0));
+  }
+  for (Scalar* q : u3) q->set_space("PFP");
+  MLG_TRY(launch_ln_adjust(up, -1.0));
+  MLG_TRY(launch_rtrans_fwd(up));
+  up.set_space("FFP");
+  if (G.nz > 1) MLG_TRY(launch_vfft_multi(u3, 3, -1));
   ur.set_space("PFF");
-  if (G.np > 1) MLG_TRY(launch_hfft_rs(up, -1, G.r));
-  else MLG_TRY(scale_r(up, 0));
-  up.set_space("PFP");
-  MLG_TRY(op_trans(up, "FFF"));
+  up.set_space("FFF");
+  uz.set_space("PFF");
   MLG_TRY(calcat_dev(up, G.at1, false));
   k_set_ln_from_calc<<<1, 32, 0, G.stream>>>(psi.ln, (const double2*)(G.dscal + DS_CALC), -1.0 / 2.0);
   MLG_LAUNCH();
@@ -857,9 +872,6 @@ static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& 
   up.set_space("PFF");
   k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
   MLG_LAUNCH();
-  MLG_TRY(op_trans(uz, "PFP"));
-  if (G.nz > 1) MLG_TRY(vfft_checked(uz, -1));
-  uz.set_space("PFF");
   // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331); psi%ln was set above from calcat1
   MLG_TRY(launch_zero(psi.e));
   MLG_TRY(launch_zero(chi.e));
@@ -887,27 +899,51 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
   return vec2tp_core(ur, up, uz, psi, chi);
 }
 
-// vector_reconstruction into (ur, up, uz), none of them aliasing psi or chi: they are the workspace
-// (the same steps as copying chi / psi into temporaries and the temporaries into the outputs)
-static int tp2vec_into(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
+// vector_reconstruction up to its transforms: (ur, up, uz) in FFF from (psi, chi), none of them
+// aliasing psi or chi (they are the workspace: the same steps as copying chi / psi into temporaries and
+// the temporaries into the outputs)
+static int tp2vec_spec(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
   for (Scalar* q : {&ur, &up, &uz}) { q->set_space("FFF"); q->off[0] = 3; q->off[1] = q->off[2] = 0; }
   ChopIdx c;
   MLG_TRY(chop_index(ur, c));
   MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c));       // r d/dr chi, r d/dr psi and their mix
-  ur.off[0] = 0; up.off[0] = 0;
-  MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
-  // to PPP, the last φ transform dividing by r (scale_r folded into it)
-  for (Scalar* q : {&ur, &up}) {
-    MLG_TRY(op_trans(*q, "PFP"));
-    if (G.np > 1) MLG_TRY(launch_hfft_rs(*q, +1, G.rinv));
-    else MLG_TRY(scale_r(*q, 1));
-    q->set_space("PPP");
-  }
   MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0));   // -del2h chi
-  uz.off[0] = 0;
-  MLG_TRY(op_chop(uz));
-  MLG_TRY(op_trans(uz, "PPP"));
+  for (Scalar* q : {&ur, &up, &uz}) { q->off[0] = 0; MLG_TRY(op_chop(*q)); }
   return 0;
+}
+
+// FFF -> PPP of n fields (the components of one or two vector fields), stage by stage, each stage one
+// launch over all of them: z backward, radial backward, phi backward, the rows of the fields with
+// by_r[i] divided by r (scale_r folded into the last transform)
+static int to_ppp_batch(Scalar* const* f, const bool* by_r, int n) {
+  for (int i = 0; i < n; ++i) {
+    if (!f[i]->is("FFF")) return set_error(MLG_ESPACE, "trans: batched backward transforms start from FFF");
+    if (G.nz > 1) MLG_TRY(vfft_check(*f[i], +1));
+  }
+  if (G.nz > 1) MLG_TRY(launch_vfft_multi(f, n, +1));
+  for (int i = n - 1; i >= 0; --i) {   // the last z output first: it is the likeliest still in L2
+    f[i]->set_space("FFP");
+    MLG_TRY(launch_rtrans_bwd(*f[i], true));
+    f[i]->set_space("PFP");
+  }
+  if (G.np > 1) {
+    const double* rs[6];
+    for (int i = 0; i < n; ++i) rs[i] = by_r[i] ? G.rinv : nullptr;
+    MLG_TRY(launch_hfft_multi(f, rs, n, +1));
+  } else {
+    for (int i = 0; i < n; ++i)
+      if (by_r[i]) MLG_TRY(scale_r(*f[i], 1));
+  }
+  for (int i = 0; i < n; ++i) f[i]->set_space("PPP");
+  return 0;
+}
+
+// vector_reconstruction into (ur, up, uz)
+static int tp2vec_into(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
+  MLG_TRY(tp2vec_spec(psi, chi, ur, up, uz));
+  Scalar* f[3] = {&ur, &up, &uz};
+  const bool by_r[3] = {true, true, false};
+  return to_ppp_batch(f, by_r, 3);
 }
 
 static bool aliases(const Scalar& a, const Scalar& b) { return a.e == b.e; }
@@ -946,6 +982,8 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
   if (keep) for (int i = 0; i < 6; ++i) vw[i] = keep[i];
   for (Scalar* q : vw) q->set_space("PPP");
   Scalar &vr = *vw[0], &vp = *vw[1], &vz = *vw[2], &wr = *vw[3], &wp = *vw[4], &wz = *vw[5];
+  // v and w, each with its three transforms to PPP batched (three fields, 78 MB at 192x128x128, stay
+  // in L2 from one stage to the next; six would not)
   MLG_TRY(tp2vec_into(psi, chi, vr, vp, vz));
   MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
   // (vz + uz) with the background flow; in place, or into the temporaries when v and w are kept
