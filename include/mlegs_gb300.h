@@ -197,6 +197,53 @@ int mlg_adj_vec2tp(mlg_scalar psi_bar, mlg_scalar chi_bar, mlg_scalar vr_bar, ml
 int mlg_adj_advection(mlg_scalar psi, mlg_scalar chi, mlg_scalar uz, mlg_scalar nlpsi_bar, mlg_scalar nlchi_bar,
                       mlg_scalar psi_bar, mlg_scalar chi_bar);
 
+/* ---- field I/O (src/submodules/mlegs_scalar_io.f90) ---------------------------------------- */
+/* msave (:6-103): the field, ln, chop offsets and space tag to the file fn.
+ *  is_binary != 0: stream-access unformatted -- the three sizes as int32, the complex128 array in
+ *    Fortran order, ln as float64, the three chop offsets as int32, the 3-character space tag;
+ *  is_binary == 0: formatted -- the sizes as '(3(1X,I10))', then for each z and each radial row one
+ *    line of 2*npdim values (re, im) as '1PE24.15E3', a blank line between z blocks, then a line with
+ *    ln and the offsets and a line with the space tag.
+ *  is_global != 0: one file fn with the global layout above; is_global == 0: the per-rank form, file
+ *    fn_0, whose header holds the global size, local size and local start (one process: the whole
+ *    array).  The reference's optional arguments default to formatted and global. */
+int mlg_msave(mlg_scalar s, const char* fn, int is_binary, int is_global);
+/* mload (:105-249): the inverse of mlg_msave into s (device).  The stored sizes must equal
+ * (nrdim, npdim, nzdim) (MLG_ESIZE, the reference's 'size inconsistency'); a file that cannot be
+ * opened or parsed gives MLG_EPARAM. */
+int mlg_mload(mlg_scalar s, const char* fn, int is_binary, int is_global);
+
+/* ---- diagnostics ------------------------------------------------------------------------- */
+/* fftreat (mlegs_scalar_ops.f90:1002-1063): delsqp, to (physical r, Fourier phi, z), the rows times
+ * (1-x)^2, rows from 3nr/4+4 of m >= 1 zeroed, five passes of smooth over the rows from 3nr/4,
+ * divided by (1-x)^2, back, idelsqp (ln kept), zeroat1; in place on an FFF field. */
+int mlg_fftreat(mlg_scalar s);
+/* The field of save_vort_mag (src/apps/vortical_flow_3d.f90:411-465), without the file: out (PPP,
+ * ln 0) <- |curl v| of the velocity of (psi, chi) per physical sample (the real and imaginary parts
+ * of each slot are the two packed phi samples).  psi, chi: FFF, unchanged. */
+int mlg_vort_mag(mlg_scalar psi, mlg_scalar chi, mlg_scalar out);
+/* Kinetic-energy spectrum of the velocity v of (psi, chi): E[m + npdim*k] = 1/2 sum_i W_i c_m
+ * sum_{v_r, v_phi, v_z} |v_hat(i, m, k)|^2, v_hat the phi (1/np) and z (1/nz) Fourier coefficients of
+ * the physical samples, W_i = w_i r_i^2/(1-x_i^2) 2 pi zlen, c_m = 1 for m = 0 and m = np/2, else 2:
+ * sum over (m, k) is the kinetic energy.  Computed in FP64 in either precision form. */
+int mlg_ke_spectrum(mlg_scalar psi, mlg_scalar chi, double* E);
+
+/* ---- parameter file: read_input (src/submodules/mlegs_misc_io.f90:307-388) ---------------- */
+/* The time-stepping and output settings of the input file besides the kit parameters. */
+typedef struct mlg_run_params {
+    double dt, ti, totaltime;
+    int    ni, totaln;
+    int    isfldsav, fldsavintvl;
+    int    islogsav, logsavintvl;
+    char   flddir[260];                /* with a trailing '/'                                      */
+    char   logdir[260];
+} mlg_run_params;
+/* Reads fn in the reference's layout (a comment line before each group of values; the optional SVV
+ * line at the end) into p (the reference defaults for anything the file leaves out) and run, and
+ * checks it as read_input does (MLG_EPARAM with the reference's message).  make_dirs != 0 creates
+ * flddir and logdir (mkdir -p) as the reference does. */
+int mlg_read_input(const char* fn, mlg_params* p, mlg_run_params* run, int make_dirs);
+
 /* ---- kernel timing (CUDA events around each launch of one kernel class) ----------------- */
 /* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators (applies and the
  *       fused abcn right-hand side), 3 = backward radial contraction, 4 = vec2tp projection

@@ -65,6 +65,9 @@ def load(path=None):
         "mlg_adj_idel2_proln": [_P], "mlg_adj_zeroat1": [_P],
         "mlg_adj_tp2vec": [_P] * 5, "mlg_adj_tp2curlvec": [_P] * 5, "mlg_adj_vec2tp": [_P] * 5,
         "mlg_adj_advection": [_P] * 7,
+        "mlg_msave": [_P, ctypes.c_char_p, _I, _I], "mlg_mload": [_P, ctypes.c_char_p, _I, _I],
+        "mlg_fftreat": [_P], "mlg_vort_mag": [_P, _P, _P], "mlg_ke_spectrum": [_P, _P, _P],
+        "mlg_read_input": [ctypes.c_char_p, _P, _P, _I],
     }
     for name in ["mlg_chop", "mlg_dealias", "mlg_zeroat1", "mlg_delsqp", "mlg_idelsqp", "mlg_xxdx", "mlg_del2h",
                  "mlg_del2", "mlg_idel2_proln"]:
@@ -246,6 +249,26 @@ class Kit:
     def vec2tp(self, vr, vp, vz, psi, chi): _chk(load().mlg_vec2tp(vr.h, vp.h, vz.h, psi.h, chi.h))
     def tp2vec(self, psi, chi, vr, vp, vz): _chk(load().mlg_tp2vec(psi.h, chi.h, vr.h, vp.h, vz.h))
     def tp2curlvec(self, psi, chi, wr, wp, wz): _chk(load().mlg_tp2curlvec(psi.h, chi.h, wr.h, wp.h, wz.h))
+
+    # ---- field I/O (mlegs_scalar_io.f90) and diagnostics ----
+    def msave(self, s, fn, is_binary=False, is_global=True):
+        """msave: the reference's optional arguments default to formatted and global."""
+        _chk(load().mlg_msave(s.h, os.fsencode(fn), int(bool(is_binary)), int(bool(is_global))))
+
+    def mload(self, s, fn, is_binary=False, is_global=True):
+        _chk(load().mlg_mload(s.h, os.fsencode(fn), int(bool(is_binary)), int(bool(is_global))))
+
+    def fftreat(self, s): _chk(load().mlg_fftreat(s.h))
+
+    def vort_mag(self, psi, chi, out):
+        """The field of save_vort_mag: out (PPP) <- |curl v| per physical sample."""
+        _chk(load().mlg_vort_mag(psi.h, chi.h, out.h))
+
+    def ke_spectrum(self, psi, chi):
+        """Kinetic-energy spectrum E[m, k] (npdim x nzdim) of the velocity of (psi, chi), FP64."""
+        E = np.zeros((self.dims[2], self.dims[1]), dtype=np.float64)   # k-major rows: E[m + npdim*k]
+        _chk(load().mlg_ke_spectrum(psi.h, chi.h, E.ctypes.data))
+        return E.T.copy()
 
     def advection_rhs(self, psi, chi, nlpsi, nlchi, uz):
         _chk(load().mlg_advection_rhs(psi.h, chi.h, nlpsi.h, nlchi.h, uz.h))

@@ -37,3 +37,27 @@ def make_params(**kw):
 def dims_of(p):
     """(nrdim, npdim, nzdim) of a field for these parameters (mlegs_spectfm_init.f90:117-136)."""
     return (p.nr + max(3, p.hyperpow), p.np // 2 + 1, p.nz)
+
+
+class MlgRunParams(ctypes.Structure):
+    """The time-stepping and output settings of an input file (mlg_run_params)."""
+    _fields_ = [
+        ("dt", ctypes.c_double), ("ti", ctypes.c_double), ("totaltime", ctypes.c_double),
+        ("ni", ctypes.c_int), ("totaln", ctypes.c_int),
+        ("isfldsav", ctypes.c_int), ("fldsavintvl", ctypes.c_int),
+        ("islogsav", ctypes.c_int), ("logsavintvl", ctypes.c_int),
+        ("flddir", ctypes.c_char * 260), ("logdir", ctypes.c_char * 260),
+    ]
+
+
+def read_input(fn, make_dirs=False):
+    """read_input (mlegs_misc_io.f90:307-388): (kit parameters, run settings as a dict) from an input
+    file in the reference's layout; raises MlgError with the reference's message when it is invalid."""
+    import os
+    from .kit import load, _chk
+    p, r = MlgParams(), MlgRunParams()
+    _chk(load().mlg_read_input(os.fsencode(fn), ctypes.byref(p), ctypes.byref(r), int(bool(make_dirs))))
+    run = {f: getattr(r, f) for f, _ in MlgRunParams._fields_}
+    run["flddir"] = r.flddir.decode()
+    run["logdir"] = r.logdir.decode()
+    return p, run
