@@ -74,6 +74,31 @@ module mlegs_gb300_c
       type(c_ptr), value :: s
       integer(c_int), value :: a, b, c
     end function
+    integer(c_int) function mlg_msave(s, fn, is_binary, is_global) bind(c, name='mlg_msave')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: s
+      character(kind=c_char), intent(in) :: fn(*)
+      integer(c_int), value :: is_binary, is_global
+    end function
+    integer(c_int) function mlg_mload(s, fn, is_binary, is_global) bind(c, name='mlg_mload')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: s
+      character(kind=c_char), intent(in) :: fn(*)
+      integer(c_int), value :: is_binary, is_global
+    end function
+    integer(c_int) function mlg_fftreat(s) bind(c, name='mlg_fftreat')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s
+    end function
+    integer(c_int) function mlg_vort_mag(psi, chi, out) bind(c, name='mlg_vort_mag')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: psi, chi, out
+    end function
+    integer(c_int) function mlg_ke_spectrum(psi, chi, e) bind(c, name='mlg_ke_spectrum')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: psi, chi
+      real(c_double), intent(out) :: e(*)
+    end function
     integer(c_int) function mlg_trans(s, space) bind(c, name='mlg_trans')
       import :: c_int, c_ptr, c_char
       type(c_ptr), value :: s
@@ -329,4 +354,22 @@ contains
     type(scalar_gpu) :: psi, chi, wr, wp, wz; class(*) :: tfm
     call check(mlg_tp2curlvec(psi%h, chi%h, wr%h, wp%h, wz%h))
   end subroutine
+  ! msave / mload (mlegs_scalar_io.f90): formatted and global unless told otherwise
+  subroutine msave(s, fn, is_binary, is_global)
+    type(scalar_gpu) :: s; character(len=*), intent(in) :: fn; logical, optional :: is_binary, is_global
+    integer(c_int) :: b, g
+    b = 0; g = 1
+    if (present(is_binary)) b = merge(1, 0, is_binary)
+    if (present(is_global)) g = merge(1, 0, is_global)
+    call check(mlg_msave(s%h, trim(fn) // c_null_char, b, g))
+  end subroutine
+  subroutine mload(s, fn, is_binary, is_global)
+    type(scalar_gpu) :: s; character(len=*), intent(in) :: fn; logical, optional :: is_binary, is_global
+    integer(c_int) :: b, g
+    b = 0; g = 1
+    if (present(is_binary)) b = merge(1, 0, is_binary)
+    if (present(is_global)) g = merge(1, 0, is_global)
+    call check(mlg_mload(s%h, trim(fn) // c_null_char, b, g))
+  end subroutine
+  subroutine fftreat(s, tfm); type(scalar_gpu) :: s; class(*) :: tfm; call check(mlg_fftreat(s%h)); end subroutine
 end module
