@@ -173,33 +173,13 @@ def run_reference(args, rank, world, pg):
 
 
 def ke_spectrum(kit, st_fields, dims, xw):
-    """Kinetic-energy spectrum E(m, k) of the velocity of (psi, chi), computed from the FP64 tp2vec
-    (PPP samples downloaded) with numpy FFTs in phi and z and the radial quadrature of the volume
-    integral: E(m, k) = 1/2 sum_i w_i r_i^2/(1 - x_i^2) 2 pi zlen c_m |u_hat(i, m, k)|^2, c_m = 2 for
+    """Kinetic-energy spectrum E(m, k) of the velocity of (psi, chi) from the library's FP64 diagnostic
+    (mlg_ke_spectrum): E(m, k) = 1/2 sum_i w_i r_i^2/(1 - x_i^2) 2 pi zlen c_m |u_hat(i, m, k)|^2 over
+    the three components, u_hat the phi and z Fourier coefficients of the physical velocity, c_m = 2 for
     0 < m < np/2.  Sum over (m, k) = the kinetic energy."""
-    from mlegs_gb300.kit import PLAIN_FP64
-    x, w, r = xw
-    nr = len(x)
-    p = kit.params
-    kit.set_precision(PLAIN_FP64)
     psi = kit.scalar(*st_fields["psi"][:3])
     chi = kit.scalar(*st_fields["chi"][:3])
-    v = [kit.scalar(np.zeros(dims, complex, order="F"), 0.0, "PPP") for _ in range(3)]
-    kit.tp2vec(psi, chi, *v)
-    W = w * r ** 2 / (1.0 - x ** 2) * 2.0 * np.pi * p.zlen
-    E = 0.0
-    for s in v:
-        e = s.e[:nr, : p.np // 2, :]
-        f = np.empty((nr, p.np, dims[2]))
-        f[:, 0::2, :] = e.real
-        f[:, 1::2, :] = e.imag
-        F = np.fft.fft(np.fft.rfft(f, axis=1) / p.np, axis=2) / dims[2]
-        cm = np.full(F.shape[1], 2.0)
-        cm[0] = 1.0
-        if p.np % 2 == 0:
-            cm[-1] = 1.0
-        E = E + 0.5 * np.einsum("i,imk->mk", W, np.abs(F) ** 2) * cm[:, None]
-        s.free()
+    E = kit.ke_spectrum(psi, chi)
     for s in (psi, chi):
         s.free()
     return E

@@ -104,7 +104,9 @@ int mlg_scalar_set_space(mlg_scalar s, const char* space);
 /* dst%e = a*x%e + b*y%e (y may be NULL), ln and tags of dst unchanged: the device-side form of the
  * apps' direct array arithmetic on s%e (e.g. the Richardson step, vortical_flow_3d.f90:136-137). */
 int mlg_scalar_axpby(mlg_scalar dst, double a, mlg_scalar x, double b, mlg_scalar y);
-/* Raw device pointer of the field (for interop; valid until mlg_scalar_free). */
+/* Raw device pointer of the field (for interop).  Valid until the scalar is freed or passed to a
+ * call that transforms it (trans, and the operators that move it between spaces): a radial transform
+ * writes into a fresh buffer and the scalar takes it.  Query it again after such calls. */
 void* mlg_scalar_device_ptr(mlg_scalar s);
 
 /* ---- transforms and masks (mlegs_scalar_ops.f90) -------------------------------------- */

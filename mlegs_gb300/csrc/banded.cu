@@ -280,7 +280,7 @@ template <typename T>
 __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __restrict__ src, const double* __restrict__ lnsrc,
                                 double* __restrict__ lndst, BandTabs tb, const double* __restrict__ lognorm, int op,
                                 int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell,
-                                double scale, int smode) {
+                                double scale, int smode, PostChop pc) {
   extern __shared__ __align__(16) unsigned char bat_smem[];
   double2* sv = (double2*)bat_smem;   // the column, then its band product on the active rows (FP64)
   int m = blockIdx.y, k = blockIdx.x;
@@ -370,10 +370,12 @@ __global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __rest
     *lndst = 0.0;
   }
   __syncthreads();
+  const int zf = chop_from(pc, m, k, nrdim);
   for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
     double2 v = sv[i];
     if (smode == 1) v = neg_d2(v);
     else if (smode == 2) v = make_double2(0.0 + scale * v.x, 0.0 + scale * v.y);
+    if (i >= zf) v = make_double2(0.0, 0.0);   // the chop that follows
     dst[off + i] = v;
   }
 }
@@ -388,7 +390,7 @@ template <typename U>
 __device__ __forceinline__ void uv_col(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
                                        const double2* __restrict__ chi, double lnp, double lnc, const BandTabs& tb,
                                        const double* __restrict__ lognorm, int nrdim, int ne, int nn, int cnt, bool act,
-                                       int m, int k, bool lnblk, unsigned char* smem) {
+                                       int m, int k, bool lnblk, int zf, unsigned char* smem) {
   typedef typename BC<U>::C C;
   C* a0 = (C*)smem;
   C* a1 = a0 + nrdim;
@@ -422,6 +424,11 @@ __device__ __forceinline__ void uv_col(double2* __restrict__ ur, double2* __rest
   }
   const double kv = tb.ak[k], mv = (double)m;
   for (int i = threadIdx.x; i < nrdim; i += blockDim.x) {
+    if (i >= zf) {   // the chop that follows
+      ur[i] = make_double2(0.0, 0.0);
+      up[i] = make_double2(0.0, 0.0);
+      continue;
+    }
     const double2 c = chi[i], p = psi[i];
     const bool in = act && i < nn;
     double2 av = c, bv = p;
@@ -449,7 +456,7 @@ __global__ void k_tp2vec_uv(double2* __restrict__ ur, double2* __restrict__ up, 
                             const double2* __restrict__ chi, const double* __restrict__ lnpsi,
                             const double* __restrict__ lnchi, double* __restrict__ lnur, double* __restrict__ lnup,
                             BandTabs tb, const double* __restrict__ lognorm, int nrdim, int npdim, int ne, int nrc,
-                            int npc, int nzc, int nzcu, int nzdim) {
+                            int npc, int nzc, int nzcu, int nzdim, PostChop pc) {
   extern __shared__ __align__(16) unsigned char uv_smem[];
   const int m = blockIdx.y, k = blockIdx.x;
   const int nn = max(min(nrc, nrc - m), 0);
@@ -458,12 +465,13 @@ __global__ void k_tp2vec_uv(double2* __restrict__ ur, double2* __restrict__ up, 
   const bool lnblk = m == 0 && k == 0;
   const double lnp = lnblk ? *lnpsi : 0.0, lnc = lnblk ? *lnchi : 0.0;
   const bool act = m < npc && nn > 0 && cnt > 0;
-  if (m == 0) uv_col<double>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, uv_smem);
-  else uv_col<T>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, uv_smem);
+  const int zf = chop_from(pc, m, k, nrdim);
+  if (m == 0) uv_col<double>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, zf, uv_smem);
+  else uv_col<T>(ur + off, up + off, psi + off, chi + off, lnp, lnc, tb, lognorm, nrdim, ne, nn, cnt, act, m, k, lnblk, zf, uv_smem);
   if (lnblk && threadIdx.x == 0) { *lnur = 0.0; *lnup = 0.0; }
 }
 
-int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c) {
+int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c, PostChop pc) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   dim3 grid(G.nzdim, G.npdim);
   size_t sm = 4ull * G.nrdim * sizeof(double2);
@@ -471,18 +479,18 @@ int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& ch
   if (G.precision == MLG_MIXED) {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_tp2vec_uv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_tp2vec_uv<float><<<grid, 128, sm, G.stream>>>(ur.e, up.e, psi.e, chi.e, psi.ln, chi.ln, ur.ln, up.ln, band_tabs(),
-                                                    G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim);
+                                                    G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, pc);
   } else {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_tp2vec_uv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_tp2vec_uv<double><<<grid, 128, sm, G.stream>>>(ur.e, up.e, psi.e, chi.e, psi.ln, chi.ln, ur.ln, up.ln, band_tabs(),
-                                                     G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim);
+                                                     G.lognorm, G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, pc);
   }
   MLG_LAUNCH();
   kt_end(KT_BAND, 4.0 * G.fsize * 16);
   return 0;
 }
 
-int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale) {
+int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale, PostChop pc) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   const int smode = scale == 1.0 ? 0 : scale == -1.0 ? 1 : 2;   // identity, exact negation, FP64 product
   dim3 grid(G.nzdim, G.npdim);
@@ -492,12 +500,12 @@ int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& 
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_band_apply_to<float><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                         G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
-                                                        scale, smode);
+                                                        scale, smode, pc);
   } else {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_band_apply_to<double><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                          G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
-                                                         scale, smode);
+                                                         scale, smode, pc);
   }
   MLG_LAUNCH();
   kt_end(KT_BAND, 2.0 * G.fsize * 16);

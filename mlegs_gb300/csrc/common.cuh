@@ -38,6 +38,16 @@ struct Scalar {
 
 // chop_index (mlegs_scalar_ops.f90:2012-2063) on one process
 struct ChopIdx { int nrc, npc, nzc, nzcu; };
+// chop (mlegs_scalar_ops.f90:6-41) of an FFF field folded into a kernel's output: on == 0 leaves the
+// output as it is; else column (m, k) keeps only its rows below chop_from(m, k)
+struct PostChop { int on, nrc, npc, nzc, nzcu; };
+__host__ __device__ inline int chop_from(const PostChop& p, int m, int k, int nrdim) {
+  if (!p.on) return nrdim;
+  if (m >= p.npc || (p.nzc < p.nzcu && k + 1 >= p.nzc + 1 && k + 1 <= p.nzcu - 1)) return 0;
+  int n = p.nrc - m;
+  return n < 0 ? 0 : (n < p.nrc ? n : p.nrc);
+}
+inline PostChop post_chop(const ChopIdx& c) { return PostChop{1, c.nrc, c.npc, c.nzc, c.nzcu}; }
 
 // kernel-time accounting per kernel class (mlg_kernel_timing)
 enum { KT_RFWD = 0, KT_FFT = 1, KT_BAND = 2, KT_RBWD = 3, KT_V2TP = 4, KT_SOLVE = 5, KT_N = 6 };
@@ -189,8 +199,10 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
                        Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep = nullptr);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
-int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale);
-int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c);
+int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale,
+                         PostChop pc = PostChop{0, 0, 0, 0, 0});
+int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c,
+                     PostChop pc = PostChop{0, 0, 0, 0, 0});
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);
 int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, double beta, double preln, int power);
 int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha);

@@ -904,11 +904,12 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
 // the temporaries into the outputs)
 static int tp2vec_spec(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar& up, Scalar& uz) {
   for (Scalar* q : {&ur, &up, &uz}) { q->set_space("FFF"); q->off[0] = 3; q->off[1] = q->off[2] = 0; }
-  ChopIdx c;
+  ChopIdx c, c0;
   MLG_TRY(chop_index(ur, c));
-  MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c));       // r d/dr chi, r d/dr psi and their mix
-  MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0));   // -del2h chi
-  for (Scalar* q : {&ur, &up, &uz}) { q->off[0] = 0; MLG_TRY(op_chop(*q)); }
+  for (Scalar* q : {&ur, &up, &uz}) q->off[0] = 0;
+  MLG_TRY(chop_index(ur, c0));   // the chop after the products (offsets 0), folded into their kernels
+  MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c, post_chop(c0)));       // r d/dr chi, r d/dr psi, their mix
+  MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0, post_chop(c0)));   // -del2h chi
   return 0;
 }
 
