@@ -22,8 +22,9 @@
 // With NS = 6 digits of w = 7 bits (6 when nr/2 > 173, keeping the orders exact) the term carries
 // 42 (36) bits.
 //
-// Engine: one CTA per (m, parity, 128-row tile, 8 complex z columns), 128 threads (warp = role in
-// the staging: ur, up, Re uz, Im uz), 57 KiB of shared memory and 128 TMEM columns.  Per K chunk of
+// Engine: one CTA per (m, parity, 128-row tile, 8 complex z columns), 256 threads (warp w takes role
+// w % 4 in the staging -- ur, up, Re uz, Im uz -- for half the K of each group), about 64 KiB of
+// shared memory and 128 TMEM columns, three CTAs per SM.  Per K chunk of
 // 16 radial points the table tiles (V, D splits and T digits, laid out at kit init in the UMMA
 // canonical K-major layout) arrive by one bulk copy on an mbarrier; the threads fold and split the
 // field operand; one thread issues 53 tcgen05.mma (M = 128, N = 16, K = 16).  Every wait is bounded.
@@ -37,7 +38,8 @@ constexpr int PV_KC = 16;                  // K chunk (radial points): one MMA K
 constexpr int PV_NZ = 8;                   // complex z columns per CTA
 constexpr int PV_N = 2 * PV_NZ;            // real columns (N of the MMA)
 constexpr int PV_NS = 6;                   // digits of the T term
-constexpr int PV_THREADS = 128;
+constexpr int PV_RW = 2;                   // warps per staging role
+constexpr int PV_THREADS = 128 * PV_RW;
 constexpr int PV_SBO = PV_KC * 16;         // 8 rows x 16 K x 2 B between 8-row core-matrix groups
 constexpr int PV_LBO = 128;                // between the two 8-K core matrices of a row group
 __host__ __device__ constexpr int pv_off(int row, int k) {
@@ -49,7 +51,7 @@ constexpr int PV_NA = 6 + PV_NS;           // A tiles per chunk: V s0..2, D s0..
 constexpr int PV_NB = 12 + PV_NS;          // B tiles: psi1 (3), psi2 (3), chi1 (3), chi2 (3), uz digits
 constexpr int PV_TMEM_COLS = 128;          // psi, chi, then the NS digit orders, N columns each
 static_assert((2 + PV_NS) * PV_N <= PV_TMEM_COLS, "TMEM columns");
-constexpr int PV_KQ = PV_KC * PV_NZ / 32;  // consecutive K per staging item: 32 items per warp
+constexpr int PV_KQ = PV_KC * PV_NZ / (32 * PV_RW);   // consecutive K per staging item
 
 // the NS signed w-bit digits of x / 2^fexp (|x| < 2^fexp), most significant first, by integer ops
 __device__ __forceinline__ void pv_digits(double x, int fexp, int w, int* d) {
@@ -150,13 +152,12 @@ struct PvSmem {
 };
 
 // PV_KQ consecutive K of one B row as three BF16 splits into tiles t0, t0+1, t0+2
-__device__ __forceinline__ void pv_store_split(uint8_t* b, int t0, int n, int kg, const float* v) {
-  static_assert(PV_KQ == 4, "staging items of 4 K");
-  uint32_t w[2][3];
+__device__ __forceinline__ void pv_store_split(uint8_t* b, int t0, int n, int k0, const float* v) {
+  static_assert(PV_KQ == 2, "staging items of 2 K");
+  uint32_t w[3];
+  split3x2(v[0], v[1], w);
 #pragma unroll
-  for (int q = 0; q < 2; ++q) split3x2(v[2 * q], v[2 * q + 1], w[q]);
-#pragma unroll
-  for (int s = 0; s < 3; ++s) *(uint2*)(b + (t0 + s) * PV_BTILE + pv_off(n, kg * PV_KQ)) = make_uint2(w[0][s], w[1][s]);
+  for (int s = 0; s < 3; ++s) *(uint32_t*)(b + (t0 + s) * PV_BTILE + pv_off(n, k0)) = w[s];
 }
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
@@ -182,7 +183,7 @@ __device__ __forceinline__ float pv_pow2(int e) {   // 2^e as float, 0 below the
 }
 
 // grid (z tiles, 2 * nmt, npc - 1): blockIdx.y = mt * 2 + par, m = blockIdx.z + 1
-__global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
+__global__ void __launch_bounds__(PV_THREADS, 3) k_pv_contract(
     const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
     double2* __restrict__ psi, double2* __restrict__ chi, const uint16_t* __restrict__ img, const int* __restrict__ texp,
     const double* __restrict__ ak, int nr, int nrh, int nrdim, int npdim, int nzdim, int nrc, int nzc, int nzcu,
@@ -231,8 +232,10 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
     sm.fexp[tid] = mx ? pv_ebound(mx) + 1 : -1000;   // +1: the fold can double the magnitude
   }
   const uint32_t tmem = sm.tmem;
-  // staging role of this warp: 0 ur, 1 up, 2 Re uz, 3 Im uz; lane: z column zz, K group kg (8 K)
-  const int role = warp, zz = lane % PV_NZ, kg = lane / PV_NZ;
+  // staging role of this warp: 0 ur, 1 up, 2 Re uz, 3 Im uz, two warps per role (half of each K group of
+  // 4); lane: z column zz, K group kg; the item's K: kbase .. kbase + PV_KQ - 1 of the chunk
+  const int role = warp & 3, half = warp >> 2, zz = lane % PV_NZ, kg = lane / PV_NZ;
+  const int kbase = kg * (PV_KQ * PV_RW) + half * PV_KQ;
   const int z = z0 + zz;
   const bool zok = z < nzdim;
   const size_t cbase = (size_t)nrdim * (m + (size_t)npdim * (zok ? z : 0));
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
   auto fetch = [&](int kc) {
 #pragma unroll
     for (int q = 0; q < PV_KQ; ++q) {
-      int i = kc * PV_KC + kg * PV_KQ + q;
+      int i = kc * PV_KC + kbase + q;
       bool ok = zok && i < nrh;
       if (role < 2) {
         const double2* src = role == 0 ? ur : up;
@@ -278,10 +281,10 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
         }
       }
       const int tp = role == 0 ? 0 : 3, tc = role == 0 ? 6 : 9;
-      pv_store_split(sm.b, tp, 2 * zz, kg, v0);
-      pv_store_split(sm.b, tp, 2 * zz + 1, kg, v1);
-      pv_store_split(sm.b, tc, 2 * zz, kg, v2);
-      pv_store_split(sm.b, tc, 2 * zz + 1, kg, v3);
+      pv_store_split(sm.b, tp, 2 * zz, kbase, v0);
+      pv_store_split(sm.b, tp, 2 * zz + 1, kbase, v1);
+      pv_store_split(sm.b, tc, 2 * zz, kbase, v2);
+      pv_store_split(sm.b, tc, 2 * zz + 1, kbase, v3);
     } else {
       const int n = 2 * zz + (role - 2);
       const int fe = sm.fexp[n];
@@ -296,8 +299,7 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
       }
 #pragma unroll
       for (int s = 0; s < PV_NS; ++s)
-        *(uint2*)(sm.b + (12 + s) * PV_BTILE + pv_off(n, kg * PV_KQ)) =
-            make_uint2(h[s][0] | (h[s][1] << 16), h[s][2] | (h[s][3] << 16));
+        *(uint32_t*)(sm.b + (12 + s) * PV_BTILE + pv_off(n, kbase)) = h[s][0] | (h[s][1] << 16);
     }
     fence_async_smem();
     __syncthreads();
@@ -333,14 +335,15 @@ __global__ void __launch_bounds__(PV_THREADS) k_pv_contract(
     __syncthreads();
   }
   tc_fence_after();
-  // epilogue: warp w holds rows t = mt*128 + 32 w + lane
-  const int t = mt * 128 + warp * 32 + lane;
+  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows t = mt*128 + 32 (w % 4) + lane) and the column
+  // blocks cb = w / 4 (mod PV_RW)
+  const int t = mt * 128 + (warp & 3) * 32 + lane;
   const int j = 2 * t + par;
   const bool rok = j < nn && t < ntr;
   const int ej = rok ? texp[(size_t)((m - 1) * 2 + par) * ntr + t] : -1000;
-  const uint32_t lrow = (uint32_t)(warp * 32) << 16;
+  const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
 #pragma unroll 1
-  for (int cb = 0; cb < PV_N / 8; ++cb) {
+  for (int cb = half; cb < PV_N / 8; cb += PV_RW) {
     float pv[8], cv[8], g[PV_NS][8];
     tmem_ld8(tmem + lrow + cb * 8, pv);
     tmem_ld8(tmem + lrow + PV_N + cb * 8, cv);
