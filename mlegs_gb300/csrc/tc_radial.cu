@@ -47,8 +47,10 @@ __host__ __device__ constexpr int tc_off(int row, int k) {
 constexpr int TC_TILE_BYTES = 128 * TC_KC * 2;  // 8 KiB: 128 rows x 32 BF16 (table tiles, M = 128)
 constexpr int TC_NZ = 32;                       // complex z columns per CTA (N = 64)
 constexpr int TC_BTILE_BYTES = 2 * TC_NZ * TC_KC * 2;   // 4 KiB: 64 rows x 32 BF16 (field tiles)
-constexpr int TC_THREADS = 256;   // 8 warps: the operand staging is split in two halves, the epilogue in
-                                  // two column halves of the four TMEM lane quarters
+constexpr int TC_THREADS = 512;   // 16 warps: the operand staging split in two halves (parity or fold sign)
+                                  // of 8 K groups of 4, the epilogue in four column blocks of the four
+                                  // TMEM lane quarters
+constexpr int TC_KQ = 4;          // consecutive K per staging item
 
 // ------------------------------------------------------------------------------------------------
 // table images, split and laid out once per kit: for (m, row tile, K chunk): [par 2][split 3][tile]
@@ -88,14 +90,15 @@ struct TcSmem {
   uint32_t tmem;
 };
 
-// store the 8 values of one K group of one field row (n) as the three BF16 splits
-__device__ __forceinline__ void store_split8(uint8_t* b, int par, int n, int kg, const float* v) {
-  uint32_t w[4][3];
+// store the TC_KQ values of one K group of one field row (n) as the three BF16 splits
+__device__ __forceinline__ void store_split4(uint8_t* b, int par, int n, int kg, const float* v) {
+  static_assert(TC_KQ == 4, "staging items of 4 K: 8 bytes of a core-matrix row");
+  uint32_t w[2][3];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) split3x2(v[2 * q], v[2 * q + 1], w[q]);
+  for (int q = 0; q < 2; ++q) split3x2(v[2 * q], v[2 * q + 1], w[q]);
 #pragma unroll
   for (int s = 0; s < 3; ++s)
-    *(uint4*)(b + (par * 3 + s) * TC_BTILE_BYTES + tc_off(n, kg * 8)) = make_uint4(w[0][s], w[1][s], w[2][s], w[3][s]);
+    *(uint2*)(b + (par * 3 + s) * TC_BTILE_BYTES + tc_off(n, kg * TC_KQ)) = make_uint2(w[0][s], w[1][s]);
 }
 
 // the two-parity bf16x3 MMA group of one K chunk: D_par += A_par * B_par, six split products
@@ -147,15 +150,16 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
   const uint8_t* img_m = (const uint8_t*)img + ((size_t)m * nmt + mt) * nkc * (size_t)(6 * TC_TILE_BYTES);
   // staging item of this thread: z column zz, K group kg (8 consecutive K indices) and half: the row
   // parity it writes (forward: the fold sign, backward: the parity of the rows it reads)
-  const int zz = tid % TC_NZ, kg = (tid / TC_NZ) & 3, half = tid / (4 * TC_NZ);
+  constexpr int NKG = TC_KC / TC_KQ;   // K groups per chunk
+  const int zz = tid % TC_NZ, kg = (tid / TC_NZ) % NKG, half = tid / (NKG * TC_NZ);
   const int z = z0 + zz;
   const double2* col = in + (size_t)nrdim * (m + (size_t)npdim * min(z, nzdim - 1));
-  float2 ra[8], rb[8];
-  float wv[8];
+  float2 ra[TC_KQ], rb[TC_KQ];
+  float wv[TC_KQ];
   auto fetch = [&](int kc) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      int k = kc * TC_KC + kg * 8 + q;
+    for (int q = 0; q < TC_KQ; ++q) {
+      int k = kc * TC_KC + kg * TC_KQ + q;
       ra[q] = make_float2(0.f, 0.f); rb[q] = make_float2(0.f, 0.f); wv[q] = 0.f;
       if (MODE == 0) {
         if (k < nrh && z < nzdim) { ra[q] = ld_c32(col + k); rb[q] = ld_c32(col + nr - 1 - k); wv[q] = w32[k]; }
@@ -172,22 +176,22 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
       bulk_g2s(sm.a, img_m + (size_t)kc * (6 * TC_TILE_BYTES), 6 * TC_TILE_BYTES, &sm.bar_a);
     }
     {
-      float v[8];
+      float v[TC_KQ];
       if (MODE == 0) {
         const float sg = half ? -1.f : 1.f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].x + sg * rb[q].x) * wv[q];
-        store_split8(sm.b, half, 2 * zz, kg, v);
+        for (int q = 0; q < TC_KQ; ++q) v[q] = (ra[q].x + sg * rb[q].x) * wv[q];
+        store_split4(sm.b, half, 2 * zz, kg, v);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = (ra[q].y + sg * rb[q].y) * wv[q];
-        store_split8(sm.b, half, 2 * zz + 1, kg, v);
+        for (int q = 0; q < TC_KQ; ++q) v[q] = (ra[q].y + sg * rb[q].y) * wv[q];
+        store_split4(sm.b, half, 2 * zz + 1, kg, v);
       } else {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = ra[q].x;
-        store_split8(sm.b, half, 2 * zz, kg, v);
+        for (int q = 0; q < TC_KQ; ++q) v[q] = ra[q].x;
+        store_split4(sm.b, half, 2 * zz, kg, v);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = ra[q].y;
-        store_split8(sm.b, half, 2 * zz + 1, kg, v);
+        for (int q = 0; q < TC_KQ; ++q) v[q] = ra[q].y;
+        store_split4(sm.b, half, 2 * zz + 1, kg, v);
       }
     }
     fence_async_smem();
@@ -204,9 +208,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_rtrans(const double2* __restr
     __syncthreads();
   }
   tc_fence_after();
-  // warp w reads TMEM lanes 32 (w % 4) .. +31 and the column half w / 4 of each accumulator
+  // warp w reads TMEM lanes 32 (w % 4) .. +31 and the column part w / 4 of each accumulator
   const int lq = warp & 3, ch = warp >> 2;
-  constexpr int CBH = (2 * TC_NZ) / 32;   // 16-column blocks per column half
+  constexpr int NCP = TC_THREADS / 128;            // column parts
+  constexpr int CBH = (2 * TC_NZ) / (16 * NCP);    // 16-column blocks per part
+  static_assert(CBH >= 1, "at least one 16-column block per part");
   if (MODE == 0) {
     // lane quarter lq holds rows t = mt*128 + 32 lq + lane of both parities
     const int t = mt * 128 + lq * 32 + lane;
