@@ -332,10 +332,13 @@ def run_ours(args, rank, world, local, pg):
     achieved_gbs = bytes_launch / (avg_ms * 1e-3) / 1e9
     # DRAM traffic per launch of the class's largest kernel from one ncu capture at this workload
     # (dram__bytes_read.sum + dram__bytes_write.sum), and what limits it
-    ncu = {"solve": {"kernel": "k_band_subst<2> (psi and chi Helmholtz substitutions)", "traffic": 157.33e6,
-                     "algorithmic_bytes": 2.0 * 2 * 195 * 65 * 128 * 16 + 192 * 8 * 65 * 128 * 8,
-                     "limit": "FP64 pipe 48.8% busy (ncu), 5% of warps active: serial recurrences, ~2 FP64 FMA/clk/SM "
-                              "on GB300; the solves stay FP64 in both forms"}}
+    # (the solve class is one k_band_subst<2> and one k_band_subst<1> per step: the class mean)
+    ncu = {"solve": {"kernel": "k_band_subst<2> (psi and chi Helmholtz) + k_band_subst<1> (idel2)",
+                     "traffic": (164.02e6 + 118.82e6) / 2,
+                     "traffic_per_kernel": {"k_band_subst<2>": 164.02e6, "k_band_subst<1>": 118.82e6},
+                     "limit": "FP64 pipe 56% busy and 10% of warps active (ncu): 8320 systems x 2 parts x NR fields "
+                              "of serial recurrences are about one warp per SM sub-partition; the solves stay FP64 "
+                              "in both forms"}}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
             "frac": achieved_gbs / hbm, "traffic": ncu.get(dom, {}).get("traffic"),
             "avg_launch_us": 1e3 * avg_ms, "launches_per_step": d_n / 2,
@@ -344,6 +347,8 @@ def run_ours(args, rank, world, local, pg):
     if dom in ncu:
         roof["ncu_kernel"] = ncu[dom]["kernel"]
         roof["limit"] = ncu[dom]["limit"]
+        if "traffic_per_kernel" in ncu[dom]:
+            roof["traffic_per_kernel"] = ncu[dom]["traffic_per_kernel"]
     # the tensor-core Legendre transforms (backward, m >= 1 on tcgen05 plus the m = 0 plane beside it):
     # algorithmic flops 4 sum_m nn(m) nrh nz per launch against the bf16 peak
     r_ms, r_n, r_flops = kt["radial_bwd"]
