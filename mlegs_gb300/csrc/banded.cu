@@ -1358,19 +1358,53 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   return 0;
 }
 
-// transposes for the adjoint (FP64 in both forms)
+// transposes for the adjoint: the band products in the precision of their forwards (FP64, or FP32
+// for the mixed form's m >= 1 columns), the solves FP64 in both forms
+
+// B^T applied cnt times to the rows [0, nn) of a column held in shared memory as U (in place in c0)
+template <typename U>
+__device__ __forceinline__ typename BC<U>::C* band_T_col(typename BC<U>::C* c0, typename BC<U>::C* c1,
+                                                         const BandTabs& tb, int k, int op, int m, int ne, int nn,
+                                                         int cnt) {
+  typedef typename BC<U>::C C;
+  const U akv2 = bakv2<U>(tb, k);
+  for (int rep = 0; rep < cnt; ++rep) {
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      C acc; acc.x = 0; acc.y = 0;
+      if (op == 0) {
+        if (j + 1 < nn) {
+          U v = btab<U>(tb.bxx, tb.bxxf, 3 * ((size_t)(j + 1) + (size_t)ne * m) + 0);
+          acc.x += v * c0[j + 1].x; acc.y += v * c0[j + 1].y;
+        }
+        if (j - 1 >= 0) {
+          U v = btab<U>(tb.bxx, tb.bxxf, 3 * ((size_t)(j - 1) + (size_t)ne * m) + 2);
+          acc.x += v * c0[j - 1].x; acc.y += v * c0[j - 1].y;
+        }
+      } else {
+        for (int i = max(0, j - 2); i <= min(nn - 1, j + 2); ++i) {
+          U v = btab<U>(tb.bd2, tb.bd2f, (j - i + 2) + 5 * ((size_t)i + (size_t)ne * m));
+          if (i == j && op == 2) v -= akv2;
+          acc.x += v * c0[i].x;
+          acc.y += v * c0[i].y;
+        }
+      }
+      c1[j] = acc;
+    }
+    __syncthreads();
+    C* t = c0; c0 = c1; c1 = t;
+  }
+  return c0;
+}
 
 // k_band_apply^T: x <- B^T x per active column (cnt times, as the forward), rows >= nn and inactive
 // columns untouched (the forward is the identity there).  The forward adds c_n * ln to Re e(n,0,0)
 // after the product and zeroes ln, so the adjoint of ln is read off the incoming adjoint of e first:
 // ln_bar = sum_n c_n Re(e_bar(n,0,0)); the adjoint of the output ln (a constant zero) is dropped.
-__global__ void k_band_apply_T(double2* __restrict__ e, const double* __restrict__ bd2, const double* __restrict__ bxx,
-                               const double* __restrict__ ak, double* __restrict__ lnp, const double* __restrict__ lognorm,
-                               int op, int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim,
-                               double ell) {
+template <typename T>
+__global__ void k_band_apply_T(double2* __restrict__ e, BandTabs tb, double* __restrict__ lnp,
+                               const double* __restrict__ lognorm, int op, int nrdim, int npdim, int ne, int nrc,
+                               int npc, int nzc, int nzcu, int nzdim, double ell) {
   extern __shared__ __align__(16) unsigned char bandt_smem[];
-  double2* c0 = (double2*)bandt_smem;
-  double2* c1 = c0 + nrdim;
   int m = blockIdx.y, k = blockIdx.x;
   int nn = max(min(nrc, nrc - m), 0);
   int cnt = k_count(k, nzc, nzcu, nzdim);
@@ -1383,40 +1417,37 @@ __global__ void k_band_apply_T(double2* __restrict__ e, const double* __restrict
   }
   __syncthreads();
   if (m >= npc || nn <= 0 || cnt <= 0) return;
-  for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = g[i];
-  __syncthreads();
-  double akd = ak[k], akv2 = akd * akd;
-  for (int rep = 0; rep < cnt; ++rep) {
-    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
-      double2 acc = make_double2(0.0, 0.0);
-      if (op == 0) {
-        if (j + 1 < nn) { double v = bxx[3 * ((size_t)(j + 1) + (size_t)ne * m) + 0]; acc.x += v * c0[j + 1].x; acc.y += v * c0[j + 1].y; }
-        if (j - 1 >= 0) { double v = bxx[3 * ((size_t)(j - 1) + (size_t)ne * m) + 2]; acc.x += v * c0[j - 1].x; acc.y += v * c0[j - 1].y; }
-      } else {
-        for (int i = max(0, j - 2); i <= min(nn - 1, j + 2); ++i) {
-          double v = bd2[(j - i + 2) + 5 * ((size_t)i + (size_t)ne * m)];
-          if (i == j && op == 2) v -= akv2;
-          acc.x += v * c0[i].x;
-          acc.y += v * c0[i].y;
-        }
-      }
-      c1[j] = acc;
-    }
+  if (m == 0 || sizeof(T) == sizeof(double)) {
+    double2* c0 = (double2*)bandt_smem;
+    double2* c1 = c0 + nrdim;
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = g[i];
     __syncthreads();
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = c1[i];
+    c0 = band_T_col<double>(c0, c1, tb, k, op, m, ne, nn, cnt);
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) g[i] = c0[i];
+  } else {
+    float2* c0 = (float2*)bandt_smem;
+    float2* c1 = c0 + nrdim;
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) c0[i] = ld_c32(g + i);
     __syncthreads();
+    c0 = band_T_col<float>(c0, c1, tb, k, op, m, ne, nn, cnt);
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) st_c32(g + i, c0[i]);
   }
-  for (int i = threadIdx.x; i < nn; i += blockDim.x) g[i] = c0[i];
 }
 
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c) {
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   dim3 grid(G.nzdim, std::max(c.npc, 1));
   size_t sm = 2ull * G.nrdim * sizeof(double2);
-  if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_T, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   kt_begin(2);
-  k_band_apply_T<<<grid, 128, sm, G.stream>>>(s.e, G.bd2, G.bxx, G.ak, s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne, c.nrc,
-                                              c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  if (G.precision == MLG_MIXED) {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_T<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply_T<float><<<grid, 128, sm, G.stream>>>(s.e, band_tabs(), s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+                                                       c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  } else {
+    if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_T<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_band_apply_T<double><<<grid, 128, sm, G.stream>>>(s.e, band_tabs(), s.ln, G.lognorm, op, G.nrdim, G.npdim, G.ne,
+                                                        c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell);
+  }
   MLG_LAUNCH();
   kt_end(2, 2.0 * G.fsize * 16);
   return 0;

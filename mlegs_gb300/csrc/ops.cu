@@ -149,12 +149,18 @@ struct LinArgs {
   size_t n;
 };
 __global__ void k_lincomb(LinArgs a) {
+  const bool scaled = a.post != 1.0;   // multiplying by 1 changes nothing: skipped
   GRID_STRIDE(idx, a.n) {
     double2 acc = make_double2(0, 0);
+    bool first = true;
 #pragma unroll
     for (int t = 0; t < 4; ++t)
-      if (a.in[t]) { double2 v = a.in[t][idx]; acc.x += a.c[t] * v.x; acc.y += a.c[t] * v.y; }
-    a.out[idx] = make_double2(a.post * acc.x, a.post * acc.y);
+      if (a.in[t]) {
+        double2 v = a.in[t][idx];
+        if (first) { acc.x = a.c[t] * v.x; acc.y = a.c[t] * v.y; first = false; }   // 0 + c v, exactly
+        else { acc.x += a.c[t] * v.x; acc.y += a.c[t] * v.y; }
+      }
+    a.out[idx] = scaled ? make_double2(a.post * acc.x, a.post * acc.y) : acc;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && a.lnout) {
     double l = 0.0;
