@@ -20,6 +20,7 @@
 // TR*16 bytes) and TT threads per transform, keeps the TR transforms in shared memory as
 // [point][TR] and runs a Stockham autosort FFT (radix 4, 2, 3, 5) between two shared buffers.
 #include "common.cuh"
+#include "dfloat.cuh"
 #include <type_traits>
 
 namespace mlg {
@@ -417,21 +418,30 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
   C a[R1];
   double sum = 0.0;
   if (DC) {
-    double2 d[R1];
-    double part = 0.0;
+    // the row scale, the row sum and the mean subtraction in double-float (about 47 bits, on the FP32
+    // and integer pipes; FP64 would occupy GB300's narrow FP64 pipe with 4-6 operations per sample);
+    // the samples less their mean are then rounded to FP32 for the transform
+    dfl dx[R1], dy[R1];
+    dfl part(0);
+    const dfl rvd = rsc ? dfl(rv) : dfl(1);
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
-      d[n1] = ok ? base[(size_t)(w + R2 * n1) * nrdim] : make_double2(0.0, 0.0);
-      if (rsc) { d[n1].x *= rv; d[n1].y *= rv; }
-      part += d[n1].x + d[n1].y;
+      const double2 v = ok ? base[(size_t)(w + R2 * n1) * nrdim] : make_double2(0.0, 0.0);
+      dx[n1] = dfl(v.x);
+      dy[n1] = dfl(v.y);
+      if (rsc) { dx[n1] = dx[n1] * rvd; dy[n1] = dy[n1] * rvd; }
+      part = part + dx[n1] + dy[n1];
     }
-    red[w * TRL + lane] = part;
+    dfl* redf = reinterpret_cast<dfl*>(red);
+    redf[w * TRL + lane] = part;
     __syncthreads();
+    dfl sd(0);
 #pragma unroll
-    for (int q = 0; q < R2; ++q) sum += red[q * TRL + lane];
-    double mu = sum * inv_np;
+    for (int q = 0; q < R2; ++q) sd = sd + redf[q * TRL + lane];
+    const dfl mu = sd * dfl((float)inv_np, 0.f);   // inv_np = 1/np, a power of two for these lengths
+    sum = f2d_fast(sd.h) + f2d_fast(sd.l);
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>((T)d2f_fast(d[n1].x - mu), (T)d2f_fast(d[n1].y - mu));
+    for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>((T)(dx[n1] - mu).h, (T)(dy[n1] - mu).h);
   } else {
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
