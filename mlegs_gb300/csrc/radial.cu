@@ -349,12 +349,41 @@ static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool
   return 0;
 }
 
+// the rows of each column (m, z) of a radial transform's output that the mixed form's contractions
+// leave unwritten, to zero: rows >= nn(m) after the forward (the chopped rows), rows >= nr after the
+// backward (the padding, the whole column where nn(m) = 0); columns m >= npc whole.  One warp per column.
+__global__ void k_zero_tails(double2* __restrict__ out, int mode, int nr, int nrdim, int npdim, int nzdim, int nrc,
+                             int npc) {
+  const int lane = threadIdx.x & 31;
+  const size_t ncols = (size_t)npdim * nzdim, nw = (size_t)gridDim.x * (blockDim.x >> 5);
+  for (size_t c = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < ncols; c += nw) {
+    const int m = (int)(c % npdim);
+    const int nn = m < npc ? max(min(nrc, nrc - m), 0) : 0;
+    const int lim = mode == 0 ? nn : (nn > 0 ? nr : 0);
+    double2* col = out + (size_t)nrdim * c;
+    for (int j = lim + lane; j < nrdim; j += 32) col[j] = make_double2(0.0, 0.0);
+  }
+}
+
+static int zero_tails(cd* out, int mode, int nrc, int npc) {
+  const size_t ncols = (size_t)G.npdim * G.nzdim;
+  k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, G.stream>>>(out, mode, G.nr, G.nrdim, G.npdim,
+                                                                                    G.nzdim, nrc, npc);
+  MLG_LAUNCH();
+  return 0;
+}
+
 int launch_rtrans_fwd(Scalar& s) {
   int nrc, npc;
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_forward"));
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
-  MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  // the mixed form's contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
+  if (G.precision == MLG_MIXED) {
+    MLG_TRY(zero_tails(out, 0, nrc, npc));
+  } else {
+    MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  }
   kt_begin(KT_RFWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
@@ -382,7 +411,13 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_backward"));
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_backward: out of device memory");
-  MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  // the mixed form's contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
+  // plane included): only the rest needs zeros
+  if (G.precision == MLG_MIXED) {
+    MLG_TRY(zero_tails(out, 1, nrc, npc));
+  } else {
+    MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
+  }
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
