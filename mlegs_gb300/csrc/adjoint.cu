@@ -813,9 +813,11 @@ static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* con
 
 // keep (optional): receives the step's velocity and vorticity for step_T
 static int forward_step(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const* keep = nullptr) {
+  // psi_p and chi_p of the step are not part of the state: left unwritten
   TMP(pp); TMP(cp);
-  MLG_TRY(assign(pp, *st[0])); MLG_TRY(assign(cp, *st[1]));
-  return op_vortex_step_dev(*st[0], *st[1], *st[2], *st[3], pp, cp, *st[4], *st[5], uzb, dt, G.dscal + DS_GAIN0, keep);
+  pp.set_space("FFF"); cp.set_space("FFF");
+  return op_vortex_step_dev(*st[0], *st[1], *st[2], *st[3], pp, cp, *st[4], *st[5], uzb, dt, G.dscal + DS_GAIN0, keep,
+                            false);
 }
 
 // startup from (psi0, chi0): psi <- dealias(psi0), nl <- advection_rhs, nl_p <- nl

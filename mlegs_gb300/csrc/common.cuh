@@ -148,6 +148,8 @@ void tc_free();
 int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc);
 int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln);
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
+// zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
+int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);
 int pv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc);
 void pv_free();
 
@@ -196,8 +198,11 @@ int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi,
 // vz without the background) the nonlinear term was formed from
 int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz,
                      Scalar* const* keep = nullptr);
+// write_prev = false leaves psip and chip unwritten: for every step of a run but its last, whose
+// psip and chip no later step reads
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
-                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep = nullptr);
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep = nullptr,
+                       bool write_prev = true);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale,
                          PostChop pc = PostChop{0, 0, 0, 0, 0});

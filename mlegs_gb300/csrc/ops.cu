@@ -788,11 +788,21 @@ int op_abcn(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, double dt) {
   return 0;
 }
 
+// d = s where s is rewritten in full before it is next read: d takes s's buffer, s keeps d's old one
+static int move_into(Scalar& d, Scalar& s) {
+  std::swap(d.e, s.e);
+  MLG_TRY(launch_copy_ln(d.ln, s.ln));
+  std::memcpy(d.space, s.space, 4);
+  for (int i = 0; i < 3; ++i) d.off[i] = s.off[i];
+  return 0;
+}
+
 // abcn of the two fields of a vortex step, (psi, psi_p, nlpsi, nlpsi_p) and (chi, ...): the same
 // operations as two abcn calls, with the two Helmholtz solves (same alpha, same chop window) done in
-// one substitution pass
+// one substitution pass.  in_step: the caller recomputes nl and ml in full before reading them again,
+// so nl_p and ml_p take their buffers instead of copies; write_prev = false leaves s_p and t_p unwritten.
 static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar& t, Scalar& t_p, Scalar& ml,
-                        Scalar& ml_p, double dt) {
+                        Scalar& ml_p, double dt, bool in_step, bool write_prev) {
   if (G.P.hyperpow != 0) {
     MLG_TRY(op_abcn(s, s_p, nl, nl_p, dt));
     return op_abcn(t, t_p, ml, ml_p, dt);
@@ -814,10 +824,12 @@ static int op_abcn_pair(Scalar& s, Scalar& s_p, Scalar& nl, Scalar& nl_p, Scalar
     MLG_TRY(launch_band_solve(s, 0, c1, a, 0.0, 0.0, 0));
     MLG_TRY(launch_band_solve(t, 0, c2, a, 0.0, 0.0, 0));
   }
-  MLG_TRY(assign(s_p, s));
-  MLG_TRY(assign(nl_p, nl));
-  MLG_TRY(assign(t_p, t));
-  MLG_TRY(assign(ml_p, ml));
+  if (write_prev) { MLG_TRY(assign(s_p, s)); MLG_TRY(assign(t_p, t)); }
+  if (in_step) {
+    MLG_TRY(move_into(nl_p, nl)); MLG_TRY(move_into(ml_p, ml));
+  } else {
+    MLG_TRY(assign(nl_p, nl)); MLG_TRY(assign(ml_p, ml));
+  }
   return 0;
 }
 
@@ -878,9 +890,8 @@ static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& 
   up.set_space("PFF");
   k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
   MLG_LAUNCH();
-  // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331); psi%ln was set above from calcat1
-  MLG_TRY(launch_zero(psi.e));
-  MLG_TRY(launch_zero(chi.e));
+  // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331), the zeros written by the contraction below;
+  // psi%ln was set above from calcat1
   MLG_TRY(launch_set_ln(chi.ln, 0.0));
   MLG_TRY(launch_vec2tp_contract(ur.e, up.e, uz.e, psi.e, chi.e, 3));
   MLG_TRY(op_idel2(chi, false, 0.0));
@@ -1004,9 +1015,11 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
 
 // main-loop step (vortical_flow_3d.f90:168-180) with the gains in device memory
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,
-                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep) {
+                       Scalar& nlchip, const Scalar& uz, double dt, double* gains_dev, Scalar* const* keep,
+                       bool write_prev) {
   for (Scalar* q : {&psi, &chi, &nlpsi, &nlchi, &psip, &chip, &nlpsip, &nlchip}) MLG_TRY(op_trans(*q, "FFF"));
-  MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt));
+  // nlpsi and nlchi are recomputed in full by the advection below
+  MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt, true, write_prev));
   MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
   MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
   MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
@@ -1279,8 +1292,9 @@ static int vortex_loop(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, m
   double* gd = G.dscal + DS_GAIN0;
   MLG_CUDA(cudaMemcpyAsync(gd, gains, 2 * sizeof(double), cudaMemcpyHostToDevice, G.stream));
   MLG_CUDA(cudaMemsetAsync(G.dscal + DS_FLAG, 0, sizeof(double), G.stream));
-  for (int t = 0; t < nsteps; ++t)
-    MLG_TRY(op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd));
+  for (int t = 0; t < nsteps; ++t)   // psip and chip are read by no step: written by the last
+    MLG_TRY(op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd, nullptr,
+                               t == nsteps - 1));
   MLG_CUDA(cudaMemcpyAsync(gains, gd, 2 * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
   int flag = 0;
   MLG_CUDA(cudaMemcpyAsync(&flag, G.dscal + DS_FLAG, sizeof(int), cudaMemcpyDeviceToHost, G.stream));

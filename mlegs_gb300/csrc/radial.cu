@@ -349,26 +349,27 @@ static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool
   return 0;
 }
 
-// the rows of each column (m, z) of a radial transform's output that the mixed form's contractions
-// leave unwritten, to zero: rows >= nn(m) after the forward (the chopped rows), rows >= nr after the
-// backward (the padding, the whole column where nn(m) = 0); columns m >= npc whole.  One warp per column.
+// the rows of each column (m, z) of a mixed-form contraction's output that its kernels leave
+// unwritten, to zero: mode 0 (forward radial transform, projection) rows >= nn(m), and the whole column
+// where z is outside the kept band k <= nzc or k >= nzcu; mode 1 (backward radial transform) rows >= nr
+// (the padding), the whole column where nn(m) = 0; columns m >= npc whole.  One warp per column.
 __global__ void k_zero_tails(double2* __restrict__ out, int mode, int nr, int nrdim, int npdim, int nzdim, int nrc,
-                             int npc) {
+                             int npc, int nzc, int nzcu) {
   const int lane = threadIdx.x & 31;
   const size_t ncols = (size_t)npdim * nzdim, nw = (size_t)gridDim.x * (blockDim.x >> 5);
   for (size_t c = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < ncols; c += nw) {
-    const int m = (int)(c % npdim);
-    const int nn = m < npc ? max(min(nrc, nrc - m), 0) : 0;
+    const int m = (int)(c % npdim), kk = (int)(c / npdim) + 1;
+    const int nn = (m < npc && (kk <= nzc || kk >= nzcu)) ? max(min(nrc, nrc - m), 0) : 0;
     const int lim = mode == 0 ? nn : (nn > 0 ? nr : 0);
     double2* col = out + (size_t)nrdim * c;
     for (int j = lim + lane; j < nrdim; j += 32) col[j] = make_double2(0.0, 0.0);
   }
 }
 
-static int zero_tails(cd* out, int mode, int nrc, int npc) {
+int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu) {
   const size_t ncols = (size_t)G.npdim * G.nzdim;
   k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, G.stream>>>(out, mode, G.nr, G.nrdim, G.npdim,
-                                                                                    G.nzdim, nrc, npc);
+                                                                                    G.nzdim, nrc, npc, nzc, nzcu);
   MLG_LAUNCH();
   return 0;
 }
@@ -380,7 +381,7 @@ int launch_rtrans_fwd(Scalar& s) {
   if (!out) return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
   // the mixed form's contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
   if (G.precision == MLG_MIXED) {
-    MLG_TRY(zero_tails(out, 0, nrc, npc));
+    MLG_TRY(launch_zero_tails(out, 0, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
@@ -414,7 +415,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   // the mixed form's contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
   // plane included): only the rest needs zeros
   if (G.precision == MLG_MIXED) {
-    MLG_TRY(zero_tails(out, 1, nrc, npc));
+    MLG_TRY(launch_zero_tails(out, 1, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
@@ -439,11 +440,19 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   return 0;
 }
 
-// ur, up, uz in (r physical, m, k) space; psi and chi zeroed by the caller
+// ur, up, uz in (r physical, m, k) space; psi and chi written in full
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off) {
   int nrc = G.nrchop + nrc_off, npc = G.npchop;
   int nzc = G.chopzl, nzcu = G.chopzu;
   if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
+  // the mixed form's contractions write rows < nn(m) of the kept columns: only the rest needs zeros
+  if (G.precision == MLG_MIXED) {
+    MLG_TRY(launch_zero_tails(psi, 0, nrc, npc, nzc, nzcu));
+    MLG_TRY(launch_zero_tails(chi, 0, nrc, npc, nzc, nzcu));
+  } else {
+    MLG_CUDA(cudaMemsetAsync(psi, 0, G.fsize * sizeof(cd), G.stream));
+    MLG_CUDA(cudaMemsetAsync(chi, 0, G.fsize * sizeof(cd), G.stream));
+  }
   kt_begin(KT_V2TP);
   constexpr int MT = 16, ZT = 32, KC = 16, ZPT = 4;
   int tt = cdiv((nrc + 1) / 2, MT);

@@ -306,6 +306,43 @@ def test_mixed_vortex_steps_within_1e6_of_fp64():
         assert abs(a[1] - b[1]) <= 1e-6 * max(1.0, abs(b[1])), f"mixed {n} ln: {a[1]} vs {b[1]}"
 
 
+def test_vortex_run_equals_single_steps():
+    """A run of 5 steps leaves the same bytes in all eight fields as 5 single-step calls, in both
+    forms: a run writes psi_p and chi_p on its last step only, and nlpsi_p and nlchi_p take the
+    buffers of nlpsi and nlchi each step, which the step's advection then recomputes."""
+    from mlegs_gb300 import vortex
+    from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
+    from mlegs_gb300.params import make_params
+    p = make_params(nr=48, np=32, nz=32, nrchop=48, npchop=17, nzchop=17, ell=4.0, visc=1.0e-3)
+    k = Kit(p)
+    st = vortex.VortexState(k)
+    pert = (fields.spectral_noise(p, k.dims, 91, amp=1e-3, decay=0.3, m_max=4, k_max=8),
+            fields.spectral_noise(p, k.dims, 92, amp=1e-3, decay=0.3, m_max=4, k_max=8))
+    vortex.qvort_init(k, st, q=4.0, uz_b=-0.5, pert=pert)
+    vortex.bootstrap(k, st, 1e-3)
+    snap = {n: getattr(st, n).get() for n in st.names}
+    names = ("psi", "chi", "nlpsi", "nlchi", "psi_p", "chi_p", "nlpsi_p", "nlchi_p")
+    for mode in (PLAIN_FP64, MIXED):
+        k.set_precision(mode)
+        out = []
+        for run in (True, False):
+            for n, (e, ln, sp, _) in snap.items():
+                getattr(st, n).set(e, ln, sp)
+            st.gains = [0.0, 0.0]
+            if run:
+                k.vortex_run(*st.args(), 1e-3, 5, st.gains)
+            else:
+                for _ in range(5):
+                    vortex.step(k, st, 1e-3)
+            out.append(({n: getattr(st, n).get() for n in names}, list(st.gains)))
+        (a, ga), (b, gb) = out
+        assert ga == gb, f"form {mode}: gains {ga} vs {gb}"
+        for n in names:
+            assert np.array_equal(a[n][0], b[n][0]) and a[n][1] == b[n][1] and a[n][2] == b[n][2], \
+                f"form {mode}: {n} of a 5-step run differs from 5 single steps"
+    k.close()
+
+
 @pytest.mark.parametrize("op", ["idel2_pro", "idel2_pre", "ihelm", "abcn"])
 def test_mixed_solves_stay_fp64(mixed_pair, op):
     """The mixed form keeps the banded solves in FP64 (only abcn's explicit increment is summed in
