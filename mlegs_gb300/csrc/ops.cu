@@ -1074,6 +1074,7 @@ int mlg_finalize(void) {
   lu_cache_clear();
   tc_free();
   pv_free();
+  m0_free();
   for (cd* b : G.all_bufs) cudaFree(b);
   void* arrs[] = {G.x, G.w, G.w32, G.r, G.rinv, G.lnx, G.ak, G.lognorm, G.pf, G.at0, G.at1, G.bd2, G.bxx, G.bd2f, G.bxxf, G.ak2f, G.tV, G.tD, G.tT,
                   G.tV32, G.tD32, G.tT32, G.tw_p, G.tw_z, G.tw_pr, G.tw_p32, G.tw_z32, G.tw_pr32, G.ln_slots, G.dscal, G.band_ws};

@@ -301,36 +301,79 @@ static int m0_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
   MLG_LAUNCH();
   return 0;
 }
-// the m = 0 plane of the backward transform in double-float: one warp per (radial point pair i, column
-// z), the lanes splitting the sums over the rows of each parity and reducing them by shuffles (the
-// plane is 1/50 of the work: spread over every SM it stays shorter than the tensor-core kernel beside it)
-__global__ void __launch_bounds__(256) k_m0_bwd_df(const double2* __restrict__ in, double2* __restrict__ out,
-                                                   const double* __restrict__ pf, const double* __restrict__ lnx,
+// the m = 0 plane of the Legendre table in double-float, tab0[i + nrh j] = pf(i, j) split into an
+// FP32 pair on the integer pipe; built once per kit
+__global__ void k_m0_tab(const double* __restrict__ pf, float2* __restrict__ t, size_t n) {
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) t[o] = d2ff(pf[o]);
+}
+static float2* g_m0tab = nullptr;
+static float4* g_m0col = nullptr;   // the m = 0 plane's rows split, [z][j]: (re.h, re.l, im.h, im.l)
+static size_t g_m0bytes = 0, g_m0cbytes = 0;
+void m0_free() {
+  if (g_m0tab) dfree(g_m0tab, g_m0bytes);
+  if (g_m0col) dfree(g_m0col, g_m0cbytes);
+  g_m0tab = nullptr; g_m0col = nullptr;
+  g_m0bytes = g_m0cbytes = 0;
+}
+static int m0_tab() {
+  if (g_m0tab) return 0;
+  const size_t n = (size_t)G.nrh * G.ne;
+  g_m0bytes = n * sizeof(float2);
+  g_m0cbytes = (size_t)G.nzdim * G.ne * sizeof(float4);
+  MLG_TRY(dmalloc((void**)&g_m0tab, g_m0bytes));
+  MLG_TRY(dmalloc((void**)&g_m0col, g_m0cbytes));
+  k_m0_tab<<<nblk(n), 256, 0, G.stream>>>(G.pf, g_m0tab, n);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// the m = 0 plane's rows j < nn of every column z split into FP32 pairs, once per transform
+__global__ void k_m0_split(const double2* __restrict__ in, float4* __restrict__ col, int nrdim, int npdim, int nzdim,
+                           int nn) {
+  const size_t n = (size_t)nzdim * nn;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
+    const int z = (int)(o / nn), j = (int)(o % nn);
+    const double2 v = in[(size_t)nrdim * npdim * z + j];
+    const float2 a = d2ff(v.x), b = d2ff(v.y);
+    col[o] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+// the m = 0 plane of the backward transform in double-float: one warp per (column z, four radial
+// point pairs i), its lanes (i, row group g) summing rows 2t, 2t+1 for t = g mod 8 and reducing the
+// eight groups by shuffles.  Table and column arrive split (no conversion in the loop).  The plane is
+// 1/65 of the work and runs beside the tensor-core kernel, which holds most SMs' register files.
+__global__ void __launch_bounds__(256) k_m0_bwd_df(const float4* __restrict__ col, double2* __restrict__ out,
+                                                   const float2* __restrict__ tab, const double* __restrict__ lnx,
                                                    const double* __restrict__ lnp, int add_ln, int nr, int nrh, int nrdim,
                                                    int npdim, int nzdim, int nn) {
   const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  const int i = wid % nrh, z = wid / nrh;
+  const int nig = (nrh + 3) / 4;
+  const int z = wid / nig, i0 = (wid % nig) * 4;
   if (z >= nzdim) return;
-  const double2* col = in + (size_t)nrdim * npdim * z;
+  const int g = lane >> 2, i = i0 + (lane & 3), ic = min(i, nrh - 1);
+  const float4* c = col + (size_t)nn * z;
   dfl er = 0, ei = 0, orr = 0, oi = 0;
   const int nt = (nn + 1) / 2;
-  for (int t = lane; t < nt; t += 32) {
-    int je = 2 * t, jo = je + 1;
-    dfl ae(pf[i + (size_t)nrh * je]);
-    dfl2 ce = ldc<dfl>(col + je);
-    er = tmac(ae, ce.x, er); ei = tmac(ae, ce.y, ei);
+  for (int t = g; t < nt; t += 8) {
+    const int je = 2 * t, jo = je + 1;
+    const float2 ae = tab[ic + (size_t)nrh * je];
+    const float4 ce = c[je];
+    er = tmac(dfl(ae.x, ae.y), dfl(ce.x, ce.y), er);
+    ei = tmac(dfl(ae.x, ae.y), dfl(ce.z, ce.w), ei);
     if (jo < nn) {
-      dfl ao(pf[i + (size_t)nrh * jo]);
-      dfl2 co = ldc<dfl>(col + jo);
-      orr = tmac(ao, co.x, orr); oi = tmac(ao, co.y, oi);
+      const float2 ao = tab[ic + (size_t)nrh * jo];
+      const float4 co = c[jo];
+      orr = tmac(dfl(ao.x, ao.y), dfl(co.x, co.y), orr);
+      oi = tmac(dfl(ao.x, ao.y), dfl(co.z, co.w), oi);
     }
   }
 #pragma unroll
-  for (int o = 16; o; o >>= 1) {
+  for (int o = 4; o < 32; o <<= 1) {
     er = er + df_shfl_xor(er, o); ei = ei + df_shfl_xor(ei, o);
     orr = orr + df_shfl_xor(orr, o); oi = oi + df_shfl_xor(oi, o);
   }
-  if (lane == 0) {
+  if (g == 0 && i < nrh) {
     double2* base = out + (size_t)nrdim * npdim * z;
     double2 p = to_d2<dfl>(er + orr, ei + oi);
     double2 q = to_d2<dfl>(er - orr, ei - oi);
@@ -342,9 +385,11 @@ __global__ void __launch_bounds__(256) k_m0_bwd_df(const double2* __restrict__ i
 
 static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln, cudaStream_t st) {
   if (nrc <= 0) return 0;
-  const int warps = G.nrh * G.nzdim;
-  k_m0_bwd_df<<<cdiv(warps, 8), 256, 0, st>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh, G.nrdim, G.npdim,
-                                              G.nzdim, nrc);
+  k_m0_split<<<nblk((size_t)G.nzdim * nrc), 256, 0, st>>>(in, g_m0col, G.nrdim, G.npdim, G.nzdim, nrc);
+  MLG_LAUNCH();
+  const int warps = ((G.nrh + 3) / 4) * G.nzdim;
+  k_m0_bwd_df<<<cdiv(warps, 8), 256, 0, st>>>(g_m0col, out, g_m0tab, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh, G.nrdim,
+                                              G.npdim, G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
@@ -422,6 +467,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (G.precision == MLG_MIXED) {
+      MLG_TRY(m0_tab());
       MLG_TRY(side_fork());
       MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln, G.side));   // m = 0: double-float, beside
       MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));      // m >= 1: tensor cores, split BF16
