@@ -704,8 +704,9 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
 }
 
 // the nonlinear term around (psi, chi) (already dealiased, FFF): nl = dealias(vec2tp(v x w)), nl%ln = 0,
-// v = tp2vec(psi, chi) + (0, 0, uz), w = tp2curlvec(psi, chi).  (nlpsi_bar, nlchi_bar) -> (psi_bar, chi_bar)
-int nlcore_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scalar& nlpb, const Scalar& nlcb, Scalar& psib,
+// v = tp2vec(psi, chi) + (0, 0, uz), w = tp2curlvec(psi, chi).  (nlpsi_bar, nlchi_bar) -> (psi_bar, chi_bar).
+// psi and chi are read only when v and w are not kept (vw_kept null)
+int nlcore_T(const Scalar* psi, const Scalar* chi, const Scalar& uzb, const Scalar& nlpb, const Scalar& nlcb, Scalar& psib,
              Scalar& chib, Scalar* const* vw_kept) {
   TMP(np_); TMP(nc_);
   MLG_TRY(assign(np_, nlpb)); MLG_TRY(assign(nc_, nlcb));
@@ -721,9 +722,10 @@ int nlcore_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const Scal
   if (vw_kept) for (int i = 0; i < 6; ++i) vw[i] = vw_kept[i];
   Scalar &vr = *vw[0], &vp = *vw[1], &vz = *vw[2], &wr = *vw[3], &wp = *vw[4], &wz = *vw[5];
   if (!vw_kept) {
+    if (!psi || !chi) return set_error(MLG_EHANDLE, "adjoint: no linearisation point");
     for (Scalar* q : vw) q->set_space("PPP");
-    MLG_TRY(op_tp2vec(psi, chi, vr, vp, vz));
-    MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
+    MLG_TRY(op_tp2vec(*psi, *chi, vr, vp, vz));
+    MLG_TRY(op_tp2curlvec(*psi, *chi, wr, wp, wz));
   }
   MLG_TRY(lincomb(vz, {{&vz, 1.0}, {&uzb, 1.0}}, {}, 1.0, false));
   TMP(vbr); TMP(vbp); TMP(vbz); TMP(wbr); TMP(wbp); TMP(wbz);
@@ -749,7 +751,7 @@ int advection_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const S
   TMP(p3); TMP(c3);
   MLG_TRY(assign(p3, psi)); MLG_TRY(assign(c3, chi));
   MLG_TRY(op_dealias(p3)); MLG_TRY(op_dealias(c3));
-  MLG_TRY(nlcore_T(p3, c3, uzb, nlpb, nlcb, psib, chib, nullptr));
+  MLG_TRY(nlcore_T(&p3, &c3, uzb, nlpb, nlcb, psib, chib, nullptr));
   MLG_TRY(op_dealias(psib)); MLG_TRY(op_dealias(chib));
   return 0;
 }
@@ -786,15 +788,15 @@ static int adjoint_supported() {
   return 0;
 }
 
-// One step backward.  st = (psi, chi, nlpsi, nlchi, nlpsi_p, nlchi_p) at the step's end (the point
-// its nonlinear term was evaluated at); ad = the adjoint of that state, replaced by the adjoint of
-// the state at the step's start.
-static int step_T(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* const ad[6], Scalar* const* vw) {
+// One step backward.  vw = the velocity and vorticity the step's nonlinear term was formed from (kept
+// by its forward, consumed here); ad = the adjoint of the state (psi, chi, nlpsi, nlchi, nlpsi_p,
+// nlchi_p) at the step's end, replaced by the adjoint of the state at the step's start.
+static int step_T(const Scalar& uzb, double dt, Scalar* const ad[6], Scalar* const* vw) {
   Scalar& pb = *ad[0]; Scalar& cb = *ad[1];
   Scalar& npb = *ad[2]; Scalar& ncb = *ad[3];
   Scalar& nppb = *ad[4]; Scalar& ncpb = *ad[5];
   TMP(xp); TMP(xc);
-  MLG_TRY(nlcore_T(*st[0], *st[1], uzb, npb, ncb, xp, xc, vw));
+  MLG_TRY(nlcore_T(nullptr, nullptr, uzb, npb, ncb, xp, xc, vw));
   MLG_TRY(lincomb(pb, {{&pb, 1.0}, {&xp, 1.0}}, {{&pb, 1.0}, {&xp, 1.0}}));
   MLG_TRY(lincomb(cb, {{&cb, 1.0}, {&xc, 1.0}}, {{&cb, 1.0}, {&xc, 1.0}}));
   for (Scalar* q : {&pb, &cb}) {
@@ -933,32 +935,26 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
   rc = energy(*cur.p[0], *cur.p[1], J, ad.p[0], ad.p[1]);
   for (int i = 2; i < 6 && !rc; ++i) { rc = launch_zero(ad.p[i]->e); if (!rc) rc = launch_set_ln(ad.p[i]->ln, 0.0); set_fff0(*ad.p[i]); }
   for (int i = 0; i < 2 && !rc; ++i) rc = project_active(*ad.p[i]);
-  // backward sweep, segment by segment: recompute the end-of-step states (keeping each step's
-  // velocity and vorticity, the linearisation point of its nonlinear term), then step back
-  std::vector<State*> seg, segvw;
+  // backward sweep, segment by segment: recompute the segment's steps from its checkpoint, keeping
+  // each step's velocity and vorticity (the linearisation point of its nonlinear term, all that the
+  // step back reads of the forward), then step back
+  std::vector<State*> segvw;
   for (int c = (int)ck.size() - 1; c >= 0 && !rc; --c) {
     int s0 = c * k_ckpt, s1 = std::min(nsteps, s0 + k_ckpt);
     int len = s1 - s0;
-    while ((int)seg.size() < len) {
-      State* t = new State();
-      if (t->rc) { rc = t->rc; delete t; break; }
-      seg.push_back(t);
+    while ((int)segvw.size() < len) {
       State* v = new State();
       if (v->rc) { rc = v->rc; delete v; break; }
       segvw.push_back(v);
     }
     if (rc) break;
     rc = copy_state(cur.p, ck[c]->p);
-    for (int q = 0; q < len && !rc; ++q) {
-      rc = forward_step(cur.p, uzb, dt, segvw[q]->p);
-      if (!rc) rc = copy_state(seg[q]->p, cur.p);
-    }
+    for (int q = 0; q < len && !rc; ++q) rc = forward_step(cur.p, uzb, dt, segvw[q]->p);
     for (int q = len - 1; q >= 0 && !rc; --q) {
-      rc = step_T(seg[q]->p, uzb, dt, ad.p, segvw[q]->p);
+      rc = step_T(uzb, dt, ad.p, segvw[q]->p);
       for (int i = 0; i < 6 && !rc; ++i) rc = project_active(*ad.p[i]);
     }
   }
-  for (State* t : seg) delete t;
   for (State* t : segvw) delete t;
   if (!rc) {
     // through the startup: nl(0) = nl_p(0) = advection_rhs(psi0, chi0)
@@ -986,7 +982,7 @@ int adjoint_step(Scalar* const st[6], const Scalar& uzb, double dt, Scalar* cons
   if (vw.rc) return vw.rc;
   MLG_TRY(copy_state(e.p, st));
   MLG_TRY(forward_step(e.p, uzb, dt, vw.p));
-  return step_T(e.p, uzb, dt, ad, vw.p);
+  return step_T(uzb, dt, ad, vw.p);
 }
 
 }  // namespace mlg
