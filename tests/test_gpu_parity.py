@@ -1,7 +1,7 @@
 """GPU parity: every operator of the C ABI against the CPU oracle on the same seeded inputs.
 
-The plain form (all FP64) must agree with the oracle's FP64 restatement of the reference to the
-spec bar of 1e-12 relative (L2 over the field); the 100-step run compounds rounding over many
+The plain form (all FP64) must agree with the oracle's FP64 restatement of the reference to 1e-12
+relative (L2 over the field), the drop-in's bar; the 100-step run compounds rounding over many
 solves and is held to 1e-11.  The mixed form is checked against the same oracle at 1e-5 per operator.
 """
 import numpy as np
