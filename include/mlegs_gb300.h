@@ -249,6 +249,15 @@ typedef struct mlg_run_params {
  * flddir and logdir (mkdir -p) as the reference does. */
 int mlg_read_input(const char* fn, mlg_params* p, mlg_run_params* run, int make_dirs);
 
+/* ---- diagnostics of the bounded device waits (no counterpart in the reference) ------------ */
+/* Every wait of a tensor-core kernel on an mbarrier gives up after about a second of SM clock, sets a
+ * timeout word in device memory and lets the kernel return; the next mlg_sync (or vortex step/run)
+ * then returns MLG_ETIMEOUT.  This call enqueues one thread that takes that same path on an mbarrier:
+ * arrive = 0, nothing arrives and the wait runs out after limit_clocks (0 .. 2e9); arrive = 1, the
+ * thread arrives first and the wait succeeds.  It lets a host check, without any fault, that a wait
+ * that runs out reaches it as MLG_ETIMEOUT. */
+int mlg_selftest_bounded_wait(long long limit_clocks, int arrive);
+
 /* ---- kernel timing (CUDA events around each launch of one kernel class) ----------------- */
 /* kind: 0 = forward radial Legendre contraction, 1 = FFTs, 2 = banded operators (applies and the
  *       fused abcn right-hand side), 3 = backward radial contraction, 4 = vec2tp projection

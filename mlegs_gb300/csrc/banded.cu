@@ -1189,6 +1189,8 @@ static double* g_noalloc_ptr[64] = {nullptr};
 int ihelm_noalloc(void* e_dev, double* ln, double alpha) {
   int dev = 0;
   MLG_CUDA(cudaGetDevice(&dev));
+  if (dev != G.device)
+    return set_error(MLG_EPARAM, "ihelm_noalloc: the current CUDA device is not the one the kit was built on");
   if (dev < 0 || dev >= 64) return set_error(MLG_ESIZE, "ihelm_noalloc: device index beyond 63");
   if (!g_noalloc_ptr[dev]) {
     void* ptr = nullptr;

@@ -67,6 +67,7 @@ struct Ctx {
   double ell = 0;
   int precision = MLG_PLAIN_FP64;
   cudaStream_t stream = 0;
+  int device = -1;        // the CUDA device that was current when the kit was built
 
   // kit arrays on the device
   double *x = nullptr, *w = nullptr, *r = nullptr, *rinv = nullptr, *lnx = nullptr, *ak = nullptr;
@@ -147,6 +148,7 @@ void lu_cache_clear();
 void tc_free();
 int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc);
 int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln);
+int wait_selftest(long long limit, int arrive);
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
 // zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);

@@ -400,6 +400,7 @@ int kit_build(const mlg_params* P) {
 
   MLG_TRY(dmalloc((void**)&G.dscal, DS_COUNT * sizeof(double)));
   MLG_CUDA(cudaMemset(G.dscal, 0, DS_COUNT * sizeof(double)));
+  MLG_CUDA(cudaGetDevice(&G.device));
   G.kit_set = true;
   return 0;
 }

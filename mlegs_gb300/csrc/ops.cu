@@ -1035,6 +1035,17 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
 // C ABI
 using namespace mlg;
 
+// The error words at DS_FLAG + 1 (w[0]: a banded factorisation met a zero pivot; w[1]: a bounded
+// device-side wait of a tensor-core kernel ran out), read by the caller after a stream sync.  Clears
+// them and returns the status they stand for; a timeout wins, since the results of that launch are void.
+static int device_status(const int* w) {
+  if (!w[0] && !w[1]) return 0;
+  MLG_CUDA(cudaMemsetAsync(G.dscal + DS_FLAG + 1, 0, sizeof(double), G.stream));
+  MLG_CUDA(cudaStreamSynchronize(G.stream));
+  if (w[1]) return set_error(MLG_ETIMEOUT, "a bounded device-side wait ran out: the results of the last calls are void");
+  return set_error(MLG_ESINGULAR, "lurc: lu factorization resulted in failure");
+}
+
 static int need_kit() { return G.kit_set ? 0 : set_error(MLG_ENOKIT, "transformation kit is not initialized"); }
 #define NEED_KIT() MLG_TRY(need_kit())
 #define SC(p) if (!(p) || !(p)->e) return set_error(MLG_EHANDLE, "invalid scalar handle")
@@ -1123,14 +1134,10 @@ int mlg_set_stream(void* stream) { G.stream = (cudaStream_t)stream; return 0; }
 int mlg_sync(void) {
   MLG_CUDA(cudaStreamSynchronize(G.stream));
   if (G.kit_set) {
-    int flags[2] = {0, 0};
-    MLG_CUDA(cudaMemcpy(flags, G.dscal + DS_FLAG, sizeof(double), cudaMemcpyDeviceToHost));
-    int sing = 0;
-    MLG_CUDA(cudaMemcpy(&sing, (int*)(G.dscal + DS_FLAG + 1), sizeof(int), cudaMemcpyDeviceToHost));
-    if (sing) {
-      cudaMemset(G.dscal + DS_FLAG + 1, 0, sizeof(double));
-      return set_error(MLG_ESINGULAR, "lurc: lu factorization resulted in failure");
-    }
+    int w[2] = {0, 0};
+    MLG_CUDA(cudaMemcpyAsync(w, G.dscal + DS_FLAG + 1, sizeof(w), cudaMemcpyDeviceToHost, G.stream));
+    MLG_CUDA(cudaStreamSynchronize(G.stream));
+    return device_status(w);
   }
   return 0;
 }
@@ -1297,10 +1304,11 @@ static int vortex_loop(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, m
     MLG_TRY(op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd, nullptr,
                                t == nsteps - 1));
   MLG_CUDA(cudaMemcpyAsync(gains, gd, 2 * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
-  int flag = 0;
-  MLG_CUDA(cudaMemcpyAsync(&flag, G.dscal + DS_FLAG, sizeof(int), cudaMemcpyDeviceToHost, G.stream));
+  int w[4] = {0, 0, 0, 0};   // DS_FLAG: non-finite flag, unused; DS_FLAG + 1: singular-LU flag, timeout flag
+  MLG_CUDA(cudaMemcpyAsync(w, G.dscal + DS_FLAG, sizeof(w), cudaMemcpyDeviceToHost, G.stream));
   MLG_CUDA(cudaStreamSynchronize(G.stream));
-  if (flag) return set_error(MLG_ENONFINITE, "ERROR: non-finite vortex state");
+  MLG_TRY(device_status(w + 2));
+  if (w[0]) return set_error(MLG_ENONFINITE, "ERROR: non-finite vortex state");
   return 0;
 }
 int mlg_vortex_step(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f, mlg_scalar g,
@@ -1310,6 +1318,11 @@ int mlg_vortex_step(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_
 int mlg_vortex_run(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, mlg_scalar e, mlg_scalar f, mlg_scalar g,
                    mlg_scalar h, mlg_scalar u, double dt, int nsteps, double* gains) {
   return vortex_loop(a, b, c, d, e, f, g, h, u, dt, nsteps, gains);
+}
+
+int mlg_selftest_bounded_wait(long long limit_clocks, int arrive) {
+  NEED_KIT();
+  return wait_selftest(limit_clocks, arrive);
 }
 
 int mlg_kernel_timing(int enable) {

@@ -27,13 +27,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
-// bounded wait (~1 s of SM clock); false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+// wait bounded by `limit` SM clocks; false on timeout
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t phase, long long limit) {
   long long t0 = clock64();
   while (!mbar_try_wait(bar, phase))
-    if (clock64() - t0 > 2000000000LL) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
+// bounded wait (~1 s of SM clock); false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) { return mbar_wait_limit(bar, phase, 2000000000LL); }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
                    smem_u32(dst)),

@@ -68,6 +68,7 @@ def load(path=None):
         "mlg_msave": [_P, ctypes.c_char_p, _I, _I], "mlg_mload": [_P, ctypes.c_char_p, _I, _I],
         "mlg_fftreat": [_P], "mlg_vort_mag": [_P, _P, _P], "mlg_ke_spectrum": [_P, _P, _P],
         "mlg_read_input": [ctypes.c_char_p, _P, _P, _I],
+        "mlg_selftest_bounded_wait": [ctypes.c_longlong, _I],
     }
     for name in ["mlg_chop", "mlg_dealias", "mlg_zeroat1", "mlg_delsqp", "mlg_idelsqp", "mlg_xxdx", "mlg_del2h",
                  "mlg_del2", "mlg_idel2_proln"]:
