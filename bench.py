@@ -398,6 +398,18 @@ def run_ours(args, rank, world, local, pg):
         cpu_s = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": nstep / cpu_s, "unit": "steps/s", "cores": threads, "kind": "port",
                                 "sample": f"{nstep} steps of the same workload from the same state"}
+        # the GPU's plain form over the same steps from the same state, against the oracle
+        kit.set_precision(PLAIN_FP64)
+        restore(st, snap0)
+        st.gains = [0.0, 0.0]
+        so_gains = list(so.gains)
+        kit.vortex_run(*st.args(), DT, nstep, st.gains)
+        kit.sync()
+        line["plain_vs_oracle"] = {
+            "steps": nstep,
+            "rel_l2": {n: rel_l2(getattr(st, n).get()[0], getattr(so, n).get()[0]) for n in ("psi", "chi", "nlpsi", "nlchi")},
+            "svv_gains_abs_diff": [abs(a - b) for a, b in zip(st.gains, so_gains)],
+            "note": "GPU plain form vs the CPU oracle after the same steps from the same state (192x128x128)"}
         o.close()
     if not args.no_adjoint and world == 1:
         line["adjoint"] = adjoint_case(args)

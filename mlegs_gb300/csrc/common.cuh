@@ -149,6 +149,16 @@ void tc_free();
 int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc);
 int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln);
 int wait_selftest(long long limit, int arrive);
+// exact-slice radial contractions on the tensor cores (xs_radial.cu): mode 0 forward, 1 backward, for
+// m0 <= m < npc; plain: FP64-grade digits, else the mixed form's
+bool xs_supported(int mode, int nrc, bool plain);
+int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const double* lnp, bool add_ln, bool plain);
+void xs_free();
+// the mixed form's projection contraction as exact slices (xs_vec2tp.cu): psi, chi rows of
+// m0 <= m < npc written
+bool xv_supported();
+int xv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc, int m0);
+void xv_free();
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
 // zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);

@@ -1084,6 +1084,8 @@ int mlg_finalize(void) {
   cudaStreamSynchronize(G.stream);
   lu_cache_clear();
   tc_free();
+  xs_free();
+  xv_free();
   pv_free();
   m0_free();
   for (cd* b : G.all_bufs) cudaFree(b);

@@ -424,19 +424,24 @@ int launch_rtrans_fwd(Scalar& s) {
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_forward"));
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
-  // the mixed form's contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
-  if (G.precision == MLG_MIXED) {
+  const bool mixed = G.precision == MLG_MIXED;
+  const bool xs = xs_supported(0, nrc, !mixed);   // exact-slice tensor-core contraction (xs_radial.cu)
+  // the tensor-core contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
+  if (mixed || xs) {
     MLG_TRY(launch_zero_tails(out, 0, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RFWD);
   if (npc > 0) {
-    if (G.precision == MLG_MIXED) {
+    if (mixed) {
       MLG_TRY(side_fork());
       MLG_TRY(m0_rtrans_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
-      MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: tensor cores, split BF16 (tc_radial.cu)
+      if (xs) MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, false));   // m >= 1: 35-bit slices
+      else MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: split BF16 (tc_radial.cu)
       MLG_TRY(side_join());
+    } else if (xs) {
+      MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 0, nullptr, false, true));    // FP64-grade slices, every m
     } else {
       constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
       int tt = cdiv((nrc + 1) / 2, MT);
@@ -457,21 +462,26 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_backward"));
   cd* out = get_buf();
   if (!out) return set_error(MLG_EALLOC, "rtrans_backward: out of device memory");
-  // the mixed form's contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
+  const bool mixed = G.precision == MLG_MIXED;
+  const bool xs = xs_supported(1, nrc, !mixed);
+  // the tensor-core contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
   // plane included): only the rest needs zeros
-  if (G.precision == MLG_MIXED) {
+  if (mixed || xs) {
     MLG_TRY(launch_zero_tails(out, 1, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RBWD);
   if (npc > 0) {
-    if (G.precision == MLG_MIXED) {
+    if (mixed) {
       MLG_TRY(m0_tab());
       MLG_TRY(side_fork());
       MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln, G.side));   // m = 0: double-float, beside
-      MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));      // m >= 1: tensor cores, split BF16
+      if (xs) MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, false));   // m >= 1: 35-bit slices
+      else MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));           // m >= 1: split BF16
       MLG_TRY(side_join());
+    } else if (xs) {
+      MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 0, s.ln, add_ln, true));   // FP64-grade slices, every m
     } else {
       constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
       dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
@@ -491,8 +501,14 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int nrc = G.nrchop + nrc_off, npc = G.npchop;
   int nzc = G.chopzl, nzcu = G.chopzu;
   if (nrc > G.ne || nrc > G.nrdim) return set_error(MLG_ECHOP, "vec2tp: chopping in r too large");
-  // the mixed form's contractions write rows < nn(m) of the kept columns: only the rest needs zeros
-  if (G.precision == MLG_MIXED) {
+  const bool mixed = G.precision == MLG_MIXED;
+  // the exact-slice tensor-core contraction (xs_vec2tp.cu) in the mixed form; the plain form keeps the
+  // FP64 contraction: chi = k X - Y cancels, and the slices' truncation relative to the column maxima
+  // (54-bit digits) left chi 7e-9 from the FP64 reference on the 32^3 kit (sliced radial transforms
+  // hold 1e-12 there)
+  const bool xv = mixed && xv_supported();
+  // the tensor-core contractions write rows < nn(m) of the kept columns: only the rest needs zeros
+  if (mixed) {
     MLG_TRY(launch_zero_tails(psi, 0, nrc, npc, nzc, nzcu));
     MLG_TRY(launch_zero_tails(chi, 0, nrc, npc, nzc, nzcu));
   } else {
@@ -512,7 +528,8 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
     k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
                                                                G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
     MLG_LAUNCH();
-    MLG_TRY(pv_contract(ur, up, uz, psi, chi, nrc, npc));   // m >= 1: tensor cores (tc_vec2tp.cu)
+    if (xv) MLG_TRY(xv_contract(ur, up, uz, psi, chi, nrc, npc, 1));   // m >= 1: 35-bit slices
+    else MLG_TRY(pv_contract(ur, up, uz, psi, chi, nrc, npc));                // m >= 1: split BF16 (tc_vec2tp.cu)
     MLG_TRY(side_join());
     kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
     return 0;

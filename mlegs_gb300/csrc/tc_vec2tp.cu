@@ -160,16 +160,6 @@ __device__ __forceinline__ void pv_store_split(uint8_t* b, int t0, int n, int k0
   for (int s = 0; s < 3; ++s) *(uint32_t*)(b + (t0 + s) * PV_BTILE + pv_off(n, k0)) = w[s];
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // a + b in double-float (Knuth two-sum, renormalised); b exact float
 __device__ __forceinline__ float2 pv_dfadd(float2 a, float b) {
   float s = __fadd_rn(a.x, b), v = __fsub_rn(s, a.x);

@@ -1,0 +1,439 @@
+// xs_vec2tp.cu — the projection contraction of vector_projection (mlegs_scalar_ops.f90:1402-1438, with
+// the eomul / oemul folds :2067-2145) as exact-slice products on the 5th-generation tensor cores.
+//
+// For each m and row parity par, rows j = 2t + par, radial points i < nr/2, z columns n:
+//   psi = (m V).(-i F_s(ur)) + D.(-F_o(up))
+//   chi = k X - Y,   X = D.(i F_o(ur)) + (m V).F_s(up),   Y = T.F_s(uz)
+// F_s / F_o fold u(i) with u(nr-1-i) by the row's own / the other parity's sign.
+//
+// All three sums run in the exact-slice scheme of xs_radial.cu.  psi and X each add two products in one
+// set of digit-order accumulators, so the two products share their scales: one row scale per j over
+// m V and D (kit init), one column scale per real column n over the two field components that land in
+// it (Im ur with Re up for the real part of the output, Re ur with Im up for the imaginary part;
+// the folds may double), and the digits of the folds are exact integer sums of the rounded samples.
+// Y has its own row scale (T) and column scale (uz).  The orders are combined in 128-bit integers and
+// rounded once to FP64 (the mixed form sums the orders in double-float); chi = k X - Y is one FP64 fused
+// multiply-add.  The row parity of a CTA fixes the folds, so each CTA owns one (m, parity, 128-row
+// tile, NZ complex z columns).
+//
+// Digits: NS for psi and X, NT for Y, of w bits: the mixed form's NS = 5 (35 bits) and NT = 6 (6 and 7
+// of 6 bits beyond about 100 radial points); w and the digit counts keep every order's accumulator
+// exact: (pairs of the order) x (nr/2) x 2^(2w) < 2^24, where psi's and X's orders hold two products
+// per digit pair.  (The plain form keeps its FP64 contraction: chi = k X - Y cancels, and even 54-bit
+// slices, cut relative to the column maxima, left chi 7e-9 from the FP64 reference.)
+//
+// Engine: 32 NZ threads per CTA of NZ complex z columns; per K chunk of 16 radial points the table digits (m V, D and T, laid out at kit
+// init in the UMMA canonical K-major layout) arrive by one bulk copy on an mbarrier, the threads cut
+// the field digits (ur, up and uz at i and nr-1-i, loaded in FP64 the chunk before) into the same
+// layout, and one thread issues the chunk's tcgen05.mma (M = 128, N = 2 NZ, K = 16) and commits.  Every
+// wait is bounded.
+#include "common.cuh"
+#include "tc_common.cuh"
+#include "xs_common.cuh"
+#include <cstdint>
+
+namespace mlg {
+
+constexpr int XV_KC = 16;
+constexpr int XV_SBO = XV_KC * 16;
+constexpr int XV_LBO = 128;
+__host__ __device__ constexpr int xv_off(int row, int k) {
+  return (row >> 3) * XV_SBO + (k >> 3) * XV_LBO + (row & 7) * 16 + (k & 7) * 2;
+}
+constexpr int XV_ATILE = 128 * XV_KC * 2;    // 4 KiB
+
+// ------------------------------------------------------------------------------------------------
+// kit-time: row scales rexp[(m * 2 + par) * ntr + t] over (m V, D) and texp over T (-2000: zero row)
+__global__ void k_xv_rexp(const double* __restrict__ tV, const double* __restrict__ tD, const double* __restrict__ tT,
+                          int* __restrict__ rexp, int* __restrict__ texp, int nrh, int ne, int nrc, int ntr) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mp = blockIdx.y, m = mp >> 1, par = mp & 1;
+  if (t >= ntr) return;
+  const int j = 2 * t + par, nn = max(min(nrc, nrc - m), 0);
+  unsigned long long mv = 0, mt = 0;
+  if (j < nn)
+    for (int i = 0; i < nrh; ++i) {
+      const size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
+      unsigned long long a = (unsigned long long)__double_as_longlong((double)m * tV[o]) & 0x7FFFFFFFFFFFFFFFull;
+      unsigned long long b = (unsigned long long)__double_as_longlong(tD[o]) & 0x7FFFFFFFFFFFFFFFull;
+      unsigned long long c = (unsigned long long)__double_as_longlong(tT[o]) & 0x7FFFFFFFFFFFFFFFull;
+      mv = a > mv ? a : mv;
+      mv = b > mv ? b : mv;
+      mt = c > mt ? c : mt;
+    }
+  rexp[(size_t)mp * ntr + t] = mv ? xs_ebound(mv) : -2000;
+  texp[(size_t)mp * ntr + t] = mt ? xs_ebound(mt) : -2000;
+}
+
+// tiles per (m, par, row tile mt, chunk kc): [m V digits NS | D digits NS | T digits NT]
+template <int NS, int NT>
+__global__ void k_xv_table(const double* __restrict__ tV, const double* __restrict__ tD, const double* __restrict__ tT,
+                           const int* __restrict__ rexp, const int* __restrict__ texp, uint16_t* __restrict__ img,
+                           int nrh, int ne, int nrc, int nmt, int nkc, int ntr, int w) {
+  const size_t blk = blockIdx.x;   // ((m * 2 + par) * nmt + mt) * nkc + kc
+  const int kc = (int)(blk % nkc), mt = (int)((blk / nkc) % nmt), mp = (int)(blk / ((size_t)nkc * nmt));
+  const int m = mp >> 1, par = mp & 1;
+  const int nn = max(min(nrc, nrc - m), 0);
+  uint8_t* base = (uint8_t*)img + blk * (size_t)((2 * NS + NT) * XV_ATILE);
+  for (int idx = threadIdx.x; idx < 128 * XV_KC; idx += blockDim.x) {
+    const int k = idx % XV_KC, r = idx / XV_KC;
+    const int t = mt * 128 + r, j = 2 * t + par, i = kc * XV_KC + k;
+    double v = 0.0, d = 0.0, tt = 0.0;
+    int er = -2000, et = -2000;
+    if (t < ntr && j < nn && i < nrh) {
+      const size_t o = i + (size_t)nrh * (j + (size_t)ne * m);
+      v = (double)m * tV[o]; d = tD[o]; tt = tT[o];
+      er = rexp[(size_t)mp * ntr + t]; et = texp[(size_t)mp * ntr + t];
+    }
+    const int off = xv_off(r, k);
+    float h[NS > NT ? NS : NT];
+    xs_digits_f<NS>(xs_fix(v, er, w * NS), w, h);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) *(uint16_t*)(base + s * XV_ATILE + off) = (uint16_t)(__float_as_uint(h[s]) >> 16);
+    xs_digits_f<NS>(xs_fix(d, er, w * NS), w, h);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) *(uint16_t*)(base + (NS + s) * XV_ATILE + off) = (uint16_t)(__float_as_uint(h[s]) >> 16);
+    xs_digits_f<NT>(xs_fix(tt, et, w * NT), w, h);
+#pragma unroll
+    for (int s = 0; s < NT; ++s) *(uint16_t*)(base + (2 * NS + s) * XV_ATILE + off) = (uint16_t)(__float_as_uint(h[s]) >> 16);
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+struct XvArgs {
+  const double2 *ur, *up, *uz;
+  double2 *psi, *chi;
+  const uint16_t* img;
+  const int *rexp, *texp;
+  const double* ak;
+  int* status;
+  int nr, nrh, nrdim, npdim, nzdim, nrc, nzc, nzcu, nmt, nkc, ntr, w, m0;
+};
+
+// NS digits for psi and X, NT for Y; NZ complex z columns per CTA (N = 2 NZ), 32 NZ threads
+template <int NS, int NT, int NZ>
+__global__ void __launch_bounds__(32 * NZ, 1) k_xv_contract(XvArgs a) {
+  constexpr int N = 2 * NZ;
+  constexpr int NTH = 32 * NZ;
+  constexpr int BTILE = N * XV_KC * 2;
+  constexpr int NA = 2 * NS + NT;                 // A tiles per chunk
+  constexpr int NB = 4 * NS + NT;                 // B tiles: psi_ur, psi_up, X_ur, X_up (NS each), uz (NT)
+  constexpr int COLS = (2 * NS + NT) * N;
+  constexpr int TCOLS = COLS <= 128 ? 128 : COLS <= 256 ? 256 : 512;
+  static_assert(COLS <= 512, "accumulators exceed tensor memory");
+  extern __shared__ __align__(1024) uint8_t xv_smem_raw[];
+  uint8_t* sbase = (uint8_t*)(((uintptr_t)xv_smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = sbase;
+  uint8_t* sB = sA + NA * XV_ATILE;
+  int* cexp = (int*)(sB + NB * BTILE);            // [N]: ur/up columns
+  int* fexp = cexp + N;                           // [N]: uz columns
+  unsigned long long* cmax = (unsigned long long*)(fexp + N);   // [2][N]
+  uint64_t* bars = (uint64_t*)(cmax + 2 * N);     // a, mma
+  uint32_t* tslot = (uint32_t*)(bars + 2);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int z0 = blockIdx.x * NZ, par = blockIdx.y & 1, mt = blockIdx.y >> 1, m = blockIdx.z + a.m0;
+  const int nn = max(min(a.nrc, a.nrc - m), 0);
+  if (2 * (mt * 128) + par >= nn) return;
+  const int w = a.w, nbs = w * NS, nbt = w * NT;
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  if (tid < 2 * N) cmax[tid] = 0ull;
+  if (warp == 0) {
+    tmem_alloc(tslot, TCOLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int ss = par ? -1 : 1;   // own-parity fold sign
+  // ---- column scales: cexp(2zz) over (Im ur, Re up), cexp(2zz+1) over (Re ur, Im up); fexp over uz
+  {
+    const int zz = tid % NZ, g = tid / NZ, z = z0 + zz;   // 32 threads per column
+    unsigned long long m0 = 0, m1 = 0, u0 = 0, u1 = 0;
+    if (z < a.nzdim) {
+      const size_t cb = (size_t)a.nrdim * (m + (size_t)a.npdim * z);
+      for (int i = g; i < a.nr; i += 32) {
+        const double2 r = a.ur[cb + i], p = a.up[cb + i], q = a.uz[cb + i];
+        unsigned long long v;
+        v = (unsigned long long)__double_as_longlong(r.y) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
+        v = (unsigned long long)__double_as_longlong(p.x) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
+        v = (unsigned long long)__double_as_longlong(r.x) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
+        v = (unsigned long long)__double_as_longlong(p.y) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
+        v = (unsigned long long)__double_as_longlong(q.x) & 0x7FFFFFFFFFFFFFFFull; u0 = v > u0 ? v : u0;
+        v = (unsigned long long)__double_as_longlong(q.y) & 0x7FFFFFFFFFFFFFFFull; u1 = v > u1 ? v : u1;
+      }
+    }
+    atomicMax(&cmax[2 * zz], m0);
+    atomicMax(&cmax[2 * zz + 1], m1);
+    atomicMax(&cmax[N + 2 * zz], u0);
+    atomicMax(&cmax[N + 2 * zz + 1], u1);
+  }
+  __syncthreads();
+  if (tid < N) {
+    cexp[tid] = cmax[tid] ? xs_ebound(cmax[tid]) + 1 : -2000;          // +1: the folds may double
+    fexp[tid] = cmax[N + tid] ? xs_ebound(cmax[N + tid]) + 1 : -2000;
+  }
+  __syncthreads();
+  // staging item: (field f, column zz, K pair kp); f = 0 ur, 1 up, 2 uz: 24 NZ items
+  const int f = tid / (NZ * 8), zz = tid % NZ, kp = (tid / NZ) % 8;
+  const bool stager = tid < 3 * NZ * 8;
+  const int z = z0 + zz;
+  const bool zok = stager && z < a.nzdim;
+  const size_t cbase = (size_t)a.nrdim * (m + (size_t)a.npdim * (zok ? z : 0));
+  const double2* src = f == 0 ? a.ur : (f == 1 ? a.up : a.uz);
+  double2 va[2], vb[2];
+  auto fetch = [&](int kc) {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int i = kc * XV_KC + 2 * kp + u;
+      const bool ok = zok && i < a.nrh;
+      va[u] = ok ? src[cbase + i] : make_double2(0.0, 0.0);
+      vb[u] = ok ? src[cbase + a.nr - 1 - i] : make_double2(0.0, 0.0);
+    }
+  };
+  bool ok = true;
+  const uint8_t* img_b = (const uint8_t*)a.img + (((size_t)(m * 2 + par) * a.nmt + mt) * a.nkc) * (size_t)(NA * XV_ATILE);
+  const int nkc = a.nkc;
+  int klast = -1;   // the last chunk whose copy and MMAs were issued
+  fetch(0);
+  for (int kc = 0; kc < nkc; ++kc) {
+    klast = kc;
+    if (tid == 0) {
+      mbar_expect_tx(&bars[0], NA * XV_ATILE);
+      bulk_g2s(sA, img_b + (size_t)kc * (NA * XV_ATILE), NA * XV_ATILE, &bars[0]);
+    }
+    if (stager) {
+      const int off = xv_off(2 * zz, 2 * kp), off1 = xv_off(2 * zz + 1, 2 * kp);
+      if (f < 2) {
+        // integer folds of the two components with the column scales of the columns they land in
+        const int Ere = f == 0 ? cexp[2 * zz + 1] : cexp[2 * zz];       // Re ur -> col 2zz+1, Re up -> col 2zz
+        const int Eim = f == 0 ? cexp[2 * zz] : cexp[2 * zz + 1];
+        float h0[2][NS], h1[2][NS], g0[2][NS], g1[2][NS];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const long long ar = xs_fix(va[u].x, Ere, nbs), br = xs_fix(vb[u].x, Ere, nbs);
+          const long long ai = xs_fix(va[u].y, Eim, nbs), bi = xs_fix(vb[u].y, Eim, nbs);
+          const long long fs_re = ar + ss * br, fs_im = ai + ss * bi;
+          const long long fo_re = ar - ss * br, fo_im = ai - ss * bi;
+          if (f == 0) {   // psi_ur = -i F_s(ur): (Im, -Re); X_ur = i F_o(ur): (-Im, Re)
+            xs_digits_f<NS>(fs_im, w, h0[u]); xs_digits_f<NS>(-fs_re, w, h1[u]);
+            xs_digits_f<NS>(-fo_im, w, g0[u]); xs_digits_f<NS>(fo_re, w, g1[u]);
+          } else {        // psi_up = -F_o(up): (-Re, -Im); X_up = F_s(up): (Re, Im)
+            xs_digits_f<NS>(-fo_re, w, h0[u]); xs_digits_f<NS>(-fo_im, w, h1[u]);
+            xs_digits_f<NS>(fs_re, w, g0[u]); xs_digits_f<NS>(fs_im, w, g1[u]);
+          }
+        }
+        const int tp = f == 0 ? 0 : NS, tx = f == 0 ? 2 * NS : 3 * NS;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+          *(uint32_t*)(sB + (tp + s) * BTILE + off) = xs_pack(h0[0][s], h0[1][s]);
+          *(uint32_t*)(sB + (tp + s) * BTILE + off1) = xs_pack(h1[0][s], h1[1][s]);
+          *(uint32_t*)(sB + (tx + s) * BTILE + off) = xs_pack(g0[0][s], g0[1][s]);
+          *(uint32_t*)(sB + (tx + s) * BTILE + off1) = xs_pack(g1[0][s], g1[1][s]);
+        }
+      } else {
+        // Y: F_s(uz) with the uz column scales
+        float h0[2][NT], h1[2][NT];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const long long re = xs_fix(va[u].x, fexp[2 * zz], nbt) + ss * xs_fix(vb[u].x, fexp[2 * zz], nbt);
+          const long long im = xs_fix(va[u].y, fexp[2 * zz + 1], nbt) + ss * xs_fix(vb[u].y, fexp[2 * zz + 1], nbt);
+          xs_digits_f<NT>(re, w, h0[u]);
+          xs_digits_f<NT>(im, w, h1[u]);
+        }
+#pragma unroll
+        for (int s = 0; s < NT; ++s) {
+          *(uint32_t*)(sB + (4 * NS + s) * BTILE + off) = xs_pack(h0[0][s], h0[1][s]);
+          *(uint32_t*)(sB + (4 * NS + s) * BTILE + off1) = xs_pack(h1[0][s], h1[1][s]);
+        }
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      ok = ok && mbar_wait(&bars[0], kc & 1);
+      tc_fence_after();
+      if (ok) {
+        const uint32_t idesc = idesc_bf16(128, N);
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+        auto A = [&](int t) { return sdesc(a0 + t * XV_ATILE, XV_LBO, XV_SBO); };
+        auto B = [&](int t) { return sdesc(b0 + t * BTILE, XV_LBO, XV_SBO); };
+#pragma unroll
+        for (int d = 0; d < NS; ++d)
+#pragma unroll
+          for (int t = 0; t <= d; ++t) {
+            const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
+            umma_bf16(tmem + d * N, A(t), B(d - t), idesc, acc);                          // psi: mV . psi_ur
+            umma_bf16(tmem + d * N, A(NS + t), B(NS + d - t), idesc, 1u);                 //      D . psi_up
+            umma_bf16(tmem + (NS + d) * N, A(NS + t), B(2 * NS + d - t), idesc, acc);     // X: D . X_ur
+            umma_bf16(tmem + (NS + d) * N, A(t), B(3 * NS + d - t), idesc, 1u);           //    mV . X_up
+          }
+#pragma unroll
+        for (int d = 0; d < NT; ++d)
+#pragma unroll
+          for (int t = 0; t <= d; ++t)
+            umma_bf16(tmem + (2 * NS + d) * N, A(2 * NS + t), B(4 * NS + d - t), idesc, (kc > 0 || t > 0) ? 1u : 0u);
+      }
+      umma_commit(&bars[1]);
+    }
+    if (kc + 1 < nkc) fetch(kc + 1);
+    const bool done = mbar_wait(&bars[1], kc & 1);
+    if (!done || (tid == 0 && !ok)) atomicExch(a.status, 2);
+    ok = __syncthreads_and(ok && done);
+    if (!ok) break;
+  }
+  if (!ok && tid == 0 && klast >= 0) {
+    // a wait ran out: let what was issued finish (bounded) before the memory goes away
+    mbar_wait(&bars[0], klast & 1);
+    mbar_wait(&bars[1], klast & 1);
+  }
+  tc_fence_after();
+  // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows t) and the 8-column block w / 4
+  const int t = mt * 128 + (warp & 3) * 32 + lane;
+  const int j = 2 * t + par;
+  const bool rok = ok && j < nn && t < a.ntr;
+  const int er = rok ? a.rexp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
+  const int et = rok ? a.texp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
+  const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
+  const int cb = warp >> 2;
+  if (ok) {
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {   // four columns (two complex z) at a time
+      const int c0 = cb * 8 + half * 4;
+      double pv[4], xv[4], yv[4];
+      // the orders summed in double-float
+        float gp[NS][4], gx[NS][4], gy[NT][4];
+#pragma unroll
+        for (int d = 0; d < NS; ++d) {
+          tmem_ld4(tmem + lrow + d * N + c0, gp[d]);
+          tmem_ld4(tmem + lrow + (NS + d) * N + c0, gx[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < NT; ++d) tmem_ld4(tmem + lrow + (2 * NS + d) * N + c0, gy[d]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int E = cexp[c0 + c], F = fexp[c0 + c];
+          float g1[NS], g2[NS], g3[NT], h, l;
+#pragma unroll
+          for (int d = 0; d < NS; ++d) { g1[d] = gp[d][c]; g2[d] = gx[d][c]; }
+#pragma unroll
+          for (int d = 0; d < NT; ++d) g3[d] = gy[d][c];
+          const bool ox = er > -2000 && E > -2000, oy = et > -2000 && F > -2000;
+          xs_orders_df<NS>(g1, w, h, l);
+          pv[c] = ox ? xs_df_to_double(h, l, er + E - 2 * w) : 0.0;
+          xs_orders_df<NS>(g2, w, h, l);
+          xv[c] = ox ? xs_df_to_double(h, l, er + E - 2 * w) : 0.0;
+          xs_orders_df<NT>(g3, w, h, l);
+          yv[c] = oy ? xs_df_to_double(h, l, et + F - 2 * w) : 0.0;
+        }
+      if (rok) {
+#pragma unroll
+        for (int c = 0; c < 4; c += 2) {
+          const int n = c0 + c, zc = z0 + n / 2;
+          if (zc >= a.nzdim) continue;
+          const int kk = zc + 1;
+          if (!(kk <= a.nzc || kk >= a.nzcu)) continue;
+          const double kz = a.ak[zc];
+          const size_t o = j + (size_t)a.nrdim * (m + (size_t)a.npdim * zc);
+          a.psi[o] = make_double2(pv[c], pv[c + 1]);
+          a.chi[o] = make_double2(fma(kz, xv[c], -yv[c]), fma(kz, xv[c + 1], -yv[c + 1]));
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+// ------------------------------------------------------------------------------------------------
+struct XvImg {
+  uint16_t* p = nullptr;
+  int *rexp = nullptr, *texp = nullptr;
+  size_t bytes = 0, ebytes = 0;
+  int nrc = -1, npc = -1, ns = 0, nt = 0, w = 0;
+};
+static XvImg g_xv;
+
+void xv_free() {
+  if (g_xv.p) dfree(g_xv.p, g_xv.bytes);
+  if (g_xv.rexp) dfree(g_xv.rexp, g_xv.ebytes);
+  if (g_xv.texp) dfree(g_xv.texp, g_xv.ebytes);
+  g_xv = XvImg();
+}
+
+struct XvCfg { int ns, nt, w; };
+static bool xv_cfg(int k, XvCfg& c) {
+  const double lim = 16777216.0;
+  auto fits = [&](int ns, int nt, int w) {
+    const double d = (double)(1 << w) * (1 << w);   // largest digit product (two's-complement digits)
+    return 2.0 * ns * k * d < lim && (double)nt * k * d < lim;
+  };
+  if (fits(5, 6, 7)) { c = {5, 6, 7}; return true; }
+  if (fits(6, 7, 6)) { c = {6, 7, 6}; return true; }
+  return false;
+}
+
+bool xv_supported() {
+  XvCfg c;
+  return xv_cfg(G.nrh, c);
+}
+
+template <int NS, int NT, int NZ>
+static int xv_launch(const XvArgs& args, int npc) {
+  constexpr int N = 2 * NZ;
+  const size_t sm = 1024 + (size_t)(2 * NS + NT) * XV_ATILE + (size_t)(4 * NS + NT) * N * XV_KC * 2 + 2 * N * sizeof(int) +
+                    2 * N * sizeof(unsigned long long) + 64;
+  auto kern = k_xv_contract<NS, NT, NZ>;
+  MLG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  dim3 grid(cdiv(G.nzdim, NZ), 2 * args.nmt, npc - args.m0);
+  kern<<<grid, 32 * NZ, sm, G.stream>>>(args);
+  MLG_LAUNCH();
+  return 0;
+}
+
+// psi, chi: the rows of m0 <= m < npc written (zeroed elsewhere by the caller)
+int xv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc, int m0) {
+  if (npc <= m0) return 0;
+  XvCfg cfg;
+  if (!xv_cfg(G.nrh, cfg)) return set_error(MLG_ESIZE, "vec2tp: too many radial points for exact slices");
+  const int ntr = (nrc + 1) / 2;
+  const int nmt = cdiv(ntr, 128), nkc = cdiv(G.nrh, XV_KC);
+  XvImg& im = g_xv;
+  if (im.nrc != nrc || im.npc != npc || !im.p || im.ns != cfg.ns || im.nt != cfg.nt || im.w != cfg.w) {
+    if (im.p) dfree(im.p, im.bytes);
+    if (im.rexp) dfree(im.rexp, im.ebytes);
+    if (im.texp) dfree(im.texp, im.ebytes);
+    im = XvImg();
+    im.bytes = (size_t)npc * 2 * nmt * nkc * (2 * cfg.ns + cfg.nt) * XV_ATILE;
+    im.ebytes = (size_t)npc * 2 * ntr * sizeof(int);
+    MLG_TRY(dmalloc((void**)&im.p, im.bytes));
+    MLG_TRY(dmalloc((void**)&im.rexp, im.ebytes));
+    MLG_TRY(dmalloc((void**)&im.texp, im.ebytes));
+    k_xv_rexp<<<dim3(cdiv(ntr, 128), npc * 2), 128, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, G.nrh, G.ne, nrc, ntr);
+    MLG_LAUNCH();
+    const int nb = npc * 2 * nmt * nkc;
+    if (cfg.ns == 5)
+      k_xv_table<5, 6><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
+    else
+      k_xv_table<6, 7><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
+    MLG_LAUNCH();
+    im.nrc = nrc; im.npc = npc; im.ns = cfg.ns; im.nt = cfg.nt; im.w = cfg.w;
+  }
+  XvArgs args;
+  args.ur = ur; args.up = up; args.uz = uz; args.psi = psi; args.chi = chi; args.img = im.p; args.rexp = im.rexp;
+  args.texp = im.texp; args.ak = G.ak; args.status = (int*)(G.dscal + DS_FLAG + 1) + 1;
+  args.nr = G.nr; args.nrh = G.nrh; args.nrdim = G.nrdim; args.npdim = G.npdim; args.nzdim = G.nzdim; args.nrc = nrc;
+  args.nzc = G.chopzl; args.nzcu = G.chopzu; args.nmt = nmt; args.nkc = nkc; args.ntr = ntr; args.w = cfg.w; args.m0 = m0;
+  // 5 digits take 16 complex z columns per CTA (their accumulators fill the 512 tensor-memory
+  // columns), 6 digits 8
+  if (cfg.ns == 5) return xv_launch<5, 6, 16>(args, npc);
+  return xv_launch<6, 7, 8>(args, npc);
+}
+
+}  // namespace mlg

@@ -8,7 +8,13 @@ Sources in the reference:
   * its Laplacian (docs/tutorial/operation.md:144-150);
   * Lamb-Oseen: omega(0, t) = 1/(2 pi (1 + 2 nu t)), nu = 0.1, t = 10 (time_integration.md:37-60, 265);
   * the table recurrence of leg_tbl (mlegs_spectfm_init.f90:254-300) evaluated with 50 digits as FM
-    does (fm_parallel.f90:60), with log_fact and lognorm in FP64 as the reference computes them.
+    does (fm_parallel.f90:60), with log_fact and lognorm in FP64 as the reference computes them;
+  * the q-vortex V = (1 - exp(-r'^2))/r' e_phi' + exp(-r'^2)/q e_z about a centre (xo, yo)
+    (docs/tutorial/vector_field.md:88-106): its cylindrical components and those of its curl
+    (2 exp(-r'^2) e_z plus the curl of the axial jet) at a sample of the collocation points, and the
+    log coefficients of psi and chi that its circulation and axial flux fix, -1/2 and -1/(4q) (the
+    recipe builds psi and chi from the closed-form vorticity and axial flow,
+    src/apps/vecfld_reconstruction.f90:155-215, and tp_project.f90 projects V back to them).
 Run: python tests/golden/make_golden.py
 """
 import ctypes
@@ -120,6 +126,33 @@ def table_entries(x, m, ne, lnrm):
     return out
 
 
+def qvortex(r, ph, q, xo, yo):
+    """(V_r, V_phi, V_z) and (W_r, W_phi, W_z) = curl V of the q-vortex about (xo, yo) at (r, phi)."""
+    x, y = r * mp.cos(ph), r * mp.sin(ph)
+    dx, dy = x - xo, y - yo
+    rp2 = dx * dx + dy * dy
+    g = -mp.expm1(-rp2) / rp2 if rp2 != 0 else mp.mpf(1)     # (1 - exp(-r'^2)) / r'^2
+    vx, vy, vz = -dy * g, dx * g, mp.exp(-rp2) / q
+    wx, wy, wz = -2 * dy * vz, 2 * dx * vz, 2 * mp.exp(-rp2)
+    c, s = mp.cos(ph), mp.sin(ph)
+    return ((vx * c + vy * s, -vx * s + vy * c, vz), (wx * c + wy * s, -wx * s + wy * c, wz))
+
+
+def qvortex_samples(nr, np_, ell, q, xo, yo):
+    """The closed form at every 5th radial node and every 7th azimuthal sample of an (nr, np_) kit whose
+    nodes are the reference's FP64 Newton roots, r_i = ell sqrt((1 + x_i)/(1 - x_i))."""
+    xref = gauss_legendre_fp64(nr)
+    out = []
+    for i in range(0, nr, 5):
+        xi = mp.mpf(xref[i])
+        r = ell * mp.sqrt((1 + xi) / (1 - xi))
+        for j in range(0, np_, 7):
+            ph = 2 * mp.pi / np_ * j
+            v, w = qvortex(r, ph, q, xo, yo)
+            out.append({"i": i, "j": j, "v": [float(a) for a in v], "w": [float(a) for a in w]})
+    return out
+
+
 def main():
     NR, NP, ELL = 32, 48, 1
     xs = gauss_legendre_nodes(NR)
@@ -145,6 +178,12 @@ def main():
                      "s_re": s_re, "s_im": s_im, "lap_re": l_re, "lap_im": l_im},
         "lamb_oseen": {"nu": 0.1, "t": 10.0, "omega0": float(1 / (2 * mp.pi * (1 + 2 * mp.mpf("0.1") * 10)))},
         "table": {"nr": 32, "nrchop": 32, "npchop": 17, "ell": 4.0, "x_fp64_newton": xref, "samples": samples},
+        # the tutorial's off-centre vortex (centre (1, 1), q = 1) and the centred Batchelor vortex of the 3-D
+        # app (q = 4), on a kit that resolves both to round-off
+        "qvortex": {"nr": 96, "np": 64, "nz": 4, "ell": 3.0,
+                    "cases": [{"q": q, "xo": xo, "yo": yo, "ln_psi": -0.5, "ln_chi": float(-1 / (4 * mp.mpf(q))),
+                               "samples": qvortex_samples(96, 64, 3.0, q, xo, yo)}
+                              for q, xo, yo in ((1.0, 1.0, 1.0), (4.0, 0.0, 0.0))]},
     }
     with open(os.path.join(HERE, "known_answers.json"), "w") as f:
         json.dump(data, f)

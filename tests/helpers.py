@@ -50,3 +50,41 @@ def compare(gs, os_, tol, ln_tol=None, what=""):
     if oln != 0 or gln != 0:
         assert abs(gln - oln) <= lt * max(scale, np.max(np.abs(oe))), f"{what}: ln {gln!r} != {oln!r}"
     return err
+
+
+def qvortex_closed_form(p, dims, r, q=1.0, xo=0.0, yo=0.0):
+    """The q-vortex V = (1 - exp(-r'^2))/r' e_phi' + exp(-r'^2)/q e_z about (xo, yo)
+    (docs/tutorial/vector_field.md:88-106) and W = curl V, sampled at the collocation points and
+    packed as PPP fields (real part of slot j at phi_{2j}, imaginary part at phi_{2j+1}, every z).
+    Returns ([V_r, V_phi, V_z], [W_r, W_phi, W_z])."""
+    nph = p.np // 2
+    phi = 2 * np.pi / p.np * np.arange(p.np)
+    R, PH = np.asarray(r)[:, None], phi[None, :]
+    dx, dy = R * np.cos(PH) - xo, R * np.sin(PH) - yo
+    rp2 = dx * dx + dy * dy
+    g = np.where(rp2 > 0, -np.expm1(-rp2) / np.where(rp2 > 0, rp2, 1.0), 1.0)
+    vx, vy, vz = -dy * g, dx * g, np.exp(-rp2) / q
+    wx, wy, wz = -2 * dy * vz, 2 * dx * vz, 2 * np.exp(-rp2)
+    c, s = np.cos(PH), np.sin(PH)
+
+    def pack(a):
+        e = np.zeros(dims, complex, order="F")
+        e[: p.nr, :nph, :] = (a[:, 0::2] + 1j * a[:, 1::2])[:, :, None]
+        return e
+    return ([pack(a) for a in (vx * c + vy * s, -vx * s + vy * c, vz)],
+            [pack(a) for a in (wx * c + wy * s, -wx * s + wy * c, wz)])
+
+
+def qvortex_tp(kit, q=1.0, xo=0.0, yo=0.0):
+    """psi and chi of the q-vortex by the reference's recipe (vecfld_reconstruction.f90:155-215): the
+    closed-form vorticity and axial flow over (1-x)^2 in PPP, to FFF, idelsqp, zeroat1."""
+    from mlegs_gb300 import fields
+    a, b = fields.qvort_ppp(kit.params, kit.dims, kit.kit_get("r"), kit.kit_get("x"), q=q, centers=((xo, yo),))
+    out = []
+    for src in (a, b):
+        s = kit.scalar(src, 0.0, "PPP")
+        kit.trans(s, "FFF")
+        kit.idelsqp(s)
+        kit.zeroat1(s)
+        out.append(s)
+    return out

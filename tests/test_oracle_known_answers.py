@@ -136,3 +136,110 @@ def test_invalid_inputs_are_rejected():
     with pytest.raises(OracleError):
         o.ihelm(s, 0.0)
     o.close()
+
+
+# ---- the q-vortex closed forms (docs/tutorial/vector_field.md:88-106) -----------------------------
+QV = GOLD["qvortex"]
+
+
+@pytest.fixture(scope="module")
+def qkit():
+    o = Oracle(nr=QV["nr"], np=QV["np"], nz=QV["nz"], nrchop=QV["nr"], npchop=QV["np"] // 2 + 1,
+               nzchop=QV["nz"] // 2 + 1, ell=QV["ell"], visc=1.0e-4)
+    yield o
+    o.close()
+
+
+def _zeros(o, space):
+    return o.scalar(np.zeros(o.dims, complex, order="F"), 0.0, space)
+
+
+def _vmax_err(got, ref):
+    """Largest deviation over the three components, relative to the largest component value."""
+    scale = max(np.max(np.abs(c)) for c in ref)
+    return max(np.max(np.abs(g - c)) for g, c in zip(got, ref)) / scale
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["offcentre_q1", "centred_q4"])
+def test_qvortex_closed_form_samples(qkit, case):
+    """The numpy closed form used below agrees with the 60-digit samples of the golden file."""
+    from helpers import qvortex_closed_form
+    c = QV["cases"][case]
+    V, W = qvortex_closed_form(qkit.params, qkit.dims, qkit.kit_get("r"), c["q"], c["xo"], c["yo"])
+    for smp in c["samples"]:
+        i, j = smp["i"], smp["j"]
+        for ref, fld in ((smp["v"], V), (smp["w"], W)):
+            for comp in range(3):
+                z = fld[comp][i, j // 2, 0]
+                got = z.real if j % 2 == 0 else z.imag
+                assert abs(got - ref[comp]) <= 4e-15 * max(1.0, abs(ref[comp])), (i, j, comp, got, ref[comp])
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["offcentre_q1", "centred_q4"])
+def test_qvortex_tp2vec_and_curl_closed_form(qkit, case):
+    """tp2vec and tp2curlvec (mlegs_scalar_ops.f90:1455-1560) of the recipe's psi and chi reproduce the
+    closed-form V and curl V, and the recipe's log coefficients are the closed-form -1/2, -1/(4q)."""
+    from helpers import qvortex_closed_form, qvortex_tp
+    c = QV["cases"][case]
+    psi, chi = qvortex_tp(qkit, c["q"], c["xo"], c["yo"])
+    assert abs(psi.ln - c["ln_psi"]) < 1e-12 and abs(chi.ln - c["ln_chi"]) < 1e-12, (psi.ln, chi.ln)
+    V, W = qvortex_closed_form(qkit.params, qkit.dims, qkit.kit_get("r"), c["q"], c["xo"], c["yo"])
+    v = [_zeros(qkit, "PPP") for _ in range(3)]
+    qkit.tp2vec(psi, chi, *v)
+    assert _vmax_err([s.e for s in v], V) < 1e-12
+    w = [_zeros(qkit, "PPP") for _ in range(3)]
+    qkit.tp2curlvec(psi, chi, *w)
+    assert _vmax_err([s.e for s in w], W) < 2e-11
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["offcentre_q1", "centred_q4"])
+def test_qvortex_vec2tp_recovers_psi_chi(qkit, case):
+    """vec2tp (mlegs_scalar_ops.f90:1308-1453) of the closed-form V returns the recipe's psi and chi
+    (what src/apps/tp_project.f90 does with the vectors that vecfld_reconstruction.f90 saves)."""
+    from helpers import qvortex_closed_form, qvortex_tp
+    c = QV["cases"][case]
+    psi, chi = qvortex_tp(qkit, c["q"], c["xo"], c["yo"])
+    V, _ = qvortex_closed_form(qkit.params, qkit.dims, qkit.kit_get("r"), c["q"], c["xo"], c["yo"])
+    u = [qkit.scalar(a, 0.0, "PPP") for a in V]
+    pp, cc = _zeros(qkit, "FFF"), _zeros(qkit, "FFF")
+    qkit.vec2tp(*u, pp, cc)
+    # the projection ends with an inverse Laplacian on chi: its truncation error at this resolution is
+    # about 1e-11 absolute, 1.3e-10 of the q = 4 vortex's smaller chi
+    assert np.linalg.norm(pp.e - psi.e) / np.linalg.norm(psi.e) < 1e-10
+    assert np.linalg.norm(cc.e - chi.e) / np.linalg.norm(chi.e) < 5e-10
+    assert abs(pp.ln - c["ln_psi"]) < 1e-10 and abs(cc.ln - c["ln_chi"]) < 1e-10, (pp.ln, cc.ln)
+
+
+def test_qvortex_vecprod_closed_form(qkit):
+    """vector_product (mlegs_scalar_ops.f90:1264-1306) of the closed-form V and curl V is V x curl V
+    sample by sample."""
+    from helpers import qvortex_closed_form
+    c = QV["cases"][0]
+    V, W = qvortex_closed_form(qkit.params, qkit.dims, qkit.kit_get("r"), c["q"], c["xo"], c["yo"])
+    v = [qkit.scalar(a, 0.0, "PPP") for a in V]
+    w = [qkit.scalar(a, 0.0, "PPP") for a in W]
+    qkit.vecprod(*v, *w)
+
+    def cross(a, b):   # on the packed samples: real and imaginary parts are separate samples
+        out = []
+        for i, j, k in ((1, 2, 0), (2, 0, 1), (0, 1, 2)):
+            re = a[i].real * b[j].real - a[j].real * b[i].real
+            im = a[i].imag * b[j].imag - a[j].imag * b[i].imag
+            out.append(re + 1j * im)
+        return out
+    ref = cross(V, W)
+    assert _vmax_err([s.e for s in v], ref) < 1e-15
+
+
+def test_axisymmetric_vortex_has_no_nonlinear_term(qkit):
+    """For the centred Batchelor vortex u x omega is radial and depends on r only, a pure gradient: its
+    curl, and with it the TP projection that advection_rhs (vortical_flow_3d.f90:353-395) returns,
+    vanish.  The step's nonlinear term must come out at round-off of the vortex's own size."""
+    from mlegs_gb300 import vortex
+    c = QV["cases"][1]
+    st = vortex.VortexState(qkit)
+    vortex.qvort_init(qkit, st, q=c["q"])
+    qkit.advection_rhs(st.psi, st.chi, st.nlpsi, st.nlchi, st.uz)
+    scale = np.linalg.norm(st.psi.e)
+    assert np.linalg.norm(st.nlpsi.e) < 1e-14 * scale and np.linalg.norm(st.nlchi.e) < 1e-14 * scale
+    assert st.nlpsi.ln == 0.0 and st.nlchi.ln == 0.0
