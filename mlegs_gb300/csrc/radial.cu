@@ -419,6 +419,25 @@ int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu) {
   return 0;
 }
 
+// the FP64 DFMA contractions over m < mcount (mcount 1: the m = 0 plane alone)
+static int dfma_rtrans_fwd(const cd* in, cd* out, int nrc, int mcount, cudaStream_t st) {
+  constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
+  int tt = cdiv((nrc + 1) / 2, MT);
+  dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, mcount), blk(ZT / ZPT, MT / MPT);
+  k_rtrans_fwd<double, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim,
+                                                                    G.npdim, G.nzdim, nrc);
+  MLG_LAUNCH();
+  return 0;
+}
+static int dfma_rtrans_bwd(const cd* in, cd* out, int nrc, int mcount, const double* lnp, bool add_ln, cudaStream_t st) {
+  constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
+  dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), mcount), blk(ZT / ZPT, IT / IPT);
+  k_rtrans_bwd<double, IT, ZT, KC, IPT, ZPT><<<grid, blk, 0, st>>>(in, out, G.pf, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh,
+                                                                    G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
+  MLG_LAUNCH();
+  return 0;
+}
+
 int launch_rtrans_fwd(Scalar& s) {
   int nrc, npc;
   MLG_TRY(rtrans_check(s, nrc, npc, "rtrans_forward"));
@@ -441,14 +460,14 @@ int launch_rtrans_fwd(Scalar& s) {
       else MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: split BF16 (tc_radial.cu)
       MLG_TRY(side_join());
     } else if (xs) {
-      MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 0, nullptr, false, true));    // FP64-grade slices, every m
+      // m = 0 (the axisymmetric mean flow, whose large range within a column the fixed-point slices
+      // would cut relative to its maximum) in FP64 DFMA beside; m >= 1 as FP64-grade slices
+      MLG_TRY(side_fork());
+      MLG_TRY(dfma_rtrans_fwd(s.e, out, nrc, 1, G.side));
+      MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, true));
+      MLG_TRY(side_join());
     } else {
-      constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
-      int tt = cdiv((nrc + 1) / 2, MT);
-      dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT / MPT);
-      k_rtrans_fwd<double, MT, ZT, KC, MPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne,
-                                                                              G.nrdim, G.npdim, G.nzdim, nrc);
-      MLG_LAUNCH();
+      MLG_TRY(dfma_rtrans_fwd(s.e, out, nrc, npc, G.stream));
     }
   }
   kt_end(KT_RFWD, fwd_flops(nrc, npc));
@@ -481,13 +500,12 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
       else MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));           // m >= 1: split BF16
       MLG_TRY(side_join());
     } else if (xs) {
-      MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 0, s.ln, add_ln, true));   // FP64-grade slices, every m
+      MLG_TRY(side_fork());
+      MLG_TRY(dfma_rtrans_bwd(s.e, out, nrc, 1, s.ln, add_ln, G.side));   // m = 0: FP64 DFMA, beside
+      MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, true));   // m >= 1: FP64-grade slices
+      MLG_TRY(side_join());
     } else {
-      constexpr int IT = 32, ZT = 32, KC = 8, IPT = 2, ZPT = 2;
-      dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), npc), blk(ZT / ZPT, IT / IPT);
-      k_rtrans_bwd<double, IT, ZT, KC, IPT, ZPT><<<grid, blk, 0, G.stream>>>(s.e, out, G.pf, G.lnx, s.ln, add_ln ? 1 : 0,
-                                                                             G.nr, G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc);
-      MLG_LAUNCH();
+      MLG_TRY(dfma_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln, G.stream));
     }
   }
   kt_end(KT_RBWD, fwd_flops(nrc, npc));

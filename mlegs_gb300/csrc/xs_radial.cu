@@ -145,7 +145,9 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   constexpr int CGW = N / 8 < 4 ? N / 8 : 4;      // column groups of 8 in the epilogue (one per 4 warps)
   constexpr int NDW = NW - 2;                     // digit warps: 2 .. NW-1
   constexpr int NDIG = NDW * 32;
-  constexpr int NBLK = 2 * (N / 8) * 2;           // staging blocks per chunk: (parity, 8 columns, 4 K pairs)
+  // staging blocks per chunk: (8 columns, 4 K pairs) and, backward, the parity (forward, a block writes
+  // both parities from the same two samples)
+  constexpr int NBLK = (MODE == 0 ? 1 : 2) * (N / 8) * 2;
   static_assert(2 * NO * N <= 512, "accumulators exceed tensor memory");
   static_assert(NO <= NS, "every order's first product (t = 0) resets its accumulator");
   static_assert(N % 16 == 0 && N >= 16 && N <= 32, "MMA N");
@@ -300,30 +302,40 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
           if (!ok) break;
           uint8_t* bst = sB + s * BSTAGE;
           for (int blk = dw; blk < NBLK; blk += NDW) {
-            const int par = blk & 1, ng = (blk >> 1) % (N / 8), kh = (blk >> 1) / (N / 8);
+            const int par = MODE == 0 ? 0 : (blk & 1), bb = MODE == 0 ? blk : (blk >> 1);
+            const int ng = bb % (N / 8), kh = bb / (N / 8);
             const int n = ng * 8 + (lane & 7), kp = kh * 4 + (lane >> 3), zz = n >> 1;
             const int E = colexp[n];
             const bool zok = (z0 + zz < a.nzdim) && E > -2000;
             const double* col = raw + (size_t)2 * zz * a.rawk + (n & 1);
-            float h[2][NS];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              long long x = 0;
-              if (MODE == 0) {   // B_par(i) = f(i) + (-1)^par f(nr-1-i), exact in the integers
-                const int i = kc * XS_KC + 2 * kp + u;
-                if (zok && i < a.nrh) {
-                  const long long x1 = xs_fix(col[2 * i], E, nb), x2 = xs_fix(col[2 * (a.nr - 1 - i)], E, nb);
-                  x = par ? x1 - x2 : x1 + x2;
-                }
-              } else {           // B_par(t) = c(2t + par)
-                const int j = 2 * (kc * XS_KC + 2 * kp + u) + par;
-                if (zok && j < nn) x = xs_fix(col[2 * j], E, nb);
-              }
-              xs_digits_f<NS>(x, w, h[u]);
-            }
             const int off = xs_off(n, 2 * kp);
+            if (MODE == 0) {
+              // B_par(i) = f(i) + (-1)^par f(nr-1-i) for both parities, exact in the integers
+              float he[2][NS], ho[2][NS];
 #pragma unroll
-            for (int t = 0; t < NS; ++t) *(uint32_t*)(bst + (par * NS + t) * BT + off) = xs_pack(h[0][t], h[1][t]);
+              for (int u = 0; u < 2; ++u) {
+                const int i = kc * XS_KC + 2 * kp + u;
+                long long x1 = 0, x2 = 0;
+                if (zok && i < a.nrh) { x1 = xs_fix(col[2 * i], E, nb); x2 = xs_fix(col[2 * (a.nr - 1 - i)], E, nb); }
+                xs_digits_f<NS>(x1 + x2, w, he[u]);
+                xs_digits_f<NS>(x1 - x2, w, ho[u]);
+              }
+#pragma unroll
+              for (int t = 0; t < NS; ++t) {
+                *(uint32_t*)(bst + t * BT + off) = xs_pack(he[0][t], he[1][t]);
+                *(uint32_t*)(bst + (NS + t) * BT + off) = xs_pack(ho[0][t], ho[1][t]);
+              }
+            } else {
+              // B_par(t) = c(2t + par)
+              float h[2][NS];
+#pragma unroll
+              for (int u = 0; u < 2; ++u) {
+                const int j = 2 * (kc * XS_KC + 2 * kp + u) + par;
+                xs_digits_f<NS>((zok && j < nn) ? xs_fix(col[2 * j], E, nb) : 0ll, w, h[u]);
+              }
+#pragma unroll
+              for (int t = 0; t < NS; ++t) *(uint32_t*)(bst + (par * NS + t) * BT + off) = xs_pack(h[0][t], h[1][t]);
+            }
           }
           fence_async_smem();
           mbar_arrive(&bar_b[s]);
@@ -339,7 +351,8 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       if (!ok) break;
       tc_fence_after();
       const int lq = warp & 3, cg = warp >> 2;      // TMEM lane quarter, 8-column group
-      if (cg < CGW) {
+      // (a warp whose 32 rows all lie past the tile's valid rows has nothing to write)
+      if (cg < CGW && mt * 128 + lq * 32 < nrows) {
         const int row = mt * 128 + lq * 32 + lane;
         const uint32_t lrow = (uint32_t)(lq * 32) << 16;
         const int c0 = cg * 8;
@@ -348,14 +361,15 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
           float H[2][8], L[2][8];
 #pragma unroll
           for (int par = 0; par < 2; ++par) {
-            float g[NO][8];
+            uint32_t g[NO][8];
 #pragma unroll
-            for (int d = 0; d < NO; ++d) tmem_ld8(tmem + lrow + (uint32_t)((d * 2 + par) * N + c0), g[d]);
+            for (int d = 0; d < NO; ++d) tmem_ld8_nw(tmem + lrow + (uint32_t)((d * 2 + par) * N + c0), g[d]);
+            tmem_wait_ld();
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
               float gg[NO];
 #pragma unroll
-              for (int d = 0; d < NO; ++d) gg[d] = g[d][c];
+              for (int d = 0; d < NO; ++d) gg[d] = __uint_as_float(g[d][c]);
               xs_orders_df<NO>(gg, w, H[par][c], L[par][c]);
             }
           }

@@ -16,17 +16,21 @@
 // multiply-add.  The row parity of a CTA fixes the folds, so each CTA owns one (m, parity, 128-row
 // tile, NZ complex z columns).
 //
-// Digits: NS for psi and X, NT for Y, of w bits: the mixed form's NS = 5 (35 bits) and NT = 6 (6 and 7
-// of 6 bits beyond about 100 radial points); w and the digit counts keep every order's accumulator
-// exact: (pairs of the order) x (nr/2) x 2^(2w) < 2^24, where psi's and X's orders hold two products
-// per digit pair.  (The plain form keeps its FP64 contraction: chi = k X - Y cancels, and even 54-bit
+// Digits: NS for psi and X, NT for Y, of w bits: the mixed form's NS = 5 (35 bits) and NT = 7 (49
+// bits; 6 and 8 of 6 bits beyond about 100 radial points); w and the digit counts keep every order's
+// accumulator exact: (pairs of the order) x (nr/2) x 2^(2w) < 2^24, where psi's and X's orders hold two
+// products per digit pair.  Y needs the extra digits: at k = 0 chi is -Y alone, and the inverse
+// Laplacian that ends the projection magnifies its error in the weak low modes; with 42-bit Y the
+// (m = 1, k = 0) column left the step's nonlinear term chi 9e-6 from FP64 at 192 x 128 x 128, with
+// 49 bits 2e-7.  (The plain form keeps its FP64 contraction: chi = k X - Y cancels, and even 54-bit
 // slices, cut relative to the column maxima, left chi 7e-9 from the FP64 reference.)
 //
-// Engine: 32 NZ threads per CTA of NZ complex z columns; per K chunk of 16 radial points the table digits (m V, D and T, laid out at kit
-// init in the UMMA canonical K-major layout) arrive by one bulk copy on an mbarrier, the threads cut
-// the field digits (ur, up and uz at i and nr-1-i, loaded in FP64 the chunk before) into the same
-// layout, and one thread issues the chunk's tcgen05.mma (M = 128, N = 2 NZ, K = 16) and commits.  Every
-// wait is bounded.
+// Engine: a persistent grid of one 256-thread CTA per SM over work items (m, parity, 128-row tile, 8
+// complex z columns).  Per K chunk of 16 radial points the table digits (m V, D and T, laid out at kit
+// init in the UMMA canonical K-major layout) arrive by one bulk copy into a two-stage ring, six warps
+// cut the field digits (ur, up and uz at i and nr-1-i, fetched in FP64 a chunk ahead) into the same
+// layout and arrive on the stage's mbarrier, and one thread issues the chunk's tcgen05.mma (M = 128,
+// N = 16, K = 16) as soon as both halves of a stage are in.  Every wait is bounded.
 #include "common.cuh"
 #include "tc_common.cuh"
 #include "xs_common.cuh"
@@ -41,6 +45,12 @@ __host__ __device__ constexpr int xv_off(int row, int k) {
   return (row >> 3) * XV_SBO + (k >> 3) * XV_LBO + (row & 7) * 16 + (k & 7) * 2;
 }
 constexpr int XV_ATILE = 128 * XV_KC * 2;    // 4 KiB
+
+__device__ __forceinline__ bool xs_wait(uint64_t* bar, uint32_t phase, bool& ok) {
+  if (!ok) return false;
+  ok = mbar_wait(bar, phase);
+  return ok;
+}
 
 // ------------------------------------------------------------------------------------------------
 // kit-time: row scales rexp[(m * 2 + par) * ntr + t] over (m V, D) and texp over T (-2000: zero row)
@@ -107,41 +117,51 @@ struct XvArgs {
   const int *rexp, *texp;
   const double* ak;
   int* status;
-  int nr, nrh, nrdim, npdim, nzdim, nrc, nzc, nzcu, nmt, nkc, ntr, w, m0;
+  int nr, nrh, nrdim, npdim, nzdim, nrc, nzc, nzcu, nmt, nkc, ntr, w, m0, npc;
 };
 
-// NS digits for psi and X, NT for Y; NZ complex z columns per CTA (N = 2 NZ), 32 NZ threads
-template <int NS, int NT, int NZ>
-__global__ void __launch_bounds__(32 * NZ, 1) k_xv_contract(XvArgs a) {
+// NS digits for psi and X, NT for Y; 8 complex z columns per work item (N = 16).  Persistent: one CTA of
+// 256 threads per SM walks the items (m, parity, row tile, z tile); warp 0 (one thread) copies the table
+// chunks into a two-stage ring, warp 1 (one thread) issues the MMAs, warps 2..7 cut the field digits
+// (one staging item each: field, z column, K pair), all eight warps run the epilogue.
+constexpr int XV_NZ = 8;
+constexpr int XV_THREADS = 256;
+template <int NS, int NT>
+__global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
+  constexpr int NZ = XV_NZ;
   constexpr int N = 2 * NZ;
-  constexpr int NTH = 32 * NZ;
   constexpr int BTILE = N * XV_KC * 2;
   constexpr int NA = 2 * NS + NT;                 // A tiles per chunk
   constexpr int NB = 4 * NS + NT;                 // B tiles: psi_ur, psi_up, X_ur, X_up (NS each), uz (NT)
+  constexpr int ASTAGE = NA * XV_ATILE, BSTAGE = NB * BTILE;
   constexpr int COLS = (2 * NS + NT) * N;
   constexpr int TCOLS = COLS <= 128 ? 128 : COLS <= 256 ? 256 : 512;
+  constexpr int NDIG = 3 * NZ * 8;                // staging items = digit threads (warps 2..7)
   static_assert(COLS <= 512, "accumulators exceed tensor memory");
+  static_assert(NDIG == XV_THREADS - 64, "one staging item per digit thread");
   extern __shared__ __align__(1024) uint8_t xv_smem_raw[];
   uint8_t* sbase = (uint8_t*)(((uintptr_t)xv_smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = sbase;
-  uint8_t* sB = sA + NA * XV_ATILE;
-  int* cexp = (int*)(sB + NB * BTILE);            // [N]: ur/up columns
+  uint8_t* sA = sbase;                            // [2][ASTAGE]
+  uint8_t* sB = sA + 2 * ASTAGE;                  // [2][BSTAGE]
+  int* cexp = (int*)(sB + 2 * BSTAGE);            // [N]: ur/up columns
   int* fexp = cexp + N;                           // [N]: uz columns
   unsigned long long* cmax = (unsigned long long*)(fexp + N);   // [2][N]
-  uint64_t* bars = (uint64_t*)(cmax + 2 * N);     // a, mma
-  uint32_t* tslot = (uint32_t*)(bars + 2);
+  uint64_t* bars = (uint64_t*)(cmax + 2 * N);     // a[2], b[2], mma[2]
+  uint32_t* tslot = (uint32_t*)(bars + 6);
+  uint64_t* bar_a = bars;
+  uint64_t* bar_b = bars + 2;
+  uint64_t* bar_mma = bars + 4;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int z0 = blockIdx.x * NZ, par = blockIdx.y & 1, mt = blockIdx.y >> 1, m = blockIdx.z + a.m0;
-  const int nn = max(min(a.nrc, a.nrc - m), 0);
-  if (2 * (mt * 128) + par >= nn) return;
   const int w = a.w, nbs = w * NS, nbt = w * NT;
   if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(bar_a + i, 1);
+      mbar_init(bar_b + i, NDIG);
+      mbar_init(bar_mma + i, 1);
+    }
     fence_mbar_init();
   }
-  if (tid < 2 * N) cmax[tid] = 0ull;
   if (warp == 0) {
     tmem_alloc(tslot, TCOLS);
     tmem_relinquish();
@@ -150,179 +170,207 @@ __global__ void __launch_bounds__(32 * NZ, 1) k_xv_contract(XvArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int ss = par ? -1 : 1;   // own-parity fold sign
-  // ---- column scales: cexp(2zz) over (Im ur, Re up), cexp(2zz+1) over (Re ur, Im up); fexp over uz
-  {
-    const int zz = tid % NZ, g = tid / NZ, z = z0 + zz;   // 32 threads per column
-    unsigned long long m0 = 0, m1 = 0, u0 = 0, u1 = 0;
-    if (z < a.nzdim) {
-      const size_t cb = (size_t)a.nrdim * (m + (size_t)a.npdim * z);
-      for (int i = g; i < a.nr; i += 32) {
-        const double2 r = a.ur[cb + i], p = a.up[cb + i], q = a.uz[cb + i];
-        unsigned long long v;
-        v = (unsigned long long)__double_as_longlong(r.y) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
-        v = (unsigned long long)__double_as_longlong(p.x) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
-        v = (unsigned long long)__double_as_longlong(r.x) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
-        v = (unsigned long long)__double_as_longlong(p.y) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
-        v = (unsigned long long)__double_as_longlong(q.x) & 0x7FFFFFFFFFFFFFFFull; u0 = v > u0 ? v : u0;
-        v = (unsigned long long)__double_as_longlong(q.y) & 0x7FFFFFFFFFFFFFFFull; u1 = v > u1 ? v : u1;
-      }
-    }
-    atomicMax(&cmax[2 * zz], m0);
-    atomicMax(&cmax[2 * zz + 1], m1);
-    atomicMax(&cmax[N + 2 * zz], u0);
-    atomicMax(&cmax[N + 2 * zz + 1], u1);
-  }
-  __syncthreads();
-  if (tid < N) {
-    cexp[tid] = cmax[tid] ? xs_ebound(cmax[tid]) + 1 : -2000;          // +1: the folds may double
-    fexp[tid] = cmax[N + tid] ? xs_ebound(cmax[N + tid]) + 1 : -2000;
-  }
-  __syncthreads();
-  // staging item: (field f, column zz, K pair kp); f = 0 ur, 1 up, 2 uz: 24 NZ items
-  const int f = tid / (NZ * 8), zz = tid % NZ, kp = (tid / NZ) % 8;
-  const bool stager = tid < 3 * NZ * 8;
-  const int z = z0 + zz;
-  const bool zok = stager && z < a.nzdim;
-  const size_t cbase = (size_t)a.nrdim * (m + (size_t)a.npdim * (zok ? z : 0));
-  const double2* src = f == 0 ? a.ur : (f == 1 ? a.up : a.uz);
-  double2 va[2], vb[2];
-  auto fetch = [&](int kc) {
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int i = kc * XV_KC + 2 * kp + u;
-      const bool ok = zok && i < a.nrh;
-      va[u] = ok ? src[cbase + i] : make_double2(0.0, 0.0);
-      vb[u] = ok ? src[cbase + a.nr - 1 - i] : make_double2(0.0, 0.0);
-    }
-  };
+  const uint32_t idesc = idesc_bf16(128, N);
   bool ok = true;
-  const uint8_t* img_b = (const uint8_t*)a.img + (((size_t)(m * 2 + par) * a.nmt + mt) * a.nkc) * (size_t)(NA * XV_ATILE);
-  const int nkc = a.nkc;
-  int klast = -1;   // the last chunk whose copy and MMAs were issued
-  fetch(0);
-  for (int kc = 0; kc < nkc; ++kc) {
-    klast = kc;
-    if (tid == 0) {
-      mbar_expect_tx(&bars[0], NA * XV_ATILE);
-      bulk_g2s(sA, img_b + (size_t)kc * (NA * XV_ATILE), NA * XV_ATILE, &bars[0]);
-    }
-    if (stager) {
-      const int off = xv_off(2 * zz, 2 * kp), off1 = xv_off(2 * zz + 1, 2 * kp);
-      if (f < 2) {
-        // integer folds of the two components with the column scales of the columns they land in
-        const int Ere = f == 0 ? cexp[2 * zz + 1] : cexp[2 * zz];       // Re ur -> col 2zz+1, Re up -> col 2zz
-        const int Eim = f == 0 ? cexp[2 * zz] : cexp[2 * zz + 1];
-        float h0[2][NS], h1[2][NS], g0[2][NS], g1[2][NS];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const long long ar = xs_fix(va[u].x, Ere, nbs), br = xs_fix(vb[u].x, Ere, nbs);
-          const long long ai = xs_fix(va[u].y, Eim, nbs), bi = xs_fix(vb[u].y, Eim, nbs);
-          const long long fs_re = ar + ss * br, fs_im = ai + ss * bi;
-          const long long fo_re = ar - ss * br, fo_im = ai - ss * bi;
-          if (f == 0) {   // psi_ur = -i F_s(ur): (Im, -Re); X_ur = i F_o(ur): (-Im, Re)
-            xs_digits_f<NS>(fs_im, w, h0[u]); xs_digits_f<NS>(-fs_re, w, h1[u]);
-            xs_digits_f<NS>(-fo_im, w, g0[u]); xs_digits_f<NS>(fo_re, w, g1[u]);
-          } else {        // psi_up = -F_o(up): (-Re, -Im); X_up = F_s(up): (Re, Im)
-            xs_digits_f<NS>(-fo_re, w, h0[u]); xs_digits_f<NS>(-fo_im, w, h1[u]);
-            xs_digits_f<NS>(fs_re, w, g0[u]); xs_digits_f<NS>(fs_im, w, g1[u]);
-          }
-        }
-        const int tp = f == 0 ? 0 : NS, tx = f == 0 ? 2 * NS : 3 * NS;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-          *(uint32_t*)(sB + (tp + s) * BTILE + off) = xs_pack(h0[0][s], h0[1][s]);
-          *(uint32_t*)(sB + (tp + s) * BTILE + off1) = xs_pack(h1[0][s], h1[1][s]);
-          *(uint32_t*)(sB + (tx + s) * BTILE + off) = xs_pack(g0[0][s], g0[1][s]);
-          *(uint32_t*)(sB + (tx + s) * BTILE + off1) = xs_pack(g1[0][s], g1[1][s]);
-        }
-      } else {
-        // Y: F_s(uz) with the uz column scales
-        float h0[2][NT], h1[2][NT];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const long long re = xs_fix(va[u].x, fexp[2 * zz], nbt) + ss * xs_fix(vb[u].x, fexp[2 * zz], nbt);
-          const long long im = xs_fix(va[u].y, fexp[2 * zz + 1], nbt) + ss * xs_fix(vb[u].y, fexp[2 * zz + 1], nbt);
-          xs_digits_f<NT>(re, w, h0[u]);
-          xs_digits_f<NT>(im, w, h1[u]);
-        }
-#pragma unroll
-        for (int s = 0; s < NT; ++s) {
-          *(uint32_t*)(sB + (4 * NS + s) * BTILE + off) = xs_pack(h0[0][s], h0[1][s]);
-          *(uint32_t*)(sB + (4 * NS + s) * BTILE + off1) = xs_pack(h1[0][s], h1[1][s]);
-        }
-      }
-    }
-    fence_async_smem();
+  uint32_t it = 0;   // chunk counter (stage and phase), the same in every thread
+  const int nzt = (a.nzdim + NZ - 1) / NZ;
+  const int nmp = a.npc - a.m0;
+  const int nitems = nmp * 2 * a.nmt * nzt;   // item = ((mi * 2 + par) * nmt + mt) * nzt + zt
+  // staging item of a digit thread: field f (0 ur, 1 up, 2 uz), z column zz, K pair kp
+  const int dt = tid - 64;
+  const int f = dt / (NZ * 8), zz = dt % NZ, kp = (dt / NZ) % 8;
+
+  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    const int zt = item % nzt, mt = (item / nzt) % a.nmt, par = (item / (nzt * a.nmt)) & 1;
+    const int m = a.m0 + item / (nzt * a.nmt * 2);
+    const int nn = max(min(a.nrc, a.nrc - m), 0);
+    if (2 * (mt * 128) + par >= nn) continue;   // no rows of this parity in the tile (every thread agrees)
+    const int z0 = zt * NZ;
+    const int ss = par ? -1 : 1;   // own-parity fold sign
+    // ---- column scales: cexp(2zz) over (Im ur, Re up), cexp(2zz+1) over (Re ur, Im up); fexp over uz
+    if (tid < 2 * N) cmax[tid] = 0ull;
     __syncthreads();
-    if (tid == 0) {
-      ok = ok && mbar_wait(&bars[0], kc & 1);
-      tc_fence_after();
-      if (ok) {
-        const uint32_t idesc = idesc_bf16(128, N);
-        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-        auto A = [&](int t) { return sdesc(a0 + t * XV_ATILE, XV_LBO, XV_SBO); };
-        auto B = [&](int t) { return sdesc(b0 + t * BTILE, XV_LBO, XV_SBO); };
+    {
+      const int cz = tid % NZ, g = tid / NZ, z = z0 + cz;   // 32 threads per column
+      unsigned long long m0 = 0, m1 = 0, u0 = 0, u1 = 0;
+      if (z < a.nzdim) {
+        const size_t cb = (size_t)a.nrdim * (m + (size_t)a.npdim * z);
+        for (int i = g; i < a.nr; i += XV_THREADS / NZ) {
+          const double2 r = a.ur[cb + i], pq = a.up[cb + i], q = a.uz[cb + i];
+          unsigned long long v;
+          v = (unsigned long long)__double_as_longlong(r.y) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
+          v = (unsigned long long)__double_as_longlong(pq.x) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
+          v = (unsigned long long)__double_as_longlong(r.x) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
+          v = (unsigned long long)__double_as_longlong(pq.y) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
+          v = (unsigned long long)__double_as_longlong(q.x) & 0x7FFFFFFFFFFFFFFFull; u0 = v > u0 ? v : u0;
+          v = (unsigned long long)__double_as_longlong(q.y) & 0x7FFFFFFFFFFFFFFFull; u1 = v > u1 ? v : u1;
+        }
+      }
+      atomicMax(&cmax[2 * cz], m0);
+      atomicMax(&cmax[2 * cz + 1], m1);
+      atomicMax(&cmax[N + 2 * cz], u0);
+      atomicMax(&cmax[N + 2 * cz + 1], u1);
+    }
+    __syncthreads();
+    if (tid < N) {
+      cexp[tid] = cmax[tid] ? xs_ebound(cmax[tid]) + 1 : -2000;          // +1: the folds may double
+      fexp[tid] = cmax[N + tid] ? xs_ebound(cmax[N + tid]) + 1 : -2000;
+    }
+    __syncthreads();
+    const uint8_t* img_b = (const uint8_t*)a.img + (((size_t)(m * 2 + par) * a.nmt + mt) * a.nkc) * (size_t)ASTAGE;
+    const int nkc = a.nkc;
+    const uint32_t it0 = it;
+    if (warp == 0) {
+      // ---- producer: each table chunk into its stage once the MMAs that read the stage before are done
+      if (lane == 0)
+        for (int kc = 0; kc < nkc && ok; ++kc) {
+          const uint32_t c = it0 + kc, s = c & 1;
+          if (c >= 2) xs_wait(&bar_mma[s], ((c - 2) >> 1) & 1, ok);
+          if (!ok) break;
+          mbar_expect_tx(&bar_a[s], ASTAGE);
+          bulk_g2s(sA + s * ASTAGE, img_b + (size_t)kc * ASTAGE, ASTAGE, &bar_a[s]);
+        }
+      __syncwarp();
+    } else if (warp == 1) {
+      // ---- MMA issue
+      if (lane == 0)
+        for (int kc = 0; kc < nkc && ok; ++kc) {
+          const uint32_t c = it0 + kc, s = c & 1;
+          xs_wait(&bar_a[s], (c >> 1) & 1, ok);
+          xs_wait(&bar_b[s], (c >> 1) & 1, ok);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(sA + s * ASTAGE), b0 = smem_u32(sB + s * BSTAGE);
+          auto A = [&](int t) { return sdesc(a0 + t * XV_ATILE, XV_LBO, XV_SBO); };
+          auto B = [&](int t) { return sdesc(b0 + t * BTILE, XV_LBO, XV_SBO); };
 #pragma unroll
-        for (int d = 0; d < NS; ++d)
+          for (int d = 0; d < NS; ++d)
 #pragma unroll
-          for (int t = 0; t <= d; ++t) {
-            const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
-            umma_bf16(tmem + d * N, A(t), B(d - t), idesc, acc);                          // psi: mV . psi_ur
-            umma_bf16(tmem + d * N, A(NS + t), B(NS + d - t), idesc, 1u);                 //      D . psi_up
-            umma_bf16(tmem + (NS + d) * N, A(NS + t), B(2 * NS + d - t), idesc, acc);     // X: D . X_ur
-            umma_bf16(tmem + (NS + d) * N, A(t), B(3 * NS + d - t), idesc, 1u);           //    mV . X_up
+            for (int t = 0; t <= d; ++t) {
+              const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
+              umma_bf16(tmem + d * N, A(t), B(d - t), idesc, acc);                          // psi: mV . psi_ur
+              umma_bf16(tmem + d * N, A(NS + t), B(NS + d - t), idesc, 1u);                 //      D . psi_up
+              umma_bf16(tmem + (NS + d) * N, A(NS + t), B(2 * NS + d - t), idesc, acc);     // X: D . X_ur
+              umma_bf16(tmem + (NS + d) * N, A(t), B(3 * NS + d - t), idesc, 1u);           //    mV . X_up
+            }
+#pragma unroll
+          for (int d = 0; d < NT; ++d)
+#pragma unroll
+            for (int t = 0; t <= d; ++t)
+              umma_bf16(tmem + (2 * NS + d) * N, A(2 * NS + t), B(4 * NS + d - t), idesc, (kc > 0 || t > 0) ? 1u : 0u);
+          umma_commit(&bar_mma[s]);
+        }
+      __syncwarp();
+    } else {
+      // ---- field digits: this thread's two K of its field at i and nr-1-i, fetched a chunk ahead
+      const int z = z0 + zz;
+      const bool zok = z < a.nzdim;
+      const size_t cbase = (size_t)a.nrdim * (m + (size_t)a.npdim * (zok ? z : 0));
+      const double2* src = f == 0 ? a.ur : (f == 1 ? a.up : a.uz);
+      double2 va[2], vb[2];
+      auto fetch = [&](int kc) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int i = kc * XV_KC + 2 * kp + u;
+          const bool okk = zok && i < a.nrh;
+          va[u] = okk ? src[cbase + i] : make_double2(0.0, 0.0);
+          vb[u] = okk ? src[cbase + a.nr - 1 - i] : make_double2(0.0, 0.0);
+        }
+      };
+      fetch(0);
+      const int off = xv_off(2 * zz, 2 * kp), off1 = xv_off(2 * zz + 1, 2 * kp);
+      for (int kc = 0; kc < nkc && ok; ++kc) {
+        const uint32_t c = it0 + kc, s = c & 1;
+        if (c >= 2) xs_wait(&bar_mma[s], ((c - 2) >> 1) & 1, ok);
+        if (!ok) break;
+        uint8_t* bst = sB + s * BSTAGE;
+        if (f < 2) {
+          // integer folds of the two components with the column scales of the columns they land in
+          const int Ere = f == 0 ? cexp[2 * zz + 1] : cexp[2 * zz];       // Re ur -> col 2zz+1, Re up -> col 2zz
+          const int Eim = f == 0 ? cexp[2 * zz] : cexp[2 * zz + 1];
+          float h0[2][NS], h1[2][NS], g0[2][NS], g1[2][NS];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const long long ar = xs_fix(va[u].x, Ere, nbs), br = xs_fix(vb[u].x, Ere, nbs);
+            const long long ai = xs_fix(va[u].y, Eim, nbs), bi = xs_fix(vb[u].y, Eim, nbs);
+            const long long fs_re = ar + ss * br, fs_im = ai + ss * bi;
+            const long long fo_re = ar - ss * br, fo_im = ai - ss * bi;
+            if (f == 0) {   // psi_ur = -i F_s(ur): (Im, -Re); X_ur = i F_o(ur): (-Im, Re)
+              xs_digits_f<NS>(fs_im, w, h0[u]); xs_digits_f<NS>(-fs_re, w, h1[u]);
+              xs_digits_f<NS>(-fo_im, w, g0[u]); xs_digits_f<NS>(fo_re, w, g1[u]);
+            } else {        // psi_up = -F_o(up): (-Re, -Im); X_up = F_s(up): (Re, Im)
+              xs_digits_f<NS>(-fo_re, w, h0[u]); xs_digits_f<NS>(-fo_im, w, h1[u]);
+              xs_digits_f<NS>(fs_re, w, g0[u]); xs_digits_f<NS>(fs_im, w, g1[u]);
+            }
+          }
+          const int tp = f == 0 ? 0 : NS, tx = f == 0 ? 2 * NS : 3 * NS;
+#pragma unroll
+          for (int q = 0; q < NS; ++q) {
+            *(uint32_t*)(bst + (tp + q) * BTILE + off) = xs_pack(h0[0][q], h0[1][q]);
+            *(uint32_t*)(bst + (tp + q) * BTILE + off1) = xs_pack(h1[0][q], h1[1][q]);
+            *(uint32_t*)(bst + (tx + q) * BTILE + off) = xs_pack(g0[0][q], g0[1][q]);
+            *(uint32_t*)(bst + (tx + q) * BTILE + off1) = xs_pack(g1[0][q], g1[1][q]);
+          }
+        } else {
+          // Y: F_s(uz) with the uz column scales
+          float h0[2][NT], h1[2][NT];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const long long re = xs_fix(va[u].x, fexp[2 * zz], nbt) + ss * xs_fix(vb[u].x, fexp[2 * zz], nbt);
+            const long long im = xs_fix(va[u].y, fexp[2 * zz + 1], nbt) + ss * xs_fix(vb[u].y, fexp[2 * zz + 1], nbt);
+            xs_digits_f<NT>(re, w, h0[u]);
+            xs_digits_f<NT>(im, w, h1[u]);
           }
 #pragma unroll
-        for (int d = 0; d < NT; ++d)
-#pragma unroll
-          for (int t = 0; t <= d; ++t)
-            umma_bf16(tmem + (2 * NS + d) * N, A(2 * NS + t), B(4 * NS + d - t), idesc, (kc > 0 || t > 0) ? 1u : 0u);
+          for (int q = 0; q < NT; ++q) {
+            *(uint32_t*)(bst + (4 * NS + q) * BTILE + off) = xs_pack(h0[0][q], h0[1][q]);
+            *(uint32_t*)(bst + (4 * NS + q) * BTILE + off1) = xs_pack(h1[0][q], h1[1][q]);
+          }
+        }
+        fence_async_smem();
+        mbar_arrive(&bar_b[s]);
+        if (kc + 1 < nkc) fetch(kc + 1);
       }
-      umma_commit(&bars[1]);
     }
-    if (kc + 1 < nkc) fetch(kc + 1);
-    const bool done = mbar_wait(&bars[1], kc & 1);
-    if (!done || (tid == 0 && !ok)) atomicExch(a.status, 2);
-    ok = __syncthreads_and(ok && done);
+    it = it0 + nkc;
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows t) and the 8-column block w / 4
+    {
+      const uint32_t lst = it - 1;
+      xs_wait(&bar_mma[lst & 1], (lst >> 1) & 1, ok);
+    }
+    ok = __syncthreads_and(ok);
     if (!ok) break;
-  }
-  if (!ok && tid == 0 && klast >= 0) {
-    // a wait ran out: let what was issued finish (bounded) before the memory goes away
-    mbar_wait(&bars[0], klast & 1);
-    mbar_wait(&bars[1], klast & 1);
-  }
-  tc_fence_after();
-  // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows t) and the 8-column block w / 4
-  const int t = mt * 128 + (warp & 3) * 32 + lane;
-  const int j = 2 * t + par;
-  const bool rok = ok && j < nn && t < a.ntr;
-  const int er = rok ? a.rexp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
-  const int et = rok ? a.texp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
-  const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
-  const int cb = warp >> 2;
-  if (ok) {
+    tc_fence_after();
+    const int t = mt * 128 + (warp & 3) * 32 + lane;
+    const int j = 2 * t + par;
+    const bool rok = j < nn && t < a.ntr;
+    if (mt * 128 + (warp & 3) * 32 < a.ntr) {   // a warp of rows past the tile's rows has nothing to write
+      const int er = rok ? a.rexp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
+      const int et = rok ? a.texp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
+      const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
+      const int cb = warp >> 2;
 #pragma unroll 1
-    for (int half = 0; half < 2; ++half) {   // four columns (two complex z) at a time
-      const int c0 = cb * 8 + half * 4;
-      double pv[4], xv[4], yv[4];
-      // the orders summed in double-float
-        float gp[NS][4], gx[NS][4], gy[NT][4];
+      for (int half = 0; half < 2; ++half) {   // four columns (two complex z) at a time
+        const int c0 = cb * 8 + half * 4;
+        double pv[4], xv[4], yv[4];
+        // the orders summed in double-float
+        uint32_t gp[NS][4], gx[NS][4], gy[NT][4];
 #pragma unroll
         for (int d = 0; d < NS; ++d) {
-          tmem_ld4(tmem + lrow + d * N + c0, gp[d]);
-          tmem_ld4(tmem + lrow + (NS + d) * N + c0, gx[d]);
+          tmem_ld4_nw(tmem + lrow + d * N + c0, gp[d]);
+          tmem_ld4_nw(tmem + lrow + (NS + d) * N + c0, gx[d]);
         }
 #pragma unroll
-        for (int d = 0; d < NT; ++d) tmem_ld4(tmem + lrow + (2 * NS + d) * N + c0, gy[d]);
+        for (int d = 0; d < NT; ++d) tmem_ld4_nw(tmem + lrow + (2 * NS + d) * N + c0, gy[d]);
+        tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int E = cexp[c0 + c], F = fexp[c0 + c];
           float g1[NS], g2[NS], g3[NT], h, l;
 #pragma unroll
-          for (int d = 0; d < NS; ++d) { g1[d] = gp[d][c]; g2[d] = gx[d][c]; }
+          for (int d = 0; d < NS; ++d) { g1[d] = __uint_as_float(gp[d][c]); g2[d] = __uint_as_float(gx[d][c]); }
 #pragma unroll
-          for (int d = 0; d < NT; ++d) g3[d] = gy[d][c];
+          for (int d = 0; d < NT; ++d) g3[d] = __uint_as_float(gy[d][c]);
           const bool ox = er > -2000 && E > -2000, oy = et > -2000 && F > -2000;
           xs_orders_df<NS>(g1, w, h, l);
           pv[c] = ox ? xs_df_to_double(h, l, er + E - 2 * w) : 0.0;
@@ -331,19 +379,30 @@ __global__ void __launch_bounds__(32 * NZ, 1) k_xv_contract(XvArgs a) {
           xs_orders_df<NT>(g3, w, h, l);
           yv[c] = oy ? xs_df_to_double(h, l, et + F - 2 * w) : 0.0;
         }
-      if (rok) {
+        if (rok) {
 #pragma unroll
-        for (int c = 0; c < 4; c += 2) {
-          const int n = c0 + c, zc = z0 + n / 2;
-          if (zc >= a.nzdim) continue;
-          const int kk = zc + 1;
-          if (!(kk <= a.nzc || kk >= a.nzcu)) continue;
-          const double kz = a.ak[zc];
-          const size_t o = j + (size_t)a.nrdim * (m + (size_t)a.npdim * zc);
-          a.psi[o] = make_double2(pv[c], pv[c + 1]);
-          a.chi[o] = make_double2(fma(kz, xv[c], -yv[c]), fma(kz, xv[c + 1], -yv[c + 1]));
+          for (int c = 0; c < 4; c += 2) {
+            const int n = c0 + c, zc = z0 + n / 2;
+            if (zc >= a.nzdim) continue;
+            const int kk = zc + 1;
+            if (!(kk <= a.nzc || kk >= a.nzcu)) continue;
+            const double kz = a.ak[zc];
+            const size_t o = j + (size_t)a.nrdim * (m + (size_t)a.npdim * zc);
+            a.psi[o] = make_double2(pv[c], pv[c + 1]);
+            a.chi[o] = make_double2(fma(kz, xv[c], -yv[c]), fma(kz, xv[c + 1], -yv[c + 1]));
+          }
         }
       }
+    }
+    tc_fence_before();
+    __syncthreads();   // TMEM read out (and cexp / fexp read) before the next item
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(a.status, 2);
+    if (tid == 0 && it > 0) {   // let what was issued finish (bounded) before the memory goes away
+      bool ok2 = true;
+      const uint32_t lst = it - 1;
+      xs_wait(&bar_mma[lst & 1], (lst >> 1) & 1, ok2);
     }
   }
   tc_fence_before();
@@ -374,8 +433,8 @@ static bool xv_cfg(int k, XvCfg& c) {
     const double d = (double)(1 << w) * (1 << w);   // largest digit product (two's-complement digits)
     return 2.0 * ns * k * d < lim && (double)nt * k * d < lim;
   };
-  if (fits(5, 6, 7)) { c = {5, 6, 7}; return true; }
-  if (fits(6, 7, 6)) { c = {6, 7, 6}; return true; }
+  if (fits(5, 7, 7)) { c = {5, 7, 7}; return true; }
+  if (fits(6, 8, 6)) { c = {6, 8, 6}; return true; }
   return false;
 }
 
@@ -384,15 +443,15 @@ bool xv_supported() {
   return xv_cfg(G.nrh, c);
 }
 
-template <int NS, int NT, int NZ>
+template <int NS, int NT>
 static int xv_launch(const XvArgs& args, int npc) {
-  constexpr int N = 2 * NZ;
-  const size_t sm = 1024 + (size_t)(2 * NS + NT) * XV_ATILE + (size_t)(4 * NS + NT) * N * XV_KC * 2 + 2 * N * sizeof(int) +
-                    2 * N * sizeof(unsigned long long) + 64;
-  auto kern = k_xv_contract<NS, NT, NZ>;
+  constexpr int N = 2 * XV_NZ;
+  const size_t sm = 1024 + 2 * (size_t)(2 * NS + NT) * XV_ATILE + 2 * (size_t)(4 * NS + NT) * N * XV_KC * 2 +
+                    2 * N * sizeof(int) + 2 * N * sizeof(unsigned long long) + 64;
+  auto kern = k_xv_contract<NS, NT>;
   MLG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  dim3 grid(cdiv(G.nzdim, NZ), 2 * args.nmt, npc - args.m0);
-  kern<<<grid, 32 * NZ, sm, G.stream>>>(args);
+  const int nitems = (npc - args.m0) * 2 * args.nmt * cdiv(G.nzdim, XV_NZ);
+  kern<<<std::min(nitems, 152), XV_THREADS, sm, G.stream>>>(args);
   MLG_LAUNCH();
   return 0;
 }
@@ -419,9 +478,9 @@ int xv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int 
     MLG_LAUNCH();
     const int nb = npc * 2 * nmt * nkc;
     if (cfg.ns == 5)
-      k_xv_table<5, 6><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
+      k_xv_table<5, 7><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
     else
-      k_xv_table<6, 7><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
+      k_xv_table<6, 8><<<nb, 256, 0, G.stream>>>(G.tV, G.tD, G.tT, im.rexp, im.texp, im.p, G.nrh, G.ne, nrc, nmt, nkc, ntr, cfg.w);
     MLG_LAUNCH();
     im.nrc = nrc; im.npc = npc; im.ns = cfg.ns; im.nt = cfg.nt; im.w = cfg.w;
   }
@@ -430,10 +489,11 @@ int xv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int 
   args.texp = im.texp; args.ak = G.ak; args.status = (int*)(G.dscal + DS_FLAG + 1) + 1;
   args.nr = G.nr; args.nrh = G.nrh; args.nrdim = G.nrdim; args.npdim = G.npdim; args.nzdim = G.nzdim; args.nrc = nrc;
   args.nzc = G.chopzl; args.nzcu = G.chopzu; args.nmt = nmt; args.nkc = nkc; args.ntr = ntr; args.w = cfg.w; args.m0 = m0;
-  // 5 digits take 16 complex z columns per CTA (their accumulators fill the 512 tensor-memory
-  // columns), 6 digits 8
-  if (cfg.ns == 5) return xv_launch<5, 6, 16>(args, npc);
-  return xv_launch<6, 7, 8>(args, npc);
+  args.npc = npc;
+  // 8 complex z columns per work item: the (2 NS + NT) orders of 2 x 8 columns fit the 512
+  // tensor-memory columns
+  if (cfg.ns == 5) return xv_launch<5, 7>(args, npc);
+  return xv_launch<6, 8>(args, npc);
 }
 
 }  // namespace mlg

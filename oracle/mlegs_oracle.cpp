@@ -53,7 +53,11 @@ static const double PI = 3.14159265358979323846264338327950288;  // acos(-1.D0),
 // ------------------------------------------------------------------------------------------------
 // error handling: the reference `stop`s; the restatement returns the matching MLG_E* code.
 static std::string g_err;
-static int fail(int code, const char* msg) { g_err = msg; return code; }
+static int fail(int code, const char* msg) {
+#pragma omp critical(mlg_oracle_err)
+  g_err = msg;
+  return code;
+}
 #define CHECK(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
 
 // ------------------------------------------------------------------------------------------------
@@ -742,13 +746,27 @@ static void put_col(Scalar& s, int mm, int kk, int nn, const std::vector<cplx>& 
   for (int i = 1; i <= nn; ++i) s.at(i, mm, kk) = v[i - 1];
 }
 // per-(m,k) loops over kk = 1..nzc and kk = nzcu..nzdim (the Nyquist slot twice when nzc == nzcu),
-// as in every banded operator of mlegs_scalar_ops.f90 (e.g. :546-557)
+// as in every banded operator of mlegs_scalar_ops.f90 (e.g. :546-557).  The m columns are independent
+// and run on the host threads; each m keeps the reference's k order (so a slot visited twice is still
+// updated twice in sequence).  f(mm, kk, v) gets a per-thread work vector and returns a status; the
+// first nonzero status in m order is returned, after every column ran.
 template <class F>
-static void for_each_mk(const ChopIdx& c, F f) {
-  for (int mm = 1; mm <= c.npc; ++mm) {
-    for (int kk = 1; kk <= std::min(K.nzdim, c.nzc); ++kk) f(mm, kk);
-    for (int kk = std::max(c.nzcu, 1); kk <= K.nzdim; ++kk) f(mm, kk);
+static int for_each_mk(const ChopIdx& c, F f) {
+  std::vector<int> st(std::max(c.npc, 0), 0);
+#pragma omp parallel
+  {
+    std::vector<cplx> v;
+#pragma omp for schedule(dynamic)
+    for (int mm = 1; mm <= c.npc; ++mm) {
+      int rc = 0;
+      for (int kk = 1; kk <= std::min(K.nzdim, c.nzc) && !rc; ++kk) rc = f(mm, kk, v);
+      for (int kk = std::max(c.nzcu, 1); kk <= K.nzdim && !rc; ++kk) rc = f(mm, kk, v);
+      st[mm - 1] = rc;
+    }
   }
+  for (int r : st)
+    if (r) return r;
+  return 0;
 }
 
 static int require_fff(Scalar& s) {
@@ -795,14 +813,13 @@ static int xxdx(Scalar& s) {
   CHECK(require_fff(s));
   Scalar so = s;
   so.ln = 0;
-  std::vector<cplx> v;
-  for (int mm = 1; mm <= c.npc; ++mm) {
+  for_each_mk(c, [&](int mm, int kk, std::vector<cplx>& v) {
     int nn = c.nrcs[mm - 1];
-    if (nn < 1) continue;
+    if (nn < 1) return 0;
     Band B = leg_xxdx(mm - 1, nn, nn);
-    for (int kk = 1; kk <= std::min(K.nzdim, c.nzc); ++kk) { get_col(so, mm, kk, nn, v); band_mulvec(B, v.data()); put_col(so, mm, kk, nn, v); }
-    for (int kk = std::max(c.nzcu, 1); kk <= K.nzdim; ++kk) { get_col(so, mm, kk, nn, v); band_mulvec(B, v.data()); put_col(so, mm, kk, nn, v); }
-  }
+    get_col(so, mm, kk, nn, v); band_mulvec(B, v.data()); put_col(so, mm, kk, nn, v);
+    return 0;
+  });
   so.at(1, 1, 1) += 1.0 / std::exp(K.LN(1, 1)) * s.ln;
   so.at(2, 1, 1) += 1.0 / std::exp(K.LN(2, 1)) * s.ln;
   s = so;
@@ -822,12 +839,12 @@ static int del2_generic(Scalar& s, bool with_k) {
   CHECK(require_fff(s));
   Scalar so = s;
   so.ln = 0;
-  std::vector<cplx> v;
-  for_each_mk(c, [&](int mm, int kk) {
+  for_each_mk(c, [&](int mm, int kk, std::vector<cplx>& v) {
     int nn = c.nrcs[mm - 1];
-    if (nn < 1) return;
+    if (nn < 1) return 0;
     Band D = leg_del2(mm - 1, K.ak[kk - 1], nn, nn, with_k);
     get_col(so, mm, kk, nn, v); band_mulvec(D, v.data()); put_col(so, mm, kk, nn, v);
+    return 0;
   });
   ln_del2_terms(so, s.ln, 1.0);
   s = so;
@@ -841,12 +858,15 @@ static int idel2(Scalar& s, bool pre, double preln) {
   ChopIdx c; CHECK(chop_index(s, c));
   CHECK(require_fff(s));
   Scalar so = s;
-  std::vector<cplx> v;
   double e2 = std::pow(K.ell, 2.0);
-  int rc = 0;
-  for (int mm = 1; mm <= c.npc && !rc; ++mm) {
+  std::vector<int> st(std::max(c.npc, 0), 0);
+  // the m columns are independent: one host thread per column, the reference's k order within it
+#pragma omp parallel for schedule(dynamic)
+  for (int mm = 1; mm <= c.npc; ++mm) {
     int nn = c.nrcs[mm - 1];
     if (nn < 1) continue;
+    std::vector<cplx> v;
+    int rc = 0;
     for (int kk = 1; kk <= std::min(K.nzdim, c.nzc) && !rc; ++kk) {
       if (mm == 1 && kk == 1) {
         Band D0 = leg_del2(0, K.ak[0], nn, nn, true);
@@ -886,8 +906,10 @@ static int idel2(Scalar& s, bool pre, double preln) {
       Band D = leg_del2(mm - 1, K.ak[kk - 1], nn, nn, true);
       get_col(so, mm, kk, nn, v); rc = band_lsolve(D, v.data()); put_col(so, mm, kk, nn, v);
     }
+    st[mm - 1] = rc;
   }
-  if (rc) return rc;
+  for (int r : st)
+    if (r) return r;
   s = so;
   return 0;
 }
@@ -908,14 +930,15 @@ static int ihelm(Scalar& s, double alpha) {
   Scalar so = s;
   so.ln = s.ln / alpha;
   ln_del2_terms(so, so.ln, -1.0);
-  std::vector<cplx> v;
-  int rc = 0;
-  for_each_mk(c, [&](int mm, int kk) {
+  int rc = for_each_mk(c, [&](int mm, int kk, std::vector<cplx>& v) {
     int nn = c.nrcs[mm - 1];
-    if (nn < 1 || rc) return;
+    if (nn < 1) return 0;
     Band H = leg_del2(mm - 1, K.ak[kk - 1], nn, nn, true);
     for (int j = 1; j <= nn; ++j) H.set(j, j, H.get(j, j) + alpha);
-    get_col(so, mm, kk, nn, v); rc = band_lsolve(H, v.data()); put_col(so, mm, kk, nn, v);
+    get_col(so, mm, kk, nn, v);
+    int r = band_lsolve(H, v.data());
+    put_col(so, mm, kk, nn, v);
+    return r;
   });
   if (rc) return rc;
   s = so;
@@ -959,11 +982,9 @@ static int ihelmp(Scalar& s, int power, double alpha, double beta) {
     for (int n = 1; n <= power / 2 - 1; ++n) band_mulvec_real(D, bl.data());
     for (int i = 1; i <= nrc; ++i) so.at(i, 1, 1) -= bl[i - 1] + beta * bl2[i - 1];
   }
-  std::vector<cplx> v;
-  int rc = 0;
-  for_each_mk(c, [&](int mm, int kk) {
+  int rc = for_each_mk(c, [&](int mm, int kk, std::vector<cplx>& v) {
     int nn = c.nrcs[mm - 1];
-    if (nn < 1 || rc) return;
+    if (nn < 1) return 0;
     Band D = leg_del2(mm - 1, K.ak[kk - 1], nn, nn, true);
     Band Hp = D;
     for (int n = 1; n <= power / 2 - 1; ++n) Hp = band_mul(D, Hp);
@@ -971,7 +992,10 @@ static int ihelmp(Scalar& s, int power, double alpha, double beta) {
     for (size_t i = 0; i < w.size(); ++i) w[i] += beta * d[i];
     Band H = from_dense(w, nn, power, power);
     for (int j = 1; j <= nn; ++j) H.set(j, j, H.get(j, j) + alpha);
-    get_col(so, mm, kk, nn, v); rc = band_lsolve(H, v.data()); put_col(so, mm, kk, nn, v);
+    get_col(so, mm, kk, nn, v);
+    int r = band_lsolve(H, v.data());
+    put_col(so, mm, kk, nn, v);
+    return r;
   });
   if (rc) return rc;
   s = so;
