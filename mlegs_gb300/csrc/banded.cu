@@ -1000,10 +1000,11 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
     }
   };
   // the factor rows of group g: NSL slots from S0 of rows j(u), 256 bytes per (row, slot), 16 per copy
+  // (backward without row exchanges: 1/U(j,j) and the FKU entries of U's own band only)
   const double* fbase = fac + sys0 + 2 * (th & 15);
-  auto stage_fac_t = [&](auto bwdc, int g) {
-    constexpr bool BWD = decltype(bwdc)::value;
-    constexpr int NSL = BWD ? SNU + 1 : FKL + 1, S0 = BWD ? FKL + 1 : 0;
+  auto stage_fac_t = [&](auto bwdc, auto npc, int g) {
+    constexpr bool BWD = decltype(bwdc)::value, NP = decltype(npc)::value;
+    constexpr int NSL = BWD ? (NP ? FKU + 1 : SNU + 1) : FKL + 1, S0 = BWD ? FKL + 1 : 0;
     const int st = g % SST;
 #pragma unroll
     for (int c = th; c < SGR * NSL * 16; c += NT) {
@@ -1015,12 +1016,13 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
     }
   };
   auto stage_fac = [&](int g, bool bwd) {
-    if (bwd) stage_fac_t(std::integral_constant<bool, true>(), g);
-    else stage_fac_t(std::integral_constant<bool, false>(), g);
+    stage_fac_t(std::integral_constant<bool, false>(), std::integral_constant<bool, false>(), g);
+    (void)bwd;
   };
   for (int rep = 0; rep < cntw; ++rep) {
     // ---- forward: L y = P b, y(j) into the field's slot of row j ----
     R r[FKL + 1];
+    bool piv = false;   // a row exchange in one of this thread's staged rows
 #pragma unroll
     for (int t = 0; t <= FKL; ++t) r[t] = ((rep < cnt && t < nn) ? __ldcg(x + 2 * t) : 0.0);
     for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, false); stage_rows(g, rep, false); } cpa_commit(); }
@@ -1035,6 +1037,7 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
       for (int u = 0; u < SGR; ++u) {
         // the pivot row index p (0..FKL), stored as a double: compared by its high word, off the FP64 pipe
         const int ph = __double2hiint(sm.f[st][FKL][u][lane]);
+        piv = piv || ph != 0;
 #pragma unroll
         for (int t = 1; t <= FKL; ++t)
           if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) { R w = r[0]; r[0] = r[t]; r[t] = w; }
@@ -1051,34 +1054,47 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
     if (ng > 0) write_out(ng - 1, rep, false);
     __threadfence_block();
     __syncthreads();   // y(j) in the fields, read back below by other threads' copies
-    // ---- backward: U x = y from row nnw-1 down; a system joins at its own last row ----
-    R xs[SNU];
+    // ---- backward: U x = y from row nnw-1 down; a system joins at its own last row.  Without a row
+    // exchange in any of the block's systems (every forward pass saw pivot offset 0), U keeps the
+    // matrix's own FKU superdiagonals and its fill-in entries are exact zeros: the pass then stages and
+    // applies only those (1 / U(j,j) and FKU ratios), with the same result bit for bit, since
+    // fma(-0, x, t) = t for finite x.
+    const bool nopiv = !__syncthreads_or(piv);
+    auto backward = [&](auto npc) {
+      constexpr bool NP = decltype(npc)::value;
+      constexpr int NU = NP ? FKU : SNU;
+      auto stage_b = [&](int g) { stage_fac_t(std::integral_constant<bool, true>(), npc, g); };
+      R xs[SNU];
 #pragma unroll
-    for (int c = 0; c < SNU; ++c) xs[c] = 0.0;
-    for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, true); stage_rows(g, rep, true); } cpa_commit(); }
-    for (int g = 0; g < ng; ++g) {
-      cpa_wait<SST - 2>();
-      __syncthreads();
-      if (g + SST - 1 < ng) { stage_fac(g + SST - 1, true); stage_rows(g + SST - 1, rep, true); }
-      cpa_commit();
-      if (g > 0) write_out(g - 1, rep, true);
-      const int st = g % SST;
+      for (int c = 0; c < SNU; ++c) xs[c] = 0.0;
+      for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_b(g); stage_rows(g, rep, true); } cpa_commit(); }
+      for (int g = 0; g < ng; ++g) {
+        cpa_wait<SST - 2>();
+        __syncthreads();
+        if (g + SST - 1 < ng) { stage_b(g + SST - 1); stage_rows(g + SST - 1, rep, true); }
+        cpa_commit();
+        if (g > 0) write_out(g - 1, rep, true);
+        const int st = g % SST;
 #pragma unroll
-      for (int u = 0; u < SGR; ++u) {
-        const int j = nnw - 1 - (g * SGR + u);
-        const R f0 = sm.f[st][0][u][lane], g1 = sm.f[st][1][u][lane], g2 = sm.f[st][2][u][lane];
-        const R g3 = sm.f[st][3][u][lane], g4 = sm.f[st][4][u][lane];
-        // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
-        const R yj = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
-        const R t = fma(-g4, xs[3], fma(-g3, xs[2], fma(-g2, xs[1], yj * f0)));
-        R xj = fma(-g1, xs[0], t);
-        if (j >= nn) xj = 0.0;
-        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = xj;
+        for (int u = 0; u < SGR; ++u) {
+          const int j = nnw - 1 - (g * SGR + u);
+          const R f0 = sm.f[st][0][u][lane];
+          // x(j) = y(j)/U(j,j) - sum_c (U(j,j+c)/U(j,j)) x(j+c): only the last FMA waits on x(j+1)
+          const R yj = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
+          R t = yj * f0;
 #pragma unroll
-        for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
-        xs[0] = xj;
+          for (int c = 2; c <= NU; ++c) t = fma(-sm.f[st][c][u][lane], xs[c - 1], t);
+          R xj = fma(-sm.f[st][1][u][lane], xs[0], t);
+          if (j >= nn) xj = 0.0;
+          reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = xj;
+#pragma unroll
+          for (int c = SNU - 1; c >= 1; --c) xs[c] = xs[c - 1];
+          xs[0] = xj;
+        }
       }
-    }
+    };
+    if (nopiv) backward(std::integral_constant<bool, true>());
+    else backward(std::integral_constant<bool, false>());
     cpa_wait<0>();
     __syncthreads();
     if (ng > 0) write_out(ng - 1, rep, true);
@@ -1258,6 +1274,9 @@ static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, do
   }
   LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock};
   MLG_TRY(dmalloc((void**)&e.buf, bytes));
+  // rows past a system's own count (and systems outside the chop) stay zero: pivot offset 0, so a
+  // block's substitution can take its no-exchange path
+  MLG_CUDA(cudaMemsetAsync(e.buf, 0, bytes, G.stream));
   MLG_TRY(factor(e.buf));
   g_lu.push_back(e);
   *out = e.buf;

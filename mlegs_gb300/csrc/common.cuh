@@ -84,6 +84,7 @@ struct Ctx {
   double2 *tw_p = nullptr, *tw_z = nullptr;  // FFT twiddles exp(-2 pi i k/L): L = np/2 (phi), nz (z)
   double2 *tw_pr = nullptr;    // real-FFT post-processing twiddles exp(-2 pi i k/np), k < np/2+1
   float2 *tw_p32 = nullptr, *tw_z32 = nullptr, *tw_pr32 = nullptr;   // FP32 copies for the mixed form
+  float4 *tw_pdf = nullptr, *tw_zdf = nullptr, *tw_prdf = nullptr;   // double-float copies (re hi, re lo, im hi, im lo)
 
   // ln slots of all scalars (device), and per-step scalars (svv gains, flags, scratch reductions)
   double* ln_slots = nullptr;  int n_slots = 0;  std::vector<int> free_slots;

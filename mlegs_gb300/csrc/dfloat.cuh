@@ -14,7 +14,7 @@ struct dfl {
   float h, l;
   dfl() = default;
   __device__ __forceinline__ dfl(int v) : h((float)v), l(0.f) {}   // small integers are exact
-  __device__ __forceinline__ dfl(float a, float b) : h(a), l(b) {}
+  __host__ __device__ __forceinline__ dfl(float a, float b) : h(a), l(b) {}
   __device__ __forceinline__ explicit dfl(double x);
 };
 __device__ __forceinline__ dfl df_quick(float a, float b) {   // |a| >= |b|

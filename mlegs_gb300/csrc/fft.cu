@@ -25,34 +25,57 @@
 
 namespace mlg {
 
+// the mixed form's FFT arithmetic: FP32 or double-float
+#ifndef MLG_MIXED_FFT_DF
+#define MLG_MIXED_FFT_DF 0
+#endif
+typedef std::conditional<MLG_MIXED_FFT_DF != 0, dfl, float>::type MixFT;
+
 template <typename T> struct CT;
 template <> struct CT<double> { typedef double2 t; };
 template <> struct CT<float> { typedef float2 t; };
+template <> struct CT<dfl> { typedef dfl2 t; };
 
 template <typename T> __device__ __forceinline__ typename CT<T>::t mk(T a, T b);
 template <> __device__ __forceinline__ double2 mk<double>(double a, double b) { return make_double2(a, b); }
 template <> __device__ __forceinline__ float2 mk<float>(float a, float b) { return make_float2(a, b); }
+template <> __device__ __forceinline__ dfl2 mk<dfl>(dfl a, dfl b) { dfl2 r; r.x = a; r.y = b; return r; }
 
 template <typename C> __device__ __forceinline__ C c_add(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C> __device__ __forceinline__ C c_sub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 template <typename C> __device__ __forceinline__ C c_mul(C a, C b) {
   C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
-template <typename C> __device__ __forceinline__ C c_muli(C a, int sgn) {  // a * (sgn * i)
-  C r; r.x = -sgn * a.y; r.y = sgn * a.x; return r;
+template <typename C> __device__ __forceinline__ C c_muli(C a, int sgn) {  // a * (sgn * i), exact
+  C r; r.x = sgn > 0 ? -a.y : a.y; r.y = sgn > 0 ? a.x : -a.x; return r;
 }
 template <typename C, typename T> __device__ __forceinline__ C c_scale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
 
-// twiddle tables hold exp(-2 pi i k/L) (FP64 for the plain form, FP32 for the mixed form); sgn > 0
-// conjugates
+// twiddle tables hold exp(-2 pi i k/L) (FP64 for the plain form; FP32, or double-float as (re hi,
+// re lo, im hi, im lo), for the mixed form); sgn > 0 conjugates
 template <typename T> struct TW;
 template <> struct TW<double> { typedef double2 t; };
 template <> struct TW<float> { typedef float2 t; };
+template <> struct TW<dfl> { typedef float4 t; };
 template <typename T>
 __device__ __forceinline__ typename CT<T>::t load_tw(const typename TW<T>::t* tw, int idx, int sgn) {
   typename TW<T>::t w = tw[idx];
   return mk<T>(w.x, sgn < 0 ? w.y : -w.y);
 }
+template <>
+__device__ __forceinline__ dfl2 load_tw<dfl>(const float4* tw, int idx, int sgn) {
+  const float4 w = tw[idx];
+  const dfl im(w.z, w.w);
+  return mk<dfl>(dfl(w.x, w.y), sgn < 0 ? im : -im);
+}
+// a transform value to FP64 (FP32 and double-float exactly on the integer pipe, then one FP64 add)
+__device__ __forceinline__ double to_dbl(double v) { return v; }
+__device__ __forceinline__ double to_dbl(float v) { return f2d_fast(v); }
+__device__ __forceinline__ double to_dbl(dfl v) { return f2d_fast(v.h) + f2d_fast(v.l); }
+// a double-float sample in the transform's arithmetic
+template <typename T> __device__ __forceinline__ T from_df(dfl v);
+template <> __device__ __forceinline__ float from_df<float>(dfl v) { return v.h; }
+template <> __device__ __forceinline__ dfl from_df<dfl>(dfl v) { return v; }
 
 // small DFTs, sign sgn = -1 forward, +1 backward
 template <typename T>
@@ -123,9 +146,14 @@ __device__ void stockham(typename CT<T>::t* s0, typename CT<T>::t* s1, typename 
 template <typename T> __device__ __forceinline__ typename CT<T>::t ld(const double2* p);
 template <> __device__ __forceinline__ double2 ld<double>(const double2* p) { return *p; }
 template <> __device__ __forceinline__ float2 ld<float>(const double2* p) { return ld_c32(p); }
+template <> __device__ __forceinline__ dfl2 ld<dfl>(const double2* p) {
+  const double2 v = *p;
+  return mk<dfl>(dfl(v.x), dfl(v.y));
+}
 template <typename T> __device__ __forceinline__ void st(double2* p, typename CT<T>::t v);
 template <> __device__ __forceinline__ void st<double>(double2* p, double2 v) { *p = v; }
 template <> __device__ __forceinline__ void st<float>(double2* p, float2 v) { st_c32(p, v); }
+template <> __device__ __forceinline__ void st<dfl>(double2* p, dfl2 v) { *p = make_double2(to_dbl(v.x), to_dbl(v.y)); }
 
 // z FFT of columns (r, m): points at stride nrdim*npdim; the grid covers m = m0, m0+1, ...
 template <typename T>
@@ -401,7 +429,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
                                                                   double scale_d, double inv_np, int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
-  constexpr bool DC = std::is_same<T, float>::value;
+  constexpr bool DC = !std::is_same<T, double>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   double* red = (double*)(smem_raw + (size_t)L * TRL * sizeof(C));
@@ -417,7 +445,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
   const double rv = rsc ? rs[r] : 1.0;
   C a[R1];
   double sum = 0.0;
-  if (DC) {
+  if constexpr (DC) {
     // the row scale, the row sum and the mean subtraction in double-float (about 47 bits, on the FP32
     // and integer pipes; FP64 would occupy GB300's narrow FP64 pipe with 4-6 operations per sample);
     // the samples less their mean are then rounded to FP32 for the transform
@@ -441,7 +469,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
     const dfl mu = sd * dfl((float)inv_np, 0.f);   // inv_np = 1/np, a power of two for these lengths
     sum = f2d_fast(sd.h) + f2d_fast(sd.l);
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>((T)(dx[n1] - mu).h, (T)(dy[n1] - mu).h);
+    for (int n1 = 0; n1 < R1; ++n1) a[n1] = mk<T>(from_df<T>(dx[n1] - mu), from_df<T>(dy[n1] - mu));
   } else {
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
@@ -471,9 +499,10 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
     zc.y = -zc.y;
     C fe = c_scale(c_add(zk, zc), (T)0.5);
     C fo = c_muli(c_scale(c_sub(zk, zc), (T)0.5), -1);   // (zk - zc)/(2i)
-    typename TW<T>::t wd = twr[k];
-    C x = c_scale(c_add(fe, c_mul(mk<T>(wd.x, wd.y), fo)), scale);
-    if (DC && k == 0) base[0] = make_double2(f2d_fast((float)x.x) + sum * scale_d, f2d_fast((float)x.y));
+    C x = c_scale(c_add(fe, c_mul(load_tw<T>(twr, k, -1), fo)), scale);
+    bool dc0 = false;
+    if constexpr (DC) dc0 = k == 0;
+    if (dc0) base[0] = make_double2(to_dbl(x.x) + sum * scale_d, to_dbl(x.y));
     else st<T>(base + (size_t)k * nrdim, x);
   }
 }
@@ -487,7 +516,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int n
                                                                   int nrs) {
   typedef typename CT<T>::t C;
   constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2, Q = R1 / R2;
-  constexpr bool DC = std::is_same<T, float>::value;
+  constexpr bool DC = !std::is_same<T, double>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* S = (C*)smem_raw;
   int lane = threadIdx.x, w = threadIdx.y;
@@ -513,8 +542,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int n
       if (k == 0) { xk.y = 0; xc.y = 0; if (DC) xk.x = 0; }
       xc.y = -xc.y;
       C g = c_add(xk, xc);
-      typename TW<T>::t wd = twr[k];
-      C h = c_mul(c_sub(xk, xc), mk<T>(wd.x, -wd.y));   // exp(+2 pi i k / np)
+      C h = c_mul(c_sub(xk, xc), load_tw<T>(twr, k, +1));   // exp(+2 pi i k / np)
       v = c_add(g, c_muli(h, 1));
     }
     a[n1] = v;
@@ -533,10 +561,10 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int n
       C y = b[q][i];
       double2* o = base + (size_t)(k1 + R1 * bitrev(i, R2)) * nrdim;
       double2 v;
-      if (DC) {
+      if constexpr (DC) {
         // (y + dc) rv as one FMA per component
-        v = rsc ? make_double2(fma(f2d_fast((float)y.x), rv, dcr), fma(f2d_fast((float)y.y), rv, dcr))
-                : make_double2(f2d_fast((float)y.x) + dc, f2d_fast((float)y.y) + dc);
+        v = rsc ? make_double2(fma(to_dbl(y.x), rv, dcr), fma(to_dbl(y.y), rv, dcr))
+                : make_double2(to_dbl(y.x) + dc, to_dbl(y.y) + dc);
       } else {
         v = make_double2((double)y.x, (double)y.y);
         if (rsc) { v.x *= rv; v.y *= rv; }
@@ -551,9 +579,28 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int n
   }
 }
 
-template <typename T> const typename TW<T>::t* tw_of(const double2* d, const float2* f);
-template <> const double2* tw_of<double>(const double2* d, const float2* f) { (void)f; return d; }
-template <> const float2* tw_of<float>(const double2* d, const float2* f) { (void)d; return f; }
+// a host-side scale factor in the transform's arithmetic (double-float: hi = the FP32 rounding, lo =
+// the FP32 rounding of the rest)
+template <typename T> static T host_scale(double v) { return (T)v; }
+template <> dfl host_scale<dfl>(double v) { const float h = (float)v; return dfl(h, (float)(v - (double)h)); }
+
+// the twiddle tables of a transform's arithmetic: phi (L = np/2), phi post-processing (np), z (nz)
+template <typename T> struct TwTab;
+template <> struct TwTab<double> {
+  static const double2* p() { return G.tw_p; }
+  static const double2* pr() { return G.tw_pr; }
+  static const double2* z() { return G.tw_z; }
+};
+template <> struct TwTab<float> {
+  static const float2* p() { return G.tw_p32; }
+  static const float2* pr() { return G.tw_pr32; }
+  static const float2* z() { return G.tw_z32; }
+};
+template <> struct TwTab<dfl> {
+  static const float4* p() { return G.tw_pdf; }
+  static const float4* pr() { return G.tw_prdf; }
+  static const float4* z() { return G.tw_zdf; }
+};
 
 static int pick_tr(int L, size_t elem) {
   // two shared buffers of L*TR complex values, at most 96 KB
@@ -580,7 +627,7 @@ static int zfft2_launch(const FSet& fs, double scale, int m0, int nm, cudaStream
   MLG_TRY(set_smem<T>((const void*)k_zfft2<T, L, SGN, TRL>, sm));
   const int nlines = G.nrdim * nm;
   dim3 grid(cdiv((long long)nlines * fs.n, TRL)), blk(TRL, Split<L>::R2);
-  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(fs, G.nrdim, G.npdim, tw_of<T>(G.tw_z, G.tw_z32), (T)scale, m0,
+  k_zfft2<T, L, SGN, TRL><<<grid, blk, sm, stream>>>(fs, G.nrdim, G.npdim, TwTab<T>::z(), host_scale<T>(scale), m0,
                                                      nlines);
   MLG_LAUNCH();
   return 0;
@@ -607,16 +654,20 @@ static int vfft_t(const FSet& fs, int dir, double scale, int m0, int nm, int tr_
   int L = G.nz;
   if (L <= 1 || nm <= 0) return 0;
   if (pow2_fast(L)) return tr_max >= 32 ? zfft2_any<T, 32>(fs, dir, scale, m0, nm, stream) : zfft2_any<T, 8>(fs, dir, scale, m0, nm, stream);
+  if constexpr (std::is_same<T, dfl>::value) {
+    return vfft_t<double>(fs, dir, scale, m0, nm, tr_max, stream);   // other lengths: the FP64 Stockham kernel
+  } else {
   int TR = std::min(pick_tr(L, sizeof(typename CT<T>::t)), tr_max);
   int TT = std::max(1, std::min(256 / TR, L / 2));
   size_t sm = 2ull * L * TR * sizeof(typename CT<T>::t);
   MLG_TRY(set_smem<T>((const void*)k_vfft<T>, sm));
   dim3 grid(cdiv(G.nrdim, TR), nm), blk(TR, TT);
   for (int f = 0; f < fs.n; ++f) {   // other lengths: the Stockham kernel, field by field
-    k_vfft<T><<<grid, blk, sm, stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_z, G.tw_z32), dir, (T)scale, m0);
+    k_vfft<T><<<grid, blk, sm, stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, TwTab<T>::z(), dir, (T)scale, m0);
     MLG_LAUNCH();
   }
   return 0;
+  }
 }
 
 // plain form: FP64.  Mixed form: m >= 1 in FP32; the m = 0 lines (the axisymmetric part, with the mean
@@ -626,7 +677,7 @@ static int vfft_any(const FSet& fs, int dir, double scale) {
   if (G.precision == MLG_MIXED) {
     MLG_TRY(side_fork());
     MLG_TRY(vfft_t<double>(fs, dir, scale, 0, 1, 2, G.side));
-    MLG_TRY(vfft_t<float>(fs, dir, scale, 1, G.npdim - 1, 32, G.stream));
+    MLG_TRY(vfft_t<MixFT>(fs, dir, scale, 1, G.npdim - 1, 32, G.stream));
     MLG_TRY(side_join());
   } else {
     MLG_TRY(vfft_t<double>(fs, dir, scale, 0, G.npdim, 32, G.stream));
@@ -651,17 +702,17 @@ int launch_vfft_multi(Scalar* const* s, int n, int dir) {
 template <typename T, int L>
 static int pfft2_launch(const FSet& fs, int dir, double scale) {
   constexpr int TRL = 32;
-  constexpr bool DC = std::is_same<T, float>::value;
+  constexpr bool DC = !std::is_same<T, double>::value;
   size_t sm = (size_t)L * TRL * sizeof(typename CT<T>::t) + (DC && dir < 0 ? (size_t)Split<L>::R2 * TRL * sizeof(double) : 0);
   dim3 grid(cdiv((long long)G.nrdim * G.nzdim * fs.n, TRL)), blk(TRL, Split<L>::R2);
   if (dir < 0) {
     MLG_TRY(set_smem<T>((const void*)k_pfft_fwd2<T, L, TRL>, sm));
-    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale, scale, 1.0 / G.np, G.nr);
+    k_pfft_fwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, TwTab<T>::p(),
+                                                        TwTab<T>::pr(), host_scale<T>(scale), scale, 1.0 / G.np, G.nr);
   } else {
     MLG_TRY(set_smem<T>((const void*)k_pfft_bwd2<T, L, TRL>, sm));
-    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, tw_of<T>(G.tw_p, G.tw_p32),
-                                                        tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, G.nr);
+    k_pfft_bwd2<T, L, TRL><<<grid, blk, sm, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, TwTab<T>::p(),
+                                                        TwTab<T>::pr(), (double)G.np, G.nr);
   }
   MLG_LAUNCH();
   return 0;
@@ -683,6 +734,10 @@ static int hfft_t(const FSet& fs, int dir, double scale) {
     kt_end(1, 2.0 * fs.n * G.fsize * 16);
     return 0;
   }
+  if constexpr (std::is_same<T, dfl>::value) {
+    kt_end(1, 0.0);
+    return hfft_t<double>(fs, dir, scale);   // other lengths: the FP64 Stockham kernels
+  } else {
   int TR = pick_tr(L, sizeof(typename CT<T>::t));
   int TT = std::max(1, std::min(256 / TR, std::max(L / 2, 1)));
   constexpr bool DC = std::is_same<T, float>::value;
@@ -692,17 +747,18 @@ static int hfft_t(const FSet& fs, int dir, double scale) {
   else MLG_TRY(set_smem<T>((const void*)k_hfft_bwd<T>, sm));
   for (int f = 0; f < fs.n; ++f) {   // other lengths: the Stockham kernels, field by field
     if (dir < 0) {
-      k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                  tw_of<T>(G.tw_pr, G.tw_pr32), (T)scale,
+      k_hfft_fwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, TwTab<T>::p(),
+                                                  TwTab<T>::pr(), (T)scale,
                                                   scale, 1.0 / G.np, fs.rs[f], G.nr);
     } else {
-      k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, tw_of<T>(G.tw_p, G.tw_p32),
-                                                  tw_of<T>(G.tw_pr, G.tw_pr32), (double)G.np, fs.rs[f], G.nr);
+      k_hfft_bwd<T><<<grid, blk, sm, G.stream>>>(fs.e[f], G.nrdim, G.npdim, L, TR, TwTab<T>::p(),
+                                                  TwTab<T>::pr(), (double)G.np, fs.rs[f], G.nr);
     }
     MLG_LAUNCH();
   }
   kt_end(1, 2.0 * fs.n * G.fsize * 16);
   return 0;
+  }
 }
 
 int launch_hfft(Scalar& s, int dir) { return launch_hfft_rs(s, dir, nullptr); }
@@ -724,15 +780,15 @@ int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir)
     fs.e[i] = s[i]->e; fs.rs[i] = rs ? rs[i] : nullptr;
   }
   fs.n = n;
-  return G.precision == MLG_MIXED ? hfft_t<float>(fs, dir, 1.0 / G.np) : hfft_t<double>(fs, dir, 1.0 / G.np);
+  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fs, dir, 1.0 / G.np) : hfft_t<double>(fs, dir, 1.0 / G.np);
 }
 // the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs)
 int launch_hfft_fwd_scaled(cd* e, double scale) {
-  return G.precision == MLG_MIXED ? hfft_t<float>(fset1(e), -1, scale) : hfft_t<double>(fset1(e), -1, scale);
+  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fset1(e), -1, scale) : hfft_t<double>(fset1(e), -1, scale);
 }
 // the half-complex-to-real sum (unnormalised, Nyquist slot kept times np), on a raw buffer
 int launch_hfft_bwd_buf(cd* e) {
-  return G.precision == MLG_MIXED ? hfft_t<float>(fset1(e), +1, 1.0) : hfft_t<double>(fset1(e), +1, 1.0);
+  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fset1(e), +1, 1.0) : hfft_t<double>(fset1(e), +1, 1.0);
 }
 
 }  // namespace mlg

@@ -392,6 +392,17 @@ int kit_build(const mlg_params* P) {
   MLG_TRY(upload(&G.tw_p32, to32(tp)));
   MLG_TRY(upload(&G.tw_pr32, to32(tpr)));
   MLG_TRY(upload(&G.tw_z32, to32(tz)));
+  auto todf = [](const std::vector<double2>& t) {   // x = hi + lo, hi = x rounded to FP32
+    std::vector<float4> f(t.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+      const float rh = (float)t[i].x, ih = (float)t[i].y;
+      f[i] = make_float4(rh, (float)(t[i].x - (double)rh), ih, (float)(t[i].y - (double)ih));
+    }
+    return f;
+  };
+  MLG_TRY(upload(&G.tw_pdf, todf(tp)));
+  MLG_TRY(upload(&G.tw_prdf, todf(tpr)));
+  MLG_TRY(upload(&G.tw_zdf, todf(tz)));
 
   MLG_CUDA(cudaStreamSynchronize(G.stream));
   dfree(d_logfact, logfact.size() * sizeof(double));

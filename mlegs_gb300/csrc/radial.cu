@@ -456,7 +456,7 @@ int launch_rtrans_fwd(Scalar& s) {
     if (mixed) {
       MLG_TRY(side_fork());
       MLG_TRY(m0_rtrans_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
-      if (xs) MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, false));   // m >= 1: 35-bit slices
+      if (xs) MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, false));   // m >= 1: 42-bit slices
       else MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: split BF16 (tc_radial.cu)
       MLG_TRY(side_join());
     } else if (xs) {
@@ -496,7 +496,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
       MLG_TRY(m0_tab());
       MLG_TRY(side_fork());
       MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln, G.side));   // m = 0: double-float, beside
-      if (xs) MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, false));   // m >= 1: 35-bit slices
+      if (xs) MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, false));   // m >= 1: 42-bit slices
       else MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));           // m >= 1: split BF16
       MLG_TRY(side_join());
     } else if (xs) {

@@ -50,13 +50,7 @@ __device__ __forceinline__ void xs_digits_f(long long X, int w, float* f) {
 __device__ __forceinline__ uint32_t xs_pack(float a, float b) { return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632); }
 
 // the exact integer value of an FP32 accumulator entry (integral, |x| < 2^24)
-__device__ __forceinline__ int xs_f2i(float x) {
-  const unsigned u = __float_as_uint(x);
-  const int e = min((int)((u >> 23) & 0xFF) - 127, 23);
-  if (e < 0) return 0;
-  const int v = (int)(((u & 0x7FFFFFu) | 0x800000u) >> (23 - e));
-  return (u >> 31) ? -v : v;
-}
+__device__ __forceinline__ int xs_f2i(float x) { return __float2int_rn(x); }
 
 // x 2^s for s >= 0, floor(x 2^s) for s < 0
 __device__ __forceinline__ long long xs_shl(long long x, int s) { return s >= 0 ? (x << s) : (x >> (-s)); }

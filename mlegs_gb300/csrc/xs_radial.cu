@@ -10,13 +10,13 @@
 // d = t + s are summed over K in their own FP32 accumulator in tensor memory,
 //   G_d = sum_{t+s=d} sum_k a_t(row, k) b_s(k, n),
 // which stays exact while K * (d+1) * 2^(2w) < 2^24 (w = 7 up to K ~ 113 with nine orders, w = 6
-// beyond).  Orders d < NO are kept; the epilogue forms the exact integer
+// beyond).  Orders d < NO = NS are kept; the epilogue forms the exact integer
 //   T = sum_d G_d 2^(w (NO-1-d))
 // in 64-bit integer arithmetic (the lowest orders shifted right when T would pass 2^62: a loss below
 // 2^-60 of the largest term) and rounds T 2^(EA + EB - w (NO+1)) once to FP64, on the integer pipe.
 // The result differs from the exact product of the FP64 operands by about 2^-(w NS - 1) of
 // max|A(row,:)| max|B(:,n)| per term: NS = 9, w = 7 (63 bits) is an FP64-grade product (the plain
-// form), NS = 5 (35 bits) the mixed form's.  No floating-point rounding happens anywhere else: the
+// form), NS = 6 (42 bits) the mixed form's.  No floating-point rounding happens anywhere else: the
 // forward fold f(i) +- f(nr-1-i) is an exact integer sum of the two rounded samples, and the
 // quadrature weights are folded into the table (A = pf w, one FP64 rounding at kit init).
 //
@@ -37,9 +37,13 @@
 //  * per row tile and K chunk of 16: the table digits of both parities arrive by one bulk copy (pre-split
 //    at kit init in the UMMA canonical no-swizzle K-major layout), the threads cut the field digits
 //    from shared memory into the same layout (each warp's 32 stores in 32 banks), and one thread issues
-//    the 2 x (pairs) tcgen05.mma of the chunk (M = 128, N = 2 NZ, K = 16), commits, and as soon as the
-//    other stage is free starts the next chunk's table copy into it; the stages are double-buffered, so
-//    the digits and the table copy of chunk k + 1 overlap the MMAs of chunk k;
+//    the chunk's tcgen05.mma, commits, and as soon as the other stage is free starts the next chunk's
+//    table copy into it; the stages are double-buffered, so the digits and the table copy of chunk
+//    k + 1 overlap the MMAs of chunk k.  The field digits of a parity lie side by side (digit s at
+//    rows s N .. s N + N-1 of the B operand) and so do the accumulators of the orders, so table digit
+//    t meets all field digits s <= NO-1-t in one MMA of M = 128, N = (NO - t) 2 NZ, K = 16 whose
+//    column block s lands on order t + s: NO MMAs per parity and chunk instead of NO (NO+1)/2, and
+//    each table tile is read from shared memory once;
 //  * reads the 2 NO accumulators back with tcgen05.ld and writes FP64 results.
 // Every wait is bounded (about a second of SM clock): a timeout sets the library's timeout word and the
 // CTA stops issuing work, waits (bounded) for what it issued, frees its tensor memory and returns.
@@ -158,8 +162,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   uint8_t* sB = sA + 2 * ASTAGE;                         // [2 stages][BSTAGE]
   double* raw = (double*)(sB + 2 * BSTAGE);              // [NZ][rawk] complex (re, im)
   int* colexp = (int*)(raw + (size_t)2 * NZ * a.rawk);   // [N]
-  unsigned long long* colmax = (unsigned long long*)(colexp + N);   // [N]
-  uint64_t* bars = (uint64_t*)(colmax + N);              // raw, a[2], b[2], mma[2]
+  uint64_t* bars = (uint64_t*)(colexp + 2 * N);         // raw, a[2], b[2], mma[2]
   uint32_t* tslot = (uint32_t*)(bars + 7);
   uint64_t* bar_raw = bars;
   uint64_t* bar_a = bars + 1;     // table stage filled (bulk copy)
@@ -189,7 +192,6 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   uint32_t it = 0, raw_ph = 0;                  // chunk counter (stage and phase), raw-copy phase
   const int nzt = (a.nzdim + NZ - 1) / NZ;
   const int nitems = (a.npc - a.m0) * nzt;
-  const uint32_t idesc = idesc_bf16(128, N);
   // the items of this CTA, skipping those without rows (every thread walks the same sequence)
   auto item_nn = [&](int item) { const int m = a.m0 + item / nzt; return max(min(a.nrc, a.nrc - m), 0); };
   auto next_item = [&](int item) {
@@ -222,27 +224,25 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
     const int nkc_m = (kext + XS_KC - 1) / XS_KC;
     const int nrows = MODE == 0 ? (nn + 1) / 2 : a.nrh;
     const int nmt_m = (nrows + 127) / 128;
-    if (tid < N) colmax[tid] = 0ull;
     xs_wait(bar_raw, raw_ph, ok);
     raw_ph ^= 1;
     ok = __syncthreads_and(ok);   // every exit below is taken by the whole block
     if (!ok) break;
-    // ---- column scales: XS_THREADS / N threads per real column n (z = n/2, re/im = n&1)
+    // ---- column scales: XS_THREADS / N lanes of one warp per real column n (z = n/2, re/im = n&1)
+    // reduce the largest exponent field (the high words of the staged FP64 samples) by warp shuffles
     {
       constexpr int TPC = XS_THREADS / N;
+      static_assert(TPC == 16 || TPC == 32, "a column's lanes are a half or a whole warp");
       const int n = tid / TPC, sub = tid % TPC, zz = n >> 1;
-      unsigned long long mx = 0;
+      unsigned mx = 0;
       if (z0 + zz < a.nzdim) {
-        const double* col = raw + (size_t)2 * zz * a.rawk + (n & 1);
-        for (int i = sub; i < kraw; i += TPC) {
-          unsigned long long v = (unsigned long long)__double_as_longlong(col[2 * i]) & 0x7FFFFFFFFFFFFFFFull;
-          mx = v > mx ? v : mx;
-        }
+        const unsigned* hw = (const unsigned*)(raw + (size_t)2 * zz * a.rawk + (n & 1)) + 1;
+        for (int i = sub; i < kraw; i += TPC) mx = max(mx, (hw[4 * i] >> 20) & 0x7FFu);
       }
-      atomicMax(colmax + n, mx);
+      mx = __reduce_max_sync(TPC == 32 ? 0xFFFFFFFFu : (0xFFFFu << (lane & 16)), mx);
+      // |x| < 2^(field - 1022) for every sample; an all-zero column gets -2000
+      if (sub == 0) colexp[n] = mx ? (int)mx - 1022 + (MODE == 0 ? 1 : 0) : -2000;
     }
-    __syncthreads();
-    if (tid < N) colexp[tid] = colmax[tid] ? xs_ebound(colmax[tid]) + (MODE == 0 ? 1 : 0) : -2000;
     __syncthreads();
 
     for (int mt = 0; mt < nmt_m && ok; ++mt) {
@@ -277,17 +277,18 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
             if (!ok) break;
             tc_fence_after();
             const uint32_t a0 = smem_u32(sA + s * ASTAGE), b0 = smem_u32(sB + s * BSTAGE);
+            // table digit t times the field digits s = 0 .. NO-1-t in one MMA of N (NO - t) columns: the
+            // field digits lie side by side in shared memory and the orders d = t + s side by side in
+            // tensor memory, so the product of digit s lands on order t + s
 #pragma unroll
             for (int par = 0; par < 2; ++par)
 #pragma unroll
-              for (int d = 0; d < NO; ++d)
-#pragma unroll
-                for (int t = 0; t <= d; ++t) {
-                  if (t >= NS || d - t >= NS) continue;
-                  const uint64_t ad = sdesc(a0 + (par * NS + t) * XS_ATILE, XS_LBO, XS_SBO);
-                  const uint64_t bd = sdesc(b0 + (par * NS + (d - t)) * BT, XS_LBO, XS_SBO);
-                  umma_bf16(tmem + (uint32_t)((d * 2 + par) * N), ad, bd, idesc, (kc > 0 || t > 0) ? 1u : 0u);
-                }
+              for (int t = 0; t < NO; ++t) {
+                const uint64_t ad = sdesc(a0 + (par * NS + t) * XS_ATILE, XS_LBO, XS_SBO);
+                const uint64_t bd = sdesc(b0 + (par * NS) * BT, XS_LBO, XS_SBO);
+                umma_bf16(tmem + (uint32_t)((par * NO + t) * N), ad, bd, idesc_bf16(128, (NO - t) * N),
+                          (kc > 0 || t > 0) ? 1u : 0u);
+              }
             umma_commit(&bar_mma[s]);
           }
         }
@@ -356,73 +357,9 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
         const int row = mt * 128 + lq * 32 + lane;
         const uint32_t lrow = (uint32_t)(lq * 32) << 16;
         const int c0 = cg * 8;
-        if constexpr (NO <= 6) {
-          // mixed form: the orders summed in double-float (hi, lo) per parity and column
-          float H[2][8], L[2][8];
-#pragma unroll
-          for (int par = 0; par < 2; ++par) {
-            uint32_t g[NO][8];
-#pragma unroll
-            for (int d = 0; d < NO; ++d) tmem_ld8_nw(tmem + lrow + (uint32_t)((d * 2 + par) * N + c0), g[d]);
-            tmem_wait_ld();
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              float gg[NO];
-#pragma unroll
-              for (int d = 0; d < NO; ++d) gg[d] = __uint_as_float(g[d][c]);
-              xs_orders_df<NO>(gg, w, H[par][c], L[par][c]);
-            }
-          }
-          const int eo = -2 * w;   // sum_d G_d 2^(-w d) carries the scale 2^(EA + EB - 2w)
-          if (MODE == 0) {
-#pragma unroll
-            for (int par = 0; par < 2; ++par) {
-              const int j = 2 * row + par;
-              if (row >= nrows || j >= nn) continue;
-              const int EA = a.aexp[(size_t)(m * 2 + par) * a.nrp + row];
-#pragma unroll
-              for (int c = 0; c < 8; c += 2) {
-                const int n = c0 + c, zo = z0 + (n >> 1);
-                if (zo >= a.nzdim) continue;
-                const bool okr = EA > -2000 && colexp[n] > -2000, oki = EA > -2000 && colexp[n + 1] > -2000;
-                const double re = okr ? xs_df_to_double(H[par][c], L[par][c], EA + colexp[n] + eo) : 0.0;
-                const double im = oki ? xs_df_to_double(H[par][c + 1], L[par][c + 1], EA + colexp[n + 1] + eo) : 0.0;
-                a.out[j + (size_t)a.nrdim * (m + (size_t)a.npdim * zo)] = make_double2(re, im);
-              }
-            }
-          } else {
-            const int i = row;
-            if (i < a.nrh) {
-              const int EA = a.aexp[(size_t)m * a.nrp + i];
-              const double lnv = (a.add_ln && m == 0) ? *a.lnp : 0.0;
-#pragma unroll
-              for (int c = 0; c < 8; c += 2) {
-                const int n = c0 + c, zo = z0 + (n >> 1);
-                if (zo >= a.nzdim) continue;
-                double v[4] = {0.0, 0.0, 0.0, 0.0};   // f(i) re, im; f(nr-1-i) re, im
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                  const int E = colexp[n + q];
-                  if (EA > -2000 && E > -2000) {
-                    // D_0 +- D_1 in double-float: both parities share the scales
-                    float sh = H[0][c + q], sl = L[0][c + q], dh = sh, dl = sl;
-                    xs_df_add(sh, sl, H[1][c + q]);
-                    sl = __fadd_rn(sl, L[1][c + q]);
-                    xs_df_add(dh, dl, -H[1][c + q]);
-                    dl = __fsub_rn(dl, L[1][c + q]);
-                    v[q] = xs_df_to_double(sh, sl, EA + E + eo);
-                    v[2 + q] = xs_df_to_double(dh, dl, EA + E + eo);
-                  }
-                }
-                if (lnv != 0.0) { v[0] += lnv * a.lnx[i]; v[2] += lnv * a.lnx[a.nr - 1 - i]; }
-                const size_t b0 = (size_t)a.nrdim * (m + (size_t)a.npdim * zo);
-                a.out[b0 + i] = make_double2(v[0], v[1]);
-                a.out[b0 + a.nr - 1 - i] = make_double2(v[2], v[3]);
-              }
-            }
-          }
-        } else {
-          // plain form: the orders combined exactly in 64-bit integers
+        {
+          // the orders combined exactly in 64-bit integers, T = sum_d G_d 2^(w (NO-1-d) - esh), on the
+          // integer pipe; T 2^(EA + EB + esh - w (NO+1)) is then rounded once to FP64
         long long T[2][8];
 #pragma unroll
         for (int par = 0; par < 2; ++par)
@@ -431,13 +368,14 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
 #pragma unroll
         for (int d = 0; d < NO; ++d) {
           const int sh = w * (NO - 1 - d) - a.esh;
+          uint32_t g[2][8];
 #pragma unroll
-          for (int par = 0; par < 2; ++par) {
-            float v[8];
-            tmem_ld8(tmem + lrow + (uint32_t)((d * 2 + par) * N + c0), v);
+          for (int par = 0; par < 2; ++par) tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + d) * N + c0), g[par]);
+          tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < 8; ++c) T[par][c] += xs_shl((long long)xs_f2i(v[c]), sh);
-          }
+          for (int par = 0; par < 2; ++par)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) T[par][c] += xs_shl((long long)xs_f2i(__uint_as_float(g[par][c])), sh);
         }
         const int eo = a.esh - w * (NO + 1);
         if (MODE == 0) {
@@ -521,8 +459,12 @@ void xs_free() {
     }
 }
 
-// the digit configuration: FP64-grade (plain: 63 or 60 bits) or the mixed form's 35 (36) bits; w = 7
-// while the orders stay exact (K (pairs) 2^14 < 2^24), else w = 6 with one digit more.  The plain form
+// the digit configuration: FP64-grade (plain: 63 or 60 bits) or the mixed form's 42 bits; w = 7 while
+// the orders stay exact (K (pairs) 2^14 < 2^24), else w = 6 with one digit more.  The mixed form
+// needs 42 bits: its transform errors are deterministic, so a slowly changing flow meets the same
+// error step after step and they add up along a run; with 35-bit slices the backward transforms alone
+// left the vortex step's nonlinear term 9.6e-7 from the FP64 form after 1000 steps at 192 x 128 x 128,
+// with 42 bits the whole mixed step stayed within 7e-7.  The plain form
 // needs more than 53 bits: the rounding is relative to the column maximum, and the nonlinear term's
 // curl cancellation magnifies what that loses on small entries (at 192 x 128 x 128 the vortex step's
 // nonlinear term differed from the FP64 reference by 5e-10 with 49-bit and 2.4e-11 with 56-bit digits).
@@ -533,8 +475,8 @@ static bool xs_cfg(int kmax, bool plain, XsCfg& c) {
     if (9.0 * kmax * 128 * 128 < lim) { c = {9, 7}; return true; }
     if (10.0 * kmax * 64 * 64 < lim) { c = {10, 6}; return true; }
   } else {
-    if (5.0 * kmax * 128 * 128 < lim) { c = {5, 7}; return true; }
-    if (6.0 * kmax * 64 * 64 < lim) { c = {6, 6}; return true; }
+    if (6.0 * kmax * 128 * 128 < lim) { c = {6, 7}; return true; }
+    if (7.0 * kmax * 64 * 64 < lim) { c = {7, 6}; return true; }
   }
   return false;
 }
@@ -588,8 +530,8 @@ int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const d
     MLG_LAUNCH();
     const int nblk_t = npc * nmt * nkc;
     switch (cfg.ns) {
-      case 5: k_xs_table<5><<<nblk_t, 256, 0, G.stream>>>(G.pf, G.w, im.aexp, im.p, mode, G.nrh, G.ne, nrc, nmt, nkc, nrp, cfg.w); break;
       case 6: k_xs_table<6><<<nblk_t, 256, 0, G.stream>>>(G.pf, G.w, im.aexp, im.p, mode, G.nrh, G.ne, nrc, nmt, nkc, nrp, cfg.w); break;
+      case 7: k_xs_table<7><<<nblk_t, 256, 0, G.stream>>>(G.pf, G.w, im.aexp, im.p, mode, G.nrh, G.ne, nrc, nmt, nkc, nrp, cfg.w); break;
       case 9: k_xs_table<9><<<nblk_t, 256, 0, G.stream>>>(G.pf, G.w, im.aexp, im.p, mode, G.nrh, G.ne, nrc, nmt, nkc, nrp, cfg.w); break;
       default: k_xs_table<10><<<nblk_t, 256, 0, G.stream>>>(G.pf, G.w, im.aexp, im.p, mode, G.nrh, G.ne, nrc, nmt, nkc, nrp, cfg.w); break;
     }
@@ -617,8 +559,8 @@ int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const d
     if (mode == 0) return nz16 ? xs_launch<0, NSV, 16>(args, nitems) : xs_launch<0, NSV, 8>(args, nitems); \
     return nz16 ? xs_launch<1, NSV, 16>(args, nitems) : xs_launch<1, NSV, 8>(args, nitems);
   switch (cfg.ns) {
-    XS_CASE(5)
     XS_CASE(6)
+    XS_CASE(7)
     case 9: return mode == 0 ? xs_launch<0, 9, 8>(args, nitems) : xs_launch<1, 9, 8>(args, nitems);
     case 10: return mode == 0 ? xs_launch<0, 10, 8>(args, nitems) : xs_launch<1, 10, 8>(args, nitems);
   }

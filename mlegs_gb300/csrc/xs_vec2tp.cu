@@ -11,10 +11,10 @@
 // m V and D (kit init), one column scale per real column n over the two field components that land in
 // it (Im ur with Re up for the real part of the output, Re ur with Im up for the imaginary part;
 // the folds may double), and the digits of the folds are exact integer sums of the rounded samples.
-// Y has its own row scale (T) and column scale (uz).  The orders are combined in 128-bit integers and
-// rounded once to FP64 (the mixed form sums the orders in double-float); chi = k X - Y is one FP64 fused
-// multiply-add.  The row parity of a CTA fixes the folds, so each CTA owns one (m, parity, 128-row
-// tile, NZ complex z columns).
+// Y has its own row scale (T) and column scale (uz).  The orders of each sum are combined exactly in
+// 64-bit integers and rounded once to FP64, on the integer pipe; chi = k X - Y is one FP64 fused
+// multiply-add.  The row parity of a work item fixes the folds, so each item is one (m, parity,
+// 128-row tile, NZ complex z columns).
 //
 // Digits: NS for psi and X, NT for Y, of w bits: the mixed form's NS = 5 (35 bits) and NT = 7 (49
 // bits; 6 and 8 of 6 bits beyond about 100 radial points); w and the digit counts keep every order's
@@ -29,8 +29,10 @@
 // complex z columns).  Per K chunk of 16 radial points the table digits (m V, D and T, laid out at kit
 // init in the UMMA canonical K-major layout) arrive by one bulk copy into a two-stage ring, six warps
 // cut the field digits (ur, up and uz at i and nr-1-i, fetched in FP64 a chunk ahead) into the same
-// layout and arrive on the stage's mbarrier, and one thread issues the chunk's tcgen05.mma (M = 128,
-// N = 16, K = 16) as soon as both halves of a stage are in.  Every wait is bounded.
+// layout and arrive on the stage's mbarrier, and one thread issues the chunk's tcgen05.mma as soon as
+// both halves of a stage are in: a table digit t meets every field digit s <= n-1-t of one operand in
+// a single MMA (M = 128, N = 16 (n - t), K = 16; the field digits side by side in shared memory, the
+// orders side by side in tensor memory), 4 NS + NT MMAs per chunk.  Every wait is bounded.
 #include "common.cuh"
 #include "tc_common.cuh"
 #include "xs_common.cuh"
@@ -118,6 +120,7 @@ struct XvArgs {
   const double* ak;
   int* status;
   int nr, nrh, nrdim, npdim, nzdim, nrc, nzc, nzcu, nmt, nkc, ntr, w, m0, npc;
+  int esh_s, esh_t;   // right shifts that keep the 64-bit order sums of psi / X and of Y below 2^62
 };
 
 // NS digits for psi and X, NT for Y; 8 complex z columns per work item (N = 16).  Persistent: one CTA of
@@ -145,8 +148,7 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
   uint8_t* sB = sA + 2 * ASTAGE;                  // [2][BSTAGE]
   int* cexp = (int*)(sB + 2 * BSTAGE);            // [N]: ur/up columns
   int* fexp = cexp + N;                           // [N]: uz columns
-  unsigned long long* cmax = (unsigned long long*)(fexp + N);   // [2][N]
-  uint64_t* bars = (uint64_t*)(cmax + 2 * N);     // a[2], b[2], mma[2]
+  uint64_t* bars = (uint64_t*)(fexp + 2 * N);     // a[2], b[2], mma[2]
   uint32_t* tslot = (uint32_t*)(bars + 6);
   uint64_t* bar_a = bars;
   uint64_t* bar_b = bars + 2;
@@ -170,15 +172,15 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = idesc_bf16(128, N);
   bool ok = true;
   uint32_t it = 0;   // chunk counter (stage and phase), the same in every thread
   const int nzt = (a.nzdim + NZ - 1) / NZ;
   const int nmp = a.npc - a.m0;
   const int nitems = nmp * 2 * a.nmt * nzt;   // item = ((mi * 2 + par) * nmt + mt) * nzt + zt
-  // staging item of a digit thread: field f (0 ur, 1 up, 2 uz), z column zz, K pair kp
+  // staging item of a digit thread: field f (0 ur, 1 up, 2 uz), z column zz, K pair kp (the eight K
+  // pairs of a column in consecutive lanes, so that a warp's loads are runs of consecutive r)
   const int dt = tid - 64;
-  const int f = dt / (NZ * 8), zz = dt % NZ, kp = (dt / NZ) % 8;
+  const int f = dt / (NZ * 8), kp = dt % 8, zz = (dt / 8) % NZ;
 
   for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
     const int zt = item % nzt, mt = (item / nzt) % a.nmt, par = (item / (nzt * a.nmt)) & 1;
@@ -187,34 +189,34 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
     if (2 * (mt * 128) + par >= nn) continue;   // no rows of this parity in the tile (every thread agrees)
     const int z0 = zt * NZ;
     const int ss = par ? -1 : 1;   // own-parity fold sign
-    // ---- column scales: cexp(2zz) over (Im ur, Re up), cexp(2zz+1) over (Re ur, Im up); fexp over uz
-    if (tid < 2 * N) cmax[tid] = 0ull;
-    __syncthreads();
+    // ---- column scales: cexp(2zz) over (Im ur, Re up), cexp(2zz+1) over (Re ur, Im up); fexp over uz.
+    // Warp cz scans column z0 + cz (runs of consecutive r) for the largest exponent fields and reduces
+    // them by warp shuffles; |x| < 2^(field - 1022) for every sample, +1 because the folds may double.
     {
-      const int cz = tid % NZ, g = tid / NZ, z = z0 + cz;   // 32 threads per column
-      unsigned long long m0 = 0, m1 = 0, u0 = 0, u1 = 0;
+      static_assert(XV_THREADS / 32 == NZ, "one warp per z column");
+      const int cz = warp, z = z0 + cz;
+      unsigned e0 = 0, e1 = 0, u0 = 0, u1 = 0;
       if (z < a.nzdim) {
         const size_t cb = (size_t)a.nrdim * (m + (size_t)a.npdim * z);
-        for (int i = g; i < a.nr; i += XV_THREADS / NZ) {
+        auto ex = [](double v) { return ((unsigned)__double2hiint(v) >> 20) & 0x7FFu; };
+        for (int i = lane; i < a.nr; i += 32) {
           const double2 r = a.ur[cb + i], pq = a.up[cb + i], q = a.uz[cb + i];
-          unsigned long long v;
-          v = (unsigned long long)__double_as_longlong(r.y) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
-          v = (unsigned long long)__double_as_longlong(pq.x) & 0x7FFFFFFFFFFFFFFFull; m0 = v > m0 ? v : m0;
-          v = (unsigned long long)__double_as_longlong(r.x) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
-          v = (unsigned long long)__double_as_longlong(pq.y) & 0x7FFFFFFFFFFFFFFFull; m1 = v > m1 ? v : m1;
-          v = (unsigned long long)__double_as_longlong(q.x) & 0x7FFFFFFFFFFFFFFFull; u0 = v > u0 ? v : u0;
-          v = (unsigned long long)__double_as_longlong(q.y) & 0x7FFFFFFFFFFFFFFFull; u1 = v > u1 ? v : u1;
+          e0 = max(e0, max(ex(r.y), ex(pq.x)));
+          e1 = max(e1, max(ex(r.x), ex(pq.y)));
+          u0 = max(u0, ex(q.x));
+          u1 = max(u1, ex(q.y));
         }
       }
-      atomicMax(&cmax[2 * cz], m0);
-      atomicMax(&cmax[2 * cz + 1], m1);
-      atomicMax(&cmax[N + 2 * cz], u0);
-      atomicMax(&cmax[N + 2 * cz + 1], u1);
-    }
-    __syncthreads();
-    if (tid < N) {
-      cexp[tid] = cmax[tid] ? xs_ebound(cmax[tid]) + 1 : -2000;          // +1: the folds may double
-      fexp[tid] = cmax[N + tid] ? xs_ebound(cmax[N + tid]) + 1 : -2000;
+      e0 = __reduce_max_sync(0xFFFFFFFFu, e0);
+      e1 = __reduce_max_sync(0xFFFFFFFFu, e1);
+      u0 = __reduce_max_sync(0xFFFFFFFFu, u0);
+      u1 = __reduce_max_sync(0xFFFFFFFFu, u1);
+      if (lane == 0) {
+        cexp[2 * cz] = e0 ? (int)e0 - 1021 : -2000;
+        cexp[2 * cz + 1] = e1 ? (int)e1 - 1021 : -2000;
+        fexp[2 * cz] = u0 ? (int)u0 - 1021 : -2000;
+        fexp[2 * cz + 1] = u1 ? (int)u1 - 1021 : -2000;
+      }
     }
     __syncthreads();
     const uint8_t* img_b = (const uint8_t*)a.img + (((size_t)(m * 2 + par) * a.nmt + mt) * a.nkc) * (size_t)ASTAGE;
@@ -243,21 +245,22 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
           const uint32_t a0 = smem_u32(sA + s * ASTAGE), b0 = smem_u32(sB + s * BSTAGE);
           auto A = [&](int t) { return sdesc(a0 + t * XV_ATILE, XV_LBO, XV_SBO); };
           auto B = [&](int t) { return sdesc(b0 + t * BTILE, XV_LBO, XV_SBO); };
+          // table digit t against the field digits 0 .. n-1-t in one MMA of N (n - t) columns: the field
+          // digits lie side by side in shared memory and the accumulators of the orders side by side in
+          // tensor memory, so the product of field digit s lands on order t + s
 #pragma unroll
-          for (int d = 0; d < NS; ++d)
+          for (int t = 0; t < NS; ++t) {
+            const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
+            const uint32_t id = idesc_bf16(128, (NS - t) * N);
+            umma_bf16(tmem + t * N, A(t), B(0), id, acc);                  // psi: mV . psi_ur
+            umma_bf16(tmem + t * N, A(NS + t), B(NS), id, 1u);             //      D . psi_up
+            umma_bf16(tmem + (NS + t) * N, A(NS + t), B(2 * NS), id, acc); // X: D . X_ur
+            umma_bf16(tmem + (NS + t) * N, A(t), B(3 * NS), id, 1u);       //    mV . X_up
+          }
 #pragma unroll
-            for (int t = 0; t <= d; ++t) {
-              const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
-              umma_bf16(tmem + d * N, A(t), B(d - t), idesc, acc);                          // psi: mV . psi_ur
-              umma_bf16(tmem + d * N, A(NS + t), B(NS + d - t), idesc, 1u);                 //      D . psi_up
-              umma_bf16(tmem + (NS + d) * N, A(NS + t), B(2 * NS + d - t), idesc, acc);     // X: D . X_ur
-              umma_bf16(tmem + (NS + d) * N, A(t), B(3 * NS + d - t), idesc, 1u);           //    mV . X_up
-            }
-#pragma unroll
-          for (int d = 0; d < NT; ++d)
-#pragma unroll
-            for (int t = 0; t <= d; ++t)
-              umma_bf16(tmem + (2 * NS + d) * N, A(2 * NS + t), B(4 * NS + d - t), idesc, (kc > 0 || t > 0) ? 1u : 0u);
+          for (int t = 0; t < NT; ++t)
+            umma_bf16(tmem + (2 * NS + t) * N, A(2 * NS + t), B(4 * NS), idesc_bf16(128, (NT - t) * N),
+                      (kc > 0 || t > 0) ? 1u : 0u);
           umma_commit(&bar_mma[s]);
         }
       __syncwarp();
@@ -352,32 +355,47 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
 #pragma unroll 1
       for (int half = 0; half < 2; ++half) {   // four columns (two complex z) at a time
         const int c0 = cb * 8 + half * 4;
-        double pv[4], xv[4], yv[4];
-        // the orders summed in double-float
-        uint32_t gp[NS][4], gx[NS][4], gy[NT][4];
+        // the orders combined exactly in 64-bit integers, T = sum_d G_d 2^(w (n-1-d) - esh), then
+        // T 2^(row exp + column exp + esh - w (n+1)) rounded once to FP64
+        long long tp[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0};
+        {
+          uint32_t gp[NS][4], gx[NS][4];
 #pragma unroll
-        for (int d = 0; d < NS; ++d) {
-          tmem_ld4_nw(tmem + lrow + d * N + c0, gp[d]);
-          tmem_ld4_nw(tmem + lrow + (NS + d) * N + c0, gx[d]);
+          for (int d = 0; d < NS; ++d) {
+            tmem_ld4_nw(tmem + lrow + d * N + c0, gp[d]);
+            tmem_ld4_nw(tmem + lrow + (NS + d) * N + c0, gx[d]);
+          }
+          tmem_wait_ld();
+#pragma unroll
+          for (int d = 0; d < NS; ++d) {
+            const int sh = w * (NS - 1 - d) - a.esh_s;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              tp[c] += xs_shl((long long)xs_f2i(__uint_as_float(gp[d][c])), sh);
+              tx[c] += xs_shl((long long)xs_f2i(__uint_as_float(gx[d][c])), sh);
+            }
+          }
         }
+        {
+          uint32_t gy[NT][4];
 #pragma unroll
-        for (int d = 0; d < NT; ++d) tmem_ld4_nw(tmem + lrow + (2 * NS + d) * N + c0, gy[d]);
-        tmem_wait_ld();
+          for (int d = 0; d < NT; ++d) tmem_ld4_nw(tmem + lrow + (2 * NS + d) * N + c0, gy[d]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int d = 0; d < NT; ++d) {
+            const int sh = w * (NT - 1 - d) - a.esh_t;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ty[c] += xs_shl((long long)xs_f2i(__uint_as_float(gy[d][c])), sh);
+          }
+        }
+        double pv[4], xv[4], yv[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int E = cexp[c0 + c], F = fexp[c0 + c];
-          float g1[NS], g2[NS], g3[NT], h, l;
-#pragma unroll
-          for (int d = 0; d < NS; ++d) { g1[d] = __uint_as_float(gp[d][c]); g2[d] = __uint_as_float(gx[d][c]); }
-#pragma unroll
-          for (int d = 0; d < NT; ++d) g3[d] = __uint_as_float(gy[d][c]);
           const bool ox = er > -2000 && E > -2000, oy = et > -2000 && F > -2000;
-          xs_orders_df<NS>(g1, w, h, l);
-          pv[c] = ox ? xs_df_to_double(h, l, er + E - 2 * w) : 0.0;
-          xs_orders_df<NS>(g2, w, h, l);
-          xv[c] = ox ? xs_df_to_double(h, l, er + E - 2 * w) : 0.0;
-          xs_orders_df<NT>(g3, w, h, l);
-          yv[c] = oy ? xs_df_to_double(h, l, et + F - 2 * w) : 0.0;
+          pv[c] = ox ? xs_i64_to_double(tp[c], er + E + a.esh_s - w * (NS + 1)) : 0.0;
+          xv[c] = ox ? xs_i64_to_double(tx[c], er + E + a.esh_s - w * (NS + 1)) : 0.0;
+          yv[c] = oy ? xs_i64_to_double(ty[c], et + F + a.esh_t - w * (NT + 1)) : 0.0;
         }
         if (rok) {
 #pragma unroll
@@ -447,7 +465,7 @@ template <int NS, int NT>
 static int xv_launch(const XvArgs& args, int npc) {
   constexpr int N = 2 * XV_NZ;
   const size_t sm = 1024 + 2 * (size_t)(2 * NS + NT) * XV_ATILE + 2 * (size_t)(4 * NS + NT) * N * XV_KC * 2 +
-                    2 * N * sizeof(int) + 2 * N * sizeof(unsigned long long) + 64;
+                    4 * N * sizeof(int) + 64;
   auto kern = k_xv_contract<NS, NT>;
   MLG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const int nitems = (npc - args.m0) * 2 * args.nmt * cdiv(G.nzdim, XV_NZ);
@@ -490,6 +508,16 @@ int xv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int 
   args.nr = G.nr; args.nrh = G.nrh; args.nrdim = G.nrdim; args.npdim = G.npdim; args.nzdim = G.nzdim; args.nrc = nrc;
   args.nzc = G.chopzl; args.nzcu = G.chopzu; args.nmt = nmt; args.nkc = nkc; args.ntr = ntr; args.w = cfg.w; args.m0 = m0;
   args.npc = npc;
+  {
+    // the 64-bit order sums stay below 2^62: |G_d| <= K (pairs of order d) 2^(2w), with two products
+    // per digit pair for psi and X
+    auto esh = [&](int n, int pairs) {
+      const double mx = (double)G.nrh * pairs * (1 << cfg.w) * (1 << cfg.w);
+      return std::max(0, (int)std::ceil(std::log2(mx) + 0.05) + cfg.w * (n - 1) - 62);
+    };
+    args.esh_s = esh(cfg.ns, 2 * cfg.ns);
+    args.esh_t = esh(cfg.nt, cfg.nt);
+  }
   // 8 complex z columns per work item: the (2 NS + NT) orders of 2 x 8 columns fit the 512
   // tensor-memory columns
   if (cfg.ns == 5) return xv_launch<5, 7>(args, npc);

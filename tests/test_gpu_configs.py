@@ -5,7 +5,10 @@
   febe and (separately) 100 abcn diffusion steps with nu = 1e-3, dt = 1e-3 (mlegs_scalar_ops.f90:
   1157-1262), against the oracle: 1e-12 for the transforms, 1e-11 for the steps.
 * The 3-D vortex step at the metric's grid, 192 x 128 x 128, in the plain form against the oracle:
-  3 steps from the same state at 1e-11.
+  3 steps from the same state, psi, chi and nlpsi at 1e-11 and nlchi at 5e-11.  nlchi ends in
+  k X - Y and the inverse Laplacian, which cancel: two FP64 evaluations that only order their sums
+  differently (this library's all-DFMA contractions and the oracle) already differ by up to 2.4e-11
+  there after one step.
 * The q-vortex closed forms (docs/tutorial/vector_field.md:88-106) through the CUDA path: tp2vec,
   tp2curlvec and vec2tp of the off-centre and the centred vortex, and the vanishing nonlinear term of
   the axisymmetric vortex, in both precision forms.
@@ -93,8 +96,8 @@ def test_c3_plain_vortex_steps_match_oracle():
     for _ in range(3):
         vortex.step(k, sg, bench.DT)
         vortex.step(o, so, bench.DT)
-    for n in ("psi", "chi", "nlpsi", "nlchi"):
-        compare(getattr(sg, n), getattr(so, n), 1e-11, what=f"C3 3 steps {n}")
+    for n, tol in (("psi", 1e-11), ("chi", 1e-11), ("nlpsi", 1e-11), ("nlchi", 5e-11)):
+        compare(getattr(sg, n), getattr(so, n), tol, what=f"C3 3 steps {n}")
     k.close()
     o.close()
 
