@@ -144,6 +144,7 @@ int launch_vfft_multi(Scalar* const* s, int n, int dir);   // n <= 6 fields in o
 int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir);
 int launch_rtrans_fwd(Scalar& s);
 int launch_rtrans_bwd(Scalar& s, bool add_ln);
+int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln);   // n <= 3 fields, one launch
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
 void lu_cache_clear();
 void tc_free();
@@ -154,6 +155,8 @@ int wait_selftest(long long limit, int arrive);
 // m0 <= m < npc; plain: FP64-grade digits, else the mixed form's
 bool xs_supported(int mode, int nrc, bool plain);
 int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const double* lnp, bool add_ln, bool plain);
+int xs_rtrans_multi(int mode, const cd* const* in, cd* const* out, int nf, int nrc, int npc, int m0,
+                    const double* const* lnp, bool add_ln, bool plain);
 void xs_free();
 // the mixed form's projection contraction as exact slices (xs_vec2tp.cu): psi, chi rows of
 // m0 <= m < npc written

@@ -21,6 +21,7 @@
 // [point][TR] and runs a Stockham autosort FFT (radix 4, 2, 3, 5) between two shared buffers.
 #include "common.cuh"
 #include "dfloat.cuh"
+#include "xs_common.cuh"
 #include <type_traits>
 
 namespace mlg {
@@ -68,10 +69,28 @@ __device__ __forceinline__ dfl2 load_tw<dfl>(const float4* tw, int idx, int sgn)
   const dfl im(w.z, w.w);
   return mk<dfl>(dfl(w.x, w.y), sgn < 0 ? im : -im);
 }
-// a transform value to FP64 (FP32 and double-float exactly on the integer pipe, then one FP64 add)
+// h + l rounded to FP64 on the integer pipe, for a normalised double-float (|l| <= ulp(h)/2, so l's
+// exponent is at least 23 below h's): both significands in one 64-bit integer, h's at bits 38..61,
+// then one rounding; GB300's FP64 pipe (about 2 operations per clock per SM) stays free
+__device__ __forceinline__ double df_to_double(float h, float l) {
+  const unsigned bh = __float_as_uint(h), bl = __float_as_uint(l);
+  const int eh = (int)((bh >> 23) & 0xFFu), el = (int)((bl >> 23) & 0xFFu);
+  if (eh == 0) return f2d_fast(l);
+  long long X = (long long)((bh & 0x7FFFFFu) | 0x800000u) << 38;
+  if (bh >> 31) X = -X;
+  const int d = eh - el;
+  if (el != 0 && d < 62) {
+    const long long ml = (long long)((bl & 0x7FFFFFu) | 0x800000u);
+    const long long L = d <= 38 ? (ml << (38 - d)) : (ml >> (d - 38));
+    X += (bl >> 31) ? -L : L;
+  }
+  return xs_i64_to_double(X, eh - 150 - 38);
+}
+// a transform value to FP64 (FP32 and double-float on the integer pipe)
 __device__ __forceinline__ double to_dbl(double v) { return v; }
 __device__ __forceinline__ double to_dbl(float v) { return f2d_fast(v); }
-__device__ __forceinline__ double to_dbl(dfl v) { return f2d_fast(v.h) + f2d_fast(v.l); }
+__device__ __forceinline__ double to_dbl(dfl v) { return df_to_double(v.h, v.l); }
+
 // a double-float sample in the transform's arithmetic
 template <typename T> __device__ __forceinline__ T from_df(dfl v);
 template <> __device__ __forceinline__ float from_df<float>(dfl v) { return v.h; }

@@ -939,11 +939,9 @@ static int to_ppp_batch(Scalar* const* f, const bool* by_r, int n) {
     if (G.nz > 1) MLG_TRY(vfft_check(*f[i], +1));
   }
   if (G.nz > 1) MLG_TRY(launch_vfft_multi(f, n, +1));
-  for (int i = n - 1; i >= 0; --i) {   // the last z output first: it is the likeliest still in L2
-    f[i]->set_space("FFP");
-    MLG_TRY(launch_rtrans_bwd(*f[i], true));
-    f[i]->set_space("PFP");
-  }
+  for (int i = 0; i < n; ++i) f[i]->set_space("FFP");
+  MLG_TRY(launch_rtrans_bwd_multi(f, n, true));   // one launch over the n fields
+  for (int i = 0; i < n; ++i) f[i]->set_space("PFP");
   if (G.np > 1) {
     const double* rs[6];
     for (int i = 0; i < n; ++i) rs[i] = by_r[i] ? G.rinv : nullptr;

@@ -514,6 +514,56 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   return 0;
 }
 
+// the backward transforms of n fields (n <= 3, the components of a vector field) with the same chop:
+// one tensor-core launch over all of them (and the m = 0 planes beside it), else field by field
+int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln) {
+  if (n == 1) return launch_rtrans_bwd(*f[0], add_ln);
+  int nrc = 0, npc = 0;
+  for (int i = 0; i < n; ++i) {
+    int a, b;
+    MLG_TRY(rtrans_check(*f[i], a, b, "rtrans_backward"));
+    if (i == 0) { nrc = a; npc = b; }
+    if (a != nrc || b != npc || n > 3) {   // different chops: one at a time
+      for (int k = 0; k < n; ++k) MLG_TRY(launch_rtrans_bwd(*f[k], add_ln));
+      return 0;
+    }
+  }
+  const bool mixed = G.precision == MLG_MIXED;
+  const bool xs = xs_supported(1, nrc, !mixed);
+  if (!xs || npc < 1) {
+    for (int k = 0; k < n; ++k) MLG_TRY(launch_rtrans_bwd(*f[k], add_ln));
+    return 0;
+  }
+  cd* out[3] = {nullptr, nullptr, nullptr};
+  const cd* in[3] = {nullptr, nullptr, nullptr};
+  const double* lnp[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < n; ++i) {
+    out[i] = get_buf();
+    if (!out[i]) {
+      for (int k = 0; k < i; ++k) put_buf(out[k]);
+      return set_error(MLG_EALLOC, "rtrans_backward: out of device memory");
+    }
+    in[i] = f[i]->e;
+    lnp[i] = f[i]->ln;
+    MLG_TRY(launch_zero_tails(out[i], 1, nrc, npc, G.nzdim, G.nzdim + 1));
+  }
+  kt_begin(KT_RBWD);
+  if (mixed) MLG_TRY(m0_tab());
+  MLG_TRY(side_fork());
+  for (int i = 0; i < n; ++i) {   // m = 0 beside: double-float (mixed) or FP64 DFMA (plain)
+    if (mixed) MLG_TRY(m0_rtrans_bwd(in[i], out[i], nrc, lnp[i], add_ln, G.side));
+    else MLG_TRY(dfma_rtrans_bwd(in[i], out[i], nrc, 1, lnp[i], add_ln, G.side));
+  }
+  MLG_TRY(xs_rtrans_multi(1, in, out, n, nrc, npc, 1, lnp, add_ln, !mixed));   // m >= 1, all fields
+  MLG_TRY(side_join());
+  kt_end(KT_RBWD, n * fwd_flops(nrc, npc));
+  for (int i = 0; i < n; ++i) {
+    put_buf(f[i]->e);
+    f[i]->e = out[i];
+  }
+  return 0;
+}
+
 // ur, up, uz in (r physical, m, k) space; psi and chi written in full
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off) {
   int nrc = G.nrchop + nrc_off, npc = G.npchop;

@@ -12,6 +12,7 @@
 #pragma once
 #include "common.cuh"
 #include <cstdint>
+#include <type_traits>
 
 namespace mlg {
 
@@ -52,31 +53,35 @@ __device__ __forceinline__ uint32_t xs_pack(float a, float b) { return __byte_pe
 // the exact integer value of an FP32 accumulator entry (integral, |x| < 2^24)
 __device__ __forceinline__ int xs_f2i(float x) { return __float2int_rn(x); }
 
+// f(std::integral_constant<int, 0>()), ..., f(std::integral_constant<int, N-1>())
+template <int I, int N, class F> __device__ __forceinline__ void xs_static_for_(F& f) {
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>());
+    xs_static_for_<I + 1, N>(f);
+  }
+}
+template <int N, class F> __device__ __forceinline__ void xs_static_for(F f) { xs_static_for_<0, N>(f); }
+
 // x 2^s for s >= 0, floor(x 2^s) for s < 0
 __device__ __forceinline__ long long xs_shl(long long x, int s) { return s >= 0 ? (x << s) : (x >> (-s)); }
 
 // T 2^e2 rounded once to FP64 (round to nearest even), T a signed 64-bit integer; magnitudes below the
-// normal range flush to zero
+// normal range flush to zero.  Branch-free on the integer pipe: normalise |T| so that its top bit is
+// bit 63, keep 53 bits, round on the 11 below them, and let the implicit bit (and a rounding carry)
+// add into the exponent field.
 __device__ __forceinline__ double xs_i64_to_double(long long T, int e2) {
-  if (T == 0) return 0.0;
   const unsigned long long sign = (unsigned long long)T & 0x8000000000000000ull;
-  const unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
-  int top = 63 - __clzll((long long)a);
-  unsigned long long mant;
-  if (top <= 52) {
-    mant = a << (52 - top);
-  } else {
-    const int sh = top - 52;
-    unsigned long long m = a >> sh;
-    const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (m & 1))) m += 1;
-    if (m >> 53) { m >>= 1; ++top; }
-    mant = m;
-  }
-  const int ex = top + e2 + 1023;
-  if (ex <= 0) return __longlong_as_double((long long)sign);
+  const unsigned long long a = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+  const int lz = __clzll((long long)a);
+  const unsigned long long n = a << (lz & 63);                    // bit 63 set (a != 0)
+  unsigned long long m = n >> 11;                                 // 53 bits, the implicit one on top
+  const unsigned long long rb = (n >> 10) & 1ull, st = (n & 0x3FFull) != 0ull;
+  m += rb & (st | (m & 1ull));
+  const long long ex = (long long)(1023 + 63 - lz + e2);          // biased exponent of 2^(top bit)
+  const unsigned long long bits = ((unsigned long long)(ex - 1) << 52) + m;
+  if (a == 0ull || ex <= 0) return __longlong_as_double((long long)sign);
   if (ex >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
-  return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  return __longlong_as_double((long long)(sign | bits));
 }
 
 // y 2^e2 as FP64, exactly (FP32 subnormals and results below the normal range give zero)

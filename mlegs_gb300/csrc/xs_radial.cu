@@ -118,16 +118,23 @@ __global__ void k_xs_table(const double* __restrict__ pf, const double* __restri
 }
 
 // ------------------------------------------------------------------------------------------------
+// up to XS_NF fields with the same chop, transformed by one launch (the components of a vector field)
+constexpr int XS_NF = 3;
 struct XsArgs {
-  const double2* in;
-  double2* out;
+  const double2* in[XS_NF];
+  double2* out[XS_NF];
+  const double* lnp[XS_NF];
   const uint16_t* img;
   const int* aexp;
   const double* lnx;
-  const double* lnp;
   int* status;
-  int add_ln, nr, nrh, nrdim, npdim, nzdim, nrc, m0, npc, nmt, nkc, nrp, rawk, wbits, esh;
+  int add_ln, nf, nr, nrh, nrdim, npdim, nzdim, nrc, m0, npc, nmt, nkc, nrp, rawk;
 };
+// field f's pointer without an indexed access to the kernel parameters (which would copy them to local
+// memory)
+template <class P> __device__ __forceinline__ P xs_sel(const P (&p)[XS_NF], int f) {
+  return f == 0 ? p[0] : (f == 1 ? p[1] : p[2]);
+}
 
 __device__ __forceinline__ bool xs_wait(uint64_t* bar, uint32_t phase, bool& ok) {
   if (!ok) return false;
@@ -137,50 +144,99 @@ __device__ __forceinline__ bool xs_wait(uint64_t* bar, uint32_t phase, bool& ok)
 
 
 
-// MODE 0 forward, 1 backward; NS digits, NO orders, NZ complex z columns per item
-template <int MODE, int NS, int NO, int NZ>
+// Warp roles of the contraction kernel (512 threads, one CTA per SM):
+//   warp 0      producer: the item's field columns and the table chunks, by bulk copy
+//   warp 1      MMA issue (one thread) and the tensor-memory allocation
+//   warps 2..7  column scales and field digits
+//   warps 8..15 epilogue: tensor memory -> 64-bit order sums -> FP64 results
+// Every hand-off is an mbarrier: the table chunks and the field-digit stages are rings (2 and XS_SB
+// stages), the field columns are one buffer (the next item's columns land while the MMAs and the
+// epilogue of this one run), the accumulators are released by the epilogue as soon as it has read
+// them, so the MMAs of the next work unit overlap the FP64 conversion and the stores of this one.
+// a bounded wait whose outcome every lane of the warp shares (the warp-collective operations that
+// follow need the whole warp)
+__device__ __forceinline__ bool xs_wait_w(uint64_t* bar, uint32_t phase, bool& ok) {
+  xs_wait(bar, phase, ok);
+  ok = __all_sync(0xFFFFFFFFu, ok);
+  return ok;
+}
+
+constexpr int XS_SB = 3;                 // field-digit stages
+constexpr int XS_NDW = 6, XS_NEW = 8;    // digit warps (2..7), epilogue warps (8..15)
+constexpr int XS_NDIG = XS_NDW * 32, XS_NEPI = XS_NEW * 32;
+static_assert(2 + XS_NDW + XS_NEW == XS_THREADS / 32, "warp roles");
+
+// MODE 0 forward, 1 backward; NS digits (and orders), NZ complex z columns per item
+// digit width of a digit count (xs_cfg): 7 bits for 6 and 9 digits, 6 bits for 7 and 10
+template <int NS> __host__ __device__ constexpr int xs_w() { return (NS == 6 || NS == 9) ? 7 : 6; }
+// right shift of the 64-bit order sums: |G_d| < 2^24 / (pairs) keeps sum_d G_d 2^(w (NS-1-d) - ESH)
+// below 2^62
+template <int NS> __host__ __device__ constexpr int xs_esh() {
+  return 24 + xs_w<NS>() * (NS - 1) - 62 > 0 ? 24 + xs_w<NS>() * (NS - 1) - 62 : 0;
+}
+// T += v 2^SH (floor for SH < 0), SH a compile-time constant: one wide multiply-add for 0 <= SH <= 30
+template <int SH> __device__ __forceinline__ void xs_acc(long long& T, int v) {
+  if constexpr (SH > 30) T += (long long)v << SH;
+  else if constexpr (SH >= 0) T += (long long)v * (long long)(1 << SH);
+  else T += (long long)v >> (-SH);
+}
+template <int NO, int W, int ESH, int D> __device__ __forceinline__ void xs_acc_order(long long& T, uint32_t g) {
+  xs_acc<W * (NO - 1 - D) - ESH>(T, xs_f2i(__uint_as_float(g)));
+}
+
+template <int MODE, int NS, int NZ>
 __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
-  constexpr int N = 2 * NZ;                       // real columns (MMA N)
+  constexpr int NO = NS;
+  constexpr int W = xs_w<NS>(), ESH = xs_esh<NS>();
+  constexpr int N = 2 * NZ;                       // real columns (MMA N per digit)
   constexpr int BT = N * XS_KC * 2;               // B digit tile bytes
   constexpr int ASTAGE = 2 * NS * XS_ATILE;
   constexpr int BSTAGE = 2 * NS * BT;
   constexpr int TCOLS = 2 * NO * N <= 32 ? 32 : 2 * NO * N <= 64 ? 64 : 2 * NO * N <= 128 ? 128 : 2 * NO * N <= 256 ? 256 : 512;
-  constexpr int NW = XS_THREADS / 32;
-  constexpr int CGW = N / 8 < 4 ? N / 8 : 4;      // column groups of 8 in the epilogue (one per 4 warps)
-  constexpr int NDW = NW - 2;                     // digit warps: 2 .. NW-1
-  constexpr int NDIG = NDW * 32;
-  // staging blocks per chunk: (8 columns, 4 K pairs) and, backward, the parity (forward, a block writes
-  // both parities from the same two samples)
-  constexpr int NBLK = (MODE == 0 ? 1 : 2) * (N / 8) * 2;
+  constexpr int NBLK = (MODE == 0 ? 1 : 2) * (N / 8) * 2;   // digit blocks per chunk
+  constexpr int CPW = N / 16;                     // 8-column groups of an epilogue warp
   static_assert(2 * NO * N <= 512, "accumulators exceed tensor memory");
-  static_assert(NO <= NS, "every order's first product (t = 0) resets its accumulator");
-  static_assert(N % 16 == 0 && N >= 16 && N <= 32, "MMA N");
-  static_assert(NW == 16, "the epilogue map assumes 16 warps");
+  static_assert(N == 16 || N == 32, "MMA N per digit");
+  static_assert((NO - 1) * N + N <= 256, "MMA N of the widest digit product");
   extern __shared__ __align__(1024) uint8_t xs_smem_raw[];
   uint8_t* sbase = (uint8_t*)(((uintptr_t)xs_smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = sbase;                                   // [2 stages][ASTAGE]
-  uint8_t* sB = sA + 2 * ASTAGE;                         // [2 stages][BSTAGE]
-  double* raw = (double*)(sB + 2 * BSTAGE);              // [NZ][rawk] complex (re, im)
-  int* colexp = (int*)(raw + (size_t)2 * NZ * a.rawk);   // [N]
-  uint64_t* bars = (uint64_t*)(colexp + 2 * N);         // raw, a[2], b[2], mma[2]
-  uint32_t* tslot = (uint32_t*)(bars + 7);
-  uint64_t* bar_raw = bars;
-  uint64_t* bar_a = bars + 1;     // table stage filled (bulk copy)
-  uint64_t* bar_b = bars + 3;     // field-digit stage written (the digit warps)
-  uint64_t* bar_mma = bars + 5;   // the stage's MMAs completed (tcgen05.commit)
+  uint8_t* sA = sbase;                                   // [2][ASTAGE]
+  uint8_t* sB = sA + 2 * ASTAGE;                         // [XS_SB][BSTAGE]
+  double* raw = (double*)(sB + XS_SB * BSTAGE);          // [NZ][rawk] complex (re, im)
+  int* colexp = (int*)(raw + (size_t)2 * NZ * a.rawk);   // [2][N]: by item parity
+  uint64_t* bars = (uint64_t*)(colexp + 2 * N);
+  uint64_t* bar_rf = bars;                 // field columns landed
+  uint64_t* bar_re = bars + 1;             // field columns consumed (digit threads)
+  uint64_t* bar_af = bars + 2;             // [2] table chunk landed
+  uint64_t* bar_ae = bars + 4;             // [2] table chunk consumed (MMA commit)
+  uint64_t* bar_bf = bars + 6;             // [XS_SB] digit stage written (digit threads)
+  uint64_t* bar_be = bar_bf + XS_SB;       // [XS_SB] digit stage consumed (MMA commit)
+  uint64_t* bar_tf = bar_be + XS_SB;       // accumulators complete (MMA commit)
+  uint64_t* bar_te = bar_tf + 1;           // accumulators read (epilogue threads)
+  uint64_t* bar_cx = bar_te + 1;           // [2] column scales written (digit threads), by item parity
+  uint64_t* bar_ce = bar_cx + 2;           // [2] column scales read (epilogue threads), by item parity
+  uint32_t* tslot = (uint32_t*)(bar_ce + 2);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int w = a.wbits, nb = w * NS;
+  constexpr int w = W, nb = W * NS;
   if (tid == 0) {
-    mbar_init(bar_raw, 1);
+    mbar_init(bar_rf, 1);
+    mbar_init(bar_re, XS_NDIG);
     for (int i = 0; i < 2; ++i) {
-      mbar_init(bar_a + i, 1);
-      mbar_init(bar_b + i, NDIG);
-      mbar_init(bar_mma + i, 1);
+      mbar_init(bar_af + i, 1);
+      mbar_init(bar_ae + i, 1);
+      mbar_init(bar_cx + i, XS_NDIG);
+      mbar_init(bar_ce + i, XS_NEPI);
     }
+    for (int i = 0; i < XS_SB; ++i) {
+      mbar_init(bar_bf + i, XS_NDIG);
+      mbar_init(bar_be + i, 1);
+    }
+    mbar_init(bar_tf, 1);
+    mbar_init(bar_te, XS_NEPI);
     fence_mbar_init();
   }
-  if (warp == 0) {
+  if (warp == 1) {
     tmem_alloc(tslot, TCOLS);
     tmem_relinquish();
   }
@@ -189,94 +245,86 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   tc_fence_after();
   const uint32_t tmem = *tslot;
   bool ok = true;
-  uint32_t it = 0, raw_ph = 0;                  // chunk counter (stage and phase), raw-copy phase
+
+  // the CTA's items (field, m, z tile), item = ((m - m0) nzt + z tile) nf + field, those without rows
+  // skipped; every role walks the same sequence
   const int nzt = (a.nzdim + NZ - 1) / NZ;
-  const int nitems = (a.npc - a.m0) * nzt;
-  // the items of this CTA, skipping those without rows (every thread walks the same sequence)
-  auto item_nn = [&](int item) { const int m = a.m0 + item / nzt; return max(min(a.nrc, a.nrc - m), 0); };
+  const int nitems = (a.npc - a.m0) * nzt * a.nf;
+  auto item_m = [&](int item) { return a.m0 + item / (nzt * a.nf); };
+  auto item_z0 = [&](int item) { return ((item / a.nf) % nzt) * NZ; };
+  auto item_nn = [&](int item) { const int m = item_m(item); return max(min(a.nrc, a.nrc - m), 0); };
   auto next_item = [&](int item) {
     for (item += gridDim.x; item < nitems && item_nn(item) == 0; item += gridDim.x) {}
     return item;
   };
-  auto issue_raw = [&](int item) {   // tid 0: the item's field columns into shared memory
-    const int m = a.m0 + item / nzt, z0 = (item % nzt) * NZ;
-    const int kraw = MODE == 0 ? a.nr : item_nn(item);
-    fence_async_smem();
-    uint32_t bytes = 0;
-    for (int zz = 0; zz < NZ; ++zz)
-      if (z0 + zz < a.nzdim) bytes += (uint32_t)kraw * 16u;
-    mbar_expect_tx(bar_raw, bytes);
-    for (int zz = 0; zz < NZ; ++zz)
-      if (z0 + zz < a.nzdim)
-        bulk_g2s(raw + (size_t)2 * zz * a.rawk, a.in + (size_t)a.nrdim * (m + (size_t)a.npdim * (z0 + zz)),
-                 (uint32_t)kraw * 16u, bar_raw);
-  };
-  int item = blockIdx.x;
-  while (item < nitems && item_nn(item) == 0) item += gridDim.x;
-  if (tid == 0 && item < nitems) issue_raw(item);
-
-  for (; item < nitems && ok; item = next_item(item)) {
-    const int m = a.m0 + item / nzt, z0 = (item % nzt) * NZ;
-    const int nn = item_nn(item);
-    const int kraw = MODE == 0 ? a.nr : nn;     // field entries per column
-    // K extent: fwd radial points, bwd rows of the even parity (the longer one)
+  int first = blockIdx.x;
+  while (first < nitems && item_nn(first) == 0) first += gridDim.x;
+  // per item: K extent (fwd radial points, bwd rows of the even parity), chunks, output rows, row tiles
+  auto geom = [&](int nn, int& nkc_m, int& nrows, int& nmt_m) {
     const int kext = MODE == 0 ? a.nrh : (nn + 1) / 2;
-    const int nkc_m = (kext + XS_KC - 1) / XS_KC;
-    const int nrows = MODE == 0 ? (nn + 1) / 2 : a.nrh;
-    const int nmt_m = (nrows + 127) / 128;
-    xs_wait(bar_raw, raw_ph, ok);
-    raw_ph ^= 1;
-    ok = __syncthreads_and(ok);   // every exit below is taken by the whole block
-    if (!ok) break;
-    // ---- column scales: XS_THREADS / N lanes of one warp per real column n (z = n/2, re/im = n&1)
-    // reduce the largest exponent field (the high words of the staged FP64 samples) by warp shuffles
-    {
-      constexpr int TPC = XS_THREADS / N;
-      static_assert(TPC == 16 || TPC == 32, "a column's lanes are a half or a whole warp");
-      const int n = tid / TPC, sub = tid % TPC, zz = n >> 1;
-      unsigned mx = 0;
-      if (z0 + zz < a.nzdim) {
-        const unsigned* hw = (const unsigned*)(raw + (size_t)2 * zz * a.rawk + (n & 1)) + 1;
-        for (int i = sub; i < kraw; i += TPC) mx = max(mx, (hw[4 * i] >> 20) & 0x7FFu);
-      }
-      mx = __reduce_max_sync(TPC == 32 ? 0xFFFFFFFFu : (0xFFFFu << (lane & 16)), mx);
-      // |x| < 2^(field - 1022) for every sample; an all-zero column gets -2000
-      if (sub == 0) colexp[n] = mx ? (int)mx - 1022 + (MODE == 0 ? 1 : 0) : -2000;
-    }
-    __syncthreads();
+    nkc_m = (kext + XS_KC - 1) / XS_KC;
+    nrows = MODE == 0 ? (nn + 1) / 2 : a.nrh;
+    nmt_m = (nrows + 127) / 128;
+  };
 
-    for (int mt = 0; mt < nmt_m && ok; ++mt) {
-      const uint8_t* img_m = (const uint8_t*)a.img + ((size_t)m * a.nmt + mt) * a.nkc * (size_t)ASTAGE;
-      const uint32_t it0 = it;
-      if (warp == 0) {
-        // ---- producer: the table chunks, each into its stage once the MMAs that read it before are done
-        if (lane == 0) {
-          for (int kc = 0; kc < nkc_m && ok; ++kc) {
-            const uint32_t c = it0 + kc, s = c & 1;
-            if (c >= 2) xs_wait(&bar_mma[s], ((c - 2) >> 1) & 1, ok);
-            if (!ok) break;
-            mbar_expect_tx(&bar_a[s], ASTAGE);
-            bulk_g2s(sA + s * ASTAGE, img_m + (size_t)kc * ASTAGE, ASTAGE, &bar_a[s]);
-          }
-          // the next item's field columns, once the digit warps are done with these
-          const int nxt = next_item(item);
-          if (ok && mt == nmt_m - 1 && nxt < nitems) {
-            const uint32_t c = it0 + nkc_m - 1;
-            xs_wait(&bar_b[c & 1], (c >> 1) & 1, ok);
-            if (ok) issue_raw(nxt);
+  if (warp == 0) {
+    // ---- producer
+    if (lane == 0) {
+      uint32_t c = 0, nraw = 0;   // table chunks and field-column copies issued
+      int ii = 0;
+      for (int item = first; item < nitems && ok; item = next_item(item), ++ii) {
+        const int m = item_m(item), z0 = item_z0(item), nn = item_nn(item);
+        const double2* fin = xs_sel(a.in, item % a.nf);
+        int nkc_m, nrows, nmt_m;
+        geom(nn, nkc_m, nrows, nmt_m);
+        // the item's field columns, once the digit threads are done with the previous item's
+        if (ii > 0 && !xs_wait(bar_re, (ii - 1) & 1, ok)) break;
+        const int kraw = MODE == 0 ? a.nr : nn;
+        fence_async_smem();
+        uint32_t bytes = 0;
+        for (int zz = 0; zz < NZ; ++zz)
+          if (z0 + zz < a.nzdim) bytes += (uint32_t)kraw * 16u;
+        mbar_expect_tx(bar_rf, bytes);
+        for (int zz = 0; zz < NZ; ++zz)
+          if (z0 + zz < a.nzdim)
+            bulk_g2s(raw + (size_t)2 * zz * a.rawk, fin + (size_t)a.nrdim * (m + (size_t)a.npdim * (z0 + zz)),
+                     (uint32_t)kraw * 16u, bar_rf);
+        ++nraw;
+        for (int mt = 0; mt < nmt_m && ok; ++mt) {
+          const uint8_t* img_m = (const uint8_t*)a.img + ((size_t)m * a.nmt + mt) * a.nkc * (size_t)ASTAGE;
+          for (int kc = 0; kc < nkc_m; ++kc, ++c) {
+            const uint32_t s = c & 1;
+            if (c >= 2 && !xs_wait(&bar_ae[s], ((c - 2) >> 1) & 1, ok)) break;
+            mbar_expect_tx(&bar_af[s], ASTAGE);
+            bulk_g2s(sA + s * ASTAGE, img_m + (size_t)kc * ASTAGE, ASTAGE, &bar_af[s]);
           }
         }
-        __syncwarp();
-      } else if (warp == 1) {
-        // ---- MMA issue: one thread, as soon as a stage's table and digits are in
-        if (lane == 0) {
-          for (int kc = 0; kc < nkc_m && ok; ++kc) {
-            const uint32_t c = it0 + kc, s = c & 1;
-            xs_wait(&bar_a[s], (c >> 1) & 1, ok);
-            xs_wait(&bar_b[s], (c >> 1) & 1, ok);
-            if (!ok) break;
+      }
+      // the copies issued complete on their own: wait (bounded) for the last of them, so that no copy
+      // is in flight when the CTA's shared memory goes away (at once in a run without a timeout)
+      bool ok2 = true;
+      if (c >= 1) xs_wait(&bar_af[(c - 1) & 1], ((c - 1) >> 1) & 1, ok2);
+      ok2 = true;
+      if (c >= 2) xs_wait(&bar_af[c & 1], ((c - 2) >> 1) & 1, ok2);
+      ok2 = true;
+      if (nraw >= 1) xs_wait(bar_rf, (nraw - 1) & 1, ok2);
+    }
+  } else if (warp == 1) {
+    // ---- MMA issue
+    if (lane == 0) {
+      uint32_t c = 0, u = 0;
+      for (int item = first; item < nitems && ok; item = next_item(item)) {
+        int nkc_m, nrows, nmt_m;
+        geom(item_nn(item), nkc_m, nrows, nmt_m);
+        for (int mt = 0; mt < nmt_m && ok; ++mt, ++u) {
+          if (u > 0 && !xs_wait(bar_te, (u - 1) & 1, ok)) break;   // the epilogue has read the accumulators
+          tc_fence_after();
+          for (int kc = 0; kc < nkc_m; ++kc, ++c) {
+            const uint32_t sa = c & 1, sb = c % XS_SB;
+            if (!xs_wait(&bar_af[sa], (c >> 1) & 1, ok)) break;
+            if (!xs_wait(&bar_bf[sb], (c / XS_SB) & 1, ok)) break;
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * ASTAGE), b0 = smem_u32(sB + s * BSTAGE);
+            const uint32_t a0 = smem_u32(sA + sa * ASTAGE), b0 = smem_u32(sB + sb * BSTAGE);
             // table digit t times the field digits s = 0 .. NO-1-t in one MMA of N (NO - t) columns: the
             // field digits lie side by side in shared memory and the orders d = t + s side by side in
             // tensor memory, so the product of digit s lands on order t + s
@@ -289,24 +337,71 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
                 umma_bf16(tmem + (uint32_t)((par * NO + t) * N), ad, bd, idesc_bf16(128, (NO - t) * N),
                           (kc > 0 || t > 0) ? 1u : 0u);
               }
-            umma_commit(&bar_mma[s]);
+            umma_commit(&bar_ae[sa]);
+            umma_commit(&bar_be[sb]);
           }
+          if (ok) umma_commit(bar_tf);
         }
-        __syncwarp();
-      } else {
-        // ---- field digits: a warp writes one (parity, 8 columns, 4 K pairs) block, its 32 four-byte
-        // stores in 32 different banks
-        const int dw = warp - 2;
-        for (int kc = 0; kc < nkc_m && ok; ++kc) {
-          const uint32_t c = it0 + kc, s = c & 1;
-          if (c >= 2) xs_wait(&bar_mma[s], ((c - 2) >> 1) & 1, ok);
-          if (!ok) break;
+      }
+      if (c > 0) {   // the MMAs issued have finished (bounded) before tensor memory is freed
+        bool ok2 = true;
+        xs_wait(&bar_ae[(c - 1) & 1], ((c - 1) >> 1) & 1, ok2);
+      }
+    }
+  } else if (warp < 2 + XS_NDW) {
+    // ---- column scales and field digits
+    const int dw = warp - 2;
+    uint32_t c = 0;
+    int ii = 0;
+    for (int item = first; item < nitems && ok; item = next_item(item), ++ii) {
+      const int z0 = item_z0(item), nn = item_nn(item);
+      int nkc_m, nrows, nmt_m;
+      geom(nn, nkc_m, nrows, nmt_m);
+      const int kraw = MODE == 0 ? a.nr : nn;
+      int* cx = colexp + (ii & 1) * N;
+      if (!xs_wait_w(bar_rf, ii & 1, ok)) break;
+      // the column-scale slot of this item parity is free once the epilogue of item ii-2 has read it
+      if (ii >= 2 && !xs_wait_w(&bar_ce[ii & 1], ((ii - 2) >> 1) & 1, ok)) break;
+      // column scales: a warp per real column n (z = n/2, re/im = n&1), the largest exponent field of the
+      // staged FP64 samples (their high words) reduced by warp shuffles; |x| < 2^(field - 1022), and the
+      // forward folds may double
+      for (int n = dw; n < N; n += XS_NDW) {
+        const int zz = n >> 1;
+        unsigned mx = 0;
+        if (z0 + zz < a.nzdim) {
+          const unsigned* hw = (const unsigned*)(raw + (size_t)2 * zz * a.rawk + (n & 1)) + 1;
+          unsigned m1 = 0, m2 = 0, m3 = 0;
+          int i = lane;
+          // (the high words without their sign bits order like the magnitudes' exponent fields)
+          for (; i + 96 < kraw; i += 128) {
+            mx = max(mx, hw[4 * i] & 0x7FFFFFFFu);
+            m1 = max(m1, hw[4 * (i + 32)] & 0x7FFFFFFFu);
+            m2 = max(m2, hw[4 * (i + 64)] & 0x7FFFFFFFu);
+            m3 = max(m3, hw[4 * (i + 96)] & 0x7FFFFFFFu);
+          }
+          for (; i < kraw; i += 32) mx = max(mx, hw[4 * i] & 0x7FFFFFFFu);
+          mx = max(max(mx, m1), max(m2, m3)) >> 20;
+        }
+        mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+        if (lane == 0) cx[n] = mx ? (int)mx - 1022 + (MODE == 0 ? 1 : 0) : -2000;
+      }
+      mbar_arrive(&bar_cx[ii & 1]);
+      if (!xs_wait_w(&bar_cx[ii & 1], (ii >> 1) & 1, ok)) break;
+      for (int mt = 0; mt < nmt_m && ok; ++mt) {
+        for (int kc = 0; kc < nkc_m; ++kc, ++c) {
+          const uint32_t s = c % XS_SB;
+          if (c >= XS_SB && !xs_wait_w(&bar_be[s], ((c - XS_SB) / XS_SB) & 1, ok)) break;
           uint8_t* bst = sB + s * BSTAGE;
-          for (int blk = dw; blk < NBLK; blk += NDW) {
+          // a warp writes (parity, 8 columns, 4 K pairs) blocks, each its 32 four-byte stores in 32 banks;
+          // the warp's blocks unrolled, so that their independent chains interleave
+#pragma unroll
+          for (int bi = 0; bi < (NBLK + XS_NDW - 1) / XS_NDW; ++bi) {
+            const int blk = dw + bi * XS_NDW;
+            if (blk >= NBLK) break;
             const int par = MODE == 0 ? 0 : (blk & 1), bb = MODE == 0 ? blk : (blk >> 1);
             const int ng = bb % (N / 8), kh = bb / (N / 8);
             const int n = ng * 8 + (lane & 7), kp = kh * 4 + (lane >> 3), zz = n >> 1;
-            const int E = colexp[n];
+            const int E = cx[n];
             const bool zok = (z0 + zz < a.nzdim) && E > -2000;
             const double* col = raw + (size_t)2 * zz * a.rawk + (n & 1);
             const int off = xs_off(n, 2 * kp);
@@ -339,106 +434,133 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
             }
           }
           fence_async_smem();
-          mbar_arrive(&bar_b[s]);
+          mbar_arrive(&bar_bf[s]);
         }
       }
-      it = it0 + nkc_m;
-      // ---- epilogue: every MMA of the tile has completed once the last chunk's commit has
-      {
-        const uint32_t lst = it - 1;
-        xs_wait(&bar_mma[lst & 1], (lst >> 1) & 1, ok);
-      }
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      tc_fence_after();
-      const int lq = warp & 3, cg = warp >> 2;      // TMEM lane quarter, 8-column group
-      // (a warp whose 32 rows all lie past the tile's valid rows has nothing to write)
-      if (cg < CGW && mt * 128 + lq * 32 < nrows) {
+      mbar_arrive(bar_re);   // done with the item's field columns
+    }
+  } else {
+    // ---- epilogue: warp e reads TMEM lanes 32 (e % 4) .. +31 (rows of the tile) and the column half
+    // e / 4; the orders are combined exactly in 64-bit integers, T = sum_d G_d 2^(w (NO-1-d) - esh), on the
+    // integer pipe, and T 2^(EA + EB + esh - w (NO+1)) is then rounded once to FP64
+    const int ew = warp - 2 - XS_NDW, lq = warp & 3, ch = ew >> 2;
+    const uint32_t lrow = (uint32_t)(lq * 32) << 16;
+    uint32_t u = 0;
+    int ii = 0;
+    for (int item = first; item < nitems && ok; item = next_item(item), ++ii) {
+      const int m = item_m(item), z0 = item_z0(item), nn = item_nn(item);
+      double2* fout = xs_sel(a.out, item % a.nf);
+      const double* flnp = xs_sel(a.lnp, item % a.nf);
+      int nkc_m, nrows, nmt_m;
+      geom(nn, nkc_m, nrows, nmt_m);
+      const int* cx = colexp + (ii & 1) * N;
+      // the item's column scales (this slot cannot move on to item ii+2 before this epilogue has read it)
+      if (!xs_wait_w(&bar_cx[ii & 1], (ii >> 1) & 1, ok)) break;
+      for (int mt = 0; mt < nmt_m && ok; ++mt, ++u) {
         const int row = mt * 128 + lq * 32 + lane;
-        const uint32_t lrow = (uint32_t)(lq * 32) << 16;
-        const int c0 = cg * 8;
-        {
-          // the orders combined exactly in 64-bit integers, T = sum_d G_d 2^(w (NO-1-d) - esh), on the
-          // integer pipe; T 2^(EA + EB + esh - w (NO+1)) is then rounded once to FP64
-        long long T[2][8];
+        const bool live = mt * 128 + lq * 32 < nrows;   // a warp of rows past the tile's rows reads nothing
+        // the row exponents, loaded before the wait so that their latency hides behind it
+        int EA0 = -2000, EA1 = -2000;
+        if (MODE == 0) {
+          if (row < nrows) {
+            EA0 = a.aexp[(size_t)(m * 2) * a.nrp + row];
+            EA1 = a.aexp[(size_t)(m * 2 + 1) * a.nrp + row];
+          }
+        } else if (row < a.nrh) {
+          EA0 = a.aexp[(size_t)m * a.nrp + row];
+        }
+        if (!xs_wait_w(bar_tf, u & 1, ok)) break;
+        tc_fence_after();
+        constexpr int eo = ESH - W * (NO + 1);
+        // the warp's columns eight at a time; after the last group's loads the accumulators are free for
+        // the next unit's MMAs (and, after the item's last unit, the column scales for item ii+2), so the
+        // last group's conversions and stores overlap them
+#pragma unroll 1
+        for (int q = 0; q < CPW; ++q) {
+          const int cb = ch * (N / 2) + q * 8;
+          int E[8];
 #pragma unroll
-        for (int par = 0; par < 2; ++par)
-#pragma unroll
-          for (int c = 0; c < 8; ++c) T[par][c] = 0;
-#pragma unroll
-        for (int d = 0; d < NO; ++d) {
-          const int sh = w * (NO - 1 - d) - a.esh;
-          uint32_t g[2][8];
-#pragma unroll
-          for (int par = 0; par < 2; ++par) tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + d) * N + c0), g[par]);
-          tmem_wait_ld();
+          for (int c = 0; c < 8; ++c) E[c] = cx[cb + c];
+          long long T[2][8];
 #pragma unroll
           for (int par = 0; par < 2; ++par)
 #pragma unroll
-            for (int c = 0; c < 8; ++c) T[par][c] += xs_shl((long long)xs_f2i(__uint_as_float(g[par][c])), sh);
-        }
-        const int eo = a.esh - w * (NO + 1);
-        if (MODE == 0) {
+            for (int c = 0; c < 8; ++c) T[par][c] = 0;
+          if (live) {
+            // two orders per load batch (one wait for four 8-column loads)
+            auto order2 = [&](auto dc) {
+              constexpr int D = 2 * decltype(dc)::value, D2 = D + 1 < NO ? D + 1 : D;
+              uint32_t g[2][8], h[2][8];
 #pragma unroll
-          for (int par = 0; par < 2; ++par) {
-            const int j = 2 * row + par;
-            if (row >= nrows || j >= nn) continue;
-            const int EA = a.aexp[(size_t)(m * 2 + par) * a.nrp + row];
-#pragma unroll
-            for (int c = 0; c < 8; c += 2) {
-              const int n = c0 + c, zo = z0 + (n >> 1);
-              if (zo >= a.nzdim) continue;
-              const double re = EA > -2000 && colexp[n] > -2000 ? xs_i64_to_double(T[par][c], EA + colexp[n] + eo) : 0.0;
-              const double im = EA > -2000 && colexp[n + 1] > -2000 ? xs_i64_to_double(T[par][c + 1], EA + colexp[n + 1] + eo) : 0.0;
-              a.out[j + (size_t)a.nrdim * (m + (size_t)a.npdim * zo)] = make_double2(re, im);
-            }
-          }
-        } else {
-          const int i = row;
-          if (i < a.nrh) {
-            const int EA = a.aexp[(size_t)m * a.nrp + i];
-            const double lnv = (a.add_ln && m == 0) ? *a.lnp : 0.0;
-#pragma unroll
-            for (int c = 0; c < 8; c += 2) {
-              const int n = c0 + c, zo = z0 + (n >> 1);
-              if (zo >= a.nzdim) continue;
-              double v[4] = {0.0, 0.0, 0.0, 0.0};   // f(i) re, im; f(nr-1-i) re, im
-#pragma unroll
-              for (int q = 0; q < 2; ++q) {
-                const int E = colexp[n + q];
-                if (EA > -2000 && E > -2000) {
-                  v[q] = xs_i64_to_double(T[0][c + q] + T[1][c + q], EA + E + eo);
-                  v[2 + q] = xs_i64_to_double(T[0][c + q] - T[1][c + q], EA + E + eo);
-                }
+              for (int par = 0; par < 2; ++par) {
+                tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + D) * N + cb), g[par]);
+                if constexpr (D2 != D) tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + D2) * N + cb), h[par]);
               }
-              if (lnv != 0.0) { v[0] += lnv * a.lnx[i]; v[2] += lnv * a.lnx[a.nr - 1 - i]; }
-              const size_t b0 = (size_t)a.nrdim * (m + (size_t)a.npdim * zo);
-              a.out[b0 + i] = make_double2(v[0], v[1]);
-              a.out[b0 + a.nr - 1 - i] = make_double2(v[2], v[3]);
+              tmem_wait_ld();
+#pragma unroll
+              for (int par = 0; par < 2; ++par)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  xs_acc_order<NO, W, ESH, D>(T[par][c], g[par][c]);
+                  if constexpr (D2 != D) xs_acc_order<NO, W, ESH, D2>(T[par][c], h[par][c]);
+                }
+            };
+            xs_static_for<(NO + 1) / 2>(order2);
+          }
+          if (q == CPW - 1) {
+            tc_fence_before();
+            mbar_arrive(bar_te);
+            if (mt == nmt_m - 1) mbar_arrive(&bar_ce[ii & 1]);
+          }
+          if (!live) continue;
+          if (MODE == 0) {
+#pragma unroll
+            for (int par = 0; par < 2; ++par) {
+              const int j = 2 * row + par;
+              if (row >= nrows || j >= nn) continue;
+              const int EA = par ? EA1 : EA0;
+#pragma unroll
+              for (int c = 0; c < 8; c += 2) {
+                const int zo = z0 + ((cb + c) >> 1);
+                if (zo >= a.nzdim) continue;
+                const double re = EA > -2000 && E[c] > -2000 ? xs_i64_to_double(T[par][c], EA + E[c] + eo) : 0.0;
+                const double im = EA > -2000 && E[c + 1] > -2000 ? xs_i64_to_double(T[par][c + 1], EA + E[c + 1] + eo) : 0.0;
+                fout[j + (size_t)a.nrdim * (m + (size_t)a.npdim * zo)] = make_double2(re, im);
+              }
+            }
+          } else {
+            const int i = row;
+            if (i < a.nrh) {
+              const int EA = EA0;
+              const double lnv = (a.add_ln && m == 0) ? *flnp : 0.0;
+#pragma unroll
+              for (int c = 0; c < 8; c += 2) {
+                const int zo = z0 + ((cb + c) >> 1);
+                if (zo >= a.nzdim) continue;
+                double v[4] = {0.0, 0.0, 0.0, 0.0};   // f(i) re, im; f(nr-1-i) re, im
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                  if (EA > -2000 && E[c + h] > -2000) {
+                    // f(i) = D_0 + D_1, f(nr-1-i) = D_0 - D_1: both parities share the scales
+                    v[h] = xs_i64_to_double(T[0][c + h] + T[1][c + h], EA + E[c + h] + eo);
+                    v[2 + h] = xs_i64_to_double(T[0][c + h] - T[1][c + h], EA + E[c + h] + eo);
+                  }
+                }
+                if (lnv != 0.0) { v[0] += lnv * a.lnx[i]; v[2] += lnv * a.lnx[a.nr - 1 - i]; }
+                const size_t b0 = (size_t)a.nrdim * (m + (size_t)a.npdim * zo);
+                fout[b0 + i] = make_double2(v[0], v[1]);
+                fout[b0 + a.nr - 1 - i] = make_double2(v[2], v[3]);
+              }
             }
           }
-        }
         }
       }
-      tc_fence_before();
-      __syncthreads();   // TMEM read out before the next tile's MMAs
     }
   }
-  if (!ok) {
-    if (tid == 0) atomicExch(a.status, 2);
-    // let what was issued finish (bounded) before the memory goes away: the last commit completes
-    // after every earlier MMA; a table or field copy completes on its own barrier
-    if (tid == 0 && it > 0) {
-      bool ok2 = true;
-      const uint32_t lst = it - 1;
-      xs_wait(&bar_mma[lst & 1], (lst >> 1) & 1, ok2);
-      ok2 = true;
-      xs_wait(bar_raw, raw_ph, ok2);
-    }
-  }
+  if (!ok) atomicExch(a.status, 2);
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, TCOLS);
+  if (warp == 1) tmem_dealloc(tmem, TCOLS);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -483,8 +605,8 @@ static bool xs_cfg(int kmax, bool plain, XsCfg& c) {
 
 static size_t xs_smem(int ns, int nz, int rawk) {
   const int n = 2 * nz;
-  return 1024 + 2 * (size_t)(2 * ns * XS_ATILE) + 2 * (size_t)(2 * ns * n * XS_KC * 2) + (size_t)2 * nz * rawk * sizeof(double) +
-         n * (sizeof(int) + sizeof(unsigned long long)) + 64;
+  return 1024 + 2 * (size_t)(2 * ns * XS_ATILE) + XS_SB * (size_t)(2 * ns * n * XS_KC * 2) +
+         (size_t)2 * nz * rawk * sizeof(double) + 2 * n * sizeof(int) + 256;
 }
 // complex z columns per work item: 16 while the accumulators (2 NS orders x 2 NZ columns) fit the
 // 512 columns of tensor memory and the field columns fit shared memory, else 8
@@ -501,7 +623,7 @@ template <int MODE, int NS, int NZ>
 static int xs_launch(const XsArgs& args, int nitems) {
   const size_t sm = xs_smem(NS, NZ, args.rawk);
   if (sm > 227 * 1024) return set_error(MLG_ESIZE, "radial contraction: shared-memory stage too large");
-  auto kern = k_xs_rtrans<MODE, NS, NS, NZ>;
+  auto kern = k_xs_rtrans<MODE, NS, NZ>;
   MLG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int grid = std::min(nitems, 152);
   kern<<<grid, XS_THREADS, sm, G.stream>>>(args);
@@ -510,8 +632,10 @@ static int xs_launch(const XsArgs& args, int nitems) {
 }
 
 // mode 0 forward, 1 backward, for m0 <= m < npc; out's rows that it writes are overwritten, the rest left
-int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const double* lnp, bool add_ln, bool plain) {
-  if (npc <= m0) return 0;
+int xs_rtrans_multi(int mode, const cd* const* in, cd* const* out, int nf, int nrc, int npc, int m0,
+                    const double* const* lnp, bool add_ln, bool plain) {
+  if (npc <= m0 || nf < 1) return 0;
+  if (nf > XS_NF) return set_error(MLG_EPARAM, "radial contraction: at most three fields per launch");
   const int nrows = mode == 0 ? (nrc + 1) / 2 : G.nrh;
   const int kmax = mode == 0 ? G.nrh : (nrc + 1) / 2;
   XsCfg cfg;
@@ -539,21 +663,21 @@ int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const d
     im.nrc = nrc; im.npc = npc; im.ns = cfg.ns; im.w = cfg.w; im.nmt = nmt; im.nkc = nkc; im.nrp = nrp;
   }
   XsArgs args;
-  args.in = in; args.out = out; args.img = im.p; args.aexp = im.aexp; args.lnx = G.lnx; args.lnp = lnp;
+  for (int f = 0; f < XS_NF; ++f) {
+    const int g = f < nf ? f : 0;
+    args.in[f] = in[g]; args.out[f] = out[g]; args.lnp[f] = lnp ? lnp[g] : nullptr;
+  }
+  args.nf = nf;
+  args.img = im.p; args.aexp = im.aexp; args.lnx = G.lnx;
   args.status = (int*)(G.dscal + DS_FLAG + 1) + 1;
   args.add_ln = add_ln ? 1 : 0; args.nr = G.nr; args.nrh = G.nrh; args.nrdim = G.nrdim; args.npdim = G.npdim;
   args.nzdim = G.nzdim; args.nrc = nrc; args.m0 = m0; args.npc = npc; args.nmt = nmt; args.nkc = nkc; args.nrp = nrp;
   // odd, so that the columns of the staged field start in different shared-memory banks
   args.rawk = std::max(G.nr, nrc) | 1;
-  args.wbits = cfg.w;
-  {
-    // the epilogue's 64-bit integer T = sum_d G_d 2^(w (NS-1-d) - esh) stays below 2^62:
-    // |G_d| <= K NS 2^(2w)
-    const double mx = (double)kmax * cfg.ns * (1 << cfg.w) * (1 << cfg.w);
-    args.esh = std::max(0, (int)std::ceil(std::log2(mx) + 0.05) + cfg.w * (cfg.ns - 1) - 62);
-  }
+  // the kernels' compile-time digit widths (xs_w) are those of xs_cfg
+  if (cfg.w != (cfg.ns == 6 || cfg.ns == 9 ? 7 : 6)) return set_error(MLG_EPARAM, "radial contraction: digit configuration");
   const int nz16 = xs_nz(cfg.ns) == 16;
-  const int nitems = (npc - m0) * cdiv(G.nzdim, nz16 ? 16 : 8);
+  const int nitems = (npc - m0) * cdiv(G.nzdim, nz16 ? 16 : 8) * nf;
 #define XS_CASE(NSV)                                                                                   \
   case NSV:                                                                                            \
     if (mode == 0) return nz16 ? xs_launch<0, NSV, 16>(args, nitems) : xs_launch<0, NSV, 8>(args, nitems); \
@@ -566,6 +690,10 @@ int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const d
   }
 #undef XS_CASE
   return set_error(MLG_EPARAM, "radial contraction: digit configuration");
+}
+
+int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const double* lnp, bool add_ln, bool plain) {
+  return xs_rtrans_multi(mode, &in, &out, 1, nrc, npc, m0, &lnp, add_ln, plain);
 }
 
 }  // namespace mlg

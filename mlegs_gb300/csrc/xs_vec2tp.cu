@@ -30,9 +30,9 @@
 // init in the UMMA canonical K-major layout) arrive by one bulk copy into a two-stage ring, six warps
 // cut the field digits (ur, up and uz at i and nr-1-i, fetched in FP64 a chunk ahead) into the same
 // layout and arrive on the stage's mbarrier, and one thread issues the chunk's tcgen05.mma as soon as
-// both halves of a stage are in: a table digit t meets every field digit s <= n-1-t of one operand in
-// a single MMA (M = 128, N = 16 (n - t), K = 16; the field digits side by side in shared memory, the
-// orders side by side in tensor memory), 4 NS + NT MMAs per chunk.  Every wait is bounded.
+// both halves of a stage are in: a table digit t meets every field digit s <= n-1-t of its operands in
+// a single MMA (M = 128, K = 16; the field digits side by side in shared memory, the orders side by
+// side in tensor memory, psi's and X's alternating), 2 NS + NT MMAs per chunk.  Every wait is bounded.
 #include "common.cuh"
 #include "tc_common.cuh"
 #include "xs_common.cuh"
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
   constexpr int N = 2 * NZ;
   constexpr int BTILE = N * XV_KC * 2;
   constexpr int NA = 2 * NS + NT;                 // A tiles per chunk
-  constexpr int NB = 4 * NS + NT;                 // B tiles: psi_ur, psi_up, X_ur, X_up (NS each), uz (NT)
+  constexpr int NB = 4 * NS + NT;                 // B tiles: [psi_ur, X_up] and [psi_up, X_ur] by digit, uz (NT)
   constexpr int ASTAGE = NA * XV_ATILE, BSTAGE = NB * BTILE;
   constexpr int COLS = (2 * NS + NT) * N;
   constexpr int TCOLS = COLS <= 128 ? 128 : COLS <= 256 ? 256 : 512;
@@ -245,17 +245,17 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
           const uint32_t a0 = smem_u32(sA + s * ASTAGE), b0 = smem_u32(sB + s * BSTAGE);
           auto A = [&](int t) { return sdesc(a0 + t * XV_ATILE, XV_LBO, XV_SBO); };
           auto B = [&](int t) { return sdesc(b0 + t * BTILE, XV_LBO, XV_SBO); };
-          // table digit t against the field digits 0 .. n-1-t in one MMA of N (n - t) columns: the field
-          // digits lie side by side in shared memory and the accumulators of the orders side by side in
-          // tensor memory, so the product of field digit s lands on order t + s
+          // table digit t against the field digits 0 .. n-1-t in one MMA: the field digits lie side by
+          // side in shared memory and the accumulators of the orders side by side in tensor memory, so
+          // the product of field digit s lands on order t + s.  psi and X alternate by order (psi_d at
+          // 2d N, X_d at (2d+1) N) and their field digits alternate the same way ([psi_ur_s, X_up_s]
+          // against m V, [psi_up_s, X_ur_s] against D), so one MMA of 2 N (NS - t) columns covers
+          // both sums
 #pragma unroll
           for (int t = 0; t < NS; ++t) {
-            const uint32_t acc = (kc > 0 || t > 0) ? 1u : 0u;
-            const uint32_t id = idesc_bf16(128, (NS - t) * N);
-            umma_bf16(tmem + t * N, A(t), B(0), id, acc);                  // psi: mV . psi_ur
-            umma_bf16(tmem + t * N, A(NS + t), B(NS), id, 1u);             //      D . psi_up
-            umma_bf16(tmem + (NS + t) * N, A(NS + t), B(2 * NS), id, acc); // X: D . X_ur
-            umma_bf16(tmem + (NS + t) * N, A(t), B(3 * NS), id, 1u);       //    mV . X_up
+            const uint32_t id = idesc_bf16(128, 2 * (NS - t) * N);
+            umma_bf16(tmem + 2 * t * N, A(t), B(0), id, (kc > 0 || t > 0) ? 1u : 0u);   // m V . [psi_ur | X_up]
+            umma_bf16(tmem + 2 * t * N, A(NS + t), B(2 * NS), id, 1u);                 // D . [psi_up | X_ur]
           }
 #pragma unroll
           for (int t = 0; t < NT; ++t)
@@ -306,13 +306,14 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
               xs_digits_f<NS>(fs_re, w, g0[u]); xs_digits_f<NS>(fs_im, w, g1[u]);
             }
           }
-          const int tp = f == 0 ? 0 : NS, tx = f == 0 ? 2 * NS : 3 * NS;
+          // B tiles: [psi_ur_s, X_up_s] at 2s, 2s+1; [psi_up_s, X_ur_s] at 2 NS + 2s, 2 NS + 2s + 1
+          const int tp = f == 0 ? 0 : 2 * NS, tx = f == 0 ? 2 * NS + 1 : 1;
 #pragma unroll
           for (int q = 0; q < NS; ++q) {
-            *(uint32_t*)(bst + (tp + q) * BTILE + off) = xs_pack(h0[0][q], h0[1][q]);
-            *(uint32_t*)(bst + (tp + q) * BTILE + off1) = xs_pack(h1[0][q], h1[1][q]);
-            *(uint32_t*)(bst + (tx + q) * BTILE + off) = xs_pack(g0[0][q], g0[1][q]);
-            *(uint32_t*)(bst + (tx + q) * BTILE + off1) = xs_pack(g1[0][q], g1[1][q]);
+            *(uint32_t*)(bst + (tp + 2 * q) * BTILE + off) = xs_pack(h0[0][q], h0[1][q]);
+            *(uint32_t*)(bst + (tp + 2 * q) * BTILE + off1) = xs_pack(h1[0][q], h1[1][q]);
+            *(uint32_t*)(bst + (tx + 2 * q) * BTILE + off) = xs_pack(g0[0][q], g0[1][q]);
+            *(uint32_t*)(bst + (tx + 2 * q) * BTILE + off1) = xs_pack(g1[0][q], g1[1][q]);
           }
         } else {
           // Y: F_s(uz) with the uz column scales
@@ -337,6 +338,12 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
     }
     it = it0 + nkc;
     // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows t) and the 8-column block w / 4
+    const int t = mt * 128 + (warp & 3) * 32 + lane;
+    const int j = 2 * t + par;
+    const bool rok = j < nn && t < a.ntr;
+    // the row exponents, loaded before the wait so that their latency hides behind it
+    const int er = rok ? a.rexp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
+    const int et = rok ? a.texp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
     {
       const uint32_t lst = it - 1;
       xs_wait(&bar_mma[lst & 1], (lst >> 1) & 1, ok);
@@ -344,12 +351,7 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
     ok = __syncthreads_and(ok);
     if (!ok) break;
     tc_fence_after();
-    const int t = mt * 128 + (warp & 3) * 32 + lane;
-    const int j = 2 * t + par;
-    const bool rok = j < nn && t < a.ntr;
     if (mt * 128 + (warp & 3) * 32 < a.ntr) {   // a warp of rows past the tile's rows has nothing to write
-      const int er = rok ? a.rexp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
-      const int et = rok ? a.texp[(size_t)(m * 2 + par) * a.ntr + t] : -2000;
       const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
       const int cb = warp >> 2;
 #pragma unroll 1
@@ -362,8 +364,8 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
           uint32_t gp[NS][4], gx[NS][4];
 #pragma unroll
           for (int d = 0; d < NS; ++d) {
-            tmem_ld4_nw(tmem + lrow + d * N + c0, gp[d]);
-            tmem_ld4_nw(tmem + lrow + (NS + d) * N + c0, gx[d]);
+            tmem_ld4_nw(tmem + lrow + 2 * d * N + c0, gp[d]);
+            tmem_ld4_nw(tmem + lrow + (2 * d + 1) * N + c0, gx[d]);
           }
           tmem_wait_ld();
 #pragma unroll
