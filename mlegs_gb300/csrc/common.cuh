@@ -168,7 +168,6 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);
 int pv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc);
 void pv_free();
-void m0_free();   // the m = 0 double-float table of the backward radial transform (radial.cu)
 
 // pointwise
 int launch_zero(cd* e);

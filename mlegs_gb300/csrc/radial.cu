@@ -97,16 +97,16 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const ty
   }
 }
 
-// backward: grid (ztiles, itiles, npc); each thread owns IPT rows i and ZPT columns and both parities
+// backward: tile (itile blockIdx.y, ztile blockIdx.x) of mode m; each thread owns IPT rows i and ZPT
+// columns and both parities
 template <typename T, int IT, int ZT, int KC, int IPT, int ZPT>
-__global__ void __launch_bounds__((IT / IPT) * (ZT / ZPT))
-k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const typename TabT<T>::t* __restrict__ pf,
-             const double* __restrict__ lnx, const double* __restrict__ lnp, int add_ln, int nr, int nrh, int ne,
-             int nrdim, int npdim, int nzdim, int nrc) {
+__device__ __forceinline__ void rtrans_bwd_tile(const double2* __restrict__ in, double2* __restrict__ out,
+                                                const typename TabT<T>::t* __restrict__ pf, const double* __restrict__ lnx,
+                                                const double* __restrict__ lnp, int add_ln, int nr, int nrh, int ne,
+                                                int nrdim, int npdim, int nzdim, int nrc, int m) {
   typedef typename V2<T>::t C;
   __shared__ T Ae[KC][IT + 1], Ao[KC][IT + 1];
   __shared__ C Be[KC][ZT], Bo[KC][ZT];
-  int m = blockIdx.z;
   int i0 = blockIdx.y * IT;
   int z0 = blockIdx.x * ZT;
   int nn = max(min(nrc, nrc - m), 0);
@@ -174,6 +174,93 @@ k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const ty
       out[base + nr - 1 - i] = q;
     }
   }
+}
+
+// backward over modes m < gridDim.z: grid (ztiles, itiles, mcount)
+template <typename T, int IT, int ZT, int KC, int IPT, int ZPT>
+__global__ void __launch_bounds__((IT / IPT) * (ZT / ZPT))
+k_rtrans_bwd(const double2* __restrict__ in, double2* __restrict__ out, const typename TabT<T>::t* __restrict__ pf,
+             const double* __restrict__ lnx, const double* __restrict__ lnp, int add_ln, int nr, int nrh, int ne,
+             int nrdim, int npdim, int nzdim, int nrc) {
+  rtrans_bwd_tile<T, IT, ZT, KC, IPT, ZPT>(in, out, pf, lnx, lnp, add_ln, nr, nrh, ne, nrdim, npdim, nzdim, nrc,
+                                           blockIdx.z);
+}
+
+// the m = 0 planes of up to three fields (the components of a vector field) in one launch: grid
+// (ztiles, itiles, fields), one output pair (i, nr-1-i) of one column per thread of a slice.  The plane is
+// 1/65 of the radial work at 192 x 128 x 128, so a grid over m alone would leave most SMs idle: small
+// tiles, the fields in the grid and KS slices of the K range (rows t, chunks of KC dealt round-robin, in
+// the block's z dimension, their partial sums added in shared memory in slice order) give it several
+// thousand warps.
+struct PlaneSet {
+  const double2* in[3];
+  double2* out[3];
+  const double* lnp[3];
+};
+template <typename T, int IT, int ZT, int KC, int KS>
+__global__ void __launch_bounds__(IT * ZT * KS)
+k_rtrans_bwd_plane(PlaneSet ps, const typename TabT<T>::t* __restrict__ pf, const double* __restrict__ lnx, int add_ln,
+                   int nr, int nrh, int ne, int nrdim, int npdim, int nzdim, int nrc) {
+  typedef typename V2<T>::t C;
+  __shared__ T Ae[KS][KC][IT + 1], Ao[KS][KC][IT + 1];
+  __shared__ C Be[KS][KC][ZT], Bo[KS][KC][ZT];
+  __shared__ T red[KS - 1][4][IT][ZT];
+  const int f = blockIdx.z;
+  const double2* in = f == 0 ? ps.in[0] : (f == 1 ? ps.in[1] : ps.in[2]);
+  double2* out = f == 0 ? ps.out[0] : (f == 1 ? ps.out[1] : ps.out[2]);
+  const double* lnp = f == 0 ? ps.lnp[0] : (f == 1 ? ps.lnp[1] : ps.lnp[2]);
+  (void)ne;
+  const int i0 = blockIdx.y * IT, z0 = blockIdx.x * ZT;
+  const int nn = max(nrc, 0);
+  const int tx = threadIdx.x, ty = threadIdx.y, ks = threadIdx.z;
+  const int nthr = IT * ZT, tid = ty * ZT + tx;
+  T er = 0, ei = 0, orr = 0, oi = 0;
+  const int nt = (nn + 1) / 2, nchunk = (nt + KC - 1) / KC, nround = (nchunk + KS - 1) / KS;
+  for (int rd = 0; rd < nround; ++rd) {   // the same trip count in every slice (barriers below)
+    const int t0 = (rd * KS + ks) * KC;
+    for (int idx = tid; idx < KC * IT; idx += nthr) {
+      const int ii = idx % IT, tt = idx / IT;
+      const int i = i0 + ii, je = 2 * (t0 + tt), jo = je + 1;
+      T ve = 0, vo = 0;
+      if (i < nrh) {
+        if (je < nn) ve = tab<T>(pf, i + (size_t)nrh * je);
+        if (jo < nn) vo = tab<T>(pf, i + (size_t)nrh * jo);
+      }
+      Ae[ks][tt][ii] = ve; Ao[ks][tt][ii] = vo;
+    }
+    for (int idx = tid; idx < KC * ZT * 2; idx += nthr) {
+      const int jj = idx % (2 * KC), zz = idx / (2 * KC);
+      const int j = 2 * t0 + jj, z = z0 + zz;
+      C v; v.x = 0; v.y = 0;
+      if (j < nn && z < nzdim) v = ldc<T>(in + j + (size_t)nrdim * npdim * z);
+      if (jj & 1) Bo[ks][jj >> 1][zz] = v; else Be[ks][jj >> 1][zz] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int tt = 0; tt < KC; ++tt) {
+      const T ae = Ae[ks][tt][ty], ao = Ao[ks][tt][ty];
+      const C be = Be[ks][tt][tx], bo = Bo[ks][tt][tx];
+      er = tmac(ae, be.x, er); ei = tmac(ae, be.y, ei);
+      orr = tmac(ao, bo.x, orr); oi = tmac(ao, bo.y, oi);
+    }
+    __syncthreads();
+  }
+  if (ks > 0) { red[ks - 1][0][ty][tx] = er; red[ks - 1][1][ty][tx] = ei; red[ks - 1][2][ty][tx] = orr; red[ks - 1][3][ty][tx] = oi; }
+  __syncthreads();
+  if (ks > 0) return;
+#pragma unroll
+  for (int q = 0; q < KS - 1; ++q) {
+    er = er + red[q][0][ty][tx]; ei = ei + red[q][1][ty][tx];
+    orr = orr + red[q][2][ty][tx]; oi = oi + red[q][3][ty][tx];
+  }
+  const int i = i0 + ty, z = z0 + tx;
+  if (i >= nrh || z >= nzdim) return;
+  const size_t base = (size_t)nrdim * npdim * z;
+  double2 p = to_d2<T>(er + orr, ei + oi);
+  double2 q = to_d2<T>(er - orr, ei - oi);
+  if (add_ln) { const double lnv = *lnp; p.x += lnv * lnx[i]; q.x += lnv * lnx[nr - 1 - i]; }
+  out[base + i] = p;
+  out[base + nr - 1 - i] = q;
 }
 
 // vec2tp: psi(j) = -i m (V.F_s(ur))_j - (D.F_o(up))_j,
@@ -274,6 +361,93 @@ k_vec2tp(const double2* __restrict__ ur, const double2* __restrict__ up, const d
   }
 }
 
+// the m = 0 plane of vec2tp (mixed form, double-float): the m V terms vanish at m = 0, so
+//   psi = -D.F_o(up),   chi = i k D.F_o(ur) - T.F_s(uz),
+// three contractions instead of five.  One output (j, z) per thread of a slice; KS slices of the K
+// range (radial points, chunks of KC dealt round-robin) in the block's z dimension give the plane
+// several thousand warps, and their partial sums are added in shared memory in slice order.
+template <typename T, int MT, int ZT, int KC, int KS>
+__global__ void __launch_bounds__(MT * ZT * KS)
+k_vec2tp_plane(const double2* __restrict__ ur, const double2* __restrict__ up, const double2* __restrict__ uz,
+               double2* __restrict__ psi, double2* __restrict__ chi, const typename TabT<T>::t* __restrict__ tD,
+               const typename TabT<T>::t* __restrict__ tT, const double* __restrict__ ak, int nr, int nrh, int ne,
+               int nrdim, int npdim, int nzdim, int nrc, int nzc, int nzcu) {
+  typedef typename V2<T>::t C;
+  __shared__ T Ad[KS][KC][MT + 1], At[KS][KC][MT + 1];
+  __shared__ C Bro[KS][KC][ZT], Bpo[KS][KC][ZT], Bzs[KS][KC][ZT];
+  __shared__ C red[KS - 1][3][MT][ZT];
+  const int par = blockIdx.y & 1, t0 = (blockIdx.y >> 1) * MT;
+  const int nn = max(nrc, 0);
+  if (2 * t0 + par >= nn) return;   // uniform over the block
+  const int z0 = blockIdx.x * ZT;
+  const int tx = threadIdx.x, ty = threadIdx.y, ks = threadIdx.z;
+  const int nthr = MT * ZT, tid = ty * ZT + tx;
+  C a2, a3, a5;   // D.F_o(up), D.F_o(ur), T.F_s(uz)
+  a2.x = a2.y = 0; a3.x = a3.y = 0; a5.x = a5.y = 0;
+  const T ss = par ? (T)-1 : (T)1;
+  const int nchunk = (nrh + KC - 1) / KC, nround = (nchunk + KS - 1) / KS;
+  for (int rd = 0; rd < nround; ++rd) {   // the same trip count in every slice (barriers below)
+    const int i0 = (rd * KS + ks) * KC;
+    for (int idx = tid; idx < KC * MT; idx += nthr) {
+      const int ii = idx % KC, tt = idx / KC;
+      const int j = 2 * (t0 + tt) + par, i = i0 + ii;
+      T d = 0, t = 0;
+      if (j < nn && i < nrh) {
+        const size_t o = i + (size_t)nrh * j;
+        d = tab<T>(tD, o); t = tab<T>(tT, o);
+      }
+      Ad[ks][ii][tt] = d; At[ks][ii][tt] = t;
+    }
+    for (int idx = tid; idx < KC * ZT; idx += nthr) {
+      const int ii = idx % KC, zz = idx / KC;
+      const int i = i0 + ii, z = z0 + zz;
+      C ro, po, zs;
+      ro.x = ro.y = po.x = po.y = zs.x = zs.y = 0;
+      if (i < nrh && z < nzdim) {
+        const size_t base = (size_t)nrdim * npdim * z;
+        C a = ldc<T>(ur + base + i), b = ldc<T>(ur + base + nr - 1 - i);
+        ro.x = a.x - ss * b.x; ro.y = a.y - ss * b.y;
+        a = ldc<T>(up + base + i); b = ldc<T>(up + base + nr - 1 - i);
+        po.x = a.x - ss * b.x; po.y = a.y - ss * b.y;
+        a = ldc<T>(uz + base + i); b = ldc<T>(uz + base + nr - 1 - i);
+        zs.x = a.x + ss * b.x; zs.y = a.y + ss * b.y;
+      }
+      Bro[ks][ii][zz] = ro; Bpo[ks][ii][zz] = po; Bzs[ks][ii][zz] = zs;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < KC; ++ii) {
+      const T d = Ad[ks][ii][ty], t = At[ks][ii][ty];
+      const C ro = Bro[ks][ii][tx], po = Bpo[ks][ii][tx], zs = Bzs[ks][ii][tx];
+      a2.x = tmac(d, po.x, a2.x); a2.y = tmac(d, po.y, a2.y);
+      a3.x = tmac(d, ro.x, a3.x); a3.y = tmac(d, ro.y, a3.y);
+      a5.x = tmac(t, zs.x, a5.x); a5.y = tmac(t, zs.y, a5.y);
+    }
+    __syncthreads();
+  }
+  if (ks > 0) { red[ks - 1][0][ty][tx] = a2; red[ks - 1][1][ty][tx] = a3; red[ks - 1][2][ty][tx] = a5; }
+  __syncthreads();
+  if (ks > 0) return;
+#pragma unroll
+  for (int q = 0; q < KS - 1; ++q) {
+    const C b2 = red[q][0][ty][tx], b3 = red[q][1][ty][tx], b5 = red[q][2][ty][tx];
+    a2.x = a2.x + b2.x; a2.y = a2.y + b2.y;
+    a3.x = a3.x + b3.x; a3.y = a3.y + b3.y;
+    a5.x = a5.x + b5.x; a5.y = a5.y + b5.y;
+  }
+  const int j = 2 * (t0 + ty) + par, z = z0 + tx;
+  if (j >= nn || z >= nzdim) return;
+  const int kk = z + 1;
+  if (!(kk <= nzc || kk >= nzcu)) return;
+  const T kv = (T)ak[z];
+  // psi = -D.F_o(up); chi = i k D.F_o(ur) - T.F_s(uz)
+  const double2 p = to_d2<T>(-a2.x, -a2.y);
+  const double2 q = to_d2<T>(-(kv * a3.y) - a5.x, kv * a3.x - a5.y);
+  const size_t o = j + (size_t)nrdim * npdim * z;
+  psi[o] = p;
+  chi[o] = q;
+}
+
 static int rtrans_check(const Scalar& s, int& nrc, int& npc, const char* who) {
   nrc = G.nrchop + s.off[0];
   npc = G.npchop + s.off[1];
@@ -289,110 +463,49 @@ static double fwd_flops(int nrc, int npc) {
   return f;
 }
 
-// the m = 0 plane of the mixed form in double-float: small tiles (about 190 CTAs at 192x128x128), one
-// output per thread
-static int m0_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
+// The m = 0 plane, in double-float (mixed form) or FP64 (plain form), with small tiles: the plane is
+// 1/65 of the radial work at 192 x 128 x 128, and the tiles of the all-m kernels would give it a few
+// dozen CTAs.  Forward: one output (j, z) per thread, about 190 CTAs of 128 threads per field.
+template <typename T>
+static int plane_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
   constexpr int MT = 16, ZT = 8, KC = 16;
   int nn = std::max(nrc, 0);
   if (nn == 0) return 0;
   dim3 grid(cdiv(G.nzdim, ZT), 2 * cdiv((nn + 1) / 2, MT), 1), blk(ZT, MT);
-  k_rtrans_fwd<dfl, MT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim,
-                                                                 G.npdim, G.nzdim, nrc);
+  k_rtrans_fwd<T, MT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim, G.npdim,
+                                                          G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
-// the m = 0 plane of the Legendre table in double-float, tab0[i + nrh j] = pf(i, j) split into an
-// FP32 pair on the integer pipe; built once per kit
-__global__ void k_m0_tab(const double* __restrict__ pf, float2* __restrict__ t, size_t n) {
-  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) t[o] = d2ff(pf[o]);
-}
-static float2* g_m0tab = nullptr;
-static float4* g_m0col = nullptr;   // the m = 0 plane's rows split, [z][j]: (re.h, re.l, im.h, im.l)
-static size_t g_m0bytes = 0, g_m0cbytes = 0;
-void m0_free() {
-  if (g_m0tab) dfree(g_m0tab, g_m0bytes);
-  if (g_m0col) dfree(g_m0col, g_m0cbytes);
-  g_m0tab = nullptr; g_m0col = nullptr;
-  g_m0bytes = g_m0cbytes = 0;
-}
-static int m0_tab() {
-  if (g_m0tab) return 0;
-  const size_t n = (size_t)G.nrh * G.ne;
-  g_m0bytes = n * sizeof(float2);
-  g_m0cbytes = (size_t)G.nzdim * G.ne * sizeof(float4);
-  MLG_TRY(dmalloc((void**)&g_m0tab, g_m0bytes));
-  MLG_TRY(dmalloc((void**)&g_m0col, g_m0cbytes));
-  k_m0_tab<<<nblk(n), 256, 0, G.stream>>>(G.pf, g_m0tab, n);
+// Backward: the planes of n <= 3 fields in one launch, 8 x 16 tiles with four K slices (288 CTAs of 512
+// threads for three fields at 192 x 128 x 128).
+template <typename T>
+static int plane_rtrans_bwd(const cd* const* in, cd* const* out, const double* const* lnp, int n, int nrc, bool add_ln,
+                            cudaStream_t st) {
+  constexpr int IT = 8, ZT = 16, KC = 8, KS = 4;
+  if (nrc <= 0 || n < 1) return 0;
+  if (n > 3) return set_error(MLG_EPARAM, "rtrans_backward: at most three m = 0 planes per launch");
+  PlaneSet ps;
+  for (int f = 0; f < 3; ++f) {
+    const int g = f < n ? f : 0;
+    ps.in[f] = in[g]; ps.out[f] = out[g]; ps.lnp[f] = lnp[g];
+  }
+  dim3 grid(cdiv(G.nzdim, ZT), cdiv(G.nrh, IT), n), blk(ZT, IT, KS);
+  k_rtrans_bwd_plane<T, IT, ZT, KC, KS><<<grid, blk, 0, st>>>(ps, G.pf, G.lnx, add_ln ? 1 : 0, G.nr, G.nrh, G.ne, G.nrdim,
+                                                              G.npdim, G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
-
-// the m = 0 plane's rows j < nn of every column z split into FP32 pairs, once per transform
-__global__ void k_m0_split(const double2* __restrict__ in, float4* __restrict__ col, int nrdim, int npdim, int nzdim,
-                           int nn) {
-  const size_t n = (size_t)nzdim * nn;
-  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
-    const int z = (int)(o / nn), j = (int)(o % nn);
-    const double2 v = in[(size_t)nrdim * npdim * z + j];
-    const float2 a = d2ff(v.x), b = d2ff(v.y);
-    col[o] = make_float4(a.x, a.y, b.x, b.y);
-  }
+// the m = 0 plane of one or more fields in the arithmetic of the form: double-float (mixed), FP64 (plain)
+static int plane_bwd(const cd* const* in, cd* const* out, const double* const* lnp, int n, int nrc, bool add_ln,
+                     cudaStream_t st) {
+  return G.precision == MLG_MIXED ? plane_rtrans_bwd<dfl>(in, out, lnp, n, nrc, add_ln, st)
+                                  : plane_rtrans_bwd<double>(in, out, lnp, n, nrc, add_ln, st);
+}
+static int plane_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
+  return G.precision == MLG_MIXED ? plane_rtrans_fwd<dfl>(in, out, nrc, st) : plane_rtrans_fwd<double>(in, out, nrc, st);
 }
 
-// the m = 0 plane of the backward transform in double-float: one warp per (column z, four radial
-// point pairs i), its lanes (i, row group g) summing rows 2t, 2t+1 for t = g mod 8 and reducing the
-// eight groups by shuffles.  Table and column arrive split (no conversion in the loop).  The plane is
-// 1/65 of the work and runs beside the tensor-core kernel, which holds most SMs' register files.
-__global__ void __launch_bounds__(256) k_m0_bwd_df(const float4* __restrict__ col, double2* __restrict__ out,
-                                                   const float2* __restrict__ tab, const double* __restrict__ lnx,
-                                                   const double* __restrict__ lnp, int add_ln, int nr, int nrh, int nrdim,
-                                                   int npdim, int nzdim, int nn) {
-  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  const int nig = (nrh + 3) / 4;
-  const int z = wid / nig, i0 = (wid % nig) * 4;
-  if (z >= nzdim) return;
-  const int g = lane >> 2, i = i0 + (lane & 3), ic = min(i, nrh - 1);
-  const float4* c = col + (size_t)nn * z;
-  dfl er = 0, ei = 0, orr = 0, oi = 0;
-  const int nt = (nn + 1) / 2;
-  for (int t = g; t < nt; t += 8) {
-    const int je = 2 * t, jo = je + 1;
-    const float2 ae = tab[ic + (size_t)nrh * je];
-    const float4 ce = c[je];
-    er = tmac(dfl(ae.x, ae.y), dfl(ce.x, ce.y), er);
-    ei = tmac(dfl(ae.x, ae.y), dfl(ce.z, ce.w), ei);
-    if (jo < nn) {
-      const float2 ao = tab[ic + (size_t)nrh * jo];
-      const float4 co = c[jo];
-      orr = tmac(dfl(ao.x, ao.y), dfl(co.x, co.y), orr);
-      oi = tmac(dfl(ao.x, ao.y), dfl(co.z, co.w), oi);
-    }
-  }
-#pragma unroll
-  for (int o = 4; o < 32; o <<= 1) {
-    er = er + df_shfl_xor(er, o); ei = ei + df_shfl_xor(ei, o);
-    orr = orr + df_shfl_xor(orr, o); oi = oi + df_shfl_xor(oi, o);
-  }
-  if (g == 0 && i < nrh) {
-    double2* base = out + (size_t)nrdim * npdim * z;
-    double2 p = to_d2<dfl>(er + orr, ei + oi);
-    double2 q = to_d2<dfl>(er - orr, ei - oi);
-    if (add_ln) { double lnv = *lnp; p.x += lnv * lnx[i]; q.x += lnv * lnx[nr - 1 - i]; }
-    base[i] = p;
-    base[nr - 1 - i] = q;
-  }
-}
-
-static int m0_rtrans_bwd(const cd* in, cd* out, int nrc, const double* lnp, bool add_ln, cudaStream_t st) {
-  if (nrc <= 0) return 0;
-  k_m0_split<<<nblk((size_t)G.nzdim * nrc), 256, 0, st>>>(in, g_m0col, G.nrdim, G.npdim, G.nzdim, nrc);
-  MLG_LAUNCH();
-  const int warps = ((G.nrh + 3) / 4) * G.nzdim;
-  k_m0_bwd_df<<<cdiv(warps, 8), 256, 0, st>>>(g_m0col, out, g_m0tab, G.lnx, lnp, add_ln ? 1 : 0, G.nr, G.nrh, G.nrdim,
-                                              G.npdim, G.nzdim, nrc);
-  MLG_LAUNCH();
-  return 0;
-}
 
 // the rows of each column (m, z) of a mixed-form contraction's output that its kernels leave
 // unwritten, to zero: mode 0 (forward radial transform, projection) rows >= nn(m), and the whole column
@@ -419,7 +532,7 @@ int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu) {
   return 0;
 }
 
-// the FP64 DFMA contractions over m < mcount (mcount 1: the m = 0 plane alone)
+// the FP64 DFMA contractions over every m < mcount (kits the exact-slice contraction does not cover)
 static int dfma_rtrans_fwd(const cd* in, cd* out, int nrc, int mcount, cudaStream_t st) {
   constexpr int MT = 32, ZT = 32, KC = 16, MPT = 2, ZPT = 4;
   int tt = cdiv((nrc + 1) / 2, MT);
@@ -455,7 +568,7 @@ int launch_rtrans_fwd(Scalar& s) {
   if (npc > 0) {
     if (mixed) {
       MLG_TRY(side_fork());
-      MLG_TRY(m0_rtrans_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
+      MLG_TRY(plane_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
       if (xs) MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, false));   // m >= 1: 42-bit slices
       else MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: split BF16 (tc_radial.cu)
       MLG_TRY(side_join());
@@ -463,7 +576,7 @@ int launch_rtrans_fwd(Scalar& s) {
       // m = 0 (the axisymmetric mean flow, whose large range within a column the fixed-point slices
       // would cut relative to its maximum) in FP64 DFMA beside; m >= 1 as FP64-grade slices
       MLG_TRY(side_fork());
-      MLG_TRY(dfma_rtrans_fwd(s.e, out, nrc, 1, G.side));
+      MLG_TRY(plane_fwd(s.e, out, nrc, G.side));
       MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, true));
       MLG_TRY(side_join());
     } else {
@@ -493,15 +606,14 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (mixed) {
-      MLG_TRY(m0_tab());
       MLG_TRY(side_fork());
-      MLG_TRY(m0_rtrans_bwd(s.e, out, nrc, s.ln, add_ln, G.side));   // m = 0: double-float, beside
+      MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));   // m = 0: double-float, beside
       if (xs) MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, false));   // m >= 1: 42-bit slices
       else MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));           // m >= 1: split BF16
       MLG_TRY(side_join());
     } else if (xs) {
       MLG_TRY(side_fork());
-      MLG_TRY(dfma_rtrans_bwd(s.e, out, nrc, 1, s.ln, add_ln, G.side));   // m = 0: FP64 DFMA, beside
+      MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));   // m = 0: FP64 DFMA, beside
       MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, true));   // m >= 1: FP64-grade slices
       MLG_TRY(side_join());
     } else {
@@ -548,12 +660,9 @@ int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln) {
     MLG_TRY(launch_zero_tails(out[i], 1, nrc, npc, G.nzdim, G.nzdim + 1));
   }
   kt_begin(KT_RBWD);
-  if (mixed) MLG_TRY(m0_tab());
   MLG_TRY(side_fork());
-  for (int i = 0; i < n; ++i) {   // m = 0 beside: double-float (mixed) or FP64 DFMA (plain)
-    if (mixed) MLG_TRY(m0_rtrans_bwd(in[i], out[i], nrc, lnp[i], add_ln, G.side));
-    else MLG_TRY(dfma_rtrans_bwd(in[i], out[i], nrc, 1, lnp[i], add_ln, G.side));
-  }
+  // the m = 0 planes of all fields beside, in one launch: double-float (mixed) or FP64 DFMA (plain)
+  MLG_TRY(plane_bwd(in, out, lnp, n, nrc, add_ln, G.side));
   MLG_TRY(xs_rtrans_multi(1, in, out, n, nrc, npc, 1, lnp, add_ln, !mixed));   // m >= 1, all fields
   MLG_TRY(side_join());
   kt_end(KT_RBWD, n * fwd_flops(nrc, npc));
@@ -591,10 +700,10 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
     // m >= 1 on the tensor cores (split BF16, the u_z term in exact digit slices), m = 0 in
     // double-float beside it
     MLG_TRY(side_fork());
-    constexpr int DMT = 16, DZT = 8;
-    dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT);
-    k_vec2tp<dfl, DMT, DZT, KC, 1><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr, G.nrh,
-                                                               G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
+    constexpr int DMT = 16, DZT = 8, DKC = 8, DKS = 4;
+    dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT, DKS);
+    k_vec2tp_plane<dfl, DMT, DZT, DKC, DKS><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tD, G.tT, G.ak, G.nr, G.nrh,
+                                                                         G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
     MLG_LAUNCH();
     if (xv) MLG_TRY(xv_contract(ur, up, uz, psi, chi, nrc, npc, 1));   // m >= 1: 35-bit slices
     else MLG_TRY(pv_contract(ur, up, uz, psi, chi, nrc, npc));                // m >= 1: split BF16 (tc_vec2tp.cu)
