@@ -558,6 +558,7 @@ struct SolveArgs {
   int no_ln;            // substitution: skip the log-term handling of the (0,0) column
   double2* e2 = nullptr;  // substitution: a second field with the same matrices (paired solve), or null
   double* lnp2 = nullptr;
+  int* pivflag = nullptr;  // per 32 systems: non-zero when one of them exchanges rows (factor writes, substitution reads)
 };
 
 // entry (i, j) (0-based) of D(m,k) = D0(m) - ak^2 I for an n x n truncation
@@ -851,6 +852,7 @@ __global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restr
     for (int t = 1; t <= FKL; ++t)
       if (t <= km && fabs(W[t][0]) > best) { best = fabs(W[t][0]); p = t; }
     if (best == 0.0) { atomicExch(a.status, 1); return; }
+    if (p != 0 && a.pivflag) atomicOr(&a.pivflag[sys >> 5], 1);
 #pragma unroll
     for (int t = 1; t <= FKL; ++t)
       if (t == p) {
@@ -1004,7 +1006,7 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
   const double* fbase = fac + sys0 + 2 * (th & 15);
   auto stage_fac_t = [&](auto bwdc, auto npc, int g) {
     constexpr bool BWD = decltype(bwdc)::value, NP = decltype(npc)::value;
-    constexpr int NSL = BWD ? (NP ? FKU + 1 : SNU + 1) : FKL + 1, S0 = BWD ? FKL + 1 : 0;
+    constexpr int NSL = BWD ? (NP ? FKU + 1 : SNU + 1) : (NP ? FKL : FKL + 1), S0 = BWD ? FKL + 1 : 0;
     const int st = g % SST;
 #pragma unroll
     for (int c = th; c < SGR * NSL * 16; c += NT) {
@@ -1015,40 +1017,47 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
       cpa16cg(&sm.f[st][t][u][2 * (th & 15)], ok ? (const void*)(fbase + ((size_t)j * FSL + S0 + t) * nsp) : (const void*)dummy, ok);
     }
   };
-  auto stage_fac = [&](int g, bool bwd) {
-    stage_fac_t(std::integral_constant<bool, false>(), std::integral_constant<bool, false>(), g);
-    (void)bwd;
-  };
+  // the factorisation records, per 32 systems, whether any of them exchanges rows; a block whose systems
+  // never do runs the forward pass without the pivot slot and the exchanges (the same result bit for bit)
+  const bool blk_nopiv = a.pivflag != nullptr && __ldcg(&a.pivflag[blockIdx.x]) == 0;
   for (int rep = 0; rep < cntw; ++rep) {
     // ---- forward: L y = P b, y(j) into the field's slot of row j ----
     R r[FKL + 1];
     bool piv = false;   // a row exchange in one of this thread's staged rows
 #pragma unroll
     for (int t = 0; t <= FKL; ++t) r[t] = ((rep < cnt && t < nn) ? __ldcg(x + 2 * t) : 0.0);
-    for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_fac(g, false); stage_rows(g, rep, false); } cpa_commit(); }
-    for (int g = 0; g < ng; ++g) {
-      cpa_wait<SST - 2>();
-      __syncthreads();   // group g staged; group g-1 computed; stage (g-1)%SST free
-      if (g + SST - 1 < ng) { stage_fac(g + SST - 1, false); stage_rows(g + SST - 1, rep, false); }
-      cpa_commit();
-      if (g > 0) write_out(g - 1, rep, false);
-      const int st = g % SST;
+    auto forward = [&](auto npc) {
+      constexpr bool NP = decltype(npc)::value;
+      auto stage_f = [&](int g) { stage_fac_t(std::integral_constant<bool, false>(), npc, g); };
+      for (int g = 0; g < SST - 1; ++g) { if (g < ng) { stage_f(g); stage_rows(g, rep, false); } cpa_commit(); }
+      for (int g = 0; g < ng; ++g) {
+        cpa_wait<SST - 2>();
+        __syncthreads();   // group g staged; group g-1 computed; stage (g-1)%SST free
+        if (g + SST - 1 < ng) { stage_f(g + SST - 1); stage_rows(g + SST - 1, rep, false); }
+        cpa_commit();
+        if (g > 0) write_out(g - 1, rep, false);
+        const int st = g % SST;
 #pragma unroll
-      for (int u = 0; u < SGR; ++u) {
-        // the pivot row index p (0..FKL), stored as a double: compared by its high word, off the FP64 pipe
-        const int ph = __double2hiint(sm.f[st][FKL][u][lane]);
-        piv = piv || ph != 0;
+        for (int u = 0; u < SGR; ++u) {
+          if constexpr (!NP) {
+            // the pivot row index p (0..FKL), stored as a double: compared by its high word, off the FP64 pipe
+            const int ph = __double2hiint(sm.f[st][FKL][u][lane]);
+            piv = piv || ph != 0;
 #pragma unroll
-        for (int t = 1; t <= FKL; ++t)
-          if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) { R w = r[0]; r[0] = r[t]; r[t] = w; }
+            for (int t = 1; t <= FKL; ++t)
+              if (ph == (t == 1 ? 0x3FF00000 : 0x40000000)) { R w = r[0]; r[0] = r[t]; r[t] = w; }
+          }
 #pragma unroll
-        for (int t = 1; t <= FKL; ++t) r[t] = fma(-sm.f[st][t - 1][u][lane], r[0], r[t]);
-        reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = r[0];
+          for (int t = 1; t <= FKL; ++t) r[t] = fma(-sm.f[st][t - 1][u][lane], r[0], r[t]);
+          reinterpret_cast<double*>(&sm.o[q][g & 1][u][lane])[comp] = r[0];
 #pragma unroll
-        for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
-        r[FKL] = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
+          for (int t = 0; t < FKL; ++t) r[t] = r[t + 1];
+          r[FKL] = reinterpret_cast<const double*>(&sm.v[q][st][u][lane])[comp];
+        }
       }
-    }
+    };
+    if (blk_nopiv) forward(std::integral_constant<bool, true>());
+    else forward(std::integral_constant<bool, false>());
     cpa_wait<0>();
     __syncthreads();
     if (ng > 0) write_out(ng - 1, rep, false);
@@ -1255,8 +1264,15 @@ void lu_cache_clear() {
   g_lu.clear();
 }
 
+// the factors' per-32-system row-exchange flags follow the factor rows in the cache entry
+static size_t lu_flag_offset(int nrc, size_t nsp) {
+  const int nnmax = std::max(std::min(nrc, G.nrdim), 1);
+  return (size_t)nnmax * FSL * nsp;
+}
+static int* lu_flags(double* buf, int nrc, size_t nsp) { return (int*)(buf + lu_flag_offset(nrc, nsp)); }
+
 // the cached factors of (kind, alpha, chop window), laid out [row][slot][system] with system stride
-// nsp, made by factor() on a miss
+// nsp, then nsp/32 row-exchange flags; made by factor() on a miss
 template <class F>
 static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, double** out, F factor) {
   for (auto& e : g_lu)
@@ -1265,8 +1281,7 @@ static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, do
       *out = e.buf;
       return 0;
     }
-  int nnmax = std::max(std::min(c.nrc, G.nrdim), 1);
-  size_t bytes = (size_t)nnmax * FSL * nsp * sizeof(double);
+  size_t bytes = lu_flag_offset(c.nrc, nsp) * sizeof(double) + (nsp / 32) * sizeof(int);
   if (g_lu.size() >= LU_MAX_ENTRIES) {
     auto it = std::min_element(g_lu.begin(), g_lu.end(), [](const LUEntry& x, const LUEntry& y) { return x.used < y.used; });
     dfree(it->buf, it->bytes);
@@ -1275,7 +1290,7 @@ static int lu_cache_get(int kind, double alpha, const ChopIdx& c, size_t nsp, do
   LUEntry e{kind, alpha, c.nrc, c.npc, c.nzc, c.nzcu, nullptr, bytes, ++g_lu_clock};
   MLG_TRY(dmalloc((void**)&e.buf, bytes));
   // rows past a system's own count (and systems outside the chop) stay zero: pivot offset 0, so a
-  // block's substitution can take its no-exchange path
+  // block's substitution can take its no-exchange paths; the flags start at zero
   MLG_CUDA(cudaMemsetAsync(e.buf, 0, bytes, G.stream));
   MLG_TRY(factor(e.buf));
   g_lu.push_back(e);
@@ -1338,10 +1353,13 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
     b.skip_root = (kind == 2) ? 1 : 0;
     b.nsp = (int)((nsys + 31) / 32 * 32);
     MLG_TRY(lu_cache_get(fkind, alpha, c, (size_t)b.nsp, &fac, [&](double* buf) -> int {
-      k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(b, buf);
+      SolveArgs fa = b;
+      fa.pivflag = lu_flags(buf, b.nrc, (size_t)b.nsp);
+      k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
       MLG_LAUNCH();
       return 0;
     }));
+    b.pivflag = lu_flags(fac, b.nrc, (size_t)b.nsp);
     MLG_TRY(launch_subst<1>(b, fac, nsys));
     if (kind == 2) {
       k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
@@ -1370,10 +1388,13 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   double* fac = nullptr;
   a.nsp = (int)((nsys + 31) / 32 * 32);
   MLG_TRY(lu_cache_get(0, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    SolveArgs fa = a;
+    fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
+  a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
   MLG_TRY(launch_subst<2>(a, fac, nsys));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
@@ -1492,10 +1513,13 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   double* fac = nullptr;
   a.nsp = (int)((nsys + 31) / 32 * 32);
   MLG_TRY(lu_cache_get(kind + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    SolveArgs fa = a;
+    fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
+  a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
   MLG_TRY(launch_subst<1>(a, fac, nsys));
   kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
@@ -1518,10 +1542,13 @@ int launch_band_solve_T_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double al
   double* fac = nullptr;
   a.nsp = (int)((nsys + 31) / 32 * 32);
   MLG_TRY(lu_cache_get(0 + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(a, buf);
+    SolveArgs fa = a;
+    fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
+    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
+  a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
   MLG_TRY(launch_subst<2>(a, fac, nsys));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;

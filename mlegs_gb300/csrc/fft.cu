@@ -672,7 +672,11 @@ template <typename T>
 static int vfft_t(const FSet& fs, int dir, double scale, int m0, int nm, int tr_max, cudaStream_t stream) {
   int L = G.nz;
   if (L <= 1 || nm <= 0) return 0;
-  if (pow2_fast(L)) return tr_max >= 32 ? zfft2_any<T, 32>(fs, dir, scale, m0, nm, stream) : zfft2_any<T, 8>(fs, dir, scale, m0, nm, stream);
+  if (pow2_fast(L)) {
+    if (tr_max >= 32) return zfft2_any<T, 32>(fs, dir, scale, m0, nm, stream);
+    // a single plane (m = 0): four lines per CTA, so that its few hundred lines spread over most SMs
+    return tr_max >= 8 ? zfft2_any<T, 8>(fs, dir, scale, m0, nm, stream) : zfft2_any<T, 4>(fs, dir, scale, m0, nm, stream);
+  }
   if constexpr (std::is_same<T, dfl>::value) {
     return vfft_t<double>(fs, dir, scale, m0, nm, tr_max, stream);   // other lengths: the FP64 Stockham kernel
   } else {

@@ -97,6 +97,72 @@ k_rtrans_fwd(const double2* __restrict__ in, double2* __restrict__ out, const ty
   }
 }
 
+// the m = 0 plane of the forward transform: one output (j, z) per thread of a slice, KS slices of the K
+// range (radial points, chunks of KC dealt round-robin) in the block's z dimension, their partial sums
+// added in shared memory in slice order; grid (ztiles, 2 * ttiles)
+template <typename T, int MT, int ZT, int KC, int KS>
+__global__ void __launch_bounds__(MT * ZT * KS)
+k_rtrans_fwd_plane(const double2* __restrict__ in, double2* __restrict__ out, const typename TabT<T>::t* __restrict__ pf,
+                   const double* __restrict__ w, const float* __restrict__ w32, int nr, int nrh, int nrdim, int npdim,
+                   int nzdim, int nrc) {
+  typedef typename V2<T>::t C;
+  __shared__ T As[KS][KC][MT + 1];
+  __shared__ C Bs[KS][KC][ZT];
+  __shared__ C red[KS - 1][MT][ZT];
+  const int par = blockIdx.y & 1, t0 = (blockIdx.y >> 1) * MT;
+  const int nn = max(nrc, 0);
+  if (2 * t0 + par >= nn) return;   // uniform over the block
+  const int z0 = blockIdx.x * ZT;
+  const int tx = threadIdx.x, ty = threadIdx.y, ks = threadIdx.z;
+  const int nthr = MT * ZT, tid = ty * ZT + tx;
+  C acc;
+  acc.x = 0; acc.y = 0;
+  const T sgn = par ? (T)-1 : (T)1;
+  const int nchunk = (nrh + KC - 1) / KC, nround = (nchunk + KS - 1) / KS;
+  for (int rd = 0; rd < nround; ++rd) {   // the same trip count in every slice (barriers below)
+    const int i0 = (rd * KS + ks) * KC;
+    for (int idx = tid; idx < KC * MT; idx += nthr) {
+      const int ii = idx % KC, tt = idx / KC;
+      const int j = 2 * (t0 + tt) + par, i = i0 + ii;
+      T v = 0;
+      if (j < nn && i < nrh) v = tab<T>(pf, i + (size_t)nrh * j);
+      As[ks][ii][tt] = v;
+    }
+    for (int idx = tid; idx < KC * ZT; idx += nthr) {
+      const int ii = idx % KC, zz = idx / KC;
+      const int i = i0 + ii, z = z0 + zz;
+      C v; v.x = 0; v.y = 0;
+      if (i < nrh && z < nzdim) {
+        const double2* col = in + (size_t)nrdim * npdim * z;
+        const C a = ldc<T>(col + i), b = ldc<T>(col + nr - 1 - i);
+        const T wi = wsel<T>(w, w32, i);
+        v.x = (a.x + sgn * b.x) * wi;
+        v.y = (a.y + sgn * b.y) * wi;
+      }
+      Bs[ks][ii][zz] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < KC; ++ii) {
+      const T av = As[ks][ii][ty];
+      const C bv = Bs[ks][ii][tx];
+      acc.x = tmac(av, bv.x, acc.x);
+      acc.y = tmac(av, bv.y, acc.y);
+    }
+    __syncthreads();
+  }
+  if (ks > 0) red[ks - 1][ty][tx] = acc;
+  __syncthreads();
+  if (ks > 0) return;
+#pragma unroll
+  for (int q = 0; q < KS - 1; ++q) {
+    const C b = red[q][ty][tx];
+    acc.x = acc.x + b.x; acc.y = acc.y + b.y;
+  }
+  const int j = 2 * (t0 + ty) + par, z = z0 + tx;
+  if (j < nn && z < nzdim) out[j + (size_t)nrdim * npdim * z] = to_d2<T>(acc.x, acc.y);
+}
+
 // backward: tile (itile blockIdx.y, ztile blockIdx.x) of mode m; each thread owns IPT rows i and ZPT
 // columns and both parities
 template <typename T, int IT, int ZT, int KC, int IPT, int ZPT>
@@ -465,15 +531,15 @@ static double fwd_flops(int nrc, int npc) {
 
 // The m = 0 plane, in double-float (mixed form) or FP64 (plain form), with small tiles: the plane is
 // 1/65 of the radial work at 192 x 128 x 128, and the tiles of the all-m kernels would give it a few
-// dozen CTAs.  Forward: one output (j, z) per thread, about 190 CTAs of 128 threads per field.
+// dozen CTAs.  Forward: 16 x 8 tiles with four K slices (192 CTAs of 512 threads at 192 x 128 x 128).
 template <typename T>
 static int plane_rtrans_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
-  constexpr int MT = 16, ZT = 8, KC = 16;
+  constexpr int MT = 16, ZT = 8, KC = 8, KS = 4;
   int nn = std::max(nrc, 0);
   if (nn == 0) return 0;
-  dim3 grid(cdiv(G.nzdim, ZT), 2 * cdiv((nn + 1) / 2, MT), 1), blk(ZT, MT);
-  k_rtrans_fwd<T, MT, ZT, KC, 1, 1><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.ne, G.nrdim, G.npdim,
-                                                          G.nzdim, nrc);
+  dim3 grid(cdiv(G.nzdim, ZT), 2 * cdiv((nn + 1) / 2, MT), 1), blk(ZT, MT, KS);
+  k_rtrans_fwd_plane<T, MT, ZT, KC, KS><<<grid, blk, 0, st>>>(in, out, G.pf, G.w, G.w32, G.nr, G.nrh, G.nrdim, G.npdim,
+                                                              G.nzdim, nrc);
   MLG_LAUNCH();
   return 0;
 }
