@@ -36,6 +36,9 @@ DT = 1.0e-3
 Q = 4.0
 PERT = 1.0e-4
 METRIC = "steps/s @192x128x128 (3-D vortex NS step, mixed precision on GPU)"
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the step's largest kernels, from
+# one ncu capture of `bench.py --profile-run` at this workload (profiles/)
+NCU_TRAFFIC = {"k_band_subst<2>": 105.8e6, "k_band_subst<1>": 93.6e6, "k_xs_rtrans<1, 6, 16>": 85.5e6}
 
 
 def workload_params():
@@ -323,22 +326,46 @@ def run_ours(args, rank, world, local, pg):
     dom = max(kt, key=lambda n: kt[n][0])
     d_ms, d_n, d_work = kt[dom]
     avg_ms = d_ms / max(d_n, 1)
-    sum_nn = sum(max(192 - m, 0) for m in range(65))
-    flop_class_bytes = {   # the contraction classes count flops; their algorithmic bytes per launch
-        "radial_fwd": 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2,
-        "radial_bwd": 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2,
-        "vec2tp": 3 * 192 * 65 * 128 * 16 + 2 * (sum_nn + 3 * 65) * 128 * 16 + 12 * sum_nn * 96 * 2}
-    bytes_launch = flop_class_bytes.get(dom, d_work / max(d_n, 1))
+    nrc, npc, nz, nrh, nr = 192, 65, 128, 96, 192
+    sum_nn = sum(max(nrc - m, 0) for m in range(npc))
+    field_full = nr * npc * nz * 16          # rows < nr of every column m < npc (the physical side)
+    field_spec = sum_nn * nz * 16            # rows < nn(m) (the spectral side)
+    flops_field = 4.0 * sum_nn * nrh * nz    # one field's radial transform (complex x real MACs)
+    # the exact-slice table images (mixed form, 42-bit: six BF16 digits per entry and parity, one
+    # 128-row tile, K chunks of 16): read once per launch, from L2 after the first
+    xs_table = npc * 1 * ((nrh + 15) // 16) * 2 * 6 * 128 * 16 * 2
+    xv_table = (npc - 1) * 2 * ((nrh + 15) // 16) * (5 + 5 + 7) * 128 * 16 * 2
+
+    def flop_class_bytes(name, flops, launches):
+        """Algorithmic bytes per launch of a contraction class: the fields its launches transform (counted
+        from its algorithmic flops, one field = flops_field), each read and written once, plus the table
+        images once per launch."""
+        if name in ("radial_fwd", "radial_bwd"):
+            nf = flops / flops_field
+            return (nf * (field_full + field_spec) + launches * xs_table) / max(launches, 1)
+        if name == "vec2tp":
+            nf = flops / (5 * flops_field)
+            return (nf * (3 * field_full + 2 * field_spec) + launches * xv_table) / max(launches, 1)
+        return None
+
+    bytes_launch = flop_class_bytes(dom, d_work, d_n)
+    if bytes_launch is None:
+        bytes_launch = d_work / max(d_n, 1)
     achieved_gbs = bytes_launch / (avg_ms * 1e-3) / 1e9
-    # DRAM traffic per launch of the class's largest kernel from one ncu capture at this workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum), and what limits it
-    # (the solve class is one k_band_subst<2> and one k_band_subst<1> per step: the class mean)
+    # DRAM traffic per launch of the class's kernels from one ncu capture at this workload
+    # (dram__bytes_read.sum + dram__bytes_write.sum), and what limits them
+    r_fields = kt["radial_bwd"][2] / flops_field / max(kt["radial_bwd"][1], 1)   # fields per backward launch
     ncu = {"solve": {"kernel": "k_band_subst<2> (psi and chi Helmholtz) + k_band_subst<1> (idel2)",
-                     "traffic": (164.02e6 + 118.82e6) / 2,
-                     "traffic_per_kernel": {"k_band_subst<2>": 164.02e6, "k_band_subst<1>": 118.82e6},
-                     "limit": "FP64 pipe 56% busy and 10% of warps active (ncu): 8320 systems x 2 parts x NR fields "
-                              "of serial recurrences are about one warp per SM sub-partition; the solves stay FP64 "
-                              "in both forms"}}
+                     "traffic": (NCU_TRAFFIC["k_band_subst<2>"] + NCU_TRAFFIC["k_band_subst<1>"]) / 2,
+                     "traffic_per_kernel": {k: NCU_TRAFFIC[k] for k in ("k_band_subst<2>", "k_band_subst<1>")},
+                     "limit": "latency of each system's serial FP64 recurrence: 8320 systems x 2 parts x NR fields "
+                              "are about one or two warps per SM sub-partition; the FP64 pipe at 48% (ncu); the "
+                              "solves stay FP64 in both forms"},
+           "radial_bwd": {"kernel": "k_xs_rtrans<1, 6, 16> (three fields per launch) + the m = 0 planes beside it",
+                          "traffic": NCU_TRAFFIC["k_xs_rtrans<1, 6, 16>"] * r_fields / 3.0,
+                          "traffic_per_kernel": {"k_xs_rtrans<1, 6, 16> (3 fields)": NCU_TRAFFIC["k_xs_rtrans<1, 6, 16>"]},
+                          "limit": "integer work of the digit cuts and the order sums between mbarrier hand-offs "
+                                   "(ALU pipe 38%, tensor pipe 16%, issue 39% active; ncu)"}}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
             "frac": achieved_gbs / hbm, "traffic": ncu.get(dom, {}).get("traffic"),
             "avg_launch_us": 1e3 * avg_ms, "launches_per_step": d_n / 2,
@@ -349,15 +376,17 @@ def run_ours(args, rank, world, local, pg):
         roof["limit"] = ncu[dom]["limit"]
         if "traffic_per_kernel" in ncu[dom]:
             roof["traffic_per_kernel"] = ncu[dom]["traffic_per_kernel"]
-    # the tensor-core Legendre transforms (backward, m >= 1 on tcgen05 plus the m = 0 plane beside it):
-    # algorithmic flops 4 sum_m nn(m) nrh nz per launch against the bf16 peak
+    # the tensor-core Legendre transforms (backward: m >= 1 on tcgen05, the m = 0 planes beside it):
+    # algorithmic flops 4 sum_m nn(m) nrh nz per field against the bf16 peak; the exact-slice scheme
+    # issues 21 BF16 digit products per algorithmic MAC (six digits a side, orders below six)
     r_ms, r_n, r_flops = kt["radial_bwd"]
     r_avg = r_ms / max(r_n, 1)
     r_tf = (r_flops / max(r_n, 1)) / (r_avg * 1e-3) / 1e12
-    r_bytes = 192 * 65 * 128 * 16 + sum_nn * 128 * 16 + 3 * 2 * sum_nn * 96 * 2
-    roof_tc = {"bound": "tensor", "kernel": "radial_bwd (k_tc_rtrans<1>, split BF16 on tcgen05)", "achieved": r_tf,
-               "peak": bf16, "unit": "TFLOP/s", "frac": r_tf / bf16, "avg_launch_us": 1e3 * r_avg,
-               "bf16_products_per_mac": 6, "algorithmic_flops_per_launch": r_flops / max(r_n, 1),
+    r_bytes = flop_class_bytes("radial_bwd", r_flops, r_n)
+    roof_tc = {"bound": "tensor", "kernel": "radial_bwd (k_xs_rtrans<1, 6, 16>: exact BF16 digit slices on tcgen05)",
+               "achieved": r_tf, "peak": bf16, "unit": "TFLOP/s", "frac": r_tf / bf16, "avg_launch_us": 1e3 * r_avg,
+               "bf16_digit_products_per_mac": 21, "fields_per_launch": r_fields,
+               "algorithmic_flops_per_launch": r_flops / max(r_n, 1),
                "hbm_view": {"algorithmic_bytes_per_launch": r_bytes,
                             "achieved_gbs": r_bytes / (r_avg * 1e-3) / 1e9,
                             "frac": r_bytes / (r_avg * 1e-3) / 1e9 / hbm},

@@ -45,7 +45,7 @@ extern "C" {
 
 /* Precision forms. */
 #define MLG_PLAIN_FP64      0   /* all-FP64: the drop-in form                                       */
-#define MLG_MIXED           1   /* split-precision tensor-core Legendre contractions, FP32 FFTs     */
+#define MLG_MIXED           1   /* 42-bit sliced tensor-core Legendre contractions, FP32 FFTs       */
 
 /* Kit parameters: the module globals of mlegs_base (src/modules/mlegs_base.f90:7-41). */
 typedef struct mlg_params {

@@ -166,6 +166,7 @@ void xv_free();
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
 // zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);
+int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu);
 int pv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc);
 void pv_free();
 
@@ -174,6 +175,7 @@ int launch_zero(cd* e);
 int launch_copy(cd* dst, const cd* src);
 int launch_copy_ln(double* dst, const double* src);
 int launch_set_ln(double* dst, double v);
+int launch_set_ln2(double* d1, double* d2, double v);
 
 // grid-stride loop over n elements (32-bit indices: a field has < 2^32 entries)
 #define GRID_STRIDE(i, n) for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < (unsigned)(n); i += gridDim.x * blockDim.x)
@@ -205,6 +207,10 @@ int op_trans(Scalar& s, const char* space);
 int op_chop(Scalar& s);
 int op_dealias(Scalar& s);
 int op_zeroat1(Scalar& s);
+// the same operators on two fields in one launch where their chop and spaces agree (else one by one)
+int op_chop2(Scalar& a, Scalar& b);
+int op_dealias2(Scalar& a, Scalar& b);
+int op_zeroat1_2(Scalar& a, Scalar& b);
 int op_band(Scalar& s, int op);
 int op_tp2vec(const Scalar& psi, const Scalar& chi, Scalar& vr, Scalar& vp, Scalar& vz);
 int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, Scalar& wz);
@@ -212,8 +218,10 @@ int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scala
 int op_vec2tp(const Scalar& vr, const Scalar& vp, const Scalar& vz, Scalar& psi, Scalar& chi);
 // keep (optional): six scalars that receive the velocity and vorticity (vr, vp, vz, wr, wp, wz, in PPP,
 // vz without the background) the nonlinear term was formed from
+// dealiased: psi and chi are dealiased already (the vortex step's own dealias ran just before), so the
+// routine's first dealias is skipped
 int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz,
-                     Scalar* const* keep = nullptr);
+                     Scalar* const* keep = nullptr, bool dealiased = false);
 // write_prev = false leaves psip and chip unwritten: for every step of a run but its last, whose
 // psip and chip no later step reads
 int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, Scalar& psip, Scalar& chip, Scalar& nlpsip,

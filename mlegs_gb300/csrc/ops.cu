@@ -107,11 +107,15 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 // chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
 // one warp per (m, k) column (8 per block): the column's first zeroed row is worked out once, and
 // only the zeroed rows are written (a column that keeps all its rows touches no memory)
-__global__ void __launch_bounds__(256) k_mask(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int mode, int f0,
-                                              int f1, int f2, int nrc, int npc, int nzc, int nzcu, int pcut, int zcut,
-                                              int zupper, int np_gt1, int nz_gt1) {
-  const int col = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (col >= npdim * nzdim) return;
+__global__ void __launch_bounds__(256) k_mask(double2* __restrict__ e0, double2* __restrict__ e1, int nrdim, int npdim,
+                                              int nzdim, int mode, int f0, int f1, int f2, int nrc, int npc, int nzc,
+                                              int nzcu, int pcut, int zcut, int zupper, int np_gt1, int nz_gt1) {
+  // one warp per column of e0 and, when e1 is given, of e1 (the same mask)
+  const int cf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int ncols = npdim * nzdim;
+  if (cf >= (e1 ? 2 : 1) * ncols) return;
+  double2* e = cf < ncols ? e0 : e1;
+  const int col = cf < ncols ? cf : cf - ncols;
   const int m = col % npdim, k = col / npdim;
   int zf = nrdim;   // rows [zf, nrdim) become zero
   if (mode == 0) {
@@ -172,12 +176,16 @@ __global__ void k_lincomb(LinArgs a) {
 
 // calcat (mlegs_scalar_ops.f90:237-309): calc(k) = sum_n e(n, 1, k) * at(n); zeroat1 (:311-325)
 // additionally subtracts calc(k)/at1(1) from e(1, 1, k).  One warp per k.
-__global__ void k_calcat(double2* __restrict__ e, const double* __restrict__ at, int nmax, int nrdim, int npdim,
-                         int nzdim, double2* __restrict__ out, int zero_mode) {
-  int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  int lane = threadIdx.x & 31;
-  if (k >= nzdim) return;
-  double2* col = e + (size_t)nrdim * npdim * k;
+__global__ void k_calcat(double2* __restrict__ e0, double2* __restrict__ e1, const double* __restrict__ at, int nmax,
+                         int nrdim, int npdim, int nzdim, double2* __restrict__ out, int zero_mode) {
+  // one warp per k of e0 and, when e1 is given, of e1; the values at the point go to out from the last
+  // field (what two calls one after the other leave there)
+  const int kf = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (kf >= (e1 ? 2 : 1) * nzdim) return;
+  const int k = kf < nzdim ? kf : kf - nzdim;
+  if (e1 && kf < nzdim) out = nullptr;
+  double2* col = (kf < nzdim ? e0 : e1) + (size_t)nrdim * npdim * k;
   double sx = 0, sy = 0;
   for (int n = lane; n < nmax; n += 32) { double2 v = col[n]; sx += v.x * at[n]; sy += v.y * at[n]; }
   for (int o = 16; o; o >>= 1) { sx += __shfl_xor_sync(0xffffffffu, sx, o); sy += __shfl_xor_sync(0xffffffffu, sy, o); }
@@ -379,6 +387,10 @@ __global__ void k_idelsqp_ln(const double2* __restrict__ e, double* __restrict__
 }
 __global__ void k_ln_zero(double* __restrict__ lnp) { if (threadIdx.x == 0) *lnp = 0.0; }
 __global__ void k_ln_set(double* __restrict__ lnp, double v) { if (threadIdx.x == 0) *lnp = v; }
+__global__ void k_ln_set2(double* __restrict__ a, double* __restrict__ b, double v) {
+  if (threadIdx.x == 0) *a = v;
+  if (threadIdx.x == 1) *b = v;
+}
 __global__ void k_ln_copy(double* __restrict__ d, const double* __restrict__ s) { if (threadIdx.x == 0) *d = *s; }
 
 // field copy that also carries the ln slot (assignment(=), mlegs_scalar_init.f90:106-140)
@@ -407,6 +419,7 @@ int launch_copy_ln(double* d, const double* s) {
   return 0;
 }
 int launch_set_ln(double* d, double v) { k_ln_set<<<1, 32, 0, G.stream>>>(d, v); MLG_LAUNCH(); return 0; }
+int launch_set_ln2(double* a, double* b, double v) { k_ln_set2<<<1, 32, 0, G.stream>>>(a, b, v); MLG_LAUNCH(); return 0; }
 
 int launch_ln_adjust(Scalar& s, double sign) {
   size_t n = (size_t)G.nr * G.nzdim;
@@ -527,21 +540,47 @@ int op_trans(Scalar& s, const char* space) {
   return 0;
 }
 
-int op_chop(Scalar& s) {
-  ChopIdx c;
-  MLG_TRY(chop_index(s, c));
-  k_mask<<<cdiv((long long)G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F',
-                                              s.space[2] == 'F', c.nrc, c.npc, c.nzc, c.nzcu, 0, 0, 0, 0, 0);
+// chop of one field, or of two (b non-null) with the same chop window and space
+static int chop_launch(Scalar& s, Scalar* b, const ChopIdx& c) {
+  k_mask<<<cdiv((long long)(b ? 2 : 1) * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
+      s.e, b ? b->e : nullptr, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F', s.space[2] == 'F', c.nrc,
+      c.npc, c.nzc, c.nzcu, 0, 0, 0, 0, 0);
   MLG_LAUNCH();
   return 0;
 }
+int op_chop(Scalar& s) {
+  ChopIdx c;
+  MLG_TRY(chop_index(s, c));
+  return chop_launch(s, nullptr, c);
+}
+int op_chop2(Scalar& a, Scalar& b) {
+  ChopIdx ca, cb;
+  MLG_TRY(chop_index(a, ca));
+  MLG_TRY(chop_index(b, cb));
+  const bool same = ca.nrc == cb.nrc && ca.npc == cb.npc && ca.nzc == cb.nzc && ca.nzcu == cb.nzcu &&
+                    std::strncmp(a.space, b.space, 3) == 0 && a.e != b.e;
+  if (!same) {
+    MLG_TRY(chop_launch(a, nullptr, ca));
+    return chop_launch(b, nullptr, cb);
+  }
+  return chop_launch(a, &b, ca);
+}
 
-int op_dealias(Scalar& s) {
+static int dealias_launch(Scalar& s, Scalar* b) {
   int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
-  k_mask<<<cdiv((long long)G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F',
-                                              0, 0, 0, 0, pcut, zcut, zupper, G.np > 1, G.nz > 1);
+  k_mask<<<cdiv((long long)(b ? 2 : 1) * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
+      s.e, b ? b->e : nullptr, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F', 0, 0, 0, 0, pcut, zcut,
+      zupper, G.np > 1, G.nz > 1);
   MLG_LAUNCH();
   return 0;
+}
+int op_dealias(Scalar& s) { return dealias_launch(s, nullptr); }
+int op_dealias2(Scalar& a, Scalar& b) {
+  if (a.space[1] != b.space[1] || a.space[2] != b.space[2] || a.e == b.e) {
+    MLG_TRY(dealias_launch(a, nullptr));
+    return dealias_launch(b, nullptr);
+  }
+  return dealias_launch(a, &b);
 }
 
 // svv_filter with the gain kept in device memory (gain_dev)
@@ -589,7 +628,7 @@ int calcat_dev(Scalar& s, const double* at, bool zero_mode) {
   ChopIdx c;
   MLG_TRY(chop_index(s, c));
   int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
-  k_calcat<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, at, nmax, G.nrdim, G.npdim, G.nzdim,
+  k_calcat<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, nullptr, at, nmax, G.nrdim, G.npdim, G.nzdim,
                                                     (double2*)(G.dscal + DS_CALC), zero_mode ? 1 : 0);
   MLG_LAUNCH();
   return 0;
@@ -614,6 +653,24 @@ int op_calcat(Scalar& s, int which, double* host_out) {
 int op_zeroat1(Scalar& s) {
   if (!s.is("FFF")) MLG_TRY(op_trans(s, "FFF"));
   return calcat_dev(s, G.at1, true);
+}
+int op_zeroat1_2(Scalar& a, Scalar& b) {
+  if (!a.is("FFF") || !b.is("FFF") || a.e == b.e) {
+    MLG_TRY(op_zeroat1(a));
+    return op_zeroat1(b);
+  }
+  ChopIdx ca, cb;
+  MLG_TRY(chop_index(a, ca));
+  MLG_TRY(chop_index(b, cb));
+  const int na = std::min(std::min(G.nrdim, ca.nrc), G.nrchop), nb = std::min(std::min(G.nrdim, cb.nrc), G.nrchop);
+  if (na != nb) {
+    MLG_TRY(op_zeroat1(a));
+    return op_zeroat1(b);
+  }
+  k_calcat<<<cdiv(2 * G.nzdim, 4), 128, 0, G.stream>>>(a.e, b.e, G.at1, na, G.nrdim, G.npdim, G.nzdim,
+                                                        (double2*)(G.dscal + DS_CALC), 1);
+  MLG_LAUNCH();
+  return 0;
 }
 
 static int require_fff(Scalar& s) {
@@ -897,8 +954,8 @@ static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& 
   MLG_TRY(op_idel2(chi, false, 0.0));
   psi.off[0] = psi.off[1] = psi.off[2] = 0;
   chi.off[0] = chi.off[1] = chi.off[2] = 0;
-  MLG_TRY(op_chop(psi)); MLG_TRY(op_chop(chi));
-  MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
+  MLG_TRY(op_chop2(psi, chi));
+  MLG_TRY(op_zeroat1_2(psi, chi));
   return 0;
 }
 
@@ -989,10 +1046,11 @@ int op_tp2curlvec(const Scalar& psi, const Scalar& chi, Scalar& wr, Scalar& wp, 
 }
 
 // advection_rhs (vortical_flow_3d.f90:353-395)
-int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz, Scalar* const* keep) {
+int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, const Scalar& uz, Scalar* const* keep,
+                     bool dealiased) {
   if (!psi.is("FFF") || !chi.is("FFF") || !nlpsi.is("FFF") || !nlchi.is("FFF") || !uz.is("PPP"))
     return set_error(MLG_ESPACE, "advection_rhs: psi, chi, nlpsi, nlchi must be in FFF and uz in PPP");
-  MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
+  if (!dealiased) MLG_TRY(op_dealias2(psi, chi));
   TMP(vr_t); TMP(vp_t); TMP(vz_t); TMP(wr_t); TMP(wp_t); TMP(wz_t);
   Scalar* vw[6] = {&vr_t, &vp_t, &vz_t, &wr_t, &wp_t, &wz_t};
   if (keep) for (int i = 0; i < 6; ++i) vw[i] = keep[i];
@@ -1006,8 +1064,8 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
   Scalar* prod[3] = {&vr_t, &vp_t, &vz_t};
   MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz, keep ? prod : nullptr));
   MLG_TRY(vec2tp_core(vr_t, vp_t, vz_t, nlpsi, nlchi));
-  MLG_TRY(launch_set_ln(nlpsi.ln, 0.0)); MLG_TRY(launch_set_ln(nlchi.ln, 0.0));
-  MLG_TRY(op_dealias(nlpsi)); MLG_TRY(op_dealias(nlchi));
+  MLG_TRY(launch_set_ln2(nlpsi.ln, nlchi.ln, 0.0));
+  MLG_TRY(op_dealias2(nlpsi, nlchi));
   return 0;
 }
 
@@ -1018,10 +1076,12 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
   for (Scalar* q : {&psi, &chi, &nlpsi, &nlchi, &psip, &chip, &nlpsip, &nlchip}) MLG_TRY(op_trans(*q, "FFF"));
   // nlpsi and nlchi are recomputed in full by the advection below
   MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt, true, write_prev));
-  MLG_TRY(op_dealias(psi)); MLG_TRY(op_dealias(chi));
+  MLG_TRY(op_dealias2(psi, chi));
   MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
-  MLG_TRY(op_zeroat1(psi)); MLG_TRY(op_zeroat1(chi));
-  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz, keep));
+  MLG_TRY(op_zeroat1_2(psi, chi));
+  // advection_rhs's own dealias of psi and chi (vortical_flow_3d.f90:368) finds them dealiased
+  // already: the SVV gain and zeroat1 leave a zero coefficient zero, so it is skipped here
+  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz, keep, true));
   k_finite<<<nblk(G.fsize), 256, 0, G.stream>>>(psi.e, chi.e, G.fsize, (int*)(G.dscal + DS_FLAG));
   MLG_LAUNCH();
   return 0;

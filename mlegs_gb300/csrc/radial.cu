@@ -577,25 +577,32 @@ static int plane_fwd(const cd* in, cd* out, int nrc, cudaStream_t st) {
 // unwritten, to zero: mode 0 (forward radial transform, projection) rows >= nn(m), and the whole column
 // where z is outside the kept band k <= nzc or k >= nzcu; mode 1 (backward radial transform) rows >= nr
 // (the padding), the whole column where nn(m) = 0; columns m >= npc whole.  One warp per column.
-__global__ void k_zero_tails(double2* __restrict__ out, int mode, int nr, int nrdim, int npdim, int nzdim, int nrc,
-                             int npc, int nzc, int nzcu) {
+__global__ void k_zero_tails(double2* __restrict__ out0, double2* __restrict__ out1, double2* __restrict__ out2, int nf,
+                             int mode, int nr, int nrdim, int npdim, int nzdim, int nrc, int npc, int nzc, int nzcu) {
   const int lane = threadIdx.x & 31;
   const size_t ncols = (size_t)npdim * nzdim, nw = (size_t)gridDim.x * (blockDim.x >> 5);
-  for (size_t c = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < ncols; c += nw) {
+  for (size_t cf = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5); cf < ncols * nf; cf += nw) {
+    const int f = (int)(cf / ncols);
+    const size_t c = cf - (size_t)f * ncols;
     const int m = (int)(c % npdim), kk = (int)(c / npdim) + 1;
     const int nn = (m < npc && (kk <= nzc || kk >= nzcu)) ? max(min(nrc, nrc - m), 0) : 0;
     const int lim = mode == 0 ? nn : (nn > 0 ? nr : 0);
-    double2* col = out + (size_t)nrdim * c;
+    double2* col = (f == 0 ? out0 : (f == 1 ? out1 : out2)) + (size_t)nrdim * c;
     for (int j = lim + lane; j < nrdim; j += 32) col[j] = make_double2(0.0, 0.0);
   }
 }
 
-int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu) {
-  const size_t ncols = (size_t)G.npdim * G.nzdim;
-  k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, G.stream>>>(out, mode, G.nr, G.nrdim, G.npdim,
-                                                                                    G.nzdim, nrc, npc, nzc, nzcu);
+// the tails of n <= 3 outputs with the same chop in one launch
+int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu) {
+  if (n < 1 || n > 3) return set_error(MLG_EPARAM, "zero_tails: one to three fields per launch");
+  const size_t ncols = (size_t)G.npdim * G.nzdim * n;
+  k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, G.stream>>>(
+      out[0], n > 1 ? out[1] : out[0], n > 2 ? out[2] : out[0], n, mode, G.nr, G.nrdim, G.npdim, G.nzdim, nrc, npc, nzc, nzcu);
   MLG_LAUNCH();
   return 0;
+}
+int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu) {
+  return launch_zero_tails_n(&out, 1, mode, nrc, npc, nzc, nzcu);
 }
 
 // the FP64 DFMA contractions over every m < mcount (kits the exact-slice contraction does not cover)
@@ -723,8 +730,8 @@ int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln) {
     }
     in[i] = f[i]->e;
     lnp[i] = f[i]->ln;
-    MLG_TRY(launch_zero_tails(out[i], 1, nrc, npc, G.nzdim, G.nzdim + 1));
   }
+  MLG_TRY(launch_zero_tails_n(out, n, 1, nrc, npc, G.nzdim, G.nzdim + 1));
   kt_begin(KT_RBWD);
   MLG_TRY(side_fork());
   // the m = 0 planes of all fields beside, in one launch: double-float (mixed) or FP64 DFMA (plain)
@@ -752,8 +759,8 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   const bool xv = mixed && xv_supported();
   // the tensor-core contractions write rows < nn(m) of the kept columns: only the rest needs zeros
   if (mixed) {
-    MLG_TRY(launch_zero_tails(psi, 0, nrc, npc, nzc, nzcu));
-    MLG_TRY(launch_zero_tails(chi, 0, nrc, npc, nzc, nzcu));
+    cd* pc[2] = {psi, chi};
+    MLG_TRY(launch_zero_tails_n(pc, 2, 0, nrc, npc, nzc, nzcu));
   } else {
     MLG_CUDA(cudaMemsetAsync(psi, 0, G.fsize * sizeof(cd), G.stream));
     MLG_CUDA(cudaMemsetAsync(chi, 0, G.fsize * sizeof(cd), G.stream));
