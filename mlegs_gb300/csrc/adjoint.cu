@@ -107,11 +107,14 @@ __global__ void __launch_bounds__(1024) k_ln_dot(const double2* __restrict__ e, 
 
 // zeroat1^T: the forward sets e(0,0,k) <- e(0,0,k) - sum_{n<nmax} at_n e(n,0,k) / at_0, so
 // e_bar(n,0,k) -= at_n / at_0 * e_bar(0,0,k) for n < nmax (which leaves e_bar(0,0,k) = 0); warp per k
-__global__ void k_zeroat1_T(double2* __restrict__ e, const double* __restrict__ at, int nmax, int nrdim, int npdim, int nzdim) {
-  int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  int lane = threadIdx.x & 31;
-  if (k >= nzdim) return;
-  double2* col = e + (size_t)nrdim * npdim * k;
+// one warp per k of e0 and, when e1 is given, of e1
+__global__ void k_zeroat1_T(double2* __restrict__ e0, double2* __restrict__ e1, const double* __restrict__ at, int nmax,
+                            int nrdim, int npdim, int nzdim) {
+  const int kf = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (kf >= (e1 ? 2 : 1) * nzdim) return;
+  const int k = kf < nzdim ? kf : kf - nzdim;
+  double2* col = (kf < nzdim ? e0 : e1) + (size_t)nrdim * npdim * k;
   double bx = 0.0, by = 0.0;
   if (lane == 0) { bx = col[0].x; by = col[0].y; }
   bx = __shfl_sync(0xffffffffu, bx, 0);
@@ -584,7 +587,21 @@ int zeroat1_T(Scalar& s) {
   ChopIdx c;
   MLG_TRY(chop_index(s, c));
   int nmax = std::min(std::min(G.nrdim, c.nrc), G.nrchop);
-  k_zeroat1_T<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, G.at1, nmax, G.nrdim, G.npdim, G.nzdim);
+  k_zeroat1_T<<<cdiv(G.nzdim, 4), 128, 0, G.stream>>>(s.e, nullptr, G.at1, nmax, G.nrdim, G.npdim, G.nzdim);
+  MLG_LAUNCH();
+  return 0;
+}
+// zeroat1^T of two distinct fields with the same chop in one launch
+static int zeroat1_T2(Scalar& a, Scalar& b) {
+  ChopIdx ca, cb;
+  MLG_TRY(chop_index(a, ca));
+  MLG_TRY(chop_index(b, cb));
+  const int na = std::min(std::min(G.nrdim, ca.nrc), G.nrchop), nb = std::min(std::min(G.nrdim, cb.nrc), G.nrchop);
+  if (na != nb || a.e == b.e) {
+    MLG_TRY(zeroat1_T(a));
+    return zeroat1_T(b);
+  }
+  k_zeroat1_T<<<cdiv(2 * G.nzdim, 4), 128, 0, G.stream>>>(a.e, b.e, G.at1, na, G.nrdim, G.npdim, G.nzdim);
   MLG_LAUNCH();
   return 0;
 }
@@ -605,7 +622,7 @@ int tp2vec_T(const Scalar& vrb, const Scalar& vpb, const Scalar& vzb, Scalar& ps
   // u_r, u_phi branches: xxdx (offset 3), combination, chop, trans to PPP, division by r
   MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
   MLG_TRY(trans_T(ur, "FFF")); MLG_TRY(trans_T(up, "FFF"));
-  MLG_TRY(op_chop(ur)); MLG_TRY(op_chop(up));
+  MLG_TRY(op_chop2(ur, up));
   ur.off[0] = 3; up.off[0] = 3;
   ChopIdx c;
   MLG_TRY(chop_index(ur, c));
@@ -638,8 +655,8 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
   TMP(pb); TMP(cb);
   MLG_TRY(assign(pb, psib_in)); MLG_TRY(assign(cb, chib_in));
   set_fff0(pb); set_fff0(cb);
-  MLG_TRY(zeroat1_T(pb)); MLG_TRY(zeroat1_T(cb));
-  MLG_TRY(op_chop(pb)); MLG_TRY(op_chop(cb));
+  MLG_TRY(zeroat1_T2(pb, cb));
+  MLG_TRY(op_chop2(pb, cb));
   MLG_TRY(idel2_proln_T(cb));
   TMP(ur); TMP(up); TMP(uz);
   MLG_TRY(launch_zero(ur.e)); MLG_TRY(launch_zero(up.e)); MLG_TRY(launch_zero(uz.e));
@@ -711,8 +728,8 @@ int nlcore_T(const Scalar* psi, const Scalar* chi, const Scalar& uzb, const Scal
   TMP(np_); TMP(nc_);
   MLG_TRY(assign(np_, nlpb)); MLG_TRY(assign(nc_, nlcb));
   set_fff0(np_); set_fff0(nc_);
-  MLG_TRY(op_dealias(np_)); MLG_TRY(op_dealias(nc_));
-  MLG_TRY(launch_set_ln(np_.ln, 0.0)); MLG_TRY(launch_set_ln(nc_.ln, 0.0));
+  MLG_TRY(op_dealias2(np_, nc_));
+  MLG_TRY(launch_set_ln2(np_.ln, nc_.ln, 0.0));
   TMP(obr); TMP(obp); TMP(obz);
   MLG_TRY(vec2tp_T(np_, nc_, obr, obp, obz));
   // the linearisation point: v and w of the forward, kept by the forward step (they are consumed
@@ -732,15 +749,20 @@ int nlcore_T(const Scalar* psi, const Scalar* chi, const Scalar& uzb, const Scal
   k_vecprod_T<<<nblk(G.fsize), 256, 0, G.stream>>>(vbr.e, vbp.e, vbz.e, wbr.e, wbp.e, wbz.e, vr.e, vp.e, vz.e, wr.e, wp.e,
                                                     wz.e, obr.e, obp.e, obz.e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
   MLG_LAUNCH();
-  for (Scalar* q : {&vbr, &vbp, &vbz, &wbr, &wbp, &wbz}) {
-    q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0;
-    MLG_TRY(launch_set_ln(q->ln, 0.0));
+  {
+    double* lns[6];
+    int i = 0;
+    for (Scalar* q : {&vbr, &vbp, &vbz, &wbr, &wbp, &wbz}) {
+      q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0;
+      lns[i++] = q->ln;
+    }
+    MLG_TRY(launch_set_ln_n(lns, 6, 0.0));
   }
   TMP(pa); TMP(ca);
   MLG_TRY(tp2vec_T(vbr, vbp, vbz, pa, ca));
   MLG_TRY(tp2curlvec_T(wbr, wbp, wbz, psib, chib));
-  MLG_TRY(lincomb(psib, {{&psib, 1.0}, {&pa, 1.0}}, {{&psib, 1.0}, {&pa, 1.0}}));
-  MLG_TRY(lincomb(chib, {{&chib, 1.0}, {&ca, 1.0}}, {{&chib, 1.0}, {&ca, 1.0}}));
+  MLG_TRY(lincomb_n({lin_args(psib, {{&psib, 1.0}, {&pa, 1.0}}, {{&psib, 1.0}, {&pa, 1.0}}),
+                     lin_args(chib, {{&chib, 1.0}, {&ca, 1.0}}, {{&chib, 1.0}, {&ca, 1.0}})}));
   return 0;
 }
 
@@ -756,28 +778,30 @@ int advection_T(const Scalar& psi, const Scalar& chi, const Scalar& uzb, const S
   return 0;
 }
 
-// abcn^T (hyperpow = 0): sb holds the adjoint of the new s; on return sb holds the adjoint w.r.t.
-// the old s, and nlb, nlpb have received the adjoints w.r.t. nl and nl_p (added)
-static int abcn_T_rest(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt);
-// abcn^T of the psi and chi chains of a step: the two transposed Helmholtz solves in one pass, the
-// rest per field (the chains touch disjoint scalars, so the order between them is free)
+// abcn^T (hyperpow = 0) of the psi and chi chains of a step: pb and cb hold the adjoints of the new
+// psi and chi; on return they hold the adjoints w.r.t. the old ones, and npb, nppb (ncb, ncpb) have
+// received the adjoints w.r.t. nl and nl_p (added).  The two transposed Helmholtz solves run in one
+// pass; the chains touch disjoint scalars, so each of their linear combinations is paired with the
+// other chain's in one launch.
 static int abcn_T_pair(Scalar& pb, Scalar& npb, Scalar& nppb, Scalar& cb, Scalar& ncb, Scalar& ncpb, double dt) {
-  double a = -2.0 / (dt * G.P.visc);
+  const double a = -2.0 / (dt * G.P.visc);
   MLG_TRY(ihelm_T_pair(pb, cb, a));
-  MLG_TRY(abcn_T_rest(pb, npb, nppb, dt));
-  return abcn_T_rest(cb, ncb, ncpb, dt);
-}
-// abcn^T after its solve: the adjoints of nl and nl_p, and sb mapped to the old s
-static int abcn_T_rest(Scalar& sb, Scalar& nlb, Scalar& nlpb, double dt) {
-  double a = -2.0 / (dt * G.P.visc);
-  MLG_TRY(lincomb(nlb, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}, {{&nlb, 1.0}, {&sb, 1.5 * dt * a}}));
-  MLG_TRY(lincomb(nlpb, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}, {{&nlpb, 1.0}, {&sb, -0.5 * dt * a}}));
-  TMP(t);   // t = (visc a dt/2) sb with sb's ln and tags, in one pass
-  std::memcpy(t.space, sb.space, 4);
-  for (int i = 0; i < 3; ++i) t.off[i] = sb.off[i];
-  MLG_TRY(lincomb(t, {{&sb, G.P.visc * a * dt / 2.0}}, {{&sb, 1.0}}));
-  MLG_TRY(band_T(t, 2));   // t.e <- del2^T t.e; t.ln <- the log-term adjoint
-  MLG_TRY(lincomb(sb, {{&sb, a}, {&t, 1.0}}, {{&sb, a}, {&t, 1.0}}));
+  // the adjoints of nl and nl_p
+  MLG_TRY(lincomb_n({lin_args(npb, {{&npb, 1.0}, {&pb, 1.5 * dt * a}}, {{&npb, 1.0}, {&pb, 1.5 * dt * a}}),
+                     lin_args(nppb, {{&nppb, 1.0}, {&pb, -0.5 * dt * a}}, {{&nppb, 1.0}, {&pb, -0.5 * dt * a}}),
+                     lin_args(ncb, {{&ncb, 1.0}, {&cb, 1.5 * dt * a}}, {{&ncb, 1.0}, {&cb, 1.5 * dt * a}}),
+                     lin_args(ncpb, {{&ncpb, 1.0}, {&cb, -0.5 * dt * a}}, {{&ncpb, 1.0}, {&cb, -0.5 * dt * a}})}));
+  TMP(tp); TMP(tc);   // t = (visc a dt/2) sb with sb's ln and tags
+  for (auto q : {std::make_pair(&tp, &pb), std::make_pair(&tc, &cb)}) {
+    std::memcpy(q.first->space, q.second->space, 4);
+    for (int i = 0; i < 3; ++i) q.first->off[i] = q.second->off[i];
+  }
+  MLG_TRY(lincomb_n({lin_args(tp, {{&pb, G.P.visc * a * dt / 2.0}}, {{&pb, 1.0}}),
+                     lin_args(tc, {{&cb, G.P.visc * a * dt / 2.0}}, {{&cb, 1.0}})}));
+  MLG_TRY(band_T(tp, 2));   // t.e <- del2^T t.e; t.ln <- the log-term adjoint
+  MLG_TRY(band_T(tc, 2));
+  MLG_TRY(lincomb_n({lin_args(pb, {{&pb, a}, {&tp, 1.0}}, {{&pb, a}, {&tp, 1.0}}),
+                     lin_args(cb, {{&cb, a}, {&tc, 1.0}}, {{&cb, a}, {&tc, 1.0}})}));
   return 0;
 }
 
@@ -797,17 +821,16 @@ static int step_T(const Scalar& uzb, double dt, Scalar* const ad[6], Scalar* con
   Scalar& nppb = *ad[4]; Scalar& ncpb = *ad[5];
   TMP(xp); TMP(xc);
   MLG_TRY(nlcore_T(nullptr, nullptr, uzb, npb, ncb, xp, xc, vw));
-  MLG_TRY(lincomb(pb, {{&pb, 1.0}, {&xp, 1.0}}, {{&pb, 1.0}, {&xp, 1.0}}));
-  MLG_TRY(lincomb(cb, {{&cb, 1.0}, {&xc, 1.0}}, {{&cb, 1.0}, {&xc, 1.0}}));
-  for (Scalar* q : {&pb, &cb}) {
-    MLG_TRY(op_dealias(*q));   // advection_rhs's in-place dealias
-    MLG_TRY(zeroat1_T(*q));
-    MLG_TRY(op_dealias(*q));   // the step's dealias
-  }
+  MLG_TRY(lincomb_n({lin_args(pb, {{&pb, 1.0}, {&xp, 1.0}}, {{&pb, 1.0}, {&xp, 1.0}}),
+                     lin_args(cb, {{&cb, 1.0}, {&xc, 1.0}}, {{&cb, 1.0}, {&xc, 1.0}})}));
+  // the psi and chi chains are independent: each transpose of the pair in one launch
+  MLG_TRY(op_dealias2(pb, cb));   // advection_rhs's in-place dealias
+  MLG_TRY(zeroat1_T2(pb, cb));
+  MLG_TRY(op_dealias2(pb, cb));   // the step's dealias
   // nl_p(out) = nl(in); the new nl(in) and nl_p(in) adjoints come from abcn^T
   MLG_TRY(assign(npb, nppb)); MLG_TRY(assign(ncb, ncpb));
-  MLG_TRY(launch_zero(nppb.e)); MLG_TRY(launch_set_ln(nppb.ln, 0.0));
-  MLG_TRY(launch_zero(ncpb.e)); MLG_TRY(launch_set_ln(ncpb.ln, 0.0));
+  MLG_TRY(launch_zero(nppb.e)); MLG_TRY(launch_zero(ncpb.e));
+  MLG_TRY(launch_set_ln2(nppb.ln, ncpb.ln, 0.0));
   MLG_TRY(abcn_T_pair(pb, npb, nppb, cb, ncb, ncpb, dt));
   for (int i = 0; i < 6; ++i) set_fff0(*ad[i]);
   return 0;
@@ -899,6 +922,11 @@ static int project_active(Scalar& s) {
   MLG_TRY(op_chop(s));
   return op_dealias(s);
 }
+// the same for the six adjoint fields of the state, chop and dealias in one launch
+static int project_active6(Scalar* const* ad) {
+  for (int i = 0; i < 6; ++i) set_fff0(*ad[i]);
+  return op_mask_n(ad, 6, true, true);
+}
 
 int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, double dt, int nsteps, int k_ckpt, Scalar* gpsi,
                 Scalar* gchi, double* J) {
@@ -952,7 +980,7 @@ int adjoint_run(const Scalar& psi0, const Scalar& chi0, const Scalar& uzb, doubl
     for (int q = 0; q < len && !rc; ++q) rc = forward_step(cur.p, uzb, dt, segvw[q]->p);
     for (int q = len - 1; q >= 0 && !rc; --q) {
       rc = step_T(uzb, dt, ad.p, segvw[q]->p);
-      for (int i = 0; i < 6 && !rc; ++i) rc = project_active(*ad.p[i]);
+      if (!rc) rc = project_active6(ad.p);
     }
   }
   for (State* t : segvw) delete t;

@@ -176,6 +176,7 @@ int launch_copy(cd* dst, const cd* src);
 int launch_copy_ln(double* dst, const double* src);
 int launch_set_ln(double* dst, double v);
 int launch_set_ln2(double* d1, double* d2, double v);
+int launch_set_ln_n(double* const* d, int n, double v);   // n <= 6 slots
 
 // grid-stride loop over n elements (32-bit indices: a field has < 2^32 entries)
 #define GRID_STRIDE(i, n) for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < (unsigned)(n); i += gridDim.x * blockDim.x)
@@ -185,6 +186,22 @@ static inline int nblk(size_t n) { return (int)std::min<size_t>((n + 255) / 256,
 int scalar_init(Scalar& s, bool zero_ln = true);
 void scalar_release(Scalar& s);
 int assign(Scalar& d, const Scalar& s);   // e, ln, space, offsets
+// one linear combination for k_lincomb: out = c0*a + c1*b + c2*c + c3*d (null inputs skipped), times
+// post; ln likewise with separate coefficients
+struct LinArgs {
+  double2* out;
+  const double2* in[4];
+  double c[4];
+  double* lnout;
+  const double* lnin[4];
+  double lc[4];
+  double post;     // overall multiplier applied after the sum (e and ln)
+  size_t n;
+};
+LinArgs lin_args(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+                 std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post = 1.0, bool do_ln = true);
+// up to four independent combinations (none reads another one's output) in one launch
+int lincomb_n(std::initializer_list<LinArgs> combos);
 // out = post * sum c_i in_i (e), ln likewise from lnterms unless do_ln is false
 int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
             std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post = 1.0, bool do_ln = true);
@@ -209,6 +226,8 @@ int op_dealias(Scalar& s);
 int op_zeroat1(Scalar& s);
 // the same operators on two fields in one launch where their chop and spaces agree (else one by one)
 int op_chop2(Scalar& a, Scalar& b);
+// chop (if chop) and then dealias (if dealias) of each of n <= 6 fields
+int op_mask_n(Scalar* const* f, int n, bool chop, bool dealias);
 int op_dealias2(Scalar& a, Scalar& b);
 int op_zeroat1_2(Scalar& a, Scalar& b);
 int op_band(Scalar& s, int op);

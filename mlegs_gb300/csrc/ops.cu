@@ -107,23 +107,31 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 // chop (mlegs_scalar_ops.f90:6-41) and dealias (:43-70) as masks
 // one warp per (m, k) column (8 per block): the column's first zeroed row is worked out once, and
 // only the zeroed rows are written (a column that keeps all its rows touches no memory)
-__global__ void __launch_bounds__(256) k_mask(double2* __restrict__ e0, double2* __restrict__ e1, int nrdim, int npdim,
-                                              int nzdim, int mode, int f0, int f1, int f2, int nrc, int npc, int nzc,
-                                              int nzcu, int pcut, int zcut, int zupper, int np_gt1, int nz_gt1) {
-  // one warp per column of e0 and, when e1 is given, of e1 (the same mask)
+// chop (:6-41) and / or dealias (:43-70) of up to six fields with the same chop window and space, one
+// warp per column: rows [zf, nrdim) of a column become zero, zf = 0 for a column the dealias band or the
+// chop's m / k window removes whole, the chop's nn(m) otherwise
+struct MaskSet {
+  double2* e[6];
+  int n;
+};
+__global__ void __launch_bounds__(256) k_mask(MaskSet fs, int nrdim, int npdim, int nzdim, int chop, int dealias, int f0,
+                                              int f1, int f2, int nrc, int npc, int nzc, int nzcu, int pcut, int zcut,
+                                              int zupper, int np_gt1, int nz_gt1) {
   const int cf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   const int ncols = npdim * nzdim;
-  if (cf >= (e1 ? 2 : 1) * ncols) return;
-  double2* e = cf < ncols ? e0 : e1;
-  const int col = cf < ncols ? cf : cf - ncols;
+  if (cf >= fs.n * ncols) return;
+  const int f = cf / ncols, col = cf - f * ncols;
+  double2* e = fs.e[0];
+#pragma unroll
+  for (int q = 1; q < 6; ++q)
+    if (f == q) e = fs.e[q];
   const int m = col % npdim, k = col / npdim;
   int zf = nrdim;   // rows [zf, nrdim) become zero
-  if (mode == 0) {
+  if (chop) {
     if ((f1 && m >= npc) || (f2 && nzc < nzcu && (k + 1) >= nzc + 1 && (k + 1) <= nzcu - 1)) zf = 0;
     else if (f0) zf = (m < npc) ? max(min(nrc, nrc - m), 0) : 0;
-  } else {
-    if ((np_gt1 && f1 && (m + 1) > pcut) || (nz_gt1 && f2 && (k + 1) > zcut && (k + 1) < zupper)) zf = 0;
   }
+  if (dealias && ((np_gt1 && f1 && (m + 1) > pcut) || (nz_gt1 && f2 && (k + 1) > zcut && (k + 1) < zupper))) zf = 0;
   double2* g = e + (size_t)nrdim * col;
   for (int i = zf + lane; i < nrdim; i += 32) g[i] = make_double2(0.0, 0.0);
 }
@@ -141,17 +149,7 @@ __global__ void k_ln_adjust(double2* __restrict__ e, const double* __restrict__ 
   }
 }
 
-// out = c0*a + c1*b + c2*c + c3*d (null inputs skipped); ln likewise with separate coefficients
-struct LinArgs {
-  double2* out;
-  const double2* in[4];
-  double c[4];
-  double* lnout;
-  const double* lnin[4];
-  double lc[4];
-  double post;     // overall multiplier applied after the sum (e and ln)
-  size_t n;
-};
+// one linear combination (LinArgs) over a field
 __global__ void k_lincomb(LinArgs a) {
   const bool scaled = a.post != 1.0;   // multiplying by 1 changes nothing: skipped
   GRID_STRIDE(idx, a.n) {
@@ -171,6 +169,41 @@ __global__ void k_lincomb(LinArgs a) {
     for (int t = 0; t < 4; ++t)
       if (a.lnin[t]) l += a.lc[t] * *a.lnin[t];
     *a.lnout = a.post * l;
+  }
+}
+
+// up to four independent linear combinations (no combination reads another one's output) in one
+// launch, each exactly as k_lincomb computes it
+struct LinSet {
+  LinArgs a[4];
+  int n;
+};
+__global__ void k_lincomb_n(LinSet s) {
+  const size_t n = s.a[0].n;
+  GRID_STRIDE(gidx, n * s.n) {
+    const int q = (int)(gidx / n);
+    const size_t idx = gidx - (size_t)q * n;
+    const LinArgs& a = q == 0 ? s.a[0] : (q == 1 ? s.a[1] : (q == 2 ? s.a[2] : s.a[3]));
+    const bool scaled = a.post != 1.0;
+    double2 acc = make_double2(0, 0);
+    bool first = true;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (a.in[t]) {
+        double2 v = a.in[t][idx];
+        if (first) { acc.x = a.c[t] * v.x; acc.y = a.c[t] * v.y; first = false; }
+        else { acc.x += a.c[t] * v.x; acc.y += a.c[t] * v.y; }
+      }
+    a.out[idx] = scaled ? make_double2(a.post * acc.x, a.post * acc.y) : acc;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (unsigned)s.n) {
+    const LinArgs& a = threadIdx.x == 0 ? s.a[0] : (threadIdx.x == 1 ? s.a[1] : (threadIdx.x == 2 ? s.a[2] : s.a[3]));
+    if (a.lnout) {
+      double l = 0.0;
+      for (int t = 0; t < 4; ++t)
+        if (a.lnin[t]) l += a.lc[t] * *a.lnin[t];
+      *a.lnout = a.post * l;
+    }
   }
 }
 
@@ -420,6 +453,27 @@ int launch_copy_ln(double* d, const double* s) {
 }
 int launch_set_ln(double* d, double v) { k_ln_set<<<1, 32, 0, G.stream>>>(d, v); MLG_LAUNCH(); return 0; }
 int launch_set_ln2(double* a, double* b, double v) { k_ln_set2<<<1, 32, 0, G.stream>>>(a, b, v); MLG_LAUNCH(); return 0; }
+struct LnSet {
+  double* p[6];
+  int n;
+};
+__global__ void k_ln_setn(LnSet s, double v) {
+  const int t = threadIdx.x;
+  double* d = s.p[0];
+#pragma unroll
+  for (int q = 1; q < 6; ++q)
+    if (t == q) d = s.p[q];
+  if (t < s.n) *d = v;
+}
+int launch_set_ln_n(double* const* d, int n, double v) {
+  if (n < 1 || n > 6) return set_error(MLG_EPARAM, "set_ln: one to six slots per launch");
+  LnSet s{};
+  for (int i = 0; i < n; ++i) s.p[i] = d[i];
+  s.n = n;
+  k_ln_setn<<<1, 32, 0, G.stream>>>(s, v);
+  MLG_LAUNCH();
+  return 0;
+}
 
 int launch_ln_adjust(Scalar& s, double sign) {
   size_t n = (size_t)G.nr * G.nzdim;
@@ -428,8 +482,8 @@ int launch_ln_adjust(Scalar& s, double sign) {
   return 0;
 }
 
-int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
-            std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post, bool do_ln) {
+LinArgs lin_args(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+                 std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post, bool do_ln) {
   LinArgs a{};
   a.out = out.e;
   a.n = G.fsize;
@@ -441,7 +495,20 @@ int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>>
   a.lnout = do_ln ? out.ln : nullptr;
   for (auto& p : lnterms) { a.lnin[t] = p.first ? p.first->ln : nullptr; a.lc[t] = p.second; ++t; }
   for (; t < 4; ++t) { a.lnin[t] = nullptr; a.lc[t] = 0; }
+  return a;
+}
+int lincomb(Scalar& out, std::initializer_list<std::pair<const Scalar*, double>> terms,
+            std::initializer_list<std::pair<const Scalar*, double>> lnterms, double post, bool do_ln) {
+  LinArgs a = lin_args(out, terms, lnterms, post, do_ln);
   k_lincomb<<<nblk(G.fsize), 256, 0, G.stream>>>(a);
+  MLG_LAUNCH();
+  return 0;
+}
+int lincomb_n(std::initializer_list<LinArgs> combos) {
+  if (combos.size() < 1 || combos.size() > 4) return set_error(MLG_EPARAM, "lincomb: one to four combinations per launch");
+  LinSet s{};
+  for (const LinArgs& a : combos) s.a[s.n++] = a;
+  k_lincomb_n<<<nblk(G.fsize * s.n), 256, 0, G.stream>>>(s);
   MLG_LAUNCH();
   return 0;
 }
@@ -540,47 +607,64 @@ int op_trans(Scalar& s, const char* space) {
   return 0;
 }
 
-// chop of one field, or of two (b non-null) with the same chop window and space
-static int chop_launch(Scalar& s, Scalar* b, const ChopIdx& c) {
-  k_mask<<<cdiv((long long)(b ? 2 : 1) * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
-      s.e, b ? b->e : nullptr, G.nrdim, G.npdim, G.nzdim, 0, s.space[0] == 'F', s.space[1] == 'F', s.space[2] == 'F', c.nrc,
-      c.npc, c.nzc, c.nzcu, 0, 0, 0, 0, 0);
+// chop and / or dealias of n <= 6 fields (the first field's chop window and space stand for all)
+static int mask_launch(Scalar* const* f, int n, bool chop, bool dealias, const ChopIdx& c) {
+  MaskSet fs{};
+  for (int i = 0; i < n; ++i) fs.e[i] = f[i]->e;
+  fs.n = n;
+  const Scalar& s = *f[0];
+  int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
+  k_mask<<<cdiv((long long)n * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
+      fs, G.nrdim, G.npdim, G.nzdim, chop ? 1 : 0, dealias ? 1 : 0, s.space[0] == 'F', s.space[1] == 'F', s.space[2] == 'F',
+      c.nrc, c.npc, c.nzc, c.nzcu, pcut, zcut, zupper, G.np > 1, G.nz > 1);
   MLG_LAUNCH();
+  return 0;
+}
+// fields that one launch can take together: distinct, the same space and chop window
+static bool mask_batchable(Scalar* const* f, int n, bool chop, ChopIdx& c) {
+  ChopIdx c0{};
+  if (chop && chop_index(*f[0], c0)) return false;   // the one-by-one path reports the error
+  for (int i = 1; i < n; ++i) {
+    if (std::strncmp(f[i]->space, f[0]->space, 3) != 0) return false;
+    for (int j = 0; j < i; ++j)
+      if (f[i]->e == f[j]->e) return false;
+    if (chop) {
+      ChopIdx ci;
+      if (chop_index(*f[i], ci)) return false;
+      if (ci.nrc != c0.nrc || ci.npc != c0.npc || ci.nzc != c0.nzc || ci.nzcu != c0.nzcu) return false;
+    }
+  }
+  c = c0;
+  return true;
+}
+// chop (if chop) and then dealias (if dealias) of each of n <= 6 fields, in one launch where they can
+// share it
+int op_mask_n(Scalar* const* f, int n, bool chop, bool dealias) {
+  if (n < 1 || n > 6) return set_error(MLG_EPARAM, "mask: one to six fields per launch");
+  ChopIdx c{};
+  if (mask_batchable(f, n, chop, c)) return mask_launch(f, n, chop, dealias, c);
+  for (int i = 0; i < n; ++i) {
+    ChopIdx ci{};
+    if (chop) MLG_TRY(chop_index(*f[i], ci));
+    MLG_TRY(mask_launch(&f[i], 1, chop, dealias, ci));
+  }
   return 0;
 }
 int op_chop(Scalar& s) {
-  ChopIdx c;
-  MLG_TRY(chop_index(s, c));
-  return chop_launch(s, nullptr, c);
+  Scalar* f[1] = {&s};
+  return op_mask_n(f, 1, true, false);
 }
 int op_chop2(Scalar& a, Scalar& b) {
-  ChopIdx ca, cb;
-  MLG_TRY(chop_index(a, ca));
-  MLG_TRY(chop_index(b, cb));
-  const bool same = ca.nrc == cb.nrc && ca.npc == cb.npc && ca.nzc == cb.nzc && ca.nzcu == cb.nzcu &&
-                    std::strncmp(a.space, b.space, 3) == 0 && a.e != b.e;
-  if (!same) {
-    MLG_TRY(chop_launch(a, nullptr, ca));
-    return chop_launch(b, nullptr, cb);
-  }
-  return chop_launch(a, &b, ca);
+  Scalar* f[2] = {&a, &b};
+  return op_mask_n(f, 2, true, false);
 }
-
-static int dealias_launch(Scalar& s, Scalar* b) {
-  int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
-  k_mask<<<cdiv((long long)(b ? 2 : 1) * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
-      s.e, b ? b->e : nullptr, G.nrdim, G.npdim, G.nzdim, 1, 0, s.space[1] == 'F', s.space[2] == 'F', 0, 0, 0, 0, pcut, zcut,
-      zupper, G.np > 1, G.nz > 1);
-  MLG_LAUNCH();
-  return 0;
+int op_dealias(Scalar& s) {
+  Scalar* f[1] = {&s};
+  return op_mask_n(f, 1, false, true);
 }
-int op_dealias(Scalar& s) { return dealias_launch(s, nullptr); }
 int op_dealias2(Scalar& a, Scalar& b) {
-  if (a.space[1] != b.space[1] || a.space[2] != b.space[2] || a.e == b.e) {
-    MLG_TRY(dealias_launch(a, nullptr));
-    return dealias_launch(b, nullptr);
-  }
-  return dealias_launch(a, &b);
+  Scalar* f[2] = {&a, &b};
+  return op_mask_n(f, 2, false, true);
 }
 
 // svv_filter with the gain kept in device memory (gain_dev)
