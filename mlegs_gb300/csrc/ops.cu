@@ -287,30 +287,41 @@ __device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, doubl
 }
 // per block: the energy of the head and of the tail (q >= cutoff) of the spectrum (:112-117).  The q
 // are in [0, 1], so q >= cutoff is compared on the FP64 bit patterns; the sums stay FP64.
-__global__ void k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ qt,
-                           unsigned long long cbits, double* __restrict__ partial) {
-  __shared__ double s0[256], s1[256];
+__global__ void __launch_bounds__(256) k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim,
+                                                  const double* __restrict__ qt, unsigned long long cbits,
+                                                  double* __restrict__ partial) {
+  // a warp per column (m, k), its lanes over the rows: the column's q bits once, the row's per lane;
+  // |e|^2 summed in FP64 into the head (q below the cutoff) and the tail
+  __shared__ double s0[8], s1[8];
   const unsigned long long* qb = reinterpret_cast<const unsigned long long*>(qt);
-  size_t n = (size_t)nrdim * npdim * nzdim;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int ncol = npdim * nzdim;
   double head = 0, tail = 0;
-  GRID_STRIDE(idx, n) {
-    int i = (int)(idx % (unsigned)nrdim);
-    int m = (int)((idx / (unsigned)nrdim) % (unsigned)npdim);
-    int k = (int)(idx / (unsigned)(nrdim * npdim));
-    double2 v = e[idx];
-    double a2 = v.x * v.x + v.y * v.y;
-    unsigned long long b = qb[i], bm = qb[nrdim + m], bk = qb[nrdim + npdim + k];
-    b = b > bm ? b : bm;
-    b = b > bk ? b : bk;
-    if (b >= cbits) tail += a2; else head += a2;
+  for (int c = blockIdx.x * 8 + wib; c < ncol; c += gridDim.x * 8) {
+    const int m = c % npdim, k = c / npdim;
+    const unsigned long long bm = qb[nrdim + m], bk = qb[nrdim + npdim + k];
+    const unsigned long long bc = bm > bk ? bm : bk;
+    const double2* col = e + (size_t)nrdim * c;
+    for (int i = lane; i < nrdim; i += 32) {
+      const double2 v = col[i];
+      const double a2 = v.x * v.x + v.y * v.y;
+      unsigned long long b = qb[i];
+      b = b > bc ? b : bc;
+      if (b >= cbits) tail += a2; else head += a2;
+    }
   }
-  s0[threadIdx.x] = head; s1[threadIdx.x] = tail;
+  for (int o = 16; o; o >>= 1) {
+    head += __shfl_xor_sync(0xffffffffu, head, o);
+    tail += __shfl_xor_sync(0xffffffffu, tail, o);
+  }
+  if (lane == 0) { s0[wib] = head; s1[wib] = tail; }
   __syncthreads();
-  for (int o = blockDim.x / 2; o; o >>= 1) {
-    if (threadIdx.x < o) { s0[threadIdx.x] += s0[threadIdx.x + o]; s1[threadIdx.x] += s1[threadIdx.x + o]; }
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    double h = 0, t = 0;
+    for (int w = 0; w < 8; ++w) { h += s0[w]; t += s1[w]; }
+    partial[2 * blockIdx.x] = h;
+    partial[2 * blockIdx.x + 1] = t;
   }
-  if (threadIdx.x == 0) { partial[2 * blockIdx.x] = s0[0]; partial[2 * blockIdx.x + 1] = s1[0]; }
 }
 // gain relaxation and strength (:119-126) and the 1-D factor tables ft[0..nrdim) (n), ft[nrdim..+npdim)
 // (m), ft[..+nzdim) (k): exp(-s*shape^8) where q > cutoff, 1 elsewhere.  Every block reduces the
@@ -433,10 +444,14 @@ __global__ void k_copy_scalar(double2* __restrict__ d, const double2* __restrict
   if (blockIdx.x == 0 && threadIdx.x == 0) *dln = *sln;
 }
 
+// non-finite (inf or NaN) from the exponent bits, on the integer pipe
+__device__ __forceinline__ unsigned nonfinite_bits(double x) {
+  return (unsigned)((__double2hiint(x) & 0x7FF00000) == 0x7FF00000);
+}
 __global__ void k_finite(const double2* __restrict__ a, const double2* __restrict__ b, size_t n, int* __restrict__ flag) {
   GRID_STRIDE(idx, n) {
-    double2 u = a[idx], v = b[idx];
-    if (!isfinite(u.x) || !isfinite(u.y) || !isfinite(v.x) || !isfinite(v.y)) { atomicExch(flag, 1); }
+    const double2 u = a[idx], v = b[idx];
+    if (nonfinite_bits(u.x) | nonfinite_bits(u.y) | nonfinite_bits(v.x) | nonfinite_bits(v.y)) atomicExch(flag, 1);
   }
 }
 

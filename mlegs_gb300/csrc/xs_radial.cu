@@ -532,7 +532,9 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
             const int i = row;
             if (i < a.nrh) {
               const int EA = EA0;
-              const double lnv = (a.add_ln && m == 0) ? *flnp : 0.0;
+              // the log term is added at m = 0 only: an integer test per item, so that the other items
+              // issue no FP64 compares or (predicated) FP64 additions on GB300's narrow FP64 pipe
+              const bool ln_here = a.add_ln && m == 0;
 #pragma unroll
               for (int c = 0; c < 8; c += 2) {
                 const int zo = z0 + ((cb + c) >> 1);
@@ -546,7 +548,11 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
                     v[2 + h] = xs_i64_to_double(T[0][c + h] - T[1][c + h], EA + E[c + h] + eo);
                   }
                 }
-                if (lnv != 0.0) { v[0] += lnv * a.lnx[i]; v[2] += lnv * a.lnx[a.nr - 1 - i]; }
+                if (ln_here) {
+                  const double lnv = *flnp;
+                  v[0] += lnv * a.lnx[i];
+                  v[2] += lnv * a.lnx[a.nr - 1 - i];
+                }
                 const size_t b0 = (size_t)a.nrdim * (m + (size_t)a.npdim * zo);
                 fout[b0 + i] = make_double2(v[0], v[1]);
                 fout[b0 + a.nr - 1 - i] = make_double2(v[2], v[3]);
