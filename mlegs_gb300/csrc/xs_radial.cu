@@ -129,6 +129,7 @@ struct XsArgs {
   const double* lnx;
   int* status;
   int add_ln, nf, nr, nrh, nrdim, npdim, nzdim, nrc, m0, npc, nmt, nkc, nrp, rawk;
+  int astages;   // table-chunk stages (2 or 3, as shared memory allows)
 };
 // field f's pointer without an indexed access to the kernel parameters (which would copy them to local
 // memory)
@@ -192,28 +193,34 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   constexpr int BT = N * XS_KC * 2;               // B digit tile bytes
   constexpr int ASTAGE = 2 * NS * XS_ATILE;
   constexpr int BSTAGE = 2 * NS * BT;
-  constexpr int TCOLS = 2 * NO * N <= 32 ? 32 : 2 * NO * N <= 64 ? 64 : 2 * NO * N <= 128 ? 128 : 2 * NO * N <= 256 ? 256 : 512;
+  // the accumulators of one work unit, and two sets of them where tensor memory holds both: the MMAs of
+  // the next unit then run while the epilogue reads this one's
+  constexpr int ACC = 2 * NO * N;
+  constexpr int TB = 2 * ACC <= 512 ? 2 : 1;
+  constexpr int TUSE = TB * ACC;
+  constexpr int TCOLS = TUSE <= 32 ? 32 : TUSE <= 64 ? 64 : TUSE <= 128 ? 128 : TUSE <= 256 ? 256 : 512;
   constexpr int NBLK = (MODE == 0 ? 1 : 2) * (N / 8) * 2;   // digit blocks per chunk
   constexpr int CPW = N / 16;                     // 8-column groups of an epilogue warp
-  static_assert(2 * NO * N <= 512, "accumulators exceed tensor memory");
+  static_assert(ACC <= 512, "accumulators exceed tensor memory");
   static_assert(N == 16 || N == 32, "MMA N per digit");
   static_assert((NO - 1) * N + N <= 256, "MMA N of the widest digit product");
   extern __shared__ __align__(1024) uint8_t xs_smem_raw[];
   uint8_t* sbase = (uint8_t*)(((uintptr_t)xs_smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = sbase;                                   // [2][ASTAGE]
-  uint8_t* sB = sA + 2 * ASTAGE;                         // [XS_SB][BSTAGE]
+  const int AS = a.astages;
+  uint8_t* sA = sbase;                                   // [AS][ASTAGE]
+  uint8_t* sB = sA + AS * ASTAGE;                        // [XS_SB][BSTAGE]
   double* raw = (double*)(sB + XS_SB * BSTAGE);          // [NZ][rawk] complex (re, im)
   int* colexp = (int*)(raw + (size_t)2 * NZ * a.rawk);   // [2][N]: by item parity
   uint64_t* bars = (uint64_t*)(colexp + 2 * N);
   uint64_t* bar_rf = bars;                 // field columns landed
   uint64_t* bar_re = bars + 1;             // field columns consumed (digit threads)
-  uint64_t* bar_af = bars + 2;             // [2] table chunk landed
-  uint64_t* bar_ae = bars + 4;             // [2] table chunk consumed (MMA commit)
-  uint64_t* bar_bf = bars + 6;             // [XS_SB] digit stage written (digit threads)
+  uint64_t* bar_af = bars + 2;             // [AS] table chunk landed
+  uint64_t* bar_ae = bars + 5;             // [AS] table chunk consumed (MMA commit)
+  uint64_t* bar_bf = bars + 8;             // [XS_SB] digit stage written (digit threads)
   uint64_t* bar_be = bar_bf + XS_SB;       // [XS_SB] digit stage consumed (MMA commit)
-  uint64_t* bar_tf = bar_be + XS_SB;       // accumulators complete (MMA commit)
-  uint64_t* bar_te = bar_tf + 1;           // accumulators read (epilogue threads)
-  uint64_t* bar_cx = bar_te + 1;           // [2] column scales written (digit threads), by item parity
+  uint64_t* bar_tf = bar_be + XS_SB;       // [TB] accumulators complete (MMA commit)
+  uint64_t* bar_te = bar_tf + 2;           // [TB] accumulators read (epilogue threads)
+  uint64_t* bar_cx = bar_te + 2;           // [2] column scales written (digit threads), by item parity
   uint64_t* bar_ce = bar_cx + 2;           // [2] column scales read (epilogue threads), by item parity
   uint32_t* tslot = (uint32_t*)(bar_ce + 2);
 
@@ -222,18 +229,20 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   if (tid == 0) {
     mbar_init(bar_rf, 1);
     mbar_init(bar_re, XS_NDIG);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
       mbar_init(bar_af + i, 1);
       mbar_init(bar_ae + i, 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(bar_cx + i, XS_NDIG);
       mbar_init(bar_ce + i, XS_NEPI);
+      mbar_init(bar_tf + i, 1);
+      mbar_init(bar_te + i, XS_NEPI);
     }
     for (int i = 0; i < XS_SB; ++i) {
       mbar_init(bar_bf + i, XS_NDIG);
       mbar_init(bar_be + i, 1);
     }
-    mbar_init(bar_tf, 1);
-    mbar_init(bar_te, XS_NEPI);
     fence_mbar_init();
   }
   if (warp == 1) {
@@ -293,8 +302,8 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
         for (int mt = 0; mt < nmt_m && ok; ++mt) {
           const uint8_t* img_m = (const uint8_t*)a.img + ((size_t)m * a.nmt + mt) * a.nkc * (size_t)ASTAGE;
           for (int kc = 0; kc < nkc_m; ++kc, ++c) {
-            const uint32_t s = c & 1;
-            if (c >= 2 && !xs_wait(&bar_ae[s], ((c - 2) >> 1) & 1, ok)) break;
+            const uint32_t s = c % (uint32_t)AS;
+            if (c >= (uint32_t)AS && !xs_wait(&bar_ae[s], ((c - AS) / AS) & 1, ok)) break;
             mbar_expect_tx(&bar_af[s], ASTAGE);
             bulk_g2s(sA + s * ASTAGE, img_m + (size_t)kc * ASTAGE, ASTAGE, &bar_af[s]);
           }
@@ -302,11 +311,11 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       }
       // the copies issued complete on their own: wait (bounded) for the last of them, so that no copy
       // is in flight when the CTA's shared memory goes away (at once in a run without a timeout)
+      for (uint32_t j = c > (uint32_t)AS ? c - AS : 0; j < c; ++j) {
+        bool ok2 = true;
+        xs_wait(&bar_af[j % AS], (j / AS) & 1, ok2);
+      }
       bool ok2 = true;
-      if (c >= 1) xs_wait(&bar_af[(c - 1) & 1], ((c - 1) >> 1) & 1, ok2);
-      ok2 = true;
-      if (c >= 2) xs_wait(&bar_af[c & 1], ((c - 2) >> 1) & 1, ok2);
-      ok2 = true;
       if (nraw >= 1) xs_wait(bar_rf, (nraw - 1) & 1, ok2);
     }
   } else if (warp == 1) {
@@ -317,11 +326,14 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
         int nkc_m, nrows, nmt_m;
         geom(item_nn(item), nkc_m, nrows, nmt_m);
         for (int mt = 0; mt < nmt_m && ok; ++mt, ++u) {
-          if (u > 0 && !xs_wait(bar_te, (u - 1) & 1, ok)) break;   // the epilogue has read the accumulators
+          // the accumulator set of this unit, once the epilogue has read what it held TB units before
+          const uint32_t tb = u % TB;
+          if (u >= (uint32_t)TB && !xs_wait(&bar_te[tb], ((u - TB) / TB) & 1, ok)) break;
           tc_fence_after();
+          const uint32_t tacc = tmem + tb * (uint32_t)ACC;
           for (int kc = 0; kc < nkc_m; ++kc, ++c) {
-            const uint32_t sa = c & 1, sb = c % XS_SB;
-            if (!xs_wait(&bar_af[sa], (c >> 1) & 1, ok)) break;
+            const uint32_t sa = c % (uint32_t)AS, sb = c % XS_SB;
+            if (!xs_wait(&bar_af[sa], (c / AS) & 1, ok)) break;
             if (!xs_wait(&bar_bf[sb], (c / XS_SB) & 1, ok)) break;
             tc_fence_after();
             const uint32_t a0 = smem_u32(sA + sa * ASTAGE), b0 = smem_u32(sB + sb * BSTAGE);
@@ -334,18 +346,18 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
               for (int t = 0; t < NO; ++t) {
                 const uint64_t ad = sdesc(a0 + (par * NS + t) * XS_ATILE, XS_LBO, XS_SBO);
                 const uint64_t bd = sdesc(b0 + (par * NS) * BT, XS_LBO, XS_SBO);
-                umma_bf16(tmem + (uint32_t)((par * NO + t) * N), ad, bd, idesc_bf16(128, (NO - t) * N),
+                umma_bf16(tacc + (uint32_t)((par * NO + t) * N), ad, bd, idesc_bf16(128, (NO - t) * N),
                           (kc > 0 || t > 0) ? 1u : 0u);
               }
             umma_commit(&bar_ae[sa]);
             umma_commit(&bar_be[sb]);
           }
-          if (ok) umma_commit(bar_tf);
+          if (ok) umma_commit(&bar_tf[tb]);
         }
       }
       if (c > 0) {   // the MMAs issued have finished (bounded) before tensor memory is freed
         bool ok2 = true;
-        xs_wait(&bar_ae[(c - 1) & 1], ((c - 1) >> 1) & 1, ok2);
+        xs_wait(&bar_ae[(c - 1) % AS], ((c - 1) / AS) & 1, ok2);
       }
     }
   } else if (warp < 2 + XS_NDW) {
@@ -469,8 +481,10 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
         } else if (row < a.nrh) {
           EA0 = a.aexp[(size_t)m * a.nrp + row];
         }
-        if (!xs_wait_w(bar_tf, u & 1, ok)) break;
+        const uint32_t tb = u % TB;
+        if (!xs_wait_w(&bar_tf[tb], (u / TB) & 1, ok)) break;
         tc_fence_after();
+        const uint32_t tacc = tmem + tb * (uint32_t)ACC;
         constexpr int eo = ESH - W * (NO + 1);
         // the warp's columns eight at a time; after the last group's loads the accumulators are free for
         // the next unit's MMAs (and, after the item's last unit, the column scales for item ii+2), so the
@@ -493,8 +507,8 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
               uint32_t g[2][8], h[2][8];
 #pragma unroll
               for (int par = 0; par < 2; ++par) {
-                tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + D) * N + cb), g[par]);
-                if constexpr (D2 != D) tmem_ld8_nw(tmem + lrow + (uint32_t)((par * NO + D2) * N + cb), h[par]);
+                tmem_ld8_nw(tacc + lrow + (uint32_t)((par * NO + D) * N + cb), g[par]);
+                if constexpr (D2 != D) tmem_ld8_nw(tacc + lrow + (uint32_t)((par * NO + D2) * N + cb), h[par]);
               }
               tmem_wait_ld();
 #pragma unroll
@@ -509,7 +523,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
           }
           if (q == CPW - 1) {
             tc_fence_before();
-            mbar_arrive(bar_te);
+            mbar_arrive(&bar_te[tb]);
             if (mt == nmt_m - 1) mbar_arrive(&bar_ce[ii & 1]);
           }
           if (!live) continue;
@@ -609,25 +623,29 @@ static bool xs_cfg(int kmax, bool plain, XsCfg& c) {
   return false;
 }
 
-static size_t xs_smem(int ns, int nz, int rawk) {
+static size_t xs_smem(int ns, int nz, int rawk, int astages) {
   const int n = 2 * nz;
-  return 1024 + 2 * (size_t)(2 * ns * XS_ATILE) + XS_SB * (size_t)(2 * ns * n * XS_KC * 2) +
+  return 1024 + astages * (size_t)(2 * ns * XS_ATILE) + XS_SB * (size_t)(2 * ns * n * XS_KC * 2) +
          (size_t)2 * nz * rawk * sizeof(double) + 2 * n * sizeof(int) + 256;
 }
-// complex z columns per work item: 16 while the accumulators (2 NS orders x 2 NZ columns) fit the
-// 512 columns of tensor memory and the field columns fit shared memory, else 8
+// table-chunk stages: three where shared memory holds them, else two
+static int xs_astages(int ns, int nz, int rawk) { return xs_smem(ns, nz, rawk, 3) <= 227 * 1024 ? 3 : 2; }
+// complex z columns per work item: 16 while the accumulators (2 NS orders x 2 NZ columns) fit the 512
+// columns of tensor memory and the field columns fit shared memory, else 8.  (With 8 columns two sets of
+// accumulators fit for up to eight digits and the kernel double-buffers them, but at 192 x 128 x 128
+// the halved items doubled the per-item costs: backward 102 -> 124 us per three-field launch.)
 static int xs_nz(int ns) { return (G.nr <= 256 && ns <= 8) ? 16 : 8; }
 
 // whether the exact-slice contraction covers this kit: the orders stay exact and the stages fit
 bool xs_supported(int mode, int nrc, bool plain) {
   XsCfg c;
   const int kmax = mode == 0 ? G.nrh : (nrc + 1) / 2;
-  return xs_cfg(kmax, plain, c) && xs_smem(c.ns, xs_nz(c.ns), std::max(G.nr, nrc) | 1) <= 227 * 1024;
+  return xs_cfg(kmax, plain, c) && xs_smem(c.ns, xs_nz(c.ns), std::max(G.nr, nrc) | 1, 2) <= 227 * 1024;
 }
 
 template <int MODE, int NS, int NZ>
 static int xs_launch(const XsArgs& args, int nitems) {
-  const size_t sm = xs_smem(NS, NZ, args.rawk);
+  const size_t sm = xs_smem(NS, NZ, args.rawk, args.astages);
   if (sm > 227 * 1024) return set_error(MLG_ESIZE, "radial contraction: shared-memory stage too large");
   auto kern = k_xs_rtrans<MODE, NS, NZ>;
   MLG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -680,6 +698,7 @@ int xs_rtrans_multi(int mode, const cd* const* in, cd* const* out, int nf, int n
   args.nzdim = G.nzdim; args.nrc = nrc; args.m0 = m0; args.npc = npc; args.nmt = nmt; args.nkc = nkc; args.nrp = nrp;
   // odd, so that the columns of the staged field start in different shared-memory banks
   args.rawk = std::max(G.nr, nrc) | 1;
+  args.astages = xs_astages(cfg.ns, xs_nz(cfg.ns), args.rawk);
   // the kernels' compile-time digit widths (xs_w) are those of xs_cfg
   if (cfg.w != (cfg.ns == 6 || cfg.ns == 9 ? 7 : 6)) return set_error(MLG_EPARAM, "radial contraction: digit configuration");
   const int nz16 = xs_nz(cfg.ns) == 16;
