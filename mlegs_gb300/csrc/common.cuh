@@ -147,9 +147,7 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln);
 int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln);   // n <= 3 fields, one launch
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
 void lu_cache_clear();
-void tc_free();
-int tc_rtrans_fwd(const cd* in, cd* out, int nrc, int npc);
-int tc_rtrans_bwd(const cd* in, cd* out, int nrc, int npc, const double* lnp, bool add_ln);
+// the bounded-wait path of the tensor-core kernels on its own (xs_radial.cu)
 int wait_selftest(long long limit, int arrive);
 // exact-slice radial contractions on the tensor cores (xs_radial.cu): mode 0 forward, 1 backward, for
 // m0 <= m < npc; plain: FP64-grade digits, else the mixed form's
@@ -167,8 +165,6 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
 // zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);
 int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu);
-int pv_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc, int npc);
-void pv_free();
 
 // pointwise
 int launch_zero(cd* e);

@@ -1240,10 +1240,8 @@ int mlg_finalize(void) {
   if (!G.kit_set) return 0;
   cudaStreamSynchronize(G.stream);
   lu_cache_clear();
-  tc_free();
   xs_free();
   xv_free();
-  pv_free();
   for (cd* b : G.all_bufs) cudaFree(b);
   void* arrs[] = {G.x, G.w, G.w32, G.r, G.rinv, G.lnx, G.ak, G.lognorm, G.pf, G.at0, G.at1, G.bd2, G.bxx, G.bd2f, G.bxxf, G.ak2f, G.tV, G.tD, G.tT,
                   G.tV32, G.tD32, G.tT32, G.tw_p, G.tw_z, G.tw_pr, G.tw_p32, G.tw_z32, G.tw_pr32, G.tw_pdf, G.tw_zdf, G.tw_prdf, G.ln_slots, G.dscal, G.band_ws};

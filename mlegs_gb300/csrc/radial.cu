@@ -10,8 +10,10 @@
 //     eomul / oemul parity folds (:2067-2145), combined into psi and chi.
 // Each CTA owns one m, one parity of rows and one tile of z columns; the folded input (f(i) +- f(nr-1-i))
 // is formed while staging the K-chunk in shared memory.  The plain form accumulates in FP64 (DFMA).
-// The mixed form runs m >= 1 on the tensor cores (tc_radial.cu) or in FP32 and the m = 0 plane in
-// double-float (below): the m = 0 plane carries the axisymmetric mean flow, and its radial functions do
+// Where the exact-slice tensor-core contractions cover the grid (xs_radial.cu, xs_vec2tp.cu) they take
+// m >= 1 in both forms and these kernels the m = 0 plane, in FP64 (plain) or double-float (mixed,
+// below); beyond that range the FP64 kernels take every m.  The m = 0 plane carries the axisymmetric
+// mean flow, and its radial functions do
 // not vanish on the axis, so regular fields such as r d/dr(chi) reach zero there only by cancellation
 // of their radial sums, which the 1/r of the velocity components then magnifies (about 40x at the
 // innermost collocation point of a 192-point grid).
@@ -632,27 +634,23 @@ int launch_rtrans_fwd(Scalar& s) {
   const bool mixed = G.precision == MLG_MIXED;
   const bool xs = xs_supported(0, nrc, !mixed);   // exact-slice tensor-core contraction (xs_radial.cu)
   // the tensor-core contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
-  if (mixed || xs) {
+  if (xs) {
     MLG_TRY(launch_zero_tails(out, 0, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RFWD);
   if (npc > 0) {
-    if (mixed) {
-      MLG_TRY(side_fork());
-      MLG_TRY(plane_fwd(s.e, out, nrc, G.side));   // m = 0: double-float, beside
-      if (xs) MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, false));   // m >= 1: 42-bit slices
-      else MLG_TRY(tc_rtrans_fwd(s.e, out, nrc, npc));      // m >= 1: split BF16 (tc_radial.cu)
-      MLG_TRY(side_join());
-    } else if (xs) {
+    if (xs) {
       // m = 0 (the axisymmetric mean flow, whose large range within a column the fixed-point slices
-      // would cut relative to its maximum) in FP64 DFMA beside; m >= 1 as FP64-grade slices
+      // would cut relative to its maximum) beside, in double-float (mixed) or FP64 (plain); m >= 1 as
+      // exact slices, 42-bit (mixed) or FP64-grade (plain)
       MLG_TRY(side_fork());
       MLG_TRY(plane_fwd(s.e, out, nrc, G.side));
-      MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, true));
+      MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, !mixed));
       MLG_TRY(side_join());
     } else {
+      // beyond the slices' range (their orders would not stay exact): FP64 DFMA over every m, in both forms
       MLG_TRY(dfma_rtrans_fwd(s.e, out, nrc, npc, G.stream));
     }
   }
@@ -671,25 +669,21 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   const bool xs = xs_supported(1, nrc, !mixed);
   // the tensor-core contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
   // plane included): only the rest needs zeros
-  if (mixed || xs) {
+  if (xs) {
     MLG_TRY(launch_zero_tails(out, 1, nrc, npc, G.nzdim, G.nzdim + 1));
   } else {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RBWD);
   if (npc > 0) {
-    if (mixed) {
+    if (xs) {
+      // m = 0 beside in double-float (mixed) or FP64 DFMA (plain); m >= 1 as exact slices
       MLG_TRY(side_fork());
-      MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));   // m = 0: double-float, beside
-      if (xs) MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, false));   // m >= 1: 42-bit slices
-      else MLG_TRY(tc_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln));           // m >= 1: split BF16
-      MLG_TRY(side_join());
-    } else if (xs) {
-      MLG_TRY(side_fork());
-      MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));   // m = 0: FP64 DFMA, beside
-      MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, true));   // m >= 1: FP64-grade slices
+      MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));
+      MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, !mixed));
       MLG_TRY(side_join());
     } else {
+      // beyond the slices' range: FP64 DFMA over every m, in both forms
       MLG_TRY(dfma_rtrans_bwd(s.e, out, nrc, npc, s.ln, add_ln, G.stream));
     }
   }
@@ -758,7 +752,7 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   // hold 1e-12 there)
   const bool xv = mixed && xv_supported();
   // the tensor-core contractions write rows < nn(m) of the kept columns: only the rest needs zeros
-  if (mixed) {
+  if (xv) {
     cd* pc[2] = {psi, chi};
     MLG_TRY(launch_zero_tails_n(pc, 2, 0, nrc, npc, nzc, nzcu));
   } else {
@@ -769,21 +763,19 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   constexpr int MT = 16, ZT = 32, KC = 16, ZPT = 4;
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
-  if (G.precision == MLG_MIXED) {
-    // m >= 1 on the tensor cores (split BF16, the u_z term in exact digit slices), m = 0 in
-    // double-float beside it
+  if (xv) {
+    // m >= 1 on the tensor cores as exact slices, m = 0 in double-float beside it
     MLG_TRY(side_fork());
     constexpr int DMT = 16, DZT = 8, DKC = 8, DKS = 4;
     dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT, DKS);
     k_vec2tp_plane<dfl, DMT, DZT, DKC, DKS><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tD, G.tT, G.ak, G.nr, G.nrh,
                                                                          G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu);
     MLG_LAUNCH();
-    if (xv) MLG_TRY(xv_contract(ur, up, uz, psi, chi, nrc, npc, 1));   // m >= 1: 35-bit slices
-    else MLG_TRY(pv_contract(ur, up, uz, psi, chi, nrc, npc));                // m >= 1: split BF16 (tc_vec2tp.cu)
+    MLG_TRY(xv_contract(ur, up, uz, psi, chi, nrc, npc, 1));   // m >= 1: 35/49-bit slices
     MLG_TRY(side_join());
     kt_end(KT_V2TP, 5.0 * fwd_flops(nrc, npc));
     return 0;
-  } else
+  } else   // the plain form, and the mixed form beyond the slices' range: FP64 DFMA over every m
     k_vec2tp<double, MT, ZT, KC, ZPT><<<grid, blk, 0, G.stream>>>(ur, up, uz, psi, chi, G.tV, G.tD, G.tT, G.ak, G.nr,
                                                                    G.nrh, G.ne, G.nrdim, G.npdim, G.nzdim, nrc, nzc, nzcu, 0);
   MLG_LAUNCH();

@@ -1,8 +1,7 @@
 // tc_common.cuh — inline-PTX wrappers for the 5th-generation tensor cores (tcgen05), the TMA bulk
-// copies and mbarriers, and the BF16 splits, shared by the tensor-core kernels.
+// copies and mbarriers, shared by the exact-slice tensor-core kernels (xs_radial.cu, xs_vec2tp.cu).
 #pragma once
 #include "common.cuh"
-#include <cuda_bf16.h>
 #include <cstdint>
 
 namespace mlg {
@@ -127,36 +126,6 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
 // instruction descriptor: kind::f16 with BF16 A and B, FP32 D, both K-major
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// three-way BF16 split of two FP32 values at once: w[s] packs split s of (a, b) as (low, high) halves,
-// by the hardware round-to-nearest-even conversion (cvt.rn.bf16x2.f32, two values per instruction);
-// each residual is exact in FP32
-__device__ __forceinline__ void split3x2(float a, float b, uint32_t* w) {
-#pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    w[s] = *reinterpret_cast<uint32_t*>(&h);
-    a = a - __low2float(h);
-    b = b - __high2float(h);
-  }
-}
-// the BF16 pattern of a small integer (|d| < 2^8, exact in BF16): the top half of its FP32 pattern
-__device__ __forceinline__ uint32_t bf16_small_int(int d) { return __float_as_uint((float)d) >> 16; }
-
-// BF16 split of an FP32 value (round to nearest even on the integer pipe)
-__device__ __forceinline__ uint16_t bf16_rn(float x) {
-  uint32_t u = __float_as_uint(x);
-  u += 0x7FFFu + ((u >> 16) & 1u);
-  return (uint16_t)(u >> 16);
-}
-__device__ __forceinline__ float bf16_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
-__device__ __forceinline__ void split3(float x, uint16_t& s0, uint16_t& s1, uint16_t& s2) {
-  s0 = bf16_rn(x);
-  float r = x - bf16_f(s0);
-  s1 = bf16_rn(r);
-  r = r - bf16_f(s1);
-  s2 = bf16_rn(r);
 }
 
 }  // namespace mlg

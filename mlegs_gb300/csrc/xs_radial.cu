@@ -721,4 +721,24 @@ int xs_rtrans(int mode, const cd* in, cd* out, int nrc, int npc, int m0, const d
   return xs_rtrans_multi(mode, &in, &out, 1, nrc, npc, m0, &lnp, add_ln, plain);
 }
 
+// The bounded-wait path of the tensor-core kernels on its own: one thread waits on an mbarrier of
+// arrival count 1.  arrive = 0: nothing arrives, so the wait runs out after `limit` clocks and the
+// kernel sets the timeout word exactly as k_xs_rtrans does; arrive = 1: the thread arrives first and
+// the wait ends at once.  Nothing is in flight and no tensor memory is held when it returns.
+__global__ void k_wait_selftest(int* __restrict__ status, long long limit, int arrive) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  if (arrive) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&bar)) : "memory");
+  if (!mbar_wait_limit(&bar, 0, limit)) atomicExch(status, 2);
+}
+
+int wait_selftest(long long limit, int arrive) {
+  if (limit < 0 || limit > 2000000000LL) return set_error(MLG_EPARAM, "wait self-test: limit must be 0 .. 2e9 clocks");
+  k_wait_selftest<<<1, 32, 0, G.stream>>>((int*)(G.dscal + DS_FLAG + 1) + 1, limit, arrive ? 1 : 0);
+  MLG_LAUNCH();
+  return 0;
+}
+
 }  // namespace mlg
