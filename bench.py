@@ -394,7 +394,9 @@ def run_ours(args, rank, world, local, pg):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded)",
+        "vs_baseline": None,
+        "dtype": "bf16 exact digit slices (42-bit radial, 35/49-bit projection) + f32 FFTs, f64 solves and state",
+        "data": "synthetic (seeded)",
         "config": config_dict(),
         "fp64_plain": {"value": plain_sps, "unit": "steps/s", "steps": k_cmp,
                        "mixed_speedup": value / world / plain_sps},
