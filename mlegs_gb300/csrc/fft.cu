@@ -407,6 +407,20 @@ struct FSet {
   const double* rs[FS_MAX];   // per field: the row scaling of the phi transforms, or null
   int n;
 };
+// field f's pointers by a chain of selects: an indexed access to the kernel parameter would copy the
+// whole set to local memory
+__device__ __forceinline__ double2* fset_e(const FSet& fs, int f) {
+  double2* p = fs.e[0];
+#pragma unroll
+  for (int q = 1; q < FS_MAX; ++q) p = f == q ? fs.e[q] : p;
+  return p;
+}
+__device__ __forceinline__ const double* fset_rs(const FSet& fs, int f) {
+  const double* p = fs.rs[0];
+#pragma unroll
+  for (int q = 1; q < FS_MAX; ++q) p = f == q ? fs.rs[q] : p;
+  return p;
+}
 
 // z FFT: the lines (r, m) of m in [m0, m0 + nm) taken flat, line r + nrdim*(m - m0) at offset
 // r + nrdim*m (so a block's lanes read one run of consecutive offsets and no block is left ragged at
@@ -424,7 +438,7 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_zfft2(FSet fs, int nrdim
   const int f = gl / nlines, line = gl - f * nlines;
   bool ok = f < fs.n;
   size_t ps = (size_t)nrdim * npdim;
-  double2* base = (ok ? fs.e[f] : fs.e[0]) + (size_t)nrdim * m0 + line;
+  double2* base = fset_e(fs, ok ? f : 0) + (size_t)nrdim * m0 + line;
   C a[R1];
 #pragma unroll
   for (int n1 = 0; n1 < R1; ++n1) a[n1] = ok ? ld<T>(base + (size_t)(w + R2 * n1) * ps) : mk<T>(0, 0);
@@ -458,8 +472,8 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_fwd2(FSet fs, int n
   const int f = gl / per, line = gl - f * per;
   bool ok = f < fs.n;
   const int r = line % nrdim, z = line / nrdim;
-  double2* base = (ok ? fs.e[f] : fs.e[0]) + r + (size_t)nrdim * npdim * z;
-  const double* rs = ok ? fs.rs[f] : nullptr;
+  double2* base = fset_e(fs, ok ? f : 0) + r + (size_t)nrdim * npdim * z;
+  const double* rs = ok ? fset_rs(fs, f) : nullptr;
   const bool rsc = rs != nullptr && ok && r < nrs;   // the row's samples times rs[r] first (scale_r)
   const double rv = rsc ? rs[r] : 1.0;
   C a[R1];
@@ -544,8 +558,8 @@ __global__ void __launch_bounds__(TRL * Split<L>::R2) k_pfft_bwd2(FSet fs, int n
   const int f = gl / per, line = gl - f * per;
   bool ok = f < fs.n;
   const int r = line % nrdim, z = line / nrdim;
-  double2* base = (ok ? fs.e[f] : fs.e[0]) + r + (size_t)nrdim * npdim * z;
-  const double* rs = ok ? fs.rs[f] : nullptr;
+  double2* base = fset_e(fs, ok ? f : 0) + r + (size_t)nrdim * npdim * z;
+  const double* rs = ok ? fset_rs(fs, f) : nullptr;
   double2 nyq = make_double2(0, 0);
   double dc = 0.0;
   if (ok && w == 0) nyq = base[(size_t)L * nrdim];
