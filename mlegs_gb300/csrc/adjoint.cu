@@ -34,7 +34,19 @@ int vfft_checked_T(Scalar& s, int dir);
 
 // hfft forward^T, before the half-complex-to-real sum: slot 0 and slot L scaled 1/np, the interior
 // 1/(2 np) (the forward's X_k for 0 < k < L stands for two conjugate terms of the real sum)
-__global__ void k_hfftT_pre(double2* __restrict__ e, int nrdim, int npdim, int nzdim, int L, double np) {
+// up to three fields of one transposed transform, the field of a block being blockIdx.y (selected
+// without an indexed access to the kernel parameter, which would copy it to local memory)
+struct Fields3 {
+  double2* e[3];
+  double2* buf[3];
+  double* ln[3];
+};
+template <class P> __device__ __forceinline__ P f3sel(const P (&p)[3]) {
+  return blockIdx.y == 0 ? p[0] : (blockIdx.y == 1 ? p[1] : p[2]);
+}
+
+__global__ void k_hfftT_pre(Fields3 fs, int nrdim, int npdim, int nzdim, int L, double np) {
+  double2* __restrict__ e = f3sel(fs.e);
   size_t n = (size_t)nrdim * (L + 1) * nzdim;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
@@ -47,7 +59,9 @@ __global__ void k_hfftT_pre(double2* __restrict__ e, int nrdim, int npdim, int n
 }
 
 // slot L of every (r, z) row: saved to buf (save = 1) or zeroed (save = 0)
-__global__ void k_slotL(double2* __restrict__ e, double2* __restrict__ buf, int nrdim, int npdim, int nzdim, int L, int save) {
+__global__ void k_slotL(Fields3 fs, int nrdim, int npdim, int nzdim, int L, int save) {
+  double2* __restrict__ e = f3sel(fs.e);
+  double2* __restrict__ buf = f3sel(fs.buf);
   size_t n = (size_t)nrdim * nzdim;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
@@ -60,8 +74,9 @@ __global__ void k_slotL(double2* __restrict__ e, double2* __restrict__ buf, int 
 
 // hfft backward^T, after the unnormalised real-to-half-complex sum X_k = sum_j f_j e^{-2 pi i jk/np}:
 // interior doubled; slot L also takes np times the saved adjoint of the forward's slot-L copy
-__global__ void k_hfftT_post(double2* __restrict__ e, const double2* __restrict__ buf, int nrdim, int npdim, int nzdim,
-                             int L, double np) {
+__global__ void k_hfftT_post(Fields3 fs, int nrdim, int npdim, int nzdim, int L, double np) {
+  double2* __restrict__ e = f3sel(fs.e);
+  const double2* __restrict__ buf = f3sel(fs.buf);
   size_t n = (size_t)nrdim * (L + 1) * nzdim;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nrdim);
@@ -74,7 +89,8 @@ __global__ void k_hfftT_post(double2* __restrict__ e, const double2* __restrict_
 }
 
 // rows i < nr of every column scaled by tab[i] (inv = 0) or divided by it (inv = 1)
-__global__ void k_scale_tab(double2* __restrict__ e, const double* __restrict__ tab, int nr, int nrdim, size_t ncol, int inv) {
+__global__ void k_scale_tab(Fields3 fs, const double* __restrict__ tab, int nr, int nrdim, size_t ncol, int inv) {
+  double2* __restrict__ e = f3sel(fs.e);
   size_t n = (size_t)nr * ncol;
   GRID_STRIDE(idx, n) {
     int i = (int)(idx % (unsigned)nr);
@@ -86,8 +102,10 @@ __global__ void k_scale_tab(double2* __restrict__ e, const double* __restrict__ 
 }
 
 // *lnp += sgn * sum_{i < nr, z} lnx_i Re e(i, 0, z): the adjoint of e(:nr, 1, :) += ln * lnx
-__global__ void __launch_bounds__(1024) k_ln_dot(const double2* __restrict__ e, const double* __restrict__ lnx, int nr,
-                                                 int nrdim, int npdim, int nzdim, double* __restrict__ lnp, double sgn) {
+__global__ void __launch_bounds__(1024) k_ln_dot(Fields3 fs, const double* __restrict__ lnx, int nr, int nrdim, int npdim,
+                                                 int nzdim, double sgn) {
+  const double2* __restrict__ e = f3sel(fs.e);
+  double* __restrict__ lnp = f3sel(fs.ln);
   __shared__ double red[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double s = 0.0;
@@ -442,72 +460,109 @@ __global__ void k_drop_mean(double2* __restrict__ e, double* __restrict__ lnp, i
 // ------------------------------------------------------------------------------------------------
 // transposed operators on Scalars (each in place on the adjoint variable s)
 
-static int hfft_fwd_T(Scalar& s) {   // PFP-side adjoint -> PPP-side
+static Fields3 fields3(Scalar* const* s, int n, cd* const* bufs = nullptr) {
+  Fields3 f{};
+  for (int i = 0; i < 3; ++i) {
+    const int g = i < n ? i : 0;
+    f.e[i] = s[g]->e;
+    f.buf[i] = bufs ? bufs[g] : nullptr;
+    f.ln[i] = s[g]->ln;
+  }
+  return f;
+}
+
+// The transposed transform steps of n <= 3 fields in one launch each (the components of a vector
+// field, each field's own sequence of operations unchanged).
+static int hfft_fwd_T_n(Scalar* const* s, int n) {   // PFP-side adjoint -> PPP-side
   if (G.np <= 1) return 0;
-  int L = G.np / 2;
-  k_hfftT_pre<<<nblk((size_t)G.nrdim * (L + 1) * G.nzdim), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, L, (double)G.np);
+  const int L = G.np / 2;
+  const Fields3 fs = fields3(s, n);
+  k_hfftT_pre<<<dim3(nblk((size_t)G.nrdim * (L + 1) * G.nzdim), n), 256, 0, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, L,
+                                                                                       (double)G.np);
   MLG_LAUNCH();
-  MLG_TRY(launch_hfft_bwd_buf(s.e));
-  k_slotL<<<nblk((size_t)G.nrdim * G.nzdim), 256, 0, G.stream>>>(s.e, nullptr, G.nrdim, G.npdim, G.nzdim, L, 0);
+  cd* e[3];
+  for (int i = 0; i < n; ++i) e[i] = s[i]->e;
+  MLG_TRY(launch_hfft_bwd_buf_n(e, n));
+  k_slotL<<<dim3(nblk((size_t)G.nrdim * G.nzdim), n), 256, 0, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, L, 0);
   MLG_LAUNCH();
   return 0;
 }
 
-static int hfft_bwd_T(Scalar& s) {   // PPP-side adjoint -> PFP-side
+static int hfft_bwd_T_n(Scalar* const* s, int n) {   // PPP-side adjoint -> PFP-side
   if (G.np <= 1) return 0;
-  int L = G.np / 2;
-  cd* buf = get_buf();
-  if (!buf) return set_error(MLG_EALLOC, "adjoint: out of device memory");
-  k_slotL<<<nblk((size_t)G.nrdim * G.nzdim), 256, 0, G.stream>>>(s.e, (double2*)buf, G.nrdim, G.npdim, G.nzdim, L, 1);
-  MLG_LAUNCH();
-  int rc = launch_hfft_fwd_scaled(s.e, 1.0);
+  const int L = G.np / 2;
+  cd* bufs[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < n; ++i) {
+    bufs[i] = get_buf();
+    if (!bufs[i]) {
+      for (int k = 0; k < i; ++k) put_buf(bufs[k]);
+      return set_error(MLG_EALLOC, "adjoint: out of device memory");
+    }
+  }
+  const Fields3 fs = fields3(s, n, bufs);
+  k_slotL<<<dim3(nblk((size_t)G.nrdim * G.nzdim), n), 256, 0, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, L, 1);
+  int rc = 0;
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) rc = set_error(MLG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+  ++G.launches;
+  cd* e[3];
+  for (int i = 0; i < n; ++i) e[i] = s[i]->e;
+  if (!rc) rc = launch_hfft_fwd_scaled_n(e, n, 1.0);
   if (!rc) {
-    k_hfftT_post<<<nblk((size_t)G.nrdim * (L + 1) * G.nzdim), 256, 0, G.stream>>>(s.e, (const double2*)buf, G.nrdim,
-                                                                                  G.npdim, G.nzdim, L, (double)G.np);
+    k_hfftT_post<<<dim3(nblk((size_t)G.nrdim * (L + 1) * G.nzdim), n), 256, 0, G.stream>>>(fs, G.nrdim, G.npdim, G.nzdim, L,
+                                                                                          (double)G.np);
     ++G.launches;
-    cudaError_t err = cudaGetLastError();
+    err = cudaGetLastError();
     if (err != cudaSuccess) rc = set_error(MLG_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
   }
-  put_buf(buf);
+  for (int i = 0; i < n; ++i) put_buf(bufs[i]);
   return rc;
 }
 
-static int scale_tab(Scalar& s, const double* tab, int inv) {
+static int scale_tab_n(Scalar* const* s, int n, const double* tab, int inv) {
   size_t ncol = (size_t)G.npdim * G.nzdim;
-  k_scale_tab<<<nblk((size_t)G.nr * ncol), 256, 0, G.stream>>>(s.e, tab, G.nr, G.nrdim, ncol, inv);
+  k_scale_tab<<<dim3(nblk((size_t)G.nr * ncol), n), 256, 0, G.stream>>>(fields3(s, n), tab, G.nr, G.nrdim, ncol, inv);
   MLG_LAUNCH();
   return 0;
 }
+static int scale_tab(Scalar& s, const double* tab, int inv) { Scalar* p = &s; return scale_tab_n(&p, 1, tab, inv); }
 
-static int ln_dot(Scalar& s, double sgn) {
-  k_ln_dot<<<1, 1024, 0, G.stream>>>(s.e, G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, s.ln, sgn);
+static int ln_dot_n(Scalar* const* s, int n, double sgn) {
+  k_ln_dot<<<dim3(1, n), 1024, 0, G.stream>>>(fields3(s, n), G.lnx, G.nr, G.nrdim, G.npdim, G.nzdim, sgn);
   MLG_LAUNCH();
   return 0;
 }
 
 // the PFP -> FFP step (e(:nr,1,:) -= ln lnx, then rtrans_forward) transposed: FFP-side -> PFP-side.
 // rtrans_forward^T = w * rtrans_backward (the quadrature weights are symmetric about the fold).
-static int rtrans_fwd_T(Scalar& s) {
-  MLG_TRY(launch_rtrans_bwd(s, false));
-  MLG_TRY(scale_tab(s, G.w, 0));
-  return ln_dot(s, -1.0);
+static int rtrans_fwd_T_n(Scalar* const* s, int n) {
+  MLG_TRY(launch_rtrans_bwd_multi(s, n, false));
+  MLG_TRY(scale_tab_n(s, n, G.w, 0));
+  return ln_dot_n(s, n, -1.0);
 }
 
 // the FFP -> PFP step (rtrans_backward with the log term) transposed: PFP-side -> FFP-side.
 // rtrans_backward^T = rtrans_forward of the input divided by the weights.
-static int rtrans_bwd_T(Scalar& s, bool with_ln) {
-  if (with_ln) MLG_TRY(ln_dot(s, 1.0));
-  MLG_TRY(scale_tab(s, G.w, 1));
-  return launch_rtrans_fwd(s);
+static int rtrans_bwd_T_n(Scalar* const* s, int n, bool with_ln) {
+  if (with_ln) MLG_TRY(ln_dot_n(s, n, 1.0));
+  MLG_TRY(scale_tab_n(s, n, G.w, 1));
+  return launch_rtrans_fwd_multi(s, n);
 }
+static int rtrans_bwd_T(Scalar& s, bool with_ln) { Scalar* p = &s; return rtrans_bwd_T_n(&p, 1, with_ln); }
 
-int vfft_checked_T(Scalar& s, int dir) {   // transpose of vertical_fft (dir -1 forward, +1 backward)
+// transpose of vertical_fft (dir -1 forward, +1 backward) of n fields with the same z chop
+static int vfft_checked_T_n(Scalar* const* s, int n, int dir) {
   if (G.nz <= 1) return 0;
-  int nzc = G.chopzl + s.off[2], nzcu = G.chopzu - s.off[2];
-  if (2 * s.off[2] > nzcu - nzc) return set_error(MLG_ECHOP, "vertical_fft: chopping in z too large");
+  cd* e[3];
+  for (int i = 0; i < n; ++i) {
+    int nzc = G.chopzl + s[i]->off[2], nzcu = G.chopzu - s[i]->off[2];
+    if (2 * s[i]->off[2] > nzcu - nzc) return set_error(MLG_ECHOP, "vertical_fft: chopping in z too large");
+    e[i] = s[i]->e;
+  }
   // forward: (1/nz) sum e^{-}; its transpose (1/nz) sum e^{+}.  backward: sum e^{+}; transpose sum e^{-}
-  return dir < 0 ? launch_vfft_scaled(s.e, +1, 1.0 / G.nz) : launch_vfft_scaled(s.e, -1, 1.0);
+  return dir < 0 ? launch_vfft_scaled_n(e, n, +1, 1.0 / G.nz) : launch_vfft_scaled_n(e, n, -1, 1.0);
 }
+int vfft_checked_T(Scalar& s, int dir) { Scalar* p = &s; return vfft_checked_T_n(&p, 1, dir); }
 
 static int space_idx(const char* sp) {
   if (!std::strncmp(sp, "PPP", 3)) return 0;
@@ -520,25 +575,32 @@ static const char* SPACES[4] = {"PPP", "PFP", "FFP", "FFF"};
 
 // trans^T: s holds the adjoint of trans(x, s.space) applied to an x in fwd_from; afterwards s holds
 // the adjoint w.r.t. x (labelled fwd_from)
-int trans_T(Scalar& s, const char* fwd_from) {
-  int to = space_idx(s.space), from = space_idx(fwd_from);
+// n <= 3 fields in the same space: each step of the transform for all of them in one launch
+static int trans_T_n(Scalar* const* s, int n, const char* fwd_from) {
+  int to = space_idx(s[0]->space), from = space_idx(fwd_from);
   if (to < 0 || from < 0) return set_error(MLG_ESPACE, "trans adjoint: unknown space");
+  for (int i = 1; i < n; ++i)
+    if (space_idx(s[i]->space) != to) return set_error(MLG_ESPACE, "trans adjoint: a batch of fields in different spaces");
   if (from < to) {          // forward went up: undo the steps from the top
     for (int c = to; c > from; --c) {
-      if (c == 3) MLG_TRY(vfft_checked_T(s, -1));
-      if (c == 2) MLG_TRY(rtrans_fwd_T(s));
-      if (c == 1) MLG_TRY(hfft_fwd_T(s));
-      s.set_space(SPACES[c - 1]);
+      if (c == 3) MLG_TRY(vfft_checked_T_n(s, n, -1));
+      if (c == 2) MLG_TRY(rtrans_fwd_T_n(s, n));
+      if (c == 1) MLG_TRY(hfft_fwd_T_n(s, n));
+      for (int i = 0; i < n; ++i) s[i]->set_space(SPACES[c - 1]);
     }
   } else if (from > to) {   // forward went down
     for (int c = to; c < from; ++c) {
-      if (c == 0) MLG_TRY(hfft_bwd_T(s));
-      if (c == 1) MLG_TRY(rtrans_bwd_T(s, true));
-      if (c == 2) MLG_TRY(vfft_checked_T(s, +1));
-      s.set_space(SPACES[c + 1]);
+      if (c == 0) MLG_TRY(hfft_bwd_T_n(s, n));
+      if (c == 1) MLG_TRY(rtrans_bwd_T_n(s, n, true));
+      if (c == 2) MLG_TRY(vfft_checked_T_n(s, n, +1));
+      for (int i = 0; i < n; ++i) s[i]->set_space(SPACES[c + 1]);
     }
   }
   return 0;
+}
+int trans_T(Scalar& s, const char* fwd_from) {
+  Scalar* p = &s;
+  return trans_T_n(&p, 1, fwd_from);
 }
 
 int band_T(Scalar& s, int op) {   // xxdx (0), del2h (1), del2 (2)
@@ -613,16 +675,16 @@ int tp2vec_T(const Scalar& vrb, const Scalar& vpb, const Scalar& vzb, Scalar& ps
   TMP(ur); TMP(up); TMP(uz);
   MLG_TRY(assign(ur, vrb)); MLG_TRY(assign(up, vpb)); MLG_TRY(assign(uz, vzb));
   for (Scalar* q : {&ur, &up, &uz}) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
-  // u_z branch: del2h (offset 3), negation, chop, trans to PPP
-  MLG_TRY(trans_T(uz, "FFF"));
-  MLG_TRY(op_chop(uz));
+  // u_z branch: del2h (offset 3), negation, chop, trans to PPP; u_r, u_phi branches: xxdx (offset 3),
+  // combination, chop, trans to PPP, division by r.  The branches are independent: the transposed
+  // transforms and chops of the three fields run together, each field's own sequence unchanged.
+  MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
+  Scalar* f3[3] = {&uz, &ur, &up};
+  MLG_TRY(trans_T_n(f3, 3, "FFF"));
+  MLG_TRY(op_mask_n(f3, 3, true, false));
   MLG_TRY(lincomb(uz, {{&uz, -1.0}}, {}, 1.0, false));
   uz.off[0] = 3;
   MLG_TRY(band_T(uz, 1));
-  // u_r, u_phi branches: xxdx (offset 3), combination, chop, trans to PPP, division by r
-  MLG_TRY(scale_r(ur, 1)); MLG_TRY(scale_r(up, 1));
-  MLG_TRY(trans_T(ur, "FFF")); MLG_TRY(trans_T(up, "FFF"));
-  MLG_TRY(op_chop2(ur, up));
   ur.off[0] = 3; up.off[0] = 3;
   ChopIdx c;
   MLG_TRY(chop_index(ur, c));
@@ -704,17 +766,17 @@ int vec2tp_T(const Scalar& psib_in, const Scalar& chib_in, Scalar& vrb, Scalar& 
     MLG_LAUNCH();
   }
   MLG_TRY(launch_set_ln(up.ln, 0.0));
-  MLG_TRY(trans_T(up, "PPP"));
+  // trans^T of up from FFF back to PPP (z, radial, phi steps); u_r (r*vr) and u_z walk back through the
+  // z and phi steps only (the PFF adjoint).  The three chains are independent: their z and phi steps run
+  // together, each field's own sequence unchanged.
+  Scalar* f3[3] = {&up, &ur, &uz};
+  MLG_TRY(vfft_checked_T_n(f3, 3, -1));
+  MLG_TRY(rtrans_fwd_T_n(f3, 1));
+  MLG_TRY(hfft_fwd_T_n(f3, 3));
+  up.set_space("PPP");
   MLG_TRY(scale_r(up, 0));
-  // u_r: hfft + vfft forward of r*vr
-  ur.set_space("FFP");   // the PFF adjoint walks back through the z and phi steps only
-  MLG_TRY(vfft_checked_T(ur, -1));
-  MLG_TRY(hfft_fwd_T(ur));
-  MLG_TRY(launch_set_ln(ur.ln, 0.0));
+  MLG_TRY(launch_set_ln2(ur.ln, uz.ln, 0.0));
   MLG_TRY(scale_r(ur, 0));
-  MLG_TRY(vfft_checked_T(uz, -1));
-  MLG_TRY(hfft_fwd_T(uz));
-  MLG_TRY(launch_set_ln(uz.ln, 0.0));
   MLG_TRY(assign(vrb, ur)); MLG_TRY(assign(vpb, up)); MLG_TRY(assign(vzb, uz));
   for (Scalar* q : {&vrb, &vpb, &vzb}) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
   return 0;

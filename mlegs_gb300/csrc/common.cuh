@@ -141,10 +141,15 @@ int launch_vfft_scaled(cd* e, int dir, double scale);
 int launch_hfft_fwd_scaled(cd* e, double scale);
 int launch_hfft_bwd_buf(cd* e);
 int launch_vfft_multi(Scalar* const* s, int n, int dir);   // n <= 6 fields in one pass
+// the adjoint's FFTs of n <= 6 buffers in one pass
+int launch_vfft_scaled_n(cd* const* e, int n, int dir, double scale);
+int launch_hfft_fwd_scaled_n(cd* const* e, int n, double scale);
+int launch_hfft_bwd_buf_n(cd* const* e, int n);
 int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir);
 int launch_rtrans_fwd(Scalar& s);
 int launch_rtrans_bwd(Scalar& s, bool add_ln);
 int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln);   // n <= 3 fields, one launch
+int launch_rtrans_fwd_multi(Scalar* const* f, int n);                // n <= 3 fields, one launch
 int launch_ln_adjust(Scalar& s, double sign);    // e(:nr,1,:) += sign * ln * lnx
 void lu_cache_clear();
 // the bounded-wait path of the tensor-core kernels on its own (xs_radial.cu)

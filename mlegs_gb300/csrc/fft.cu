@@ -819,13 +819,30 @@ int launch_hfft_multi(Scalar* const* s, const double* const* rs, int n, int dir)
   fs.n = n;
   return G.precision == MLG_MIXED ? hfft_t<MixFT>(fs, dir, 1.0 / G.np) : hfft_t<double>(fs, dir, 1.0 / G.np);
 }
-// the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs)
-int launch_hfft_fwd_scaled(cd* e, double scale) {
-  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fset1(e), -1, scale) : hfft_t<double>(fset1(e), -1, scale);
+static FSet fset_n(cd* const* e, int n) {
+  FSet fs{};
+  for (int i = 0; i < n; ++i) { fs.e[i] = e[i]; fs.rs[i] = nullptr; }
+  fs.n = n;
+  return fs;
 }
-// the half-complex-to-real sum (unnormalised, Nyquist slot kept times np), on a raw buffer
-int launch_hfft_bwd_buf(cd* e) {
-  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fset1(e), +1, 1.0) : hfft_t<double>(fset1(e), +1, 1.0);
+// the real-to-half-complex sum scaled by `scale` instead of 1/np (the adjoint's FFTs), of n <= 6 buffers
+int launch_hfft_fwd_scaled_n(cd* const* e, int n, double scale) {
+  if (n < 1 || n > FS_MAX) return set_error(MLG_EPARAM, "horizontal_fft: 1 to 6 fields per batch");
+  const FSet fs = fset_n(e, n);
+  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fs, -1, scale) : hfft_t<double>(fs, -1, scale);
+}
+int launch_hfft_fwd_scaled(cd* e, double scale) { return launch_hfft_fwd_scaled_n(&e, 1, scale); }
+// the half-complex-to-real sum (unnormalised, Nyquist slot kept times np), on n <= 6 raw buffers
+int launch_hfft_bwd_buf_n(cd* const* e, int n) {
+  if (n < 1 || n > FS_MAX) return set_error(MLG_EPARAM, "horizontal_fft: 1 to 6 fields per batch");
+  const FSet fs = fset_n(e, n);
+  return G.precision == MLG_MIXED ? hfft_t<MixFT>(fs, +1, 1.0) : hfft_t<double>(fs, +1, 1.0);
+}
+int launch_hfft_bwd_buf(cd* e) { return launch_hfft_bwd_buf_n(&e, 1); }
+// the z sum of n <= 6 buffers, any direction and scale
+int launch_vfft_scaled_n(cd* const* e, int n, int dir, double scale) {
+  if (n < 1 || n > FS_MAX) return set_error(MLG_EPARAM, "vertical_fft: 1 to 6 fields per batch");
+  return vfft_any(fset_n(e, n), dir, scale);
 }
 
 }  // namespace mlg

@@ -290,24 +290,32 @@ __device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, doubl
 __global__ void __launch_bounds__(256) k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim,
                                                   const double* __restrict__ qt, unsigned long long cbits,
                                                   double* __restrict__ partial) {
-  // a warp per column (m, k), its lanes over the rows: the column's q bits once, the row's per lane;
-  // |e|^2 summed in FP64 into the head (q below the cutoff) and the tail
+  // a warp per column (m, k), its lanes over the rows; |e|^2 summed in FP64 into the head (q below the
+  // cutoff) and the tail.  q of a row rises with the row (svv_qr), so the rows below the cutoff are
+  // the first nc: a column whose m or k is at or above the cutoff goes to the tail whole, any other
+  // splits at row nc, and no element needs a predicated FP64 add.
   __shared__ double s0[8], s1[8];
   const unsigned long long* qb = reinterpret_cast<const unsigned long long*>(qt);
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int ncol = npdim * nzdim;
+  int nc = 0;
+  for (int i0 = 0; i0 < nrdim; i0 += 32) {
+    const int i = i0 + lane;
+    nc += __popc(__ballot_sync(0xffffffffu, i < nrdim && qb[i] < cbits));
+  }
   double head = 0, tail = 0;
   for (int c = blockIdx.x * 8 + wib; c < ncol; c += gridDim.x * 8) {
     const int m = c % npdim, k = c / npdim;
     const unsigned long long bm = qb[nrdim + m], bk = qb[nrdim + npdim + k];
-    const unsigned long long bc = bm > bk ? bm : bk;
+    const int split = (bm >= cbits || bk >= cbits) ? 0 : nc;
     const double2* col = e + (size_t)nrdim * c;
-    for (int i = lane; i < nrdim; i += 32) {
+    for (int i = lane; i < split; i += 32) {
       const double2 v = col[i];
-      const double a2 = v.x * v.x + v.y * v.y;
-      unsigned long long b = qb[i];
-      b = b > bc ? b : bc;
-      if (b >= cbits) tail += a2; else head += a2;
+      head += v.x * v.x + v.y * v.y;
+    }
+    for (int i = split + lane; i < nrdim; i += 32) {
+      const double2 v = col[i];
+      tail += v.x * v.x + v.y * v.y;
     }
   }
   for (int o = 16; o; o >>= 1) {

@@ -693,6 +693,50 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   return 0;
 }
 
+// the forward transforms of n fields (n <= 3) with the same chop: one tensor-core launch over all of
+// them (the m = 0 planes beside it, one launch each), else field by field
+int launch_rtrans_fwd_multi(Scalar* const* f, int n) {
+  if (n == 1) return launch_rtrans_fwd(*f[0]);
+  int nrc = 0, npc = 0;
+  for (int i = 0; i < n; ++i) {
+    int a, b;
+    MLG_TRY(rtrans_check(*f[i], a, b, "rtrans_forward"));
+    if (i == 0) { nrc = a; npc = b; }
+    if (a != nrc || b != npc || n > 3) {   // different chops: one at a time
+      for (int k = 0; k < n; ++k) MLG_TRY(launch_rtrans_fwd(*f[k]));
+      return 0;
+    }
+  }
+  const bool mixed = G.precision == MLG_MIXED;
+  const bool xs = xs_supported(0, nrc, !mixed);
+  if (!xs || npc < 1) {
+    for (int k = 0; k < n; ++k) MLG_TRY(launch_rtrans_fwd(*f[k]));
+    return 0;
+  }
+  cd* out[3] = {nullptr, nullptr, nullptr};
+  const cd* in[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < n; ++i) {
+    out[i] = get_buf();
+    if (!out[i]) {
+      for (int k = 0; k < i; ++k) put_buf(out[k]);
+      return set_error(MLG_EALLOC, "rtrans_forward: out of device memory");
+    }
+    in[i] = f[i]->e;
+  }
+  MLG_TRY(launch_zero_tails_n(out, n, 0, nrc, npc, G.nzdim, G.nzdim + 1));
+  kt_begin(KT_RFWD);
+  MLG_TRY(side_fork());
+  for (int i = 0; i < n; ++i) MLG_TRY(plane_fwd(in[i], out[i], nrc, G.side));   // m = 0 beside
+  MLG_TRY(xs_rtrans_multi(0, in, out, n, nrc, npc, 1, nullptr, false, !mixed));   // m >= 1, all fields
+  MLG_TRY(side_join());
+  kt_end(KT_RFWD, n * fwd_flops(nrc, npc));
+  for (int i = 0; i < n; ++i) {
+    put_buf(f[i]->e);
+    f[i]->e = out[i];
+  }
+  return 0;
+}
+
 // the backward transforms of n fields (n <= 3, the components of a vector field) with the same chop:
 // one tensor-core launch over all of them (and the m = 0 planes beside it), else field by field
 int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln) {
