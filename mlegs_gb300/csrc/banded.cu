@@ -548,7 +548,7 @@ struct SolveArgs {
   const double* lognorm;
   int* status;
   int nrdim, npdim, ne, nrc, npc, nzc, nzcu, nzdim;
-  int nsys;             // npc * nzdim
+  int nsys;             // npc * nzdim (the cached-factor paths: the positions of sys_mk)
   int nsp = 0;          // the factor image's system stride: nsys rounded up to 32
   double alpha, beta, ell, preln;
   int kind;             // 0 ihelm, 1 idel2_proln, 2 idel2_preln, 3 ihelmp
@@ -559,7 +559,29 @@ struct SolveArgs {
   double2* e2 = nullptr;  // substitution: a second field with the same matrices (paired solve), or null
   double* lnp2 = nullptr;
   int* pivflag = nullptr;  // per 32 systems: non-zero when one of them exchanges rows (factor writes, substitution reads)
+  int lead = 0;            // cached factors: positions of the twice-solved systems (a multiple of 32; sys_mk)
 };
+
+// The order of the systems in the cached factors and in the substitution's blocks (position p -> (m, k);
+// false for a position that holds no system).  The k that both halves of the reference's k loop visit
+// (the shared slot when nzc == nzcu) are solved twice in a row, and a block holding one of them runs
+// both passes twice.  Those systems come first, m by m, in blocks of their own (`lead` positions, padded
+// to a whole block); then every (m, k) follows m-major as p = lead + m nzdim + k, with the twice-solved
+// k left idle there.  The 32-system blocks of the second part are those of the plain order, so the
+// systems that exchange rows (and take the substitution's slower paths) fall into the same blocks.
+__device__ __forceinline__ bool sys_mk(const SolveArgs& a, int p, int& m, int& k) {
+  const int klo = max(a.nzcu, 1) - 1, khi = min(a.nzdim, a.nzc) - 1;
+  if (p < a.lead) {
+    const int nd = max(khi - klo + 1, 1);
+    m = p / nd;
+    k = klo + (p - m * nd);
+    return m < a.npc;
+  }
+  const int q = p - a.lead;
+  m = q / a.nzdim;
+  k = q - m * a.nzdim;
+  return a.lead == 0 || k < klo || k > khi;
+}
 
 // entry (i, j) (0-based) of D(m,k) = D0(m) - ak^2 I for an n x n truncation
 __device__ __forceinline__ double dmat(const SolveArgs& a, int m, double akv, int n, int i, int j) {
@@ -828,9 +850,10 @@ __device__ void window_solve(const SolveArgs& a, int sys, int kind, bool special
 constexpr int FKL = 2, FKU = 2, FSL = 2 * FKL + FKU + 2;
 
 __global__ void __launch_bounds__(32) k_band_factor(SolveArgs a, double* __restrict__ fac) {
-  int sys = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = blockIdx.x * blockDim.x + threadIdx.x;   // position in the system order (sys_mk)
   if (sys >= a.nsys) return;
-  int m = sys / a.nzdim, k = sys % a.nzdim;
+  int m, k;
+  if (!sys_mk(a, sys, m, k)) return;
   int nn = max(min(a.nrc, a.nrc - m), 0);
   if (m >= a.npc || nn < 1 || k_count(k, a.nzc, a.nzcu, a.nzdim) == 0) return;
   bool special = (m == 0 && k == 0) && a.kind == 1;
@@ -947,7 +970,8 @@ __global__ void __launch_bounds__(64 * NR) k_band_subst(SolveArgs a, const doubl
   double* lv = q == 0 ? a.lnp : a.lnp2;
   auto sys_info = [&](int s, int& nn, int& cnt, size_t& off) {
     bool valid = s < a.nsys;
-    int m = valid ? s / a.nzdim : 0, k = valid ? s % a.nzdim : 0;
+    int m = 0, k = 0;
+    if (valid) valid = sys_mk(a, s, m, k);
     cnt = valid ? k_count(k, a.nzc, a.nzcu, a.nzdim) : 0;
     nn = max(min(a.nrc, a.nrc - m), 0);
     if (valid && m == 0 && k == 0 && a.skip_root) cnt = 0;
@@ -1251,6 +1275,17 @@ int ihelm_noalloc(void* e_dev, double* ln, double alpha) {
   return 0;
 }
 
+// the positions of the cached-factor system order (sys_mk) for a's chop window: sets lead, nsys and nsp
+static size_t set_positions(SolveArgs& a) {
+  const int klo = std::max(a.nzcu, 1) - 1, khi = std::min(a.nzdim, a.nzc) - 1;
+  const size_t nd = (size_t)std::max(khi - klo + 1, 0);
+  a.lead = (int)(((size_t)std::max(a.npc, 0) * nd + 31) / 32 * 32);
+  const size_t n = (size_t)a.lead + (size_t)std::max(a.npc, 1) * a.nzdim;
+  a.nsys = (int)n;
+  a.nsp = (int)((n + 31) / 32 * 32);
+  return n;
+}
+
 // LRU cache of factor sets, keyed by (kind, alpha, chop window)
 struct LUEntry {
   int kind; double alpha; int nrc, npc, nzc, nzcu; double* buf; size_t bytes; unsigned long long used;
@@ -1351,16 +1386,16 @@ int launch_band_solve(Scalar& s, int kind, const ChopIdx& c, double alpha, doubl
     SolveArgs b = a;
     b.kind = fkind;
     b.skip_root = (kind == 2) ? 1 : 0;
-    b.nsp = (int)((nsys + 31) / 32 * 32);
+    const size_t npos = set_positions(b);
     MLG_TRY(lu_cache_get(fkind, alpha, c, (size_t)b.nsp, &fac, [&](double* buf) -> int {
       SolveArgs fa = b;
       fa.pivflag = lu_flags(buf, b.nrc, (size_t)b.nsp);
-      k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
+      k_band_factor<<<cdiv(npos, 32), 32, 0, G.stream>>>(fa, buf);
       MLG_LAUNCH();
       return 0;
     }));
     b.pivflag = lu_flags(fac, b.nrc, (size_t)b.nsp);
-    MLG_TRY(launch_subst<1>(b, fac, nsys));
+    MLG_TRY(launch_subst<1>(b, fac, npos));
     if (kind == 2) {
       k_band_solve_special<<<1, 32, 0, G.stream>>>(a);
       MLG_LAUNCH();
@@ -1386,16 +1421,16 @@ int launch_ihelm_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double alpha) {
   a.e2 = s2.e; a.lnp2 = s2.ln;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  a.nsp = (int)((nsys + 31) / 32 * 32);
+  const size_t npos = set_positions(a);
   MLG_TRY(lu_cache_get(0, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     SolveArgs fa = a;
     fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
+    k_band_factor<<<cdiv(npos, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
   a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
-  MLG_TRY(launch_subst<2>(a, fac, nsys));
+  MLG_TRY(launch_subst<2>(a, fac, npos));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
 }
@@ -1511,16 +1546,16 @@ int launch_band_solve_T(Scalar& s, int kind, const ChopIdx& c, double alpha) {
   a.kind = kind; a.power = 0; a.skip_root = 0; a.transpose = 1; a.no_ln = 1;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  a.nsp = (int)((nsys + 31) / 32 * 32);
+  const size_t npos = set_positions(a);
   MLG_TRY(lu_cache_get(kind + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     SolveArgs fa = a;
     fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
+    k_band_factor<<<cdiv(npos, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
   a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
-  MLG_TRY(launch_subst<1>(a, fac, nsys));
+  MLG_TRY(launch_subst<1>(a, fac, npos));
   kt_end(KT_SOLVE, solve_bytes(1, c));
   return 0;
 }
@@ -1540,16 +1575,16 @@ int launch_band_solve_T_pair(Scalar& s1, Scalar& s2, const ChopIdx& c, double al
   a.e2 = s2.e; a.lnp2 = s2.ln;
   kt_begin(KT_SOLVE);
   double* fac = nullptr;
-  a.nsp = (int)((nsys + 31) / 32 * 32);
+  const size_t npos = set_positions(a);
   MLG_TRY(lu_cache_get(0 + 8, alpha, c, (size_t)a.nsp, &fac, [&](double* buf) -> int {
     SolveArgs fa = a;
     fa.pivflag = lu_flags(buf, a.nrc, (size_t)a.nsp);
-    k_band_factor<<<cdiv(nsys, 32), 32, 0, G.stream>>>(fa, buf);
+    k_band_factor<<<cdiv(npos, 32), 32, 0, G.stream>>>(fa, buf);
     MLG_LAUNCH();
     return 0;
   }));
   a.pivflag = lu_flags(fac, a.nrc, (size_t)a.nsp);
-  MLG_TRY(launch_subst<2>(a, fac, nsys));
+  MLG_TRY(launch_subst<2>(a, fac, npos));
   kt_end(KT_SOLVE, solve_bytes(2, c));
   return 0;
 }

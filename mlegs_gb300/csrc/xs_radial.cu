@@ -33,7 +33,7 @@
 // z columns); the CTA
 //  * bulk-copies the item's FP64 field columns (NZ runs of consecutive r, each contiguous in HBM) into
 //    shared memory on the TMA engine, completing on an mbarrier;
-//  * reduces the column scales there;
+//  * takes the item's column scales, which the epilogue warps computed two items ahead from global memory;
 //  * per row tile and K chunk of 16: the table digits of both parities arrive by one bulk copy (pre-split
 //    at kit init in the UMMA canonical no-swizzle K-major layout), the threads cut the field digits
 //    from shared memory into the same layout (each warp's 32 stores in 32 banks), and one thread issues
@@ -148,8 +148,9 @@ __device__ __forceinline__ bool xs_wait(uint64_t* bar, uint32_t phase, bool& ok)
 // Warp roles of the contraction kernel (512 threads, one CTA per SM):
 //   warp 0      producer: the item's field columns and the table chunks, by bulk copy
 //   warp 1      MMA issue (one thread) and the tensor-memory allocation
-//   warps 2..7  column scales and field digits
-//   warps 8..15 epilogue: tensor memory -> 64-bit order sums -> FP64 results
+//   warps 2..7  field digits
+//   warps 8..15 epilogue: tensor memory -> 64-bit order sums -> FP64 results; the column scales of
+//               the item two ahead
 // Every hand-off is an mbarrier: the table chunks and the field-digit stages are rings (2 and XS_SB
 // stages), the field columns are one buffer (the next item's columns land while the MMAs and the
 // epilogue of this one run), the accumulators are released by the epilogue as soon as it has read
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
   uint64_t* bar_be = bar_bf + XS_SB;       // [XS_SB] digit stage consumed (MMA commit)
   uint64_t* bar_tf = bar_be + XS_SB;       // [TB] accumulators complete (MMA commit)
   uint64_t* bar_te = bar_tf + 2;           // [TB] accumulators read (epilogue threads)
-  uint64_t* bar_cx = bar_te + 2;           // [2] column scales written (digit threads), by item parity
+  uint64_t* bar_cx = bar_te + 2;           // [2] column scales written (epilogue threads), by item parity
   uint64_t* bar_ce = bar_cx + 2;           // [2] column scales read (epilogue threads), by item parity
   uint32_t* tslot = (uint32_t*)(bar_ce + 2);
 
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       mbar_init(bar_ae + i, 1);
     }
     for (int i = 0; i < 2; ++i) {
-      mbar_init(bar_cx + i, XS_NDIG);
+      mbar_init(bar_cx + i, XS_NEPI);
       mbar_init(bar_ce + i, XS_NEPI);
       mbar_init(bar_tf + i, 1);
       mbar_init(bar_te + i, XS_NEPI);
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       }
     }
   } else if (warp < 2 + XS_NDW) {
-    // ---- column scales and field digits
+    // ---- field digits
     const int dw = warp - 2;
     uint32_t c = 0;
     int ii = 0;
@@ -369,35 +370,9 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       const int z0 = item_z0(item), nn = item_nn(item);
       int nkc_m, nrows, nmt_m;
       geom(nn, nkc_m, nrows, nmt_m);
-      const int kraw = MODE == 0 ? a.nr : nn;
-      int* cx = colexp + (ii & 1) * N;
+      const int* cx = colexp + (ii & 1) * N;
       if (!xs_wait_w(bar_rf, ii & 1, ok)) break;
-      // the column-scale slot of this item parity is free once the epilogue of item ii-2 has read it
-      if (ii >= 2 && !xs_wait_w(&bar_ce[ii & 1], ((ii - 2) >> 1) & 1, ok)) break;
-      // column scales: a warp per real column n (z = n/2, re/im = n&1), the largest exponent field of the
-      // staged FP64 samples (their high words) reduced by warp shuffles; |x| < 2^(field - 1022), and the
-      // forward folds may double
-      for (int n = dw; n < N; n += XS_NDW) {
-        const int zz = n >> 1;
-        unsigned mx = 0;
-        if (z0 + zz < a.nzdim) {
-          const unsigned* hw = (const unsigned*)(raw + (size_t)2 * zz * a.rawk + (n & 1)) + 1;
-          unsigned m1 = 0, m2 = 0, m3 = 0;
-          int i = lane;
-          // (the high words without their sign bits order like the magnitudes' exponent fields)
-          for (; i + 96 < kraw; i += 128) {
-            mx = max(mx, hw[4 * i] & 0x7FFFFFFFu);
-            m1 = max(m1, hw[4 * (i + 32)] & 0x7FFFFFFFu);
-            m2 = max(m2, hw[4 * (i + 64)] & 0x7FFFFFFFu);
-            m3 = max(m3, hw[4 * (i + 96)] & 0x7FFFFFFFu);
-          }
-          for (; i < kraw; i += 32) mx = max(mx, hw[4 * i] & 0x7FFFFFFFu);
-          mx = max(max(mx, m1), max(m2, m3)) >> 20;
-        }
-        mx = __reduce_max_sync(0xFFFFFFFFu, mx);
-        if (lane == 0) cx[n] = mx ? (int)mx - 1022 + (MODE == 0 ? 1 : 0) : -2000;
-      }
-      mbar_arrive(&bar_cx[ii & 1]);
+      // the item's column scales, written by the epilogue warps two items ahead
       if (!xs_wait_w(&bar_cx[ii & 1], (ii >> 1) & 1, ok)) break;
       for (int mt = 0; mt < nmt_m && ok; ++mt) {
         for (int kc = 0; kc < nkc_m; ++kc, ++c) {
@@ -457,6 +432,43 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
     // integer pipe, and T 2^(EA + EB + esh - w (NO+1)) is then rounded once to FP64
     const int ew = warp - 2 - XS_NDW, lq = warp & 3, ch = ew >> 2;
     const uint32_t lrow = (uint32_t)(lq * 32) << 16;
+    // The column scales of an item, into its slot of colexp: a warp per complex column z, its lanes over
+    // the column's samples (read from global memory through L2, before the item's own bulk copy), the
+    // largest exponent fields of the re and im parts (the high words without their sign bits order like
+    // the magnitudes' exponent fields) reduced by warp shuffles; |x| < 2^(field - 1022), and the
+    // forward folds may double.  The epilogue warps compute them two items ahead, in the time between
+    // their last stores of one item and the accumulators of the next, so that the digit warps find them
+    // ready when the item's columns land.
+    auto col_scales = [&](int item, int slot) {
+      const int m = item_m(item), z0 = item_z0(item);
+      const int kraw = MODE == 0 ? a.nr : item_nn(item);
+      const double2* fin = xs_sel(a.in, item % a.nf);
+      int* cxw = colexp + slot * N;
+      for (int zz = ew; zz < NZ; zz += XS_NEW) {
+        unsigned mr = 0, mi = 0;
+        if (z0 + zz < a.nzdim) {
+          const double2* col = fin + (size_t)a.nrdim * (m + (size_t)a.npdim * (z0 + zz));
+#pragma unroll 4
+          for (int i = lane; i < kraw; i += 32) {
+            const double2 v = __ldcg(col + i);
+            mr = max(mr, (unsigned)__double2hiint(v.x) & 0x7FFFFFFFu);
+            mi = max(mi, (unsigned)__double2hiint(v.y) & 0x7FFFFFFFu);
+          }
+        }
+        mr = __reduce_max_sync(0xFFFFFFFFu, mr >> 20);
+        mi = __reduce_max_sync(0xFFFFFFFFu, mi >> 20);
+        if (lane == 0) {
+          cxw[2 * zz] = mr ? (int)mr - 1022 + (MODE == 0 ? 1 : 0) : -2000;
+          cxw[2 * zz + 1] = mi ? (int)mi - 1022 + (MODE == 0 ? 1 : 0) : -2000;
+        }
+      }
+      mbar_arrive(&bar_cx[slot]);
+    };
+    if (first < nitems) {
+      col_scales(first, 0);
+      const int second = next_item(first);
+      if (second < nitems) col_scales(second, 1);
+    }
     uint32_t u = 0;
     int ii = 0;
     for (int item = first; item < nitems && ok; item = next_item(item), ++ii) {
@@ -466,7 +478,7 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
       int nkc_m, nrows, nmt_m;
       geom(nn, nkc_m, nrows, nmt_m);
       const int* cx = colexp + (ii & 1) * N;
-      // the item's column scales (this slot cannot move on to item ii+2 before this epilogue has read it)
+      // the item's column scales (written into this slot by all epilogue warps)
       if (!xs_wait_w(&bar_cx[ii & 1], (ii >> 1) & 1, ok)) break;
       for (int mt = 0; mt < nmt_m && ok; ++mt, ++u) {
         const int row = mt * 128 + lq * 32 + lane;
@@ -487,8 +499,8 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
         const uint32_t tacc = tmem + tb * (uint32_t)ACC;
         constexpr int eo = ESH - W * (NO + 1);
         // the warp's columns eight at a time; after the last group's loads the accumulators are free for
-        // the next unit's MMAs (and, after the item's last unit, the column scales for item ii+2), so the
-        // last group's conversions and stores overlap them
+        // the next unit's MMAs (and, after the item's last unit, this thread is done with the item's
+        // column scales), so the last group's conversions and stores overlap them
 #pragma unroll 1
         for (int q = 0; q < CPW; ++q) {
           const int cb = ch * (N / 2) + q * 8;
@@ -575,6 +587,9 @@ __global__ void __launch_bounds__(XS_THREADS, 1) k_xs_rtrans(XsArgs a) {
           }
         }
       }
+      // the scales of item ii+2 into this item's slot, once every epilogue thread has read it
+      const int ahead = next_item(next_item(item));
+      if (ok && ahead < nitems && xs_wait_w(&bar_ce[ii & 1], (ii >> 1) & 1, ok)) col_scales(ahead, ii & 1);
     }
   }
   if (!ok) atomicExch(a.status, 2);
