@@ -38,7 +38,7 @@ PERT = 1.0e-4
 METRIC = "steps/s @192x128x128 (3-D vortex NS step, mixed precision on GPU)"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the step's largest kernels, from
 # one ncu capture of `bench.py --profile-run` at this workload (profiles/)
-NCU_TRAFFIC = {"k_band_subst<2>": 105.8e6, "k_band_subst<1>": 93.6e6, "k_xs_rtrans<1, 6, 16>": 85.5e6}
+NCU_TRAFFIC = {"k_band_subst<2>": 104.9e6, "k_band_subst<1>": 93.5e6, "k_xs_rtrans<1, 6, 16>": 85.8e6}
 
 
 def workload_params():
@@ -365,7 +365,7 @@ def run_ours(args, rank, world, local, pg):
                           "traffic": NCU_TRAFFIC["k_xs_rtrans<1, 6, 16>"] * r_fields / 3.0,
                           "traffic_per_kernel": {"k_xs_rtrans<1, 6, 16> (3 fields)": NCU_TRAFFIC["k_xs_rtrans<1, 6, 16>"]},
                           "limit": "integer work of the digit cuts and the order sums between mbarrier hand-offs "
-                                   "(ALU pipe 38%, tensor pipe 16%, issue 39% active; ncu)"}}
+                                   "(ALU pipe 39%, tensor pipe 15%, issue 39% active; ncu)"}}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
             "frac": achieved_gbs / hbm, "traffic": ncu.get(dom, {}).get("traffic"),
             "avg_launch_us": 1e3 * avg_ms, "launches_per_step": d_n / 2,
