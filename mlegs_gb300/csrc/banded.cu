@@ -277,7 +277,7 @@ int launch_abcn_rhs(Scalar& s, const Scalar& nl, const Scalar& nl_p, double dt, 
 // dst = scale * band(src), out of place: the same values as copying src to dst, applying the band
 // operator in place and multiplying dst by scale (dst%ln = 0), in one pass over every column
 template <typename T>
-__global__ void k_band_apply_to(double2* __restrict__ dst, const double2* __restrict__ src, const double* __restrict__ lnsrc,
+__global__ void __launch_bounds__(128, 16) k_band_apply_to(double2* __restrict__ dst, const double2* __restrict__ src, const double* __restrict__ lnsrc,
                                 double* __restrict__ lndst, BandTabs tb, const double* __restrict__ lognorm, int op,
                                 int nrdim, int npdim, int ne, int nrc, int npc, int nzc, int nzcu, int nzdim, double ell,
                                 double scale, int smode, PostChop pc) {
@@ -452,7 +452,7 @@ __device__ __forceinline__ void uv_col(double2* __restrict__ ur, double2* __rest
 }
 
 template <typename T>
-__global__ void k_tp2vec_uv(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
+__global__ void __launch_bounds__(128, 12) k_tp2vec_uv(double2* __restrict__ ur, double2* __restrict__ up, const double2* __restrict__ psi,
                             const double2* __restrict__ chi, const double* __restrict__ lnpsi,
                             const double* __restrict__ lnchi, double* __restrict__ lnur, double* __restrict__ lnup,
                             BandTabs tb, const double* __restrict__ lognorm, int nrdim, int npdim, int ne, int nrc,

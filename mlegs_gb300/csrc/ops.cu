@@ -287,7 +287,7 @@ __device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, doubl
 }
 // per block: the energy of the head and of the tail (q >= cutoff) of the spectrum (:112-117).  The q
 // are in [0, 1], so q >= cutoff is compared on the FP64 bit patterns; the sums stay FP64.
-__global__ void __launch_bounds__(256) k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim,
+__global__ void __launch_bounds__(256, 8) k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim,
                                                   const double* __restrict__ qt, unsigned long long cbits,
                                                   double* __restrict__ partial) {
   // a warp per column (m, k), its lanes over the rows; |e|^2 summed in FP64 into the head (q below the
