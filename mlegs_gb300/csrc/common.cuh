@@ -109,7 +109,7 @@ struct Ctx {
 extern Ctx G;
 
 // indices into G.dscal
-enum { DS_SUM0 = 0, DS_SUM1 = 1, DS_GAIN0 = 4, DS_GAIN1 = 5, DS_FLAG = 8, DS_CALC = 16, DS_COUNT = 16 + 2 * 4096 };
+enum { DS_SUM0 = 0, DS_SUM1 = 1, DS_GAIN0 = 4, DS_GAIN1 = 5, DS_FLAG = 8, DS_CALC = 16, DS_COUNT = 16 + 3 * 4096 };
 
 // device memory accounting
 int dmalloc(void** p, size_t bytes);

@@ -287,9 +287,12 @@ __device__ __forceinline__ double svv_qz(int k, const double* ak, int nak, doubl
 }
 // per block: the energy of the head and of the tail (q >= cutoff) of the spectrum (:112-117).  The q
 // are in [0, 1], so q >= cutoff is compared on the FP64 bit patterns; the sums stay FP64.
-__global__ void __launch_bounds__(256, 8) k_svv_sums(const double2* __restrict__ e, int nrdim, int npdim, int nzdim,
-                                                  const double* __restrict__ qt, unsigned long long cbits,
-                                                  double* __restrict__ partial) {
+// blockIdx.y = field (e0, e1: the two fields of a paired call, or one field twice with gridDim.y = 1)
+__global__ void __launch_bounds__(256, 8) k_svv_sums(const double2* __restrict__ e0, const double2* __restrict__ e1,
+                                                  int nrdim, int npdim, int nzdim, const double* __restrict__ qt,
+                                                  unsigned long long cbits, double* __restrict__ partial) {
+  const double2* __restrict__ e = blockIdx.y ? e1 : e0;
+  partial += (size_t)blockIdx.y * 2 * gridDim.x;
   // a warp per column (m, k), its lanes over the rows; |e|^2 summed in FP64 into the head (q below the
   // cutoff) and the tail.  q of a row rises with the row (svv_qr), so the rows below the cutoff are
   // the first nc: a column whose m or k is at or above the cutoff goes to the tail whole, any other
@@ -336,10 +339,15 @@ __global__ void __launch_bounds__(256, 8) k_svv_sums(const double2* __restrict__
 // partial sums (a tree over its threads) and fills its share of the tables; block 0 stores the
 // strength in st[0] and the new gain in st[1] (copied to the gain by k_svv_apply: no block may see
 // a half-updated gain)
+// blockIdx.y = field: its partial sums, gain, st pair and factor tables
 __global__ void k_svv_gain(const double* __restrict__ partial, int nb, const double* __restrict__ gain,
                            double* __restrict__ st, double target, double relax, double strength_max,
                            double* __restrict__ ft, int nrdim, int npdim, int nzdim, int nrchop, int np, double kmax,
                            const double* __restrict__ ak, double cutoff) {
+  partial += (size_t)blockIdx.y * 2 * nb;
+  gain += blockIdx.y;
+  st += 2 * blockIdx.y;
+  ft += (size_t)blockIdx.y * (nrdim + npdim + nzdim);
   __shared__ double r0[256], r1[256];
   __shared__ double str;
   double h = 0, t = 0;
@@ -387,8 +395,13 @@ __global__ void k_svv_qtab(double* __restrict__ qt, int nrdim, int npdim, int nz
     qt[t] = (t < nrdim) ? svv_qr(t, nrchop) : (t < nrdim + npdim) ? svv_qp(t - nrdim, np)
                                                                  : svv_qz(t - nrdim - npdim, ak, nzdim, kmax);
 }
-__global__ void k_svv_apply(double2* __restrict__ e, int nrdim, int npdim, int nzdim, const double* __restrict__ st,
-                            const double* __restrict__ ft, double* __restrict__ gain) {
+// blockIdx.y = field, as in k_svv_gain
+__global__ void k_svv_apply(double2* __restrict__ e0, double2* __restrict__ e1, int nrdim, int npdim, int nzdim,
+                            const double* __restrict__ st, const double* __restrict__ ft, double* __restrict__ gain) {
+  double2* __restrict__ e = blockIdx.y ? e1 : e0;
+  st += 2 * blockIdx.y;
+  ft += (size_t)blockIdx.y * (nrdim + npdim + nzdim);
+  gain += blockIdx.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) *gain = st[1];
   if (st[0] <= 0.0) return;
   size_t n = (size_t)nrdim * npdim * nzdim;
@@ -691,9 +704,12 @@ int op_dealias2(Scalar& a, Scalar& b) {
 }
 
 // svv_filter with the gain kept in device memory (gain_dev)
-int op_svv_filter_dev(Scalar& s, double* gain_dev) {
+// svv_filter (:72-155) of one field, or of two with their own gains in one set of launches (the psi and
+// chi filters of a vortex step: gain_dev[0] and gain_dev[1]); the results are those of separate calls
+static int svv_filter_fields(Scalar* const* f, int nf, double* gain_dev) {
   if (!G.P.is_svv) return 0;
-  if (!s.is("FFF")) return set_error(MLG_ESPACE, "svv_filter: scalar must be in FFF space");
+  for (int i = 0; i < nf; ++i)
+    if (!f[i]->is("FFF")) return set_error(MLG_ESPACE, "svv_filter: scalar must be in FFF space");
   double cutoff = std::min(std::max(G.P.svv_cutoff, 0.0), 0.99);
   double target = std::max(G.P.svv_target, 1.0e-12);
   // kmax = max(maxval(abs(ak)), 1) over the kit's ak (mlegs_spectfm_init.f90:132-134)
@@ -705,12 +721,15 @@ int op_svv_filter_dev(Scalar& s, double* gain_dev) {
     for (double a : ak) kmax = std::max(kmax, std::fabs(a));
     kmax = std::max(kmax, 1.0);
   }
+  // scratch: the partial sums [field][NB][2], the factor tables [field][ntab], the q table [ntab]; the
+  // strength and new gain of field i at DS_SUM0 + 2 i
   const int NB = 304;
+  const int ntab = G.nrdim + G.npdim + G.nzdim;
   double* partial = G.dscal + DS_CALC + 2 * 2048;
-  double* ft = G.dscal + DS_CALC + 2 * 2048 + 2 * NB;
-  if (2 * (G.nrdim + G.npdim + G.nzdim) > DS_COUNT - (DS_CALC + 2 * 2048 + 2 * NB))
+  double* ft = partial + 2 * 2 * NB;
+  double* qt = ft + 2 * ntab;
+  if (DS_CALC + 2 * 2048 + 4 * NB + 3 * ntab > DS_COUNT)
     return set_error(MLG_ESIZE, "svv_filter: grid too large for the filter tables");
-  double* qt = ft + (G.nrdim + G.npdim + G.nzdim);
   if (!G.svv_q_ready) {
     k_svv_qtab<<<1, 256, 0, G.stream>>>(qt, G.nrdim, G.npdim, G.nzdim, G.nrchop, G.np, kmax, G.ak);
     MLG_LAUNCH();
@@ -718,16 +737,26 @@ int op_svv_filter_dev(Scalar& s, double* gain_dev) {
   }
   unsigned long long cbits = 0;
   std::memcpy(&cbits, &cutoff, sizeof(cbits));
-  k_svv_sums<<<NB, 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, qt, cbits, partial);
+  double2* e0 = f[0]->e;
+  double2* e1 = f[nf - 1]->e;
+  k_svv_sums<<<dim3(NB, nf), 256, 0, G.stream>>>(e0, e1, G.nrdim, G.npdim, G.nzdim, qt, cbits, partial);
   MLG_LAUNCH();
-  const int ntab = G.nrdim + G.npdim + G.nzdim;
-  k_svv_gain<<<std::max(1, std::min(8, cdiv(ntab, 64))), 256, 0, G.stream>>>(
+  k_svv_gain<<<dim3(std::max(1, std::min(8, cdiv(ntab, 64))), nf), 256, 0, G.stream>>>(
       partial, NB, gain_dev, G.dscal + DS_SUM0, target, G.P.svv_relax, G.P.svv_strength, ft, G.nrdim, G.npdim, G.nzdim,
       G.nrchop, G.np, kmax, G.ak, cutoff);
   MLG_LAUNCH();
-  k_svv_apply<<<nblk(G.fsize), 256, 0, G.stream>>>(s.e, G.nrdim, G.npdim, G.nzdim, G.dscal + DS_SUM0, ft, gain_dev);
+  k_svv_apply<<<dim3(nblk(G.fsize), nf), 256, 0, G.stream>>>(e0, e1, G.nrdim, G.npdim, G.nzdim, G.dscal + DS_SUM0, ft,
+                                                              gain_dev);
   MLG_LAUNCH();
   return 0;
+}
+int op_svv_filter_dev(Scalar& s, double* gain_dev) {
+  Scalar* f[1] = {&s};
+  return svv_filter_fields(f, 1, gain_dev);
+}
+int op_svv_filter2_dev(Scalar& a, Scalar& b, double* gains_dev) {
+  Scalar* f[2] = {&a, &b};
+  return svv_filter_fields(f, 2, gains_dev);
 }
 
 // calcat0/1 into dscal[DS_CALC..] (device), optionally zeroat1
@@ -1009,7 +1038,9 @@ static int vecprod_bg(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, cons
   k_vecprod<<<nblk(G.fsize), 256, 0, G.stream>>>(vr.e, vp.e, vz.e, ur.e, up.e, uz.e, vzb ? vzb->e : nullptr, o[0]->e,
                                                  o[1]->e, o[2]->e, G.nr, G.np / 2, G.nrdim, G.npdim, G.nzdim);
   MLG_LAUNCH();
-  for (Scalar* q : o) { MLG_TRY(launch_set_ln(q->ln, 0.0)); q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
+  double* lns[3] = {o[0]->ln, o[1]->ln, o[2]->ln};
+  MLG_TRY(launch_set_ln_n(lns, 3, 0.0));
+  for (Scalar* q : o) { q->set_space("PPP"); q->off[0] = q->off[1] = q->off[2] = 0; }
   return 0;
 }
 int op_vecprod(Scalar& vr, Scalar& vp, Scalar& vz, const Scalar& ur, const Scalar& up, const Scalar& uz) {
@@ -1184,7 +1215,7 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
   // nlpsi and nlchi are recomputed in full by the advection below
   MLG_TRY(op_abcn_pair(psi, psip, nlpsi, nlpsip, chi, chip, nlchi, nlchip, dt, true, write_prev));
   MLG_TRY(op_dealias2(psi, chi));
-  MLG_TRY(op_svv_filter_dev(psi, gains_dev)); MLG_TRY(op_svv_filter_dev(chi, gains_dev + 1));
+  MLG_TRY(op_svv_filter2_dev(psi, chi, gains_dev));
   MLG_TRY(op_zeroat1_2(psi, chi));
   // advection_rhs's own dealias of psi and chi (vortical_flow_3d.f90:368) finds them dealiased
   // already: the SVV gain and zeroat1 leave a zero coefficient zero, so it is skipped here
