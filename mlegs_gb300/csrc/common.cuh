@@ -104,6 +104,7 @@ struct Ctx {
   // side stream for work that runs beside the work stream (the mixed form's m = 0 plane), forked and
   // joined with events so that callers only ever see the work stream
   cudaStream_t side = nullptr;
+  cudaStream_t cap = nullptr;   // the stream a vortex run's interior step is captured on (a CUDA graph)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 extern Ctx G;

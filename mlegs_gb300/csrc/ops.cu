@@ -1287,10 +1287,10 @@ int mlg_finalize(void) {
   for (void* a : arrs) if (a) cudaFree(a);
   cudaStream_t st = G.stream;
   cudaEvent_t e0 = G.ev0, e1 = G.ev1, ef = G.ev_fork, ej = G.ev_join;
-  cudaStream_t side = G.side;
+  cudaStream_t side = G.side, cap = G.cap;
   G = Ctx();
   G.stream = st;
-  G.ev0 = e0; G.ev1 = e1; G.ev_fork = ef; G.ev_join = ej; G.side = side;
+  G.ev0 = e0; G.ev1 = e1; G.ev_fork = ef; G.ev_join = ej; G.side = side; G.cap = cap;
   return 0;
 }
 
@@ -1495,9 +1495,58 @@ static int vortex_loop(mlg_scalar a, mlg_scalar b, mlg_scalar c, mlg_scalar d, m
   double* gd = G.dscal + DS_GAIN0;
   MLG_CUDA(cudaMemcpyAsync(gd, gains, 2 * sizeof(double), cudaMemcpyHostToDevice, G.stream));
   MLG_CUDA(cudaMemsetAsync(G.dscal + DS_FLAG, 0, sizeof(double), G.stream));
-  for (int t = 0; t < nsteps; ++t)   // psip and chip are read by no step: written by the last
-    MLG_TRY(op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd, nullptr,
-                               t == nsteps - 1));
+  auto step = [&](bool last) {   // psip and chip are read by no step: written by the last
+    return op_vortex_step_dev(*S(a), *S(b), *S(c), *S(d), *S(e), *S(f), *S(g), *S(h), *S(u), dt, gd, nullptr, last);
+  };
+  cudaGraphExec_t gexec = nullptr;
+  if (nsteps >= 4 && !G.kt.on) {
+    // The interior steps replay one CUDA graph of two steps: the first step runs as launched (it fills
+    // the factor, table and buffer caches, so that the captured steps allocate nothing), the next two
+    // are captured on a stream of the library's own (capture cannot run on the legacy default stream),
+    // and the graph then runs them in pairs; an odd interior step and the last step (which writes psip
+    // and chip) run as launched.  A step hands nlpsi's and nlchi's buffers to nlpsi_p and nlchi_p, so
+    // two steps leave every field in its own buffer again: a replay of the pair is the two steps
+    // themselves, on the same buffers.
+    MLG_TRY(step(false));
+    if (!G.cap) MLG_CUDA(cudaStreamCreateWithFlags(&G.cap, cudaStreamNonBlocking));
+    const cudaStream_t orig = G.stream;
+    const long long l0 = G.launches;
+    G.stream = G.cap;
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(G.cap, cudaStreamCaptureModeRelaxed);
+    int rc = ce == cudaSuccess ? step(false) : 0;
+    if (ce == cudaSuccess && rc == 0) rc = step(false);
+    if (ce == cudaSuccess) ce = cudaStreamEndCapture(G.cap, &graph);
+    G.stream = orig;
+    const long long nl = G.launches - l0;
+    G.launches = l0;
+    if (rc == 0 && ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) return rc;
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MLG_ECUDA, std::string("vortex run: graph capture: ") + cudaGetErrorString(ce));
+    }
+    const int interior = nsteps - 2;
+    for (int t = 0; t + 1 < interior; t += 2) {
+      ce = cudaGraphLaunch(gexec, G.stream);
+      if (ce != cudaSuccess) break;
+      G.launches += nl;
+    }
+    if (ce == cudaSuccess) {
+      int rc2 = (interior & 1) ? step(false) : 0;
+      if (rc2 == 0) rc2 = step(true);
+      if (rc2) { cudaStreamSynchronize(G.stream); cudaGraphExecDestroy(gexec); return rc2; }
+    }
+    cudaStreamSynchronize(G.stream);
+    cudaGraphExecDestroy(gexec);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MLG_ECUDA, std::string("vortex run: graph launch: ") + cudaGetErrorString(ce));
+    }
+  } else {
+    for (int t = 0; t < nsteps; ++t) MLG_TRY(step(t == nsteps - 1));
+  }
   MLG_CUDA(cudaMemcpyAsync(gains, gd, 2 * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
   int w[4] = {0, 0, 0, 0};   // DS_FLAG: non-finite flag, unused; DS_FLAG + 1: singular-LU flag, timeout flag
   MLG_CUDA(cudaMemcpyAsync(w, G.dscal + DS_FLAG, sizeof(w), cudaMemcpyDeviceToHost, G.stream));
