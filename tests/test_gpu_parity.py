@@ -308,10 +308,13 @@ def test_mixed_vortex_steps_within_1e6_of_fp64():
         assert abs(a[1] - b[1]) <= 1e-6 * max(1.0, abs(b[1])), f"mixed {n} ln: {a[1]} vs {b[1]}"
 
 
-def test_vortex_run_equals_single_steps():
-    """A run of 5 steps leaves the same bytes in all eight fields as 5 single-step calls, in both
-    forms: a run writes psi_p and chi_p on its last step only, and nlpsi_p and nlchi_p take the
-    buffers of nlpsi and nlchi each step, which the step's advection then recomputes."""
+@pytest.mark.parametrize("nsteps", [4, 5])
+def test_vortex_run_equals_single_steps(nsteps):
+    """A run of nsteps steps leaves the same bytes in all eight fields as nsteps single-step calls, in
+    both forms: a run writes psi_p and chi_p on its last step only, and nlpsi_p and nlchi_p take the
+    buffers of nlpsi and nlchi each step, which the step's advection then recomputes.  A run of four or
+    more steps replays its interior steps as a captured graph of two steps (4: one pair; 5: one pair
+    and one step as launched)."""
     from mlegs_gb300 import vortex
     from mlegs_gb300.kit import Kit, MIXED, PLAIN_FP64
     from mlegs_gb300.params import make_params
@@ -332,16 +335,16 @@ def test_vortex_run_equals_single_steps():
                 getattr(st, n).set(e, ln, sp)
             st.gains = [0.0, 0.0]
             if run:
-                k.vortex_run(*st.args(), 1e-3, 5, st.gains)
+                k.vortex_run(*st.args(), 1e-3, nsteps, st.gains)
             else:
-                for _ in range(5):
+                for _ in range(nsteps):
                     vortex.step(k, st, 1e-3)
             out.append(({n: getattr(st, n).get() for n in names}, list(st.gains)))
         (a, ga), (b, gb) = out
         assert ga == gb, f"form {mode}: gains {ga} vs {gb}"
         for n in names:
             assert np.array_equal(a[n][0], b[n][0]) and a[n][1] == b[n][1] and a[n][2] == b[n][2], \
-                f"form {mode}: {n} of a 5-step run differs from 5 single steps"
+                f"form {mode}: {n} of a {nsteps}-step run differs from {nsteps} single steps"
     k.close()
 
 
