@@ -199,6 +199,8 @@ __global__ void __launch_bounds__(XV_THREADS, 1) k_xv_contract(XvArgs a) {
       if (z < a.nzdim) {
         const size_t cb = (size_t)a.nrdim * (m + (size_t)a.npdim * z);
         auto ex = [](double v) { return ((unsigned)__double2hiint(v) >> 20) & 0x7FFu; };
+        // unrolled, so that the loads of several rows are in flight at once (the scan waits on them)
+#pragma unroll 6
         for (int i = lane; i < a.nr; i += 32) {
           const double2 r = a.ur[cb + i], pq = a.up[cb + i], q = a.uz[cb + i];
           e0 = max(e0, max(ex(r.y), ex(pq.x)));
