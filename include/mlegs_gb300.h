@@ -168,7 +168,8 @@ int mlg_vortex_step(mlg_scalar psi, mlg_scalar chi, mlg_scalar nlpsi, mlg_scalar
  * (no host synchronisation inside the loop; gains copied back at the end).  The eight fields end
  * as after nsteps calls of mlg_vortex_step.  Both calls hand nlpsi's and nlchi's buffers to nlpsi_p
  * and nlchi_p each step (the step recomputes nlpsi and nlchi), so the device pointers of those four
- * scalars change; a run writes psi_p and chi_p on its last step only. */
+ * scalars change; a run writes psi_p and chi_p on its last step only.  With nsteps >= 4 the interior
+ * steps replay a CUDA graph of two steps (same kernels, same buffers, same bytes). */
 int mlg_vortex_run(mlg_scalar psi, mlg_scalar chi, mlg_scalar nlpsi, mlg_scalar nlchi,
                    mlg_scalar psi_p, mlg_scalar chi_p, mlg_scalar nlpsi_p, mlg_scalar nlchi_p,
                    mlg_scalar uz, double dt, int nsteps, double* gains);
