@@ -170,7 +170,7 @@ void xv_free();
 int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd* chi, int nrc_off);
 // zeros to the rows of a mixed-form contraction's output that its kernels leave unwritten (radial.cu)
 int launch_zero_tails(cd* out, int mode, int nrc, int npc, int nzc, int nzcu);
-int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu);
+int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu, cudaStream_t st = nullptr);
 
 // pointwise
 int launch_zero(cd* e);

@@ -594,11 +594,12 @@ __global__ void k_zero_tails(double2* __restrict__ out0, double2* __restrict__ o
   }
 }
 
-// the tails of n <= 3 outputs with the same chop in one launch
-int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu) {
+// the tails of n <= 3 outputs with the same chop in one launch (on G.stream, or on the side stream
+// beside the contraction that writes the other rows)
+int launch_zero_tails_n(cd* const* out, int n, int mode, int nrc, int npc, int nzc, int nzcu, cudaStream_t st) {
   if (n < 1 || n > 3) return set_error(MLG_EPARAM, "zero_tails: one to three fields per launch");
   const size_t ncols = (size_t)G.npdim * G.nzdim * n;
-  k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, G.stream>>>(
+  k_zero_tails<<<(int)std::min<size_t>(cdiv(ncols, 8), 152 * 8), 256, 0, st ? st : G.stream>>>(
       out[0], n > 1 ? out[1] : out[0], n > 2 ? out[2] : out[0], n, mode, G.nr, G.nrdim, G.npdim, G.nzdim, nrc, npc, nzc, nzcu);
   MLG_LAUNCH();
   return 0;
@@ -634,18 +635,22 @@ int launch_rtrans_fwd(Scalar& s) {
   const bool mixed = G.precision == MLG_MIXED;
   const bool xs = xs_supported(0, nrc, !mixed);   // exact-slice tensor-core contraction (xs_radial.cu)
   // the tensor-core contractions write rows < nn(m) of every column m < npc: only the rest needs zeros
-  if (xs) {
+  // (beside them, below)
+  if (xs && npc < 1) {
     MLG_TRY(launch_zero_tails(out, 0, nrc, npc, G.nzdim, G.nzdim + 1));
-  } else {
+  } else if (!xs) {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RFWD);
   if (npc > 0) {
     if (xs) {
       // m = 0 (the axisymmetric mean flow, whose large range within a column the fixed-point slices
-      // would cut relative to its maximum) beside, in double-float (mixed) or FP64 (plain); m >= 1 as
-      // exact slices, 42-bit (mixed) or FP64-grade (plain)
+      // would cut relative to its maximum) beside, in double-float (mixed) or FP64 (plain), after the
+      // zeros of the rows that no contraction writes; m >= 1 as exact slices, 42-bit (mixed) or
+      // FP64-grade (plain)
       MLG_TRY(side_fork());
+      cd* o1[1] = {out};
+      MLG_TRY(launch_zero_tails_n(o1, 1, 0, nrc, npc, G.nzdim, G.nzdim + 1, G.side));
       MLG_TRY(plane_fwd(s.e, out, nrc, G.side));
       MLG_TRY(xs_rtrans(0, s.e, out, nrc, npc, 1, nullptr, false, !mixed));
       MLG_TRY(side_join());
@@ -668,17 +673,20 @@ int launch_rtrans_bwd(Scalar& s, bool add_ln) {
   const bool mixed = G.precision == MLG_MIXED;
   const bool xs = xs_supported(1, nrc, !mixed);
   // the tensor-core contractions write rows < nr of every column m < npc with nn(m) > 0 (the m = 0
-  // plane included): only the rest needs zeros
-  if (xs) {
+  // plane included): only the rest needs zeros (beside them, below)
+  if (xs && npc < 1) {
     MLG_TRY(launch_zero_tails(out, 1, nrc, npc, G.nzdim, G.nzdim + 1));
-  } else {
+  } else if (!xs) {
     MLG_CUDA(cudaMemsetAsync(out, 0, G.fsize * sizeof(cd), G.stream));
   }
   kt_begin(KT_RBWD);
   if (npc > 0) {
     if (xs) {
-      // m = 0 beside in double-float (mixed) or FP64 DFMA (plain); m >= 1 as exact slices
+      // m = 0 beside in double-float (mixed) or FP64 DFMA (plain), after the zeros; m >= 1 as exact
+      // slices
       MLG_TRY(side_fork());
+      cd* o1[1] = {out};
+      MLG_TRY(launch_zero_tails_n(o1, 1, 1, nrc, npc, G.nzdim, G.nzdim + 1, G.side));
       MLG_TRY(plane_bwd(&s.e, &out, &s.ln, 1, nrc, add_ln, G.side));
       MLG_TRY(xs_rtrans(1, s.e, out, nrc, npc, 1, s.ln, add_ln, !mixed));
       MLG_TRY(side_join());
@@ -723,9 +731,10 @@ int launch_rtrans_fwd_multi(Scalar* const* f, int n) {
     }
     in[i] = f[i]->e;
   }
-  MLG_TRY(launch_zero_tails_n(out, n, 0, nrc, npc, G.nzdim, G.nzdim + 1));
   kt_begin(KT_RFWD);
   MLG_TRY(side_fork());
+  // beside the m >= 1 contraction: the rows it does not write (zero), then the m = 0 planes
+  MLG_TRY(launch_zero_tails_n(out, n, 0, nrc, npc, G.nzdim, G.nzdim + 1, G.side));
   for (int i = 0; i < n; ++i) MLG_TRY(plane_fwd(in[i], out[i], nrc, G.side));   // m = 0 beside
   MLG_TRY(xs_rtrans_multi(0, in, out, n, nrc, npc, 1, nullptr, false, !mixed));   // m >= 1, all fields
   MLG_TRY(side_join());
@@ -769,10 +778,11 @@ int launch_rtrans_bwd_multi(Scalar* const* f, int n, bool add_ln) {
     in[i] = f[i]->e;
     lnp[i] = f[i]->ln;
   }
-  MLG_TRY(launch_zero_tails_n(out, n, 1, nrc, npc, G.nzdim, G.nzdim + 1));
   kt_begin(KT_RBWD);
   MLG_TRY(side_fork());
-  // the m = 0 planes of all fields beside, in one launch: double-float (mixed) or FP64 DFMA (plain)
+  // beside the m >= 1 contraction: the rows it does not write (zero), then the m = 0 planes of all
+  // fields in one launch: double-float (mixed) or FP64 DFMA (plain)
+  MLG_TRY(launch_zero_tails_n(out, n, 1, nrc, npc, G.nzdim, G.nzdim + 1, G.side));
   MLG_TRY(plane_bwd(in, out, lnp, n, nrc, add_ln, G.side));
   MLG_TRY(xs_rtrans_multi(1, in, out, n, nrc, npc, 1, lnp, add_ln, !mixed));   // m >= 1, all fields
   MLG_TRY(side_join());
@@ -796,10 +806,8 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   // hold 1e-12 there)
   const bool xv = mixed && xv_supported();
   // the tensor-core contractions write rows < nn(m) of the kept columns: only the rest needs zeros
-  if (xv) {
-    cd* pc[2] = {psi, chi};
-    MLG_TRY(launch_zero_tails_n(pc, 2, 0, nrc, npc, nzc, nzcu));
-  } else {
+  // (beside them, below)
+  if (!xv) {
     MLG_CUDA(cudaMemsetAsync(psi, 0, G.fsize * sizeof(cd), G.stream));
     MLG_CUDA(cudaMemsetAsync(chi, 0, G.fsize * sizeof(cd), G.stream));
   }
@@ -808,8 +816,10 @@ int launch_vec2tp_contract(const cd* ur, const cd* up, const cd* uz, cd* psi, cd
   int tt = cdiv((nrc + 1) / 2, MT);
   dim3 grid(cdiv(G.nzdim, ZT), 2 * tt, npc), blk(ZT / ZPT, MT);
   if (xv) {
-    // m >= 1 on the tensor cores as exact slices, m = 0 in double-float beside it
+    // m >= 1 on the tensor cores as exact slices, m = 0 in double-float beside it (after the zeros)
     MLG_TRY(side_fork());
+    cd* pc[2] = {psi, chi};
+    MLG_TRY(launch_zero_tails_n(pc, 2, 0, nrc, npc, nzc, nzcu, G.side));
     constexpr int DMT = 16, DZT = 8, DKC = 8, DKS = 4;
     dim3 dgrid(cdiv(G.nzdim, DZT), 2 * cdiv((nrc + 1) / 2, DMT), 1), dblk(DZT, DMT, DKS);
     k_vec2tp_plane<dfl, DMT, DZT, DKC, DKS><<<dgrid, dblk, 0, G.side>>>(ur, up, uz, psi, chi, G.tD, G.tT, G.ak, G.nr, G.nrh,
