@@ -113,12 +113,14 @@ int launch_ihelmp_pre(Scalar& s, const ChopIdx& c, int power, double alpha, doub
 struct MaskSet {
   double2* e[6];
   int n;
+  double* lnz[2];   // ln slots set to zero by the launch (or null): a field's ln reset folded into its mask
 };
 __global__ void __launch_bounds__(256) k_mask(MaskSet fs, int nrdim, int npdim, int nzdim, int chop, int dealias, int f0,
                                               int f1, int f2, int nrc, int npc, int nzc, int nzcu, int pcut, int zcut,
                                               int zupper, int np_gt1, int nz_gt1) {
   const int cf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   const int ncols = npdim * nzdim;
+  if (blockIdx.x == 0 && threadIdx.x < 2 && fs.lnz[threadIdx.x]) *fs.lnz[threadIdx.x] = 0.0;
   if (cf >= fs.n * ncols) return;
   const int f = cf / ncols, col = cf - f * ncols;
   double2* e = fs.e[0];
@@ -228,13 +230,13 @@ __global__ void k_calcat(double2* __restrict__ e0, double2* __restrict__ e1, con
   }
 }
 
-// vec2tp: psi%ln = -0.5 * Re(calcat1(up)(1)) (:1366-1367), from the calcat output of k = 1
-__global__ void k_set_ln_from_calc(double* __restrict__ lnp, const double2* __restrict__ calc, double f) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *lnp = f * calc[0].x;
-}
-// up(:nr,1,1) += psi%ln * (1 + x) (:1371-1373)
-__global__ void k_add_ln_x(double2* __restrict__ e, const double* __restrict__ lnp, const double* __restrict__ x, int nr) {
-  double l = *lnp;
+// the projection's log-term bookkeeping in one launch: psi%ln = f Re(calcat1(up)(1)) with f = -1/2
+// (:1366-1367, from the calcat output of k = 1), up(:nr,1,1) += psi%ln (1 + x) (:1371-1373) and
+// chi%ln = 0 (:1331)
+__global__ void k_proj_ln(double2* __restrict__ e, const double2* __restrict__ calc, double f, double* __restrict__ psiln,
+                          double* __restrict__ chiln, const double* __restrict__ x, int nr) {
+  const double l = f * calc[0].x;
+  if (threadIdx.x == 0) { *psiln = l; *chiln = 0.0; }
   for (int i = threadIdx.x; i < nr; i += blockDim.x) e[i].x += l * (1.0 + x[i]);
 }
 
@@ -644,10 +646,13 @@ int op_trans(Scalar& s, const char* space) {
 }
 
 // chop and / or dealias of n <= 6 fields (the first field's chop window and space stand for all)
-static int mask_launch(Scalar* const* f, int n, bool chop, bool dealias, const ChopIdx& c) {
+static int mask_launch(Scalar* const* f, int n, bool chop, bool dealias, const ChopIdx& c, double* lnz0 = nullptr,
+                       double* lnz1 = nullptr) {
   MaskSet fs{};
   for (int i = 0; i < n; ++i) fs.e[i] = f[i]->e;
   fs.n = n;
+  fs.lnz[0] = lnz0;
+  fs.lnz[1] = lnz1;
   const Scalar& s = *f[0];
   int pcut = std::max(G.np / 3 + 1, 1), zcut = std::max(G.nz / 3 + 1, 1), zupper = G.nz - zcut + 2;
   k_mask<<<cdiv((long long)n * G.npdim * G.nzdim, 8), 256, 0, G.stream>>>(
@@ -701,6 +706,14 @@ int op_dealias(Scalar& s) {
 int op_dealias2(Scalar& a, Scalar& b) {
   Scalar* f[2] = {&a, &b};
   return op_mask_n(f, 2, false, true);
+}
+// a%ln = 0, b%ln = 0, then dealias(a), dealias(b): the ln resets ride on the mask launch
+static int op_zero_ln_dealias2(Scalar& a, Scalar& b) {
+  Scalar* f[2] = {&a, &b};
+  ChopIdx c{};
+  if (mask_batchable(f, 2, false, c)) return mask_launch(f, 2, false, true, c, a.ln, b.ln);
+  MLG_TRY(launch_set_ln2(a.ln, b.ln, 0.0));
+  return op_dealias2(a, b);
 }
 
 // svv_filter with the gain kept in device memory (gain_dev)
@@ -1079,15 +1092,12 @@ static int vec2tp_core(Scalar& ur, Scalar& up, Scalar& uz, Scalar& psi, Scalar& 
   up.set_space("FFF");
   uz.set_space("PFF");
   MLG_TRY(calcat_dev(up, G.at1, false));
-  k_set_ln_from_calc<<<1, 32, 0, G.stream>>>(psi.ln, (const double2*)(G.dscal + DS_CALC), -1.0 / 2.0);
-  MLG_LAUNCH();
-  MLG_TRY(launch_rtrans_bwd(up, false));
+  MLG_TRY(launch_rtrans_bwd(up, false));   // reads neither psi%ln nor the calcat1 values
   up.set_space("PFF");
-  k_add_ln_x<<<1, 256, 0, G.stream>>>(up.e, psi.ln, G.x, G.nr);
+  // psi%ln = -calcat1(up)/2, up(:nr,1,1) += psi%ln (1 + x), chi%ln = 0 (:1331) in one launch; psi%e = 0
+  // and chi%e = 0 (:1330-1331) are the zeros written by the contraction below
+  k_proj_ln<<<1, 256, 0, G.stream>>>(up.e, (const double2*)(G.dscal + DS_CALC), -1.0 / 2.0, psi.ln, chi.ln, G.x, G.nr);
   MLG_LAUNCH();
-  // psi%e = 0; chi%e = 0; chi%ln = 0 (:1330-1331), the zeros written by the contraction below;
-  // psi%ln was set above from calcat1
-  MLG_TRY(launch_set_ln(chi.ln, 0.0));
   MLG_TRY(launch_vec2tp_contract(ur.e, up.e, uz.e, psi.e, chi.e, 3));
   MLG_TRY(op_idel2(chi, false, 0.0));
   psi.off[0] = psi.off[1] = psi.off[2] = 0;
@@ -1202,8 +1212,7 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
   Scalar* prod[3] = {&vr_t, &vp_t, &vz_t};
   MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz, keep ? prod : nullptr));
   MLG_TRY(vec2tp_core(vr_t, vp_t, vz_t, nlpsi, nlchi));
-  MLG_TRY(launch_set_ln2(nlpsi.ln, nlchi.ln, 0.0));
-  MLG_TRY(op_dealias2(nlpsi, nlchi));
+  MLG_TRY(op_zero_ln_dealias2(nlpsi, nlchi));   // ln = 0, then dealias
   return 0;
 }
 
