@@ -490,7 +490,9 @@ int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& ch
   return 0;
 }
 
-int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale, PostChop pc) {
+int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale, PostChop pc,
+                         cudaStream_t st) {
+  if (!st) st = G.stream;
   if (c.npc > G.npchop) return set_error(MLG_ECHOP, "chop_index: chopping in p beyond the kit's azimuthal modes");
   const int smode = scale == 1.0 ? 0 : scale == -1.0 ? 1 : 2;   // identity, exact negation, FP64 product
   dim3 grid(G.nzdim, G.npdim);
@@ -498,12 +500,12 @@ int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& 
   kt_begin(KT_BAND);
   if (G.precision == MLG_MIXED) {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply_to<float><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
+    k_band_apply_to<float><<<grid, 128, sm, st>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                         G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
                                                         scale, smode, pc);
   } else {
     if (sm > 48 * 1024) MLG_CUDA(cudaFuncSetAttribute(k_band_apply_to<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_band_apply_to<double><<<grid, 128, sm, G.stream>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
+    k_band_apply_to<double><<<grid, 128, sm, st>>>(dst.e, src.e, src.ln, dst.ln, band_tabs(), G.lognorm, op,
                                                          G.nrdim, G.npdim, G.ne, c.nrc, c.npc, c.nzc, c.nzcu, G.nzdim, G.ell,
                                                          scale, smode, pc);
   }

@@ -250,7 +250,7 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
                        bool write_prev = true);
 int launch_band_apply(Scalar& s, int op, const ChopIdx& c);
 int launch_band_apply_to(Scalar& dst, const Scalar& src, int op, const ChopIdx& c, double scale,
-                         PostChop pc = PostChop{0, 0, 0, 0, 0});
+                         PostChop pc = PostChop{0, 0, 0, 0, 0}, cudaStream_t st = nullptr);
 int launch_tp2vec_uv(Scalar& ur, Scalar& up, const Scalar& psi, const Scalar& chi, const ChopIdx& c,
                      PostChop pc = PostChop{0, 0, 0, 0, 0});
 int launch_band_apply_T(Scalar& s, int op, const ChopIdx& c);

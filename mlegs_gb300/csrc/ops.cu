@@ -1130,8 +1130,12 @@ static int tp2vec_spec(const Scalar& psi, const Scalar& chi, Scalar& ur, Scalar&
   MLG_TRY(chop_index(ur, c));
   for (Scalar* q : {&ur, &up, &uz}) q->off[0] = 0;
   MLG_TRY(chop_index(ur, c0));   // the chop after the products (offsets 0), folded into their kernels
-  MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c, post_chop(c0)));       // r d/dr chi, r d/dr psi, their mix
-  MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0, post_chop(c0)));   // -del2h chi
+  // -del2h chi on the side stream beside r d/dr chi, r d/dr psi and their mix (the two read psi and chi
+  // and write different fields)
+  MLG_TRY(side_fork());
+  MLG_TRY(launch_band_apply_to(uz, chi, 1, c, -1.0, post_chop(c0), G.side));
+  MLG_TRY(launch_tp2vec_uv(ur, up, psi, chi, c, post_chop(c0)));
+  MLG_TRY(side_join());
   return 0;
 }
 
@@ -1205,9 +1209,18 @@ int op_advection_rhs(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, con
   for (Scalar* q : vw) q->set_space("PPP");
   Scalar &vr = *vw[0], &vp = *vw[1], &vz = *vw[2], &wr = *vw[3], &wp = *vw[4], &wz = *vw[5];
   // v and w, each with its three transforms to PPP batched (three fields, 78 MB at 192x128x128, stay
-  // in L2 from one stage to the next; six would not)
+  // in L2 from one stage to the next; six would not).  w = tp2vec(-del2 chi, psi) (tp2curlvec): the
+  // -del2 chi starts on the side stream beside v's kernels (the side stream's next join orders it)
+  TMP(md);
+  md.set_space("FFF");
+  md.off[0] = chi.off[0]; md.off[1] = chi.off[1]; md.off[2] = chi.off[2];
+  ChopIdx cmd;
+  MLG_TRY(chop_index(md, cmd));
+  MLG_TRY(side_fork());
+  MLG_TRY(launch_band_apply_to(md, chi, 2, cmd, -1.0, PostChop{0, 0, 0, 0, 0}, G.side));   // md = -del2 chi
   MLG_TRY(tp2vec_into(psi, chi, vr, vp, vz));
-  MLG_TRY(op_tp2curlvec(psi, chi, wr, wp, wz));
+  MLG_TRY(side_join());
+  MLG_TRY(op_tp2vec(md, psi, wr, wp, wz));
   // (vz + uz) with the background flow; in place, or into the temporaries when v and w are kept
   Scalar* prod[3] = {&vr_t, &vp_t, &vz_t};
   MLG_TRY(vecprod_bg(vr, vp, vz, wr, wp, wz, &uz, keep ? prod : nullptr));
@@ -1228,9 +1241,13 @@ int op_vortex_step_dev(Scalar& psi, Scalar& chi, Scalar& nlpsi, Scalar& nlchi, S
   MLG_TRY(op_zeroat1_2(psi, chi));
   // advection_rhs's own dealias of psi and chi (vortical_flow_3d.f90:368) finds them dealiased
   // already: the SVV gain and zeroat1 leave a zero coefficient zero, so it is skipped here
-  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz, keep, true));
-  k_finite<<<nblk(G.fsize), 256, 0, G.stream>>>(psi.e, chi.e, G.fsize, (int*)(G.dscal + DS_FLAG));
+  // check_stability's finiteness test of psi and chi, final from here on, on the side stream beside the
+  // advection (which reads them only); joined before the step ends
+  MLG_TRY(side_fork());
+  k_finite<<<nblk(G.fsize), 256, 0, G.side>>>(psi.e, chi.e, G.fsize, (int*)(G.dscal + DS_FLAG));
   MLG_LAUNCH();
+  MLG_TRY(op_advection_rhs(psi, chi, nlpsi, nlchi, uz, keep, true));
+  MLG_TRY(side_join());
   return 0;
 }
 
