@@ -16,7 +16,9 @@
  *    stand for the reference's `stop` messages; mlg_last_error() gives the message text.
  *  - All work is enqueued on one CUDA stream (mlg_set_stream); calls return once enqueued,
  *    except those that hand a value back to the host (downloads, calcat0/1, svv_filter's
- *    gain), which synchronise that stream first.
+ *    gain), which synchronise that stream first.  Inside a call the library also runs work on
+ *    a side stream of its own (forked from and joined back into the caller's stream with
+ *    events before the call returns), so stream order with the caller's work is kept.
  *  - One transform kit per process, as in the reference (mlegs_spectfm_init.f90:15-16).
  */
 #ifndef MLEGS_GB300_H
